@@ -1,0 +1,138 @@
+/* sgdyn: batched articulated-body kinematics and dynamics on GB300 (sm_103a), C ABI.
+ *
+ * Drop-in boundary for SAPIEN's PinocchioModel path. Every batched entry point below is
+ * the GPU counterpart of one method of the reference C++ class sapien::PinocchioModel
+ * (pinocchio/pinocchio_model.h:27-130, pinocchio/pinocchio_model.cpp) and its pybind
+ * binding (pinocchio/pinocchio_model.cpp:306-367). The citation beside each function
+ * names the method it replaces.
+ *
+ * Conventions
+ *  - All compute functions take DEVICE pointers (or managed memory) to FP64 arrays and
+ *    enqueue work on `stream` (a cudaStream_t; NULL = legacy default stream). They return
+ *    after the launch; results are ready when the stream reaches that point.
+ *  - Arrays are batched over n environments. layout SGDYN_ENV_MAJOR: [n][cols] row-major
+ *    (a torch tensor of shape [n, cols]); SGDYN_COL_MAJOR: [cols][n] (structure of arrays).
+ *  - q is in external (SAPIEN) joint order, one coordinate per revolute / continuous /
+ *    prismatic joint (continuous joints take their angle, exactly like posS2P,
+ *    pinocchio_model.cpp:49-72) and 7 per free-flyer joint (x y z qx qy qz qw; an
+ *    extension: the reference's posS2P rejects nq > 2). Velocities, accelerations and
+ *    torques have nv columns in external order.
+ *  - Every function returns SGDYN_OK (0) or a negative status; sgdyn_last_error()
+ *    returns a message for the calling thread's last failure.
+ *  - A model is immutable while launches that use it are in flight. The first launch on
+ *    a device uploads the model tables with cudaMalloc/cudaMemcpy; call
+ *    sgdyn_model_upload() first when launches will be captured into a CUDA graph.
+ */
+#ifndef SGDYN_H
+#define SGDYN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGDYN_OK 0
+#define SGDYN_ERR_INVALID_ARGUMENT (-1) /* bad joint/link name: reference std::invalid_argument */
+#define SGDYN_ERR_RUNTIME (-2)          /* reference std::runtime_error: bad index, bad sizes, unsupported joint */
+#define SGDYN_ERR_CUDA (-3)             /* CUDA launch or memory error */
+#define SGDYN_ERR_UNSUPPORTED (-4)      /* model outside the kernels' limits (joints, free flyers) */
+#define SGDYN_ERR_NULL (-5)             /* null or non-device pointer */
+
+#define SGDYN_ENV_MAJOR 0
+#define SGDYN_COL_MAJOR 1
+
+/* op bits for sgdyn_step */
+#define SGDYN_OP_FK 1
+#define SGDYN_OP_JACOBIAN 2
+#define SGDYN_OP_MASS_MATRIX 4
+#define SGDYN_OP_INVERSE_DYNAMICS 8
+#define SGDYN_OP_FORWARD_DYNAMICS 16
+
+typedef struct sgdyn_model sgdyn_model;
+
+/* Message for the calling thread's most recent failure ("" if none). */
+const char* sgdyn_last_error(void);
+
+/* PinocchioModel::fromURDFXML (pinocchio_model.cpp:39-47): build from URDF text with
+ * gravity g (model.gravity = (g, 0)). The default joint order is the tree order and the
+ * default link order is the URDF tree order, until set_*_order is called. */
+int sgdyn_model_from_urdf(const char* urdf_xml, const double gravity[3], sgdyn_model** out);
+void sgdyn_model_free(sgdyn_model* m);
+
+/* PinocchioModel::setJointOrder (pinocchio_model.cpp:99-128). */
+int sgdyn_model_set_joint_order(sgdyn_model* m, const char* const* names, int n);
+/* PinocchioModel::setLinkOrder (pinocchio_model.cpp:130-140). */
+int sgdyn_model_set_link_order(sgdyn_model* m, const char* const* names, int n);
+
+/* Sizes: external q columns, velocity dimension, links in the link order, joints incl. universe. */
+int sgdyn_model_info(const sgdyn_model* m, int* nq_ext, int* nv, int* nlinks, int* njoints);
+/* Kind of the k-th joint in external order: 1 revolute, 2 prismatic, 3 continuous, 4 free flyer. */
+int sgdyn_model_joint_kind(const sgdyn_model* m, int k, int* kind);
+/* Name of the moving joint with tree index j (1..njoints-1) or of BODY frame b. */
+int sgdyn_model_joint_name(const sgdyn_model* m, int j, const char** name);
+int sgdyn_model_body_count(const sgdyn_model* m, int* nbodies);
+int sgdyn_model_body_name(const sgdyn_model* m, int b, const char** name);
+/* Upload the model tables to the current device (done lazily by the first launch). */
+int sgdyn_model_upload(sgdyn_model* m);
+/* Host copy of the packed kernel tables (DModel header, DJoint[njoints], DLink[nlinks];
+ * layout in sapien_gb300/csrc/device_model.h). Valid until the model changes. */
+int sgdyn_model_table(const sgdyn_model* m, const void** data, int64_t* bytes);
+
+/* PinocchioModel::computeForwardKinematics + getLinkPose for every link
+ * (pinocchio_model.cpp:146-161), FP64: link_poses [n][nlinks*7] = (x y z qw qx qy qz)
+ * per link, in the articulation base frame. */
+int sgdyn_compute_forward_kinematics(const sgdyn_model* m, int64_t n, const double* q, double* link_poses, int layout,
+                                     void* stream);
+
+/* PinocchioModel::computeFullJacobian (pinocchio_model.cpp:163-165): the WORLD Jacobian
+ * data.J, J [n][6*nv] = rows (vx vy vz wx wy wz) x external columns. */
+int sgdyn_compute_full_jacobian(const sgdyn_model* m, int64_t n, const double* q, double* J, int layout,
+                                void* stream);
+
+/* PinocchioModel::computeFullJacobian followed by getLinkJacobian(link, local)
+ * (pinocchio_model.cpp:167-186): J [n][6*nv]. local != 0 gives the link (body) frame. */
+int sgdyn_compute_link_jacobian(const sgdyn_model* m, int64_t n, int link, int local, const double* q, double* J,
+                                int layout, void* stream);
+
+/* PinocchioModel::computeSingleLinkLocalJacobian (pinocchio_model.cpp:188-199). */
+int sgdyn_compute_single_link_local_jacobian(const sgdyn_model* m, int64_t n, int link, const double* q, double* J,
+                                             int layout, void* stream);
+
+/* PinocchioModel::computeGeneralizedMassMatrix (pinocchio_model.cpp:201-206): M [n][nv*nv], symmetric. */
+int sgdyn_compute_generalized_mass_matrix(const sgdyn_model* m, int64_t n, const double* q, double* M, int layout,
+                                          void* stream);
+
+/* PinocchioModel::computeCoriolisMatrix (pinocchio_model.cpp:208-212): C [n][nv*nv]. */
+int sgdyn_compute_coriolis_matrix(const sgdyn_model* m, int64_t n, const double* q, const double* qd, double* C,
+                                  int layout, void* stream);
+
+/* PinocchioModel::computeInverseDynamics (RNEA, pinocchio_model.cpp:214-219): tau [n][nv]. */
+int sgdyn_compute_inverse_dynamics(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                   const double* qdd, double* tau, int layout, void* stream);
+
+/* PinocchioModel::computeForwardDynamics (ABA, pinocchio_model.cpp:221-226): qdd [n][nv]. */
+int sgdyn_compute_forward_dynamics(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                   const double* tau, double* qdd, int layout, void* stream);
+
+/* One fused sweep computing any subset (ops = SGDYN_OP_* bits) of the five calls above
+ * on the same q / qd: outputs for unrequested ops may be NULL. No reference counterpart
+ * as a single call: it replaces a sequence of the reference methods. */
+int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const double* qd, const double* qdd,
+               const double* tau, double* link_poses, double* J, double* M, double* tau_out, double* qdd_out,
+               int layout, void* stream);
+
+/* PinocchioModel::computeInverseKinematics (CLIK, pinocchio_model.cpp:228-300), one solve per
+ * environment. target [n][7] = link pose (x y z qw qx qy qz) in the base frame, FP64.
+ * q0 [n][nq_ext] or NULL (neutral start), mask [nv] int (1 active, 0 frozen) or NULL (all
+ * active). Outputs: q_out [n][nq_ext] (best iterate), success [n] int, err [n][6] (log6 error
+ * of the best iterate, linear then angular). */
+int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, const double* target,
+                                     const double* q0, const int* mask, double eps, int max_iterations, double dt,
+                                     double damp, double* q_out, int* success, double* err, int layout, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGDYN_H */

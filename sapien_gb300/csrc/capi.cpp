@@ -1,0 +1,303 @@
+// C-ABI entry points (declared in include/sgdyn.h): argument validation, error
+// translation and kernel dispatch. Errors follow the reference's exception split
+// (pinocchio/pinocchio_model.cpp:33-36, 105, 121, 136): std::invalid_argument for bad
+// names -> SGDYN_ERR_INVALID_ARGUMENT, std::runtime_error -> SGDYN_ERR_RUNTIME.
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sgdyn.h"
+#include "kernels.h"
+#include "model.h"
+
+struct sgdyn_model {
+  sgdyn::Model* impl;
+};
+
+namespace sgdyn {
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const std::invalid_argument& e) {
+    return fail(SGDYN_ERR_INVALID_ARGUMENT, e.what());
+  } catch (const std::exception& e) {
+    return fail(SGDYN_ERR_RUNTIME, e.what());
+  } catch (...) {
+    return fail(SGDYN_ERR_RUNTIME, "unknown error");
+  }
+}
+
+// Rejects host pointers before they reach a kernel.
+bool device_accessible(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+Arr make_arr(const void* p, int64_t n, int64_t cols, int layout) {
+  Arr a;
+  a.p = static_cast<double*>(const_cast<void*>(p));
+  if (layout == SGDYN_ENV_MAJOR) {
+    a.es = cols;
+    a.cs = 1;
+  } else {
+    a.es = 1;
+    a.cs = n;
+  }
+  return a;
+}
+
+int check_model(const sgdyn_model* m) {
+  if (!m || !m->impl) return fail(SGDYN_ERR_NULL, "null model");
+  const Model& M = *m->impl;
+  if (stash_bucket(M.njoints()) == 0)
+    return fail(SGDYN_ERR_UNSUPPORTED, "model has more than 63 moving joints");
+  int nff = 0;
+  for (auto& J : M.joints) nff += J.kind == JK_FREEFLYER;
+  if (nff > 1) return fail(SGDYN_ERR_UNSUPPORTED, "model has more than one free-flyer joint");
+  return SGDYN_OK;
+}
+
+struct Req {
+  const void* p;
+  const char* name;
+};
+int check_ptrs(std::initializer_list<Req> reqs) {
+  for (auto& r : reqs)
+    if (!device_accessible(r.p)) return fail(SGDYN_ERR_NULL, std::string(r.name) + " is null or not device memory");
+  return SGDYN_OK;
+}
+
+int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const double* qd, const double* qdd,
+             const double* tau, double* poses, double* J, double* M, double* tau_out, double* qdd_out, int layout,
+             void* stream) {
+  if (int rc = check_model(m)) return rc;
+  if (n < 0) return fail(SGDYN_ERR_RUNTIME, "negative batch size");
+  if (layout != SGDYN_ENV_MAJOR && layout != SGDYN_COL_MAJOR) return fail(SGDYN_ERR_RUNTIME, "bad layout");
+  if (ops <= 0 || ops > OP_ALL) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
+  if (n == 0) return SGDYN_OK;
+  Model& Mo = *m->impl;
+  if (int rc = check_ptrs({{q, "q"}})) return rc;
+  if (ops & (OP_RNEA | OP_ABA))
+    if (int rc = check_ptrs({{qd, "qd"}})) return rc;
+  if (ops & OP_RNEA)
+    if (int rc = check_ptrs({{qdd, "qdd"}, {tau_out, "tau_out"}})) return rc;
+  if (ops & OP_ABA)
+    if (int rc = check_ptrs({{tau, "tau"}, {qdd_out, "qdd_out"}})) return rc;
+  if (ops & OP_FK)
+    if (int rc = check_ptrs({{poses, "link_poses"}})) return rc;
+  if (ops & OP_JAC)
+    if (int rc = check_ptrs({{J, "J"}})) return rc;
+  if (ops & OP_CRBA)
+    if (int rc = check_ptrs({{M, "M"}})) return rc;
+  int err = 0;
+  const DModel* dm = Mo.device_table(&err);
+  if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+  const int64_t nv = Mo.nv();
+  StepArgs a;
+  a.n = n;
+  a.q = make_arr(q, n, Mo.nq_ext(), layout);
+  a.qd = make_arr(qd, n, nv, layout);
+  a.qdd = make_arr(qdd, n, nv, layout);
+  a.tau = make_arr(tau, n, nv, layout);
+  a.poses = make_arr(poses, n, int64_t(Mo.nlinks()) * 7, layout);
+  a.J = make_arr(J, n, 6 * nv, layout);
+  a.M = make_arr(M, n, nv * nv, layout);
+  a.tau_out = make_arr(tau_out, n, nv, layout);
+  a.qdd_out = make_arr(qdd_out, n, nv, layout);
+  auto s = static_cast<cudaStream_t>(stream);
+  static const int fused[] = {OP_ALL, OP_RNEA | OP_ABA, OP_FK | OP_JAC};
+  int rest = ops;
+  std::vector<int> launches;
+  for (int f : fused)
+    if ((rest & f) == f && f != 0 && __builtin_popcount(f) > 1) {
+      launches.push_back(f);
+      rest &= ~f;
+    }
+  for (int b = 1; b <= OP_ABA; b <<= 1)
+    if (rest & b) launches.push_back(b);
+  for (int o : launches) {
+    cudaError_t e = launch_step(dm, Mo.njoints(), o, a, s);
+    if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  }
+  return SGDYN_OK;
+}
+
+}  // namespace
+}  // namespace sgdyn
+
+using namespace sgdyn;
+
+extern "C" {
+
+const char* sgdyn_last_error(void) { return g_err.c_str(); }
+
+int sgdyn_model_from_urdf(const char* urdf_xml, const double gravity[3], sgdyn_model** out) {
+  if (!urdf_xml || !gravity || !out) return fail(SGDYN_ERR_NULL, "null argument");
+  return guarded([&] {
+    *out = nullptr;
+    Model* M = Model::from_urdf(urdf_xml, gravity);
+    *out = new sgdyn_model{M};
+    return SGDYN_OK;
+  });
+}
+
+void sgdyn_model_free(sgdyn_model* m) {
+  if (!m) return;
+  delete m->impl;
+  delete m;
+}
+
+int sgdyn_model_set_joint_order(sgdyn_model* m, const char* const* names, int n) {
+  if (!m || (!names && n > 0) || n < 0) return fail(SGDYN_ERR_NULL, "null argument");
+  return guarded([&] {
+    std::vector<std::string> v(names, names + n);
+    m->impl->set_joint_order(v);
+    return SGDYN_OK;
+  });
+}
+
+int sgdyn_model_set_link_order(sgdyn_model* m, const char* const* names, int n) {
+  if (!m || (!names && n > 0) || n < 0) return fail(SGDYN_ERR_NULL, "null argument");
+  return guarded([&] {
+    std::vector<std::string> v(names, names + n);
+    m->impl->set_link_order(v);
+    return SGDYN_OK;
+  });
+}
+
+int sgdyn_model_info(const sgdyn_model* m, int* nq_ext, int* nv, int* nlinks, int* njoints) {
+  if (!m) return fail(SGDYN_ERR_NULL, "null model");
+  if (nq_ext) *nq_ext = m->impl->nq_ext();
+  if (nv) *nv = m->impl->nv();
+  if (nlinks) *nlinks = m->impl->nlinks();
+  if (njoints) *njoints = m->impl->njoints();
+  return SGDYN_OK;
+}
+
+int sgdyn_model_joint_kind(const sgdyn_model* m, int k, int* kind) {
+  if (!m || !kind) return fail(SGDYN_ERR_NULL, "null argument");
+  const Model& M = *m->impl;
+  // external order = increasing q column
+  for (int j = 1; j < M.njoints(); j++) {
+    int rank = 0;
+    for (int i = 1; i < M.njoints(); i++)
+      if (M.ext_qcol_of_joint(i) < M.ext_qcol_of_joint(j)) rank++;
+    if (rank == k) {
+      *kind = M.joints[j].kind;
+      return SGDYN_OK;
+    }
+  }
+  return fail(SGDYN_ERR_RUNTIME, "joint index out of bound");
+}
+
+int sgdyn_model_joint_name(const sgdyn_model* m, int j, const char** name) {
+  if (!m || !name) return fail(SGDYN_ERR_NULL, "null argument");
+  if (j < 1 || j >= m->impl->njoints()) return fail(SGDYN_ERR_RUNTIME, "joint index out of bound");
+  *name = m->impl->joints[j].name.c_str();
+  return SGDYN_OK;
+}
+
+int sgdyn_model_body_count(const sgdyn_model* m, int* nbodies) {
+  if (!m || !nbodies) return fail(SGDYN_ERR_NULL, "null argument");
+  *nbodies = int(m->impl->bodies.size());
+  return SGDYN_OK;
+}
+
+int sgdyn_model_body_name(const sgdyn_model* m, int b, const char** name) {
+  if (!m || !name) return fail(SGDYN_ERR_NULL, "null argument");
+  if (b < 0 || b >= int(m->impl->bodies.size())) return fail(SGDYN_ERR_RUNTIME, "body index out of bound");
+  *name = m->impl->bodies[b].name.c_str();
+  return SGDYN_OK;
+}
+
+int sgdyn_model_upload(sgdyn_model* m) {
+  if (!m) return fail(SGDYN_ERR_NULL, "null model");
+  int err = 0;
+  if (!m->impl->device_table(&err)) return fail(SGDYN_ERR_CUDA, "model upload failed");
+  return SGDYN_OK;
+}
+
+int sgdyn_model_table(const sgdyn_model* m, const void** data, int64_t* bytes) {
+  if (!m || !data || !bytes) return fail(SGDYN_ERR_NULL, "null argument");
+  *data = m->impl->host_table().data();
+  *bytes = int64_t(m->impl->host_table().size());
+  return SGDYN_OK;
+}
+
+int sgdyn_compute_forward_kinematics(const sgdyn_model* m, int64_t n, const double* q, double* link_poses,
+                                     int layout, void* stream) {
+  return guarded([&] {
+    return run_step(m, n, OP_FK, q, nullptr, nullptr, nullptr, link_poses, nullptr, nullptr, nullptr, nullptr, layout,
+                    stream);
+  });
+}
+
+int sgdyn_compute_full_jacobian(const sgdyn_model* m, int64_t n, const double* q, double* J, int layout,
+                                void* stream) {
+  return guarded([&] {
+    return run_step(m, n, OP_JAC, q, nullptr, nullptr, nullptr, nullptr, J, nullptr, nullptr, nullptr, layout, stream);
+  });
+}
+
+int sgdyn_compute_generalized_mass_matrix(const sgdyn_model* m, int64_t n, const double* q, double* M, int layout,
+                                          void* stream) {
+  return guarded([&] {
+    return run_step(m, n, OP_CRBA, q, nullptr, nullptr, nullptr, nullptr, nullptr, M, nullptr, nullptr, layout,
+                    stream);
+  });
+}
+
+int sgdyn_compute_inverse_dynamics(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                   const double* qdd, double* tau, int layout, void* stream) {
+  return guarded([&] {
+    return run_step(m, n, OP_RNEA, q, qd, qdd, nullptr, nullptr, nullptr, nullptr, tau, nullptr, layout, stream);
+  });
+}
+
+int sgdyn_compute_forward_dynamics(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                   const double* tau, double* qdd, int layout, void* stream) {
+  return guarded([&] {
+    return run_step(m, n, OP_ABA, q, qd, nullptr, tau, nullptr, nullptr, nullptr, nullptr, qdd, layout, stream);
+  });
+}
+
+int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const double* qd, const double* qdd,
+               const double* tau, double* link_poses, double* J, double* M, double* tau_out, double* qdd_out,
+               int layout, void* stream) {
+  return guarded([&] {
+    return run_step(m, n, ops, q, qd, qdd, tau, link_poses, J, M, tau_out, qdd_out, layout, stream);
+  });
+}
+
+int sgdyn_compute_link_jacobian(const sgdyn_model*, int64_t, int, int, const double*, double*, int, void*) {
+  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+}
+int sgdyn_compute_single_link_local_jacobian(const sgdyn_model*, int64_t, int, const double*, double*, int, void*) {
+  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+}
+int sgdyn_compute_coriolis_matrix(const sgdyn_model*, int64_t, const double*, const double*, double*, int, void*) {
+  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+}
+int sgdyn_compute_inverse_kinematics(const sgdyn_model*, int64_t, int, const double*, const double*, const int*,
+                                     double, int, double, double, double*, int*, double*, int, void*) {
+  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,435 @@
+// URDF -> kinematic tree with the conventions of pinocchio::urdf::buildModelFromXML
+// (reached from pinocchio/pinocchio_model.cpp:42). The semantics restated here:
+//  * the root link is welded to the universe joint 0 (fromURDFXML passes no root joint);
+//  * links are visited depth first, the children of a link in byte-wise order of their
+//    joint names (urdfdom stores joints in a std::map keyed by name);
+//  * a moving joint's placement is parent_body_frame.placement * origin, relative to the
+//    moving joint carrying the parent link; the child link's inertia is attached to it;
+//  * a fixed joint adds no DoF: the child's inertia is transported by
+//    parent_body_frame.placement * origin and added to the carrying joint, and the
+//    child's BODY frame gets that placement;
+//  * revolute (nq 1), continuous (nq 2 internally as cos/sin, one external angle),
+//    prismatic (nq 1), floating (free flyer x y z qx qy qz qw, nv 6);
+//  * link inertials: com = origin.xyz, rotational inertia R(origin.rpy) I R^T;
+//  * rpy -> rotation through the half-angle quaternion.
+// setJointOrder / setLinkOrder follow pinocchio/pinocchio_model.cpp:99-140.
+#include "model.h"
+
+#include <cuda_runtime.h>
+
+#include <charconv>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <set>
+#include <stdexcept>
+
+#include "xml.h"
+
+namespace sgdyn {
+namespace {
+
+struct InvalidArgument : std::invalid_argument {
+  using std::invalid_argument::invalid_argument;
+};
+
+void parse_doubles(const std::string& s, double* out, int n) {
+  const char* b = s.data();
+  const char* e = b + s.size();
+  for (int k = 0; k < n; k++) {
+    while (b < e && (*b == ' ' || *b == '\t' || *b == '\n' || *b == '\r' || *b == ',')) b++;
+    if (*b == '+') b++;
+    auto r = std::from_chars(b, e, out[k]);
+    if (r.ec != std::errc()) throw std::runtime_error("URDF: cannot parse number list '" + s + "'");
+    b = r.ptr;
+  }
+}
+double parse_double(const std::string& s) {
+  double v;
+  parse_doubles(s, &v, 1);
+  return v;
+}
+
+void mat_mul(const double* A, const double* B, double* C) {
+  double T[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) T[i * 3 + j] = A[i * 3] * B[j] + A[i * 3 + 1] * B[3 + j] + A[i * 3 + 2] * B[6 + j];
+  std::memcpy(C, T, sizeof T);
+}
+void mat_vec(const double* A, const double* x, double* y) {
+  double t[3];
+  for (int i = 0; i < 3; i++) t[i] = A[i * 3] * x[0] + A[i * 3 + 1] * x[1] + A[i * 3 + 2] * x[2];
+  std::memcpy(y, t, sizeof t);
+}
+Placement compose(const Placement& a, const Placement& b) {
+  Placement c;
+  mat_mul(a.R, b.R, c.R);
+  mat_vec(a.R, b.p, c.p);
+  for (int k = 0; k < 3; k++) c.p[k] += a.p[k];
+  return c;
+}
+Placement identity() {
+  Placement P;
+  const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  std::memcpy(P.R, I, sizeof I);
+  P.p[0] = P.p[1] = P.p[2] = 0;
+  return P;
+}
+void rpy_to_R(const double rpy[3], double* R) {
+  double phi = rpy[0] / 2, the = rpy[1] / 2, psi = rpy[2] / 2;
+  double x = std::sin(phi) * std::cos(the) * std::cos(psi) - std::cos(phi) * std::sin(the) * std::sin(psi);
+  double y = std::cos(phi) * std::sin(the) * std::cos(psi) + std::sin(phi) * std::cos(the) * std::sin(psi);
+  double z = std::cos(phi) * std::cos(the) * std::sin(psi) - std::sin(phi) * std::sin(the) * std::cos(psi);
+  double w = std::cos(phi) * std::cos(the) * std::cos(psi) + std::sin(phi) * std::sin(the) * std::sin(psi);
+  double n = std::sqrt(x * x + y * y + z * z + w * w);
+  x /= n; y /= n; z /= n; w /= n;
+  R[0] = 1 - 2 * (y * y + z * z); R[1] = 2 * (x * y - w * z);     R[2] = 2 * (x * z + w * y);
+  R[3] = 2 * (x * y + w * z);     R[4] = 1 - 2 * (x * x + z * z); R[5] = 2 * (y * z - w * x);
+  R[6] = 2 * (x * z - w * y);     R[7] = 2 * (y * z + w * x);     R[8] = 1 - 2 * (x * x + y * y);
+}
+Placement origin_of(const XmlNode* elem) {
+  Placement P = identity();
+  if (!elem) return P;
+  const XmlNode* o = elem->child("origin");
+  if (!o) return P;
+  double xyz[3] = {0, 0, 0}, rpy[3] = {0, 0, 0};
+  if (auto* a = o->attr("xyz")) parse_doubles(*a, xyz, 3);
+  if (auto* a = o->attr("rpy")) parse_doubles(*a, rpy, 3);
+  rpy_to_R(rpy, P.R);
+  std::memcpy(P.p, xyz, sizeof xyz);
+  return P;
+}
+
+// Link inertial (m, com c, Ic about com, in link frame) -> origin form in link frame.
+BodyInertia link_inertia(const XmlNode* link) {
+  BodyInertia B;
+  const XmlNode* in = link->child("inertial");
+  if (!in) return B;
+  Placement o = origin_of(in);
+  double m = 0;
+  if (auto* me = in->child("mass"))
+    if (auto* v = me->attr("value")) m = parse_double(*v);
+  double Iu[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (auto* ie = in->child("inertia")) {
+    auto get = [&](const char* k) { auto* a = ie->attr(k); return a ? parse_double(*a) : 0.0; };
+    double xx = get("ixx"), xy = get("ixy"), xz = get("ixz"), yy = get("iyy"), yz = get("iyz"), zz = get("izz");
+    double t[9] = {xx, xy, xz, xy, yy, yz, xz, yz, zz};
+    std::memcpy(Iu, t, sizeof t);
+  }
+  double Ic[9], T[9], Rt[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) Rt[i * 3 + j] = o.R[j * 3 + i];
+  mat_mul(o.R, Iu, T);
+  mat_mul(T, Rt, Ic);
+  const double* c = o.p;
+  double cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+  B.m = m;
+  for (int k = 0; k < 3; k++) B.h[k] = m * c[k];
+  // I = Ic + m (|c|^2 I - c c^T)
+  B.I[0] = Ic[0] + m * (cc - c[0] * c[0]);
+  B.I[1] = Ic[1] - m * c[0] * c[1];
+  B.I[2] = Ic[2] - m * c[0] * c[2];
+  B.I[3] = Ic[4] + m * (cc - c[1] * c[1]);
+  B.I[4] = Ic[5] - m * c[1] * c[2];
+  B.I[5] = Ic[8] + m * (cc - c[2] * c[2]);
+  return B;
+}
+
+// Express an origin-form inertia given in frame B in frame A (x_A = R x_B + p).
+BodyInertia transport(const BodyInertia& B, const Placement& P) {
+  BodyInertia O;
+  O.m = B.m;
+  double hr[3];
+  mat_vec(P.R, B.h, hr);
+  for (int k = 0; k < 3; k++) O.h[k] = hr[k] + B.m * P.p[k];
+  double I9[9] = {B.I[0], B.I[1], B.I[2], B.I[1], B.I[3], B.I[4], B.I[2], B.I[4], B.I[5]};
+  double T[9], Rt[9], Ir[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) Rt[i * 3 + j] = P.R[j * 3 + i];
+  mat_mul(P.R, I9, T);
+  mat_mul(T, Rt, Ir);
+  // I_A = R I_B R^T + m(|p|^2 I - p p^T) + 2 (hr.p) I - p hr^T - hr p^T
+  const double* p = P.p;
+  double pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+  double hp = hr[0] * p[0] + hr[1] * p[1] + hr[2] * p[2];
+  auto at = [&](int i, int j) {
+    double d = (i == j) ? (B.m * pp + 2 * hp) : 0.0;
+    return Ir[i * 3 + j] + d - B.m * p[i] * p[j] - p[i] * hr[j] - hr[i] * p[j];
+  };
+  O.I[0] = at(0, 0); O.I[1] = at(0, 1); O.I[2] = at(0, 2);
+  O.I[3] = at(1, 1); O.I[4] = at(1, 2); O.I[5] = at(2, 2);
+  return O;
+}
+void add_inertia(BodyInertia& A, const BodyInertia& B) {
+  A.m += B.m;
+  for (int k = 0; k < 3; k++) A.h[k] += B.h[k];
+  for (int k = 0; k < 6; k++) A.I[k] += B.I[k];
+}
+
+bool is_identity(const double* R) {
+  return R[0] == 1 && R[4] == 1 && R[8] == 1 && R[1] == 0 && R[2] == 0 && R[3] == 0 && R[5] == 0 && R[6] == 0 &&
+         R[7] == 0;
+}
+
+}  // namespace
+
+Model* Model::from_urdf(const std::string& xml, const double g[3]) {
+  auto root = parse_xml(xml);
+  if (root->name != "robot") throw std::runtime_error("URDF: root element is not <robot>");
+  struct JointDesc {
+    std::string type, parent, child;
+    Placement origin;
+    double axis[3];
+  };
+  std::map<std::string, const XmlNode*> links;
+  std::map<std::string, JointDesc> jdesc;  // std::map: byte-wise name order
+  std::map<std::string, std::string> parent_joint_of;  // child link -> joint name
+  for (auto& c : root->children) {
+    if (c->name == "link") {
+      auto* n = c->attr("name");
+      if (!n) throw std::runtime_error("URDF: link without name");
+      if (links.count(*n)) throw std::runtime_error("URDF: duplicate link " + *n);
+      links[*n] = c.get();
+    } else if (c->name == "joint") {
+      auto* n = c->attr("name");
+      auto* t = c->attr("type");
+      if (!n || !t) throw std::runtime_error("URDF: joint without name or type");
+      const XmlNode* pe = c->child("parent");
+      const XmlNode* ce = c->child("child");
+      if (!pe || !ce || !pe->attr("link") || !ce->attr("link"))
+        throw std::runtime_error("URDF: joint " + *n + " lacks parent/child");
+      JointDesc d;
+      d.type = *t;
+      d.parent = *pe->attr("link");
+      d.child = *ce->attr("link");
+      d.origin = origin_of(c.get());
+      d.axis[0] = 1; d.axis[1] = 0; d.axis[2] = 0;
+      if (auto* ax = c->child("axis"))
+        if (auto* a = ax->attr("xyz")) parse_doubles(*a, d.axis, 3);
+      if (jdesc.count(*n)) throw std::runtime_error("URDF: duplicate joint " + *n);
+      if (parent_joint_of.count(d.child)) throw std::runtime_error("URDF: link " + d.child + " has two parents");
+      parent_joint_of[d.child] = *n;
+      jdesc[*n] = d;
+    }
+  }
+  for (auto& kv : jdesc) {
+    if (!links.count(kv.second.parent) || !links.count(kv.second.child))
+      throw std::runtime_error("URDF: joint " + kv.first + " references an unknown link");
+  }
+  std::vector<std::string> roots;
+  for (auto& kv : links)
+    if (!parent_joint_of.count(kv.first)) roots.push_back(kv.first);
+  if (roots.size() != 1) throw std::runtime_error("URDF: expected exactly one root link");
+  std::map<std::string, std::vector<std::string>> children;  // link -> joint names (sorted)
+  for (auto& kv : jdesc) children[kv.second.parent].push_back(kv.first);
+
+  auto* M = new Model;
+  std::memcpy(M->gravity, g, sizeof(double) * 3);
+  HostJoint uni;
+  uni.name = "universe";
+  uni.placement = identity();
+  M->joints.push_back(uni);
+  M->joints[0].inertia = link_inertia(links[roots[0]]);
+  M->bodies.push_back({roots[0], 0, identity()});
+  std::function<void(const std::string&, int)> visit = [&](const std::string& link, int body_idx) {
+    const HostBody pb = M->bodies[body_idx];
+    for (auto& jn : children[link]) {
+      const JointDesc& d = jdesc[jn];
+      Placement P = compose(pb.placement, d.origin);
+      BodyInertia Yc = link_inertia(links[d.child]);
+      if (d.type == "fixed") {
+        add_inertia(M->joints[pb.joint].inertia, transport(Yc, P));
+        M->bodies.push_back({d.child, pb.joint, P});
+      } else {
+        HostJoint J;
+        J.name = jn;
+        J.parent = pb.joint;
+        J.placement = P;
+        J.inertia = Yc;
+        if (d.type == "revolute") J.kind = JK_REVOLUTE;
+        else if (d.type == "continuous") J.kind = JK_CONTINUOUS;
+        else if (d.type == "prismatic") J.kind = JK_PRISMATIC;
+        else if (d.type == "floating") J.kind = JK_FREEFLYER;
+        else throw std::runtime_error("URDF: unsupported joint type '" + d.type + "' (joint " + jn + ")");
+        if (J.kind != JK_FREEFLYER) {
+          double n = std::sqrt(d.axis[0] * d.axis[0] + d.axis[1] * d.axis[1] + d.axis[2] * d.axis[2]);
+          if (!(n > 0)) throw std::runtime_error("URDF: zero joint axis (joint " + jn + ")");
+          for (int k = 0; k < 3; k++) J.axis[k] = d.axis[k] / n;
+        }
+        J.depth = M->joints[pb.joint].depth + 1;
+        M->joints.push_back(J);
+        M->bodies.push_back({d.child, int(M->joints.size()) - 1, identity()});
+      }
+      visit(d.child, int(M->bodies.size()) - 1);
+    }
+  };
+  visit(roots[0], 0);
+  int nq = 0, nv = 0;
+  for (auto& J : M->joints) {
+    int jq = 0, jv = 0;
+    switch (J.kind) {
+      case JK_REVOLUTE: case JK_PRISMATIC: jq = 1; jv = 1; break;
+      case JK_CONTINUOUS: jq = 2; jv = 1; break;
+      case JK_FREEFLYER: jq = 7; jv = 6; break;
+      default: break;
+    }
+    J.idx_q = nq; J.idx_v = nv; J.nq = jq; J.nv = jv;
+    nq += jq; nv += jv;
+  }
+  M->nq_int_ = nq;
+  M->nv_ = nv;
+  // default orders: tree order for joints, URDF tree order for links
+  std::vector<std::string> jn, ln;
+  for (size_t j = 1; j < M->joints.size(); j++) jn.push_back(M->joints[j].name);
+  for (auto& b : M->bodies) ln.push_back(b.name);
+  M->set_joint_order(jn);
+  M->set_link_order(ln);
+  return M;
+}
+
+void Model::set_joint_order(const std::vector<std::string>& names) {
+  std::vector<int> ids;
+  std::set<int> seen;
+  for (auto& n : names) {
+    int id = -1;
+    for (size_t j = 1; j < joints.size(); j++)
+      if (joints[j].name == n) id = int(j);
+    if (id < 0 || seen.count(id)) throw InvalidArgument("invalid names in setJointOrder");
+    seen.insert(id);
+    ids.push_back(id);
+  }
+  int count = 0;
+  for (int id : ids) count += joints[id].nv;
+  if (count != nv_) throw std::runtime_error("setJointOrder failed");
+  std::vector<int> qc(joints.size(), -1), vc(joints.size(), -1);
+  int qo = 0, vo = 0;
+  for (int id : ids) {
+    qc[id] = qo;
+    vc[id] = vo;
+    qo += joints[id].kind == JK_FREEFLYER ? 7 : 1;
+    vo += joints[id].nv;
+  }
+  std::lock_guard<std::mutex> lk(mu_);
+  qcol_ = qc;
+  vcol_ = vc;
+  nq_ext_ = qo;
+  rebuild_table();
+}
+
+void Model::set_link_order(const std::vector<std::string>& names) {
+  std::vector<int> lb;
+  for (auto& n : names) {
+    int id = -1;
+    for (size_t b = 0; b < bodies.size(); b++)
+      if (bodies[b].name == n) id = int(b);
+    if (id < 0) throw InvalidArgument("invalid names in setLinkOrder");
+    lb.push_back(id);
+  }
+  std::lock_guard<std::mutex> lk(mu_);
+  link_bodies_ = lb;
+  rebuild_table();
+}
+
+int Model::max_depth() const {
+  int d = 0;
+  for (auto& J : joints) d = std::max(d, J.depth);
+  return d;
+}
+bool Model::has_free_flyer() const {
+  for (auto& J : joints)
+    if (J.kind == JK_FREEFLYER) return true;
+  return false;
+}
+
+void Model::rebuild_table() {
+  int nj = njoints(), nl = int(link_bodies_.size());
+  table_.assign(model_table_bytes(nj, nl), 0);
+  auto* hdr = reinterpret_cast<DModel*>(table_.data());
+  hdr->nj = nj;
+  hdr->nv = nv_;
+  hdr->nq_ext = nq_ext_;
+  hdr->nlinks = nl;
+  hdr->max_depth = max_depth();
+  int nff = 0;
+  for (auto& J : joints) nff += J.kind == JK_FREEFLYER;
+  hdr->n_free_flyer = nff;
+  std::memcpy(hdr->gravity, gravity, sizeof(double) * 3);
+  auto* dj = const_cast<DJoint*>(model_joints(hdr));
+  for (int j = 0; j < nj; j++) {
+    const HostJoint& J = joints[j];
+    DJoint& D = dj[j];
+    std::memcpy(D.R, J.placement.R, sizeof D.R);
+    std::memcpy(D.p, J.placement.p, sizeof D.p);
+    std::memcpy(D.axis, J.axis, sizeof D.axis);
+    D.m = J.inertia.m;
+    std::memcpy(D.h, J.inertia.h, sizeof D.h);
+    std::memcpy(D.I, J.inertia.I, sizeof D.I);
+    D.parent = J.parent;
+    D.kind = J.kind;
+    D.axis_kind = AX_GENERAL;
+    if (J.kind != JK_FREEFLYER) {
+      for (int a = 0; a < 3; a++)
+        if (J.axis[a] == 1.0 && J.axis[(a + 1) % 3] == 0.0 && J.axis[(a + 2) % 3] == 0.0) D.axis_kind = a;
+    }
+    D.flags = is_identity(J.placement.R) ? JF_ROT_IDENTITY : 0;
+    D.qcol = j < int(qcol_.size()) ? qcol_[j] : -1;
+    D.vcol = j < int(vcol_.size()) ? vcol_[j] : -1;
+    D.nv = J.nv;
+    D.depth = J.depth;
+    D.ivx = J.idx_v;
+  }
+  auto* dl = const_cast<DLink*>(model_links(hdr));
+  for (int l = 0; l < nl; l++) {
+    const HostBody& B = bodies[link_bodies_[l]];
+    std::memcpy(dl[l].R, B.placement.R, sizeof dl[l].R);
+    std::memcpy(dl[l].p, B.placement.p, sizeof dl[l].p);
+    dl[l].joint = B.joint;
+    dl[l].flags = is_identity(B.placement.R) ? JF_ROT_IDENTITY : 0;
+  }
+  // device copies are stale now
+  for (auto& kv : dev_) {
+    int cur;
+    if (cudaGetDevice(&cur) == cudaSuccess) {
+      cudaSetDevice(kv.first);
+      cudaFree(kv.second);
+      cudaSetDevice(cur);
+    }
+  }
+  dev_.clear();
+}
+
+const DModel* Model::device_table(int* err) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    *err = 1;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = dev_.find(dev);
+  if (it != dev_.end()) return static_cast<const DModel*>(it->second);
+  void* p = nullptr;
+  if (cudaMalloc(&p, table_.size()) != cudaSuccess) {
+    *err = 2;
+    return nullptr;
+  }
+  if (cudaMemcpy(p, table_.data(), table_.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(p);
+    *err = 3;
+    return nullptr;
+  }
+  dev_[dev] = p;
+  return static_cast<const DModel*>(p);
+}
+
+Model::~Model() {
+  for (auto& kv : dev_) {
+    int cur;
+    if (cudaGetDevice(&cur) == cudaSuccess) {
+      cudaSetDevice(kv.first);
+      cudaFree(kv.second);
+      cudaSetDevice(cur);
+    }
+  }
+}
+
+}  // namespace sgdyn

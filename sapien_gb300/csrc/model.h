@@ -1,0 +1,82 @@
+// Host-side kinematic model: URDF -> depth-first joint tree with Pinocchio's
+// conventions, the SAPIEN<->tree joint permutation, link frames, and the flat
+// device tables the kernels read.
+#pragma once
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "device_model.h"
+
+namespace sgdyn {
+
+struct Placement {
+  double R[9];  // row-major rotation, parent <- child
+  double p[3];
+};
+
+struct BodyInertia {  // about the frame origin: h = m c, I = Ic + m [c]x^T [c]x
+  double m = 0;
+  double h[3] = {0, 0, 0};
+  double I[6] = {0, 0, 0, 0, 0, 0};  // xx xy xz yy yz zz
+};
+
+struct HostJoint {
+  std::string name;
+  int parent = 0;
+  int kind = 0;  // JK_*
+  double axis[3] = {0, 0, 0};
+  Placement placement;
+  BodyInertia inertia;
+  int idx_q = 0, idx_v = 0, nq = 0, nv = 0, depth = 0;
+};
+
+struct HostBody {  // a BODY frame (one per URDF link)
+  std::string name;
+  int joint;
+  Placement placement;
+};
+
+class Model {
+ public:
+  // Builds from URDF XML; the root link is welded to the universe (joint 0).
+  static Model* from_urdf(const std::string& xml, const double gravity[3]);
+
+  void set_joint_order(const std::vector<std::string>& names);
+  void set_link_order(const std::vector<std::string>& names);
+
+  int njoints() const { return int(joints.size()); }
+  int nq_ext() const { return nq_ext_; }
+  int nv() const { return nv_; }
+  int nq_int() const { return nq_int_; }
+  int nlinks() const { return int(link_bodies_.size()); }
+  int max_depth() const;
+  bool has_free_flyer() const;
+
+  // Device table for the current CUDA device (uploaded on first use).
+  const DModel* device_table(int* err);
+  // Host copy of the packed table (for tests and for the heterogeneous packer).
+  const std::vector<unsigned char>& host_table() const { return table_; }
+
+  std::vector<HostJoint> joints;  // [0] = universe
+  std::vector<HostBody> bodies;
+  double gravity[3] = {0, 0, -9.81};
+  int ext_qcol_of_joint(int j) const { return qcol_[j]; }
+  int ext_vcol_of_joint(int j) const { return vcol_[j]; }
+  int link_body(int link) const { return link_bodies_[link]; }
+
+  ~Model();
+
+ private:
+  void rebuild_table();
+  int nq_ext_ = 0, nv_ = 0, nq_int_ = 0;
+  std::vector<int> qcol_, vcol_;   // per joint: external q / v column of its first coordinate
+  std::vector<int> link_bodies_;   // external link index -> bodies[]
+  std::vector<unsigned char> table_;
+  std::map<int, void*> dev_;       // device ordinal -> device copy of table_
+  std::mutex mu_;
+};
+
+}  // namespace sgdyn

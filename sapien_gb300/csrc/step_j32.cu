@@ -1,0 +1,25 @@
+// Instantiations of the fused sweep for trees of up to 32 joints (incl. universe).
+#include "step_kernel.cuh"
+
+namespace sgdyn {
+
+cudaError_t launch_step_j32(const DModel* dm, int ops, const StepArgs& a, cudaStream_t s) {
+  const unsigned blocks = unsigned((a.n + 31) / 32);
+  switch (ops) {
+#define SG_CASE(O) \
+  case O: step_kernel<32, O><<<blocks, 32, 0, s>>>(dm, a); break;
+    SG_CASE(OP_FK)
+    SG_CASE(OP_JAC)
+    SG_CASE(OP_FK | OP_JAC)
+    SG_CASE(OP_CRBA)
+    SG_CASE(OP_RNEA)
+    SG_CASE(OP_ABA)
+    SG_CASE(OP_RNEA | OP_ABA)
+    SG_CASE(OP_ALL)
+#undef SG_CASE
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace sgdyn

@@ -1,0 +1,405 @@
+// Fused batched sweep over a kinematic tree, one environment per thread, FP64.
+//
+// All spatial quantities live in the WORLD frame (the frame Pinocchio's computeJointJacobians
+// and crba use). Compared with local-frame recursions this replaces the 6x6 congruence
+// transform of articulated inertias (about 220 flops per joint) by one 10-parameter
+// rigid-inertia transport shared by CRBA, RNEA and ABA, and the three motion/force
+// transforms of RNEA by plain additions. The recursions computed:
+//   FK        oMi = oMi[parent] * placement * M_J(q)                 (pinocchio_model.cpp:146-161)
+//   Jacobian  J[:, v(i)] = oMi.act(S_i)                               (pinocchio_model.cpp:163-165)
+//   CRBA      Ic[i] = sum of world inertias of the subtree;
+//             M[j, i] = S_j . (Ic[i] S_i) for j an ancestor of i        (pinocchio_model.cpp:201-206)
+//   RNEA      v_i = v_p + S_i qd_i, a_i = a_p + S_i qdd_i + v_i x (S_i qd_i), a_0 = -g,
+//             f_i = I_i a_i + v_i x* I_i v_i, tau_i = S_i . f_i, f_p += f_i  (pinocchio_model.cpp:214-219)
+//   ABA       Featherstone's three passes with U = IA S, D = S.U, u = tau - S.pA,
+//             IA_p += IA - U D^-1 U^T, pA_p += pA + Ia c + U D^-1 u,
+//             qdd = D^-1 (u - U.(a_p + c)), a = a_p + c + S qdd        (pinocchio_model.cpp:221-226)
+// The SAPIEN<->tree permutation is applied by reading and writing external columns
+// directly (DJoint::qcol / vcol); no separate permutation pass exists.
+#pragma once
+#include "kernels.h"
+#include "spatial.cuh"
+
+namespace sgdyn {
+
+__device__ __forceinline__ double ldv(const Arr& a, int64_t e, int c) { return a.p[e * a.es + int64_t(c) * a.cs]; }
+__device__ __forceinline__ void stv(const Arr& a, int64_t e, int c, double v) { a.p[e * a.es + int64_t(c) * a.cs] = v; }
+
+// Joint placement composed with the joint motion: (R_li, p_li) and the world pose.
+struct JointFrame {
+  M3 R;
+  V3 p;
+};
+
+// Local joint transform liMi = placement * M_J(q); returns the world pose given the parent's.
+__device__ __forceinline__ void joint_world_pose(const DJoint& J, const Arr& q, int64_t e, const M3* oR, const V3* op,
+                                                 M3& Ro, V3& po) {
+  M3 Rpl;
+#pragma unroll
+  for (int k = 0; k < 9; k++) Rpl.a[k] = J.R[k];
+  const V3 ppl = mk(J.p[0], J.p[1], J.p[2]);
+  const V3 ax = mk(J.axis[0], J.axis[1], J.axis[2]);
+  M3 Rli;
+  V3 pli;
+  const bool rot_id = (J.flags & JF_ROT_IDENTITY) != 0;
+  switch (J.kind) {
+    case JK_PRISMATIC: {
+      double d = ldv(q, e, J.qcol);
+      Rli = Rpl;
+      pli = rot_id ? axpy(d, ax, ppl) : mul_add(Rpl, d * ax, ppl);
+      break;
+    }
+    case JK_FREEFLYER: {
+      const int c0 = J.qcol;
+      V3 t = mk(ldv(q, e, c0), ldv(q, e, c0 + 1), ldv(q, e, c0 + 2));
+      M3 RJ = quat_to_R(ldv(q, e, c0 + 3), ldv(q, e, c0 + 4), ldv(q, e, c0 + 5), ldv(q, e, c0 + 6));
+      Rli = rot_id ? RJ : mul(Rpl, RJ);
+      pli = rot_id ? (t + ppl) : mul_add(Rpl, t, ppl);
+      break;
+    }
+    default: {  // revolute and continuous: rotation about the axis
+      double s, c;
+      sincos(ldv(q, e, J.qcol), &s, &c);
+      M3 RJ = rodrigues(ax, s, c);
+      Rli = rot_id ? RJ : mul(Rpl, RJ);
+      pli = ppl;
+      break;
+    }
+  }
+  const int p = J.parent;
+  if (p == 0) {
+    Ro = Rli;
+    po = pli;
+  } else {
+    Ro = mul(oR[p], Rli);
+    po = mul_add(oR[p], pli, op[p]);
+  }
+}
+
+// World-frame motion subspace column k of joint J (pose Ro, po).
+__device__ __forceinline__ Mot world_S(const DJoint& J, const M3& Ro, V3 po, int k) {
+  Mot S;
+  if (J.kind == JK_FREEFLYER) {
+    V3 r = mk(Ro.a[k % 3], Ro.a[3 + k % 3], Ro.a[6 + k % 3]);  // column of Ro
+    if (k < 3) {
+      S.v = r;
+      S.w = mk(0, 0, 0);
+    } else {
+      S.v = cross(po, r);
+      S.w = r;
+    }
+  } else if (J.kind == JK_PRISMATIC) {
+    S.v = mul(Ro, mk(J.axis[0], J.axis[1], J.axis[2]));
+    S.w = mk(0, 0, 0);
+  } else {
+    S.w = mul(Ro, mk(J.axis[0], J.axis[1], J.axis[2]));
+    S.v = cross(po, S.w);
+  }
+  return S;
+}
+
+// Cholesky of a packed symmetric 6x6 (row-major lower triangle, 21 entries) in place.
+__device__ __forceinline__ void chol6(double* L) {
+  // index of (r, c), c <= r
+#define LI(r, c) ((r) * ((r) + 1) / 2 + (c))
+  for (int j = 0; j < 6; j++) {
+    double d = L[LI(j, j)];
+    for (int k = 0; k < j; k++) d = fma(-L[LI(j, k)], L[LI(j, k)], d);
+    d = sqrt(d);
+    L[LI(j, j)] = d;
+    double inv = 1.0 / d;
+    for (int i = j + 1; i < 6; i++) {
+      double s = L[LI(i, j)];
+      for (int k = 0; k < j; k++) s = fma(-L[LI(i, k)], L[LI(j, k)], s);
+      L[LI(i, j)] = s * inv;
+    }
+  }
+}
+__device__ __forceinline__ void chol6_solve(const double* L, double* b) {
+  for (int i = 0; i < 6; i++) {
+    double s = b[i];
+    for (int k = 0; k < i; k++) s = fma(-L[LI(i, k)], b[k], s);
+    b[i] = s / L[LI(i, i)];
+  }
+  for (int i = 5; i >= 0; i--) {
+    double s = b[i];
+    for (int k = i + 1; k < 6; k++) s = fma(-L[LI(k, i)], b[k], s);
+    b[i] = s / L[LI(i, i)];
+  }
+#undef LI
+}
+
+template <int MAXJ, int OPS>
+__global__ void __launch_bounds__(32) step_kernel(const DModel* __restrict__ model, const StepArgs args) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= args.n) return;
+  constexpr int MAXV = MAXJ + 5;
+  constexpr bool kFK = OPS & OP_FK, kJAC = OPS & OP_JAC, kCRBA = OPS & OP_CRBA, kRNEA = OPS & OP_RNEA,
+                 kABA = OPS & OP_ABA;
+  constexpr bool kVel = kRNEA || kABA;
+  constexpr bool kInertia = kCRBA || kRNEA || kABA;
+  const int nj = model->nj;
+  const DJoint* __restrict__ JT = model_joints(model);
+
+  M3 oR[MAXJ];
+  V3 op[MAXJ];
+  Mot Sw[MAXV];
+  Mot vel[kVel ? MAXJ : 1];
+  Mot acc[(kRNEA || kABA) ? MAXJ : 1];
+  Mot frc[kRNEA ? MAXJ : 1];
+  RBI Ic[kCRBA ? MAXJ : 1];
+  Sym6 IA[kABA ? MAXJ : 1];
+  Mot pA[kABA ? MAXJ : 1], cb[kABA ? MAXJ : 1], Uv[kABA ? MAXV : 1];
+  double uv[kABA ? MAXV : 1], Dinv[kABA ? MAXJ : 1];
+  double Lff[kABA ? 21 : 1];  // Cholesky factor of D for the (single) free-flyer joint
+
+  const Mot a0{mk(-model->gravity[0], -model->gravity[1], -model->gravity[2]), mk(0, 0, 0)};
+
+  if constexpr (kCRBA) {
+    const int nv = model->nv;
+    for (int r = 0; r < nv; r++)
+      for (int c = 0; c < nv; c++) stv(args.M, e, r * nv + c, 0.0);
+  }
+
+  // ---------------- pass 1: root to leaves ----------------
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = JT[i];
+    const int p = J.parent;
+    M3 Ro;
+    V3 po;
+    joint_world_pose(J, args.q, e, oR, op, Ro, po);
+    oR[i] = Ro;
+    op[i] = po;
+    const int nvi = J.nv, iv = J.ivx, vc = J.vcol;
+    for (int k = 0; k < nvi; k++) Sw[iv + k] = world_S(J, Ro, po, k);
+    if constexpr (kJAC) {
+      const int nv = model->nv;
+      for (int k = 0; k < nvi; k++) {
+        const Mot S = Sw[iv + k];
+        stv(args.J, e, 0 * nv + vc + k, S.v.x);
+        stv(args.J, e, 1 * nv + vc + k, S.v.y);
+        stv(args.J, e, 2 * nv + vc + k, S.v.z);
+        stv(args.J, e, 3 * nv + vc + k, S.w.x);
+        stv(args.J, e, 4 * nv + vc + k, S.w.y);
+        stv(args.J, e, 5 * nv + vc + k, S.w.z);
+      }
+    }
+    if constexpr (kInertia) {
+      RBI Yl;
+      Yl.m = J.m;
+      Yl.h = mk(J.h[0], J.h[1], J.h[2]);
+#pragma unroll
+      for (int k = 0; k < 6; k++) Yl.I[k] = J.I[k];
+      const RBI Y = rbi_transport(Yl, Ro, po);
+      if constexpr (kCRBA) Ic[i] = Y;
+      if constexpr (kVel) {
+        Mot vJ{mk(0, 0, 0), mk(0, 0, 0)};
+        for (int k = 0; k < nvi; k++) vJ = axpy6(ldv(args.qd, e, vc + k), Sw[iv + k], vJ);
+        const Mot v = (p == 0) ? vJ : add6(vel[p], vJ);
+        vel[i] = v;
+        const Mot hY = rbi_mul(Y, v);  // momentum I v
+        const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+        const Mot bias = add_crossf(zero, v, hY);  // v x* I v
+        if constexpr (kRNEA) {
+          Mot a = (p == 0) ? a0 : acc[p];
+          for (int k = 0; k < nvi; k++) a = axpy6(ldv(args.qdd, e, vc + k), Sw[iv + k], a);
+          a = add_crossm(a, v, vJ);
+          acc[i] = a;
+          frc[i] = rbi_mul_add(Y, a, bias);
+        }
+        if constexpr (kABA) {
+          cb[i] = add_crossm(zero, v, vJ);
+          IA[i] = sym6_from_rbi(Y);
+          pA[i] = bias;
+        }
+      }
+    }
+  }
+
+  if constexpr (kFK) {
+    const DLink* __restrict__ LT = model_links(model);
+    const int nl = model->nlinks;
+    for (int l = 0; l < nl; l++) {
+      const DLink& L = LT[l];
+      const int j = L.joint;
+      M3 R;
+      V3 pp;
+      M3 Rl;
+#pragma unroll
+      for (int k = 0; k < 9; k++) Rl.a[k] = L.R[k];
+      const V3 pl = mk(L.p[0], L.p[1], L.p[2]);
+      if (j == 0) {
+        R = Rl;
+        pp = pl;
+      } else {
+        R = (L.flags & JF_ROT_IDENTITY) ? oR[j] : mul(oR[j], Rl);
+        pp = mul_add(oR[j], pl, op[j]);
+      }
+      double qt[4];
+      R_to_quat(R, qt);
+      stv(args.poses, e, l * 7 + 0, pp.x);
+      stv(args.poses, e, l * 7 + 1, pp.y);
+      stv(args.poses, e, l * 7 + 2, pp.z);
+      stv(args.poses, e, l * 7 + 3, qt[0]);
+      stv(args.poses, e, l * 7 + 4, qt[1]);
+      stv(args.poses, e, l * 7 + 5, qt[2]);
+      stv(args.poses, e, l * 7 + 6, qt[3]);
+    }
+  }
+
+  if constexpr (kCRBA || kRNEA || kABA) {
+    // ---------------- pass 2: leaves to root ----------------
+    for (int i = nj - 1; i >= 1; i--) {
+      const DJoint& J = JT[i];
+      const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
+      if constexpr (kRNEA) {
+        const Mot f = frc[i];
+        for (int k = 0; k < nvi; k++) stv(args.tau_out, e, vc + k, dot6(Sw[iv + k], f));
+        if (p > 0) frc[p] = add6(frc[p], f);
+      }
+      if constexpr (kCRBA) {
+        const int nv = model->nv;
+        const RBI Y = Ic[i];
+        for (int k = 0; k < nvi; k++) {
+          const Mot F = rbi_mul(Y, Sw[iv + k]);
+          for (int l = 0; l <= k; l++) {  // own block, upper triangle mirrored
+            const double m = dot6(Sw[iv + l], F);
+            stv(args.M, e, (vc + l) * nv + vc + k, m);
+            stv(args.M, e, (vc + k) * nv + vc + l, m);
+          }
+          for (int j = p; j > 0; j = JT[j].parent) {
+            const int jv = JT[j].ivx, jc = JT[j].vcol, nvj = JT[j].nv;
+            for (int l = 0; l < nvj; l++) {
+              const double m = dot6(Sw[jv + l], F);
+              stv(args.M, e, (jc + l) * nv + vc + k, m);
+              stv(args.M, e, (vc + k) * nv + jc + l, m);
+            }
+          }
+        }
+        if (p > 0) {
+          RBI& P = Ic[p];
+          P.m += Y.m;
+          P.h = P.h + Y.h;
+#pragma unroll
+          for (int k = 0; k < 6; k++) P.I[k] += Y.I[k];
+        }
+      }
+      if constexpr (kABA) {
+        if (nvi == 1) {
+          const Mot S = Sw[iv];
+          const Mot U = sym6_mul(IA[i], S);
+          const double D = dot6(S, U);
+          const double di = 1.0 / D;
+          const double u = ldv(args.tau, e, vc) - dot6(S, pA[i]);
+          Uv[iv] = U;
+          uv[iv] = u;
+          Dinv[i] = di;
+          if (p > 0) {
+            const Mot Ud = scale6(di, U);
+            Sym6 Ia = IA[i];
+            const double ud[6] = {Ud.v.x, Ud.v.y, Ud.v.z, Ud.w.x, Ud.w.y, Ud.w.z};
+            const double uu[6] = {U.v.x, U.v.y, U.v.z, U.w.x, U.w.y, U.w.z};
+            // A -= ud_lin u_lin^T (sym), B -= ud_lin u_ang^T, C -= ud_ang u_ang^T (sym)
+            int t = 0;
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+              for (int c = r; c < 3; c++, t++) {
+                Ia.A[t] = fma(-ud[r], uu[c], Ia.A[t]);
+                Ia.C[t] = fma(-ud[3 + r], uu[3 + c], Ia.C[t]);
+              }
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+              for (int c = 0; c < 3; c++) Ia.B[r * 3 + c] = fma(-ud[r], uu[3 + c], Ia.B[r * 3 + c]);
+            Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
+            pa = axpy6(u, Ud, pa);
+            Sym6& P = IA[p];
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+              P.A[k] += Ia.A[k];
+              P.C[k] += Ia.C[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 9; k++) P.B[k] += Ia.B[k];
+            pA[p] = add6(pA[p], pa);
+          }
+        } else {
+          // free flyer: 6x6 D = S^T IA S, Cholesky-factored
+          for (int k = 0; k < 6; k++) {
+            Uv[iv + k] = sym6_mul(IA[i], Sw[iv + k]);
+            uv[iv + k] = ldv(args.tau, e, vc + k) - dot6(Sw[iv + k], pA[i]);
+          }
+          for (int r = 0; r < 6; r++)
+            for (int c = 0; c <= r; c++) Lff[r * (r + 1) / 2 + c] = dot6(Sw[iv + r], Uv[iv + c]);
+          chol6(Lff);
+          if (p > 0) {
+            // Ia = IA - U D^-1 U^T ; pa = pA + Ia c + U D^-1 u, with D^-1 applied by solves
+            Sym6 Ia = IA[i];
+            double W[6][6];  // W[:, k] = D^-1 e_k
+            for (int k = 0; k < 6; k++) {
+              for (int r = 0; r < 6; r++) W[r][k] = (r == k) ? 1.0 : 0.0;
+              double col[6];
+              for (int r = 0; r < 6; r++) col[r] = W[r][k];
+              chol6_solve(Lff, col);
+              for (int r = 0; r < 6; r++) W[r][k] = col[r];
+            }
+            Mot UD[6];
+            for (int k = 0; k < 6; k++) {
+              Mot s{mk(0, 0, 0), mk(0, 0, 0)};
+              for (int l = 0; l < 6; l++) s = axpy6(W[l][k], Uv[iv + l], s);
+              UD[k] = s;
+            }
+            for (int k = 0; k < 6; k++) {
+              const Mot a = UD[k], b = Uv[iv + k];
+              const double ud[6] = {a.v.x, a.v.y, a.v.z, a.w.x, a.w.y, a.w.z};
+              const double uu[6] = {b.v.x, b.v.y, b.v.z, b.w.x, b.w.y, b.w.z};
+              int t = 0;
+              for (int r = 0; r < 3; r++)
+                for (int c = r; c < 3; c++, t++) {
+                  Ia.A[t] = fma(-ud[r], uu[c], Ia.A[t]);
+                  Ia.C[t] = fma(-ud[3 + r], uu[3 + c], Ia.C[t]);
+                }
+              for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) Ia.B[r * 3 + c] = fma(-ud[r], uu[3 + c], Ia.B[r * 3 + c]);
+            }
+            Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
+            for (int k = 0; k < 6; k++) pa = axpy6(uv[iv + k], UD[k], pa);
+            Sym6& P = IA[p];
+            for (int k = 0; k < 6; k++) {
+              P.A[k] += Ia.A[k];
+              P.C[k] += Ia.C[k];
+            }
+            for (int k = 0; k < 9; k++) P.B[k] += Ia.B[k];
+            pA[p] = add6(pA[p], pa);
+          }
+        }
+      }
+    }
+  }
+
+  if constexpr (kABA) {
+    // ---------------- pass 3: root to leaves ----------------
+    for (int i = 1; i < nj; i++) {
+      const DJoint& J = JT[i];
+      const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
+      Mot a = add6((p == 0) ? a0 : acc[p], cb[i]);
+      if (nvi == 1) {
+        const double qdd = Dinv[i] * (uv[iv] - dot6(Uv[iv], a));
+        a = axpy6(qdd, Sw[iv], a);
+        stv(args.qdd_out, e, vc, qdd);
+      } else {
+        double b[6];
+        for (int k = 0; k < 6; k++) b[k] = uv[iv + k] - dot6(Uv[iv + k], a);
+        chol6_solve(Lff, b);
+        for (int k = 0; k < 6; k++) {
+          a = axpy6(b[k], Sw[iv + k], a);
+          stv(args.qdd_out, e, vc + k, b[k]);
+        }
+      }
+      acc[i] = a;
+    }
+  }
+}
+
+}  // namespace sgdyn

@@ -1,0 +1,423 @@
+"""Drop-in ``PinocchioModel`` backed by GB300 kernels, plus batched tensor overloads.
+
+Mirrors the reference's pybind surface (pinocchio/pinocchio_model.cpp:306-367): method
+names, argument names, defaults, return types and exception types. Every compute call
+runs on the GPU through the C ABI of libsgdyn.so; single-instance calls are batches of
+one. The ``*_batched`` methods are the additions: they take float64 CUDA tensors of
+shape [N, ...] and return tensors on the same device, enqueued on the current torch
+stream of that device.
+
+Behaviour kept from the reference:
+* the joint order must be set (``set_joint_order``) before any compute call, else
+  ``RuntimeError("posS2P failed")`` (pinocchio_model.cpp:49-72, 70);
+* bad joint / link names raise ``ValueError`` (std::invalid_argument, :105, :121, :136);
+* bad link indices raise ``RuntimeError("link index out of bound")`` (:151, :168, :189, :233);
+* ``get_link_pose`` returns a float32 Pose (p, q = w x y z) from the last
+  ``compute_forward_kinematics`` (:150-161);
+* ``get_link_jacobian(local=True)`` is the link (body) frame Jacobian, as the code does,
+  although the reference docstring states the opposite (:355-362 vs :181-183);
+* ``compute_inverse_kinematics`` follows the C++ CLIK loop (:228-300): best iterate,
+  ``eps`` early exit, ``max_iterations`` updates, returns (q, success, err6).
+Differences: ``get_link_pose`` / ``get_link_jacobian`` before the matching compute call
+raise ``RuntimeError`` instead of reading stale Pinocchio data; ``get_link_jacobian`` uses
+the configuration of the last ``compute_full_jacobian`` even if other calls followed.
+Floating (free-flyer) joints, which the reference rejects in posS2P, are accepted: their
+q block is (x y z qx qy qz qw) and their velocity block the 6-D body twist.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+KIND_REVOLUTE, KIND_PRISMATIC, KIND_CONTINUOUS, KIND_FREEFLYER = 1, 2, 3, 4
+
+
+class Pose:
+    """Stand-in for ``sapien.Pose``: float32 position ``p`` and quaternion ``q`` (w, x, y, z)."""
+
+    def __init__(self, p=(0.0, 0.0, 0.0), q=(1.0, 0.0, 0.0, 0.0)):
+        self.p = np.asarray(p, dtype=np.float32).reshape(3)
+        self.q = np.asarray(q, dtype=np.float32).reshape(4)
+
+    def to_transformation_matrix(self):
+        w, x, y, z = (float(v) for v in self.q)
+        T = np.eye(4)
+        T[:3, :3] = [
+            [1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+            [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+            [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)],
+        ]
+        T[:3, 3] = self.p
+        return T
+
+    def __repr__(self):
+        return f"Pose([{', '.join(f'{v:g}' for v in self.p)}], [{', '.join(f'{v:g}' for v in self.q)}])"
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class PinocchioModel:
+    """GPU-backed replacement of ``sapien.pysapien_pinocchio.PinocchioModel``."""
+
+    def __init__(self, urdf, gravity=(0.0, 0.0, -9.81)):
+        L = N.load()
+        g = (ctypes.c_double * 3)(*[float(x) for x in gravity])
+        h = ctypes.c_void_p()
+        N.check(L.sgdyn_model_from_urdf(urdf.encode(), g, ctypes.byref(h)))
+        self._h = h
+        self._joint_order_set = False
+        self._link_order_set = False
+        self._fk_cache = None
+        self._jac_q = None
+        self._device = None
+        self._refresh()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                N.load().sgdyn_model_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ---- model information ---------------------------------------------
+    def _refresh(self):
+        L = N.load()
+        nq, nv, nl, nj = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        N.check(L.sgdyn_model_info(self._h, ctypes.byref(nq), ctypes.byref(nv), ctypes.byref(nl), ctypes.byref(nj)))
+        self.nq_ext, self.nv, self._nlinks, self.njoints = nq.value, nv.value, nl.value, nj.value
+        kinds = []
+        for k in range(self.njoints - 1):
+            kk = ctypes.c_int()
+            N.check(L.sgdyn_model_joint_kind(self._h, k, ctypes.byref(kk)))
+            kinds.append(kk.value)
+        self._kinds = kinds
+        self._uploaded = set()
+
+    @property
+    def joint_names(self):
+        """Moving joints in tree (depth-first) order."""
+        L = N.load()
+        out = []
+        for j in range(1, self.njoints):
+            s = ctypes.c_char_p()
+            N.check(L.sgdyn_model_joint_name(self._h, j, ctypes.byref(s)))
+            out.append(s.value.decode())
+        return out
+
+    @property
+    def link_names(self):
+        """All URDF links (BODY frames) in tree order."""
+        L = N.load()
+        nb = ctypes.c_int()
+        N.check(L.sgdyn_model_body_count(self._h, ctypes.byref(nb)))
+        out = []
+        for b in range(nb.value):
+            s = ctypes.c_char_p()
+            N.check(L.sgdyn_model_body_name(self._h, b, ctypes.byref(s)))
+            out.append(s.value.decode())
+        return out
+
+    @property
+    def nlinks(self):
+        return self._nlinks if self._link_order_set else 0
+
+    def table_bytes(self):
+        """Host copy of the packed kernel tables (see csrc/device_model.h)."""
+        L = N.load()
+        p, n = ctypes.c_void_p(), ctypes.c_int64()
+        N.check(L.sgdyn_model_table(self._h, ctypes.byref(p), ctypes.byref(n)))
+        return ctypes.string_at(p, n.value)
+
+    # ---- orders ----------------------------------------------------------
+    @staticmethod
+    def _names(names):
+        arr = (ctypes.c_char_p * len(names))(*[str(n).encode() for n in names])
+        return arr, len(names)
+
+    def set_joint_order(self, names):
+        arr, n = self._names(list(names))
+        N.check(N.load().sgdyn_model_set_joint_order(self._h, arr, n))
+        self._joint_order_set = True
+        self._refresh()
+
+    def set_link_order(self, names):
+        arr, n = self._names(list(names))
+        N.check(N.load().sgdyn_model_set_link_order(self._h, arr, n))
+        self._link_order_set = True
+        self._fk_cache = None
+        self._refresh()
+
+    # ---- plumbing ----------------------------------------------------------
+    def _require_order(self):
+        if not self._joint_order_set and self.nv > 0:
+            raise RuntimeError("posS2P failed")
+
+    def _check_link(self, link_index):
+        if not (0 <= int(link_index) < self.nlinks):
+            raise RuntimeError("link index out of bound")
+
+    def _dev(self):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError("sapien_gb300 needs a CUDA device for compute calls")
+        if self._device is None:
+            self._device = torch.device("cuda", torch.cuda.current_device())
+        return self._device
+
+    def _prepare(self, device):
+        torch = _torch()
+        key = device.index
+        if key not in self._uploaded:
+            with torch.cuda.device(device):
+                N.check(N.load().sgdyn_model_upload(self._h))
+            self._uploaded.add(key)
+
+    def _vec(self, x, n, what):
+        a = np.asarray(x, dtype=np.float64).reshape(-1)
+        if a.size != n:
+            raise RuntimeError(f"{what} has size {a.size}, expected {n}" if what != "qpos" else "posS2P failed")
+        return a
+
+    def _single(self, *arrays):
+        torch = _torch()
+        dev = self._dev()
+        return [torch.from_numpy(a.reshape(1, -1)).to(dev) for a in arrays]
+
+    def _check_batch(self, t, cols, what):
+        torch = _torch()
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{what} must be a torch.Tensor")
+        if t.dtype != torch.float64 or not t.is_cuda:
+            raise TypeError(f"{what} must be a float64 CUDA tensor")
+        if t.dim() != 2 or t.shape[1] != cols:
+            raise RuntimeError(f"{what} must have shape [N, {cols}], got {tuple(t.shape)}")
+        return t.contiguous()
+
+    def _stream(self, device):
+        return ctypes.c_void_p(_torch().cuda.current_stream(device).cuda_stream)
+
+    # ---- batched overloads (additions) -------------------------------------
+    def step_batched(self, qpos, qvel=None, qacc=None, qf=None, ops=N.OP_ALL):
+        """Fused sweep: any subset of FK poses, WORLD Jacobian, mass matrix, inverse and forward
+        dynamics on one batch. Returns a dict with keys among
+        'link_poses' [N, nlinks, 7], 'jacobian' [N, 6, nv], 'mass_matrix' [N, nv, nv],
+        'qf' (RNEA torques) [N, nv], 'qacc' (ABA accelerations) [N, nv]."""
+        torch = _torch()
+        self._require_order()
+        q = self._check_batch(qpos, self.nq_ext, "qpos")
+        n = q.shape[0]
+        dev = q.device
+        qd = self._check_batch(qvel, self.nv, "qvel") if ops & (N.OP_INVERSE_DYNAMICS | N.OP_FORWARD_DYNAMICS) else None
+        qdd = self._check_batch(qacc, self.nv, "qacc") if ops & N.OP_INVERSE_DYNAMICS else None
+        tau = self._check_batch(qf, self.nv, "qf") if ops & N.OP_FORWARD_DYNAMICS else None
+        if ops & N.OP_FK and not self._link_order_set:
+            raise RuntimeError("link index out of bound")
+        out = {}
+        e = lambda *s: torch.empty(*s, dtype=torch.float64, device=dev)  # noqa: E731
+        poses = e(n, self._nlinks, 7) if ops & N.OP_FK else None
+        J = e(n, 6, self.nv) if ops & N.OP_JACOBIAN else None
+        M = e(n, self.nv, self.nv) if ops & N.OP_MASS_MATRIX else None
+        tau_o = e(n, self.nv) if ops & N.OP_INVERSE_DYNAMICS else None
+        qdd_o = e(n, self.nv) if ops & N.OP_FORWARD_DYNAMICS else None
+        self._prepare(dev)
+        with torch.cuda.device(dev):
+            N.check(N.load().sgdyn_step(self._h, n, int(ops), _ptr(q), _ptr(qd), _ptr(qdd), _ptr(tau), _ptr(poses),
+                                        _ptr(J), _ptr(M), _ptr(tau_o), _ptr(qdd_o), N.ENV_MAJOR, self._stream(dev)))
+        for k, v in (("link_poses", poses), ("jacobian", J), ("mass_matrix", M), ("qf", tau_o), ("qacc", qdd_o)):
+            if v is not None:
+                out[k] = v
+        return out
+
+    def compute_forward_kinematics_batched(self, qpos):
+        """[N, nq] -> FP64 link poses [N, nlinks, 7] = (x y z qw qx qy qz)."""
+        return self.step_batched(qpos, ops=N.OP_FK)["link_poses"]
+
+    def compute_full_jacobian_batched(self, qpos):
+        """[N, nq] -> WORLD Jacobian [N, 6, nv] (rows vx vy vz wx wy wz)."""
+        return self.step_batched(qpos, ops=N.OP_JACOBIAN)["jacobian"]
+
+    def compute_generalized_mass_matrix_batched(self, qpos):
+        return self.step_batched(qpos, ops=N.OP_MASS_MATRIX)["mass_matrix"]
+
+    def compute_inverse_dynamics_batched(self, qpos, qvel, qacc):
+        return self.step_batched(qpos, qvel, qacc, ops=N.OP_INVERSE_DYNAMICS)["qf"]
+
+    def compute_forward_dynamics_batched(self, qpos, qvel, qf):
+        return self.step_batched(qpos, qvel, qf=qf, ops=N.OP_FORWARD_DYNAMICS)["qacc"]
+
+    def _batched_matrix_op(self, fn, qpos, extra, cols):
+        torch = _torch()
+        self._require_order()
+        q = self._check_batch(qpos, self.nq_ext, "qpos")
+        dev = q.device
+        out = torch.empty(q.shape[0], cols, dtype=torch.float64, device=dev)
+        self._prepare(dev)
+        with torch.cuda.device(dev):
+            N.check(fn(q, out, dev))
+        return out
+
+    def compute_link_jacobian_batched(self, qpos, link_index, local=False):
+        """[N, nq] -> Jacobian of one link [N, 6, nv] (WORLD, or the link frame if local)."""
+        self._check_link(link_index)
+        L = N.load()
+        out = self._batched_matrix_op(
+            lambda q, o, d: L.sgdyn_compute_link_jacobian(self._h, q.shape[0], int(link_index), int(bool(local)),
+                                                          _ptr(q), _ptr(o), N.ENV_MAJOR, self._stream(d)),
+            qpos, None, 6 * self.nv)
+        return out.view(-1, 6, self.nv)
+
+    def compute_single_link_local_jacobian_batched(self, qpos, link_index):
+        self._check_link(link_index)
+        L = N.load()
+        out = self._batched_matrix_op(
+            lambda q, o, d: L.sgdyn_compute_single_link_local_jacobian(self._h, q.shape[0], int(link_index), _ptr(q),
+                                                                       _ptr(o), N.ENV_MAJOR, self._stream(d)),
+            qpos, None, 6 * self.nv)
+        return out.view(-1, 6, self.nv)
+
+    def compute_coriolis_matrix_batched(self, qpos, qvel):
+        L = N.load()
+        qd = self._check_batch(qvel, self.nv, "qvel")
+        out = self._batched_matrix_op(
+            lambda q, o, d: L.sgdyn_compute_coriolis_matrix(self._h, q.shape[0], _ptr(q), _ptr(qd), _ptr(o),
+                                                            N.ENV_MAJOR, self._stream(d)),
+            qpos, None, self.nv * self.nv)
+        return out.view(-1, self.nv, self.nv)
+
+    def compute_inverse_kinematics_batched(self, link_index, target_poses, initial_qpos=None, active_qmask=None,
+                                           eps=1e-4, max_iterations=1000, dt=0.1, damp=1e-6):
+        """Batched CLIK. target_poses [N, 7] = (x y z qw qx qy qz) FP64 CUDA. Returns
+        (q [N, nq], success [N] bool, err [N, 6])."""
+        torch = _torch()
+        self._require_order()
+        self._check_link(link_index)
+        tgt = self._check_batch(target_poses, 7, "target_poses")
+        n = tgt.shape[0]
+        dev = tgt.device
+        q0 = self._check_batch(initial_qpos, self.nq_ext, "initial_qpos") if initial_qpos is not None else None
+        mask = None
+        if active_qmask is not None and len(active_qmask):
+            mask = torch.as_tensor(np.asarray(active_qmask, dtype=np.int32).reshape(-1), device=dev)
+            if mask.numel() != self.nv:
+                raise RuntimeError(f"active_qmask must have {self.nv} entries")
+        q = torch.empty(n, self.nq_ext, dtype=torch.float64, device=dev)
+        ok = torch.empty(n, dtype=torch.int32, device=dev)
+        err = torch.empty(n, 6, dtype=torch.float64, device=dev)
+        self._prepare(dev)
+        with torch.cuda.device(dev):
+            N.check(N.load().sgdyn_compute_inverse_kinematics(
+                self._h, n, int(link_index), _ptr(tgt), _ptr(q0), _ptr(mask), float(eps), int(max_iterations),
+                float(dt), float(damp), _ptr(q), _ptr(ok), _ptr(err), N.ENV_MAJOR, self._stream(dev)))
+        return q, ok.bool(), err
+
+    # ---- reference single-instance API -----------------------------------
+    def compute_forward_kinematics(self, qpos):
+        """Compute and cache forward kinematics. After computation, use get_link_pose to
+        retrieve the computed pose for a specific link."""
+        self._require_order()
+        (q,) = self._single(self._vec(qpos, self.nq_ext, "qpos"))
+        if self._link_order_set and self._nlinks > 0:
+            self._fk_cache = self.compute_forward_kinematics_batched(q)[0].cpu().numpy()
+        else:
+            self._fk_cache = np.zeros((0, 7))
+
+    def get_link_pose(self, link_index):
+        """Given link index, get link pose (in articulation base frame) from forward
+        kinematics. Must be called after compute_forward_kinematics."""
+        self._check_link(link_index)
+        if self._fk_cache is None:
+            raise RuntimeError("compute_forward_kinematics must be called before get_link_pose")
+        r = self._fk_cache[int(link_index)]
+        return Pose(r[:3], r[3:7])
+
+    def compute_full_jacobian(self, qpos):
+        """Compute and cache Jacobian for all links"""
+        self._require_order()
+        self._jac_q = self._vec(qpos, self.nq_ext, "qpos").copy()
+
+    def get_link_jacobian(self, link_index, local=False):
+        """Given link index, get the Jacobian. Must be called after compute_full_jacobian.
+
+        Args:
+          link_index: index of the link
+          local: True for the link (body) frame; False for the world (spatial) frame
+        """
+        self._check_link(link_index)
+        if self._jac_q is None:
+            raise RuntimeError("compute_full_jacobian must be called before get_link_jacobian")
+        (q,) = self._single(self._jac_q)
+        return self.compute_link_jacobian_batched(q, link_index, local)[0].cpu().numpy()
+
+    def compute_single_link_local_jacobian(self, qpos, link_index):
+        """Compute the link(body) Jacobian for a single link. It is faster than
+        compute_full_jacobian followed by get_link_jacobian"""
+        self._require_order()
+        self._check_link(link_index)
+        (q,) = self._single(self._vec(qpos, self.nq_ext, "qpos"))
+        return self.compute_single_link_local_jacobian_batched(q, link_index)[0].cpu().numpy()
+
+    def compute_generalized_mass_matrix(self, qpos):
+        self._require_order()
+        (q,) = self._single(self._vec(qpos, self.nq_ext, "qpos"))
+        return self.compute_generalized_mass_matrix_batched(q)[0].cpu().numpy()
+
+    def compute_coriolis_matrix(self, qpos, qvel):
+        self._require_order()
+        q, qd = self._single(self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"))
+        return self.compute_coriolis_matrix_batched(q, qd)[0].cpu().numpy()
+
+    def compute_inverse_dynamics(self, qpos, qvel, qacc):
+        self._require_order()
+        q, qd, qdd = self._single(self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
+                                  self._vec(qacc, self.nv, "qacc"))
+        return self.compute_inverse_dynamics_batched(q, qd, qdd)[0].cpu().numpy()
+
+    def compute_forward_dynamics(self, qpos, qvel, qf):
+        self._require_order()
+        q, qd, tau = self._single(self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
+                                  self._vec(qf, self.nv, "qf"))
+        return self.compute_forward_dynamics_batched(q, qd, tau)[0].cpu().numpy()
+
+    def compute_inverse_kinematics(self, link_index, pose, initial_qpos=(), active_qmask=(), eps=1e-4,
+                                   max_iterations=1000, dt=0.1, damp=1e-6):
+        """Compute inverse kinematics with CLIK algorithm.
+
+        Args:
+            link_index: index of the link
+            pose: target pose of the link in articulation base frame
+            initial_qpos: initial qpos to start CLIK
+            active_qmask: dof sized integer array, 1 to indicate active joints and 0 for inactive joints, default to all 1s
+            max_iterations: number of iterations steps
+            dt: iteration step "speed"
+            damp: iteration step "damping"
+        Returns:
+            result: qpos from IK
+            success: whether IK is successful
+            error: se3 norm error
+        """
+        self._require_order()
+        self._check_link(link_index)
+        torch = _torch()
+        dev = self._dev()
+        p = np.asarray(pose.p, dtype=np.float32).astype(np.float64)
+        qq = np.asarray(pose.q, dtype=np.float32).astype(np.float64)
+        tgt = torch.from_numpy(np.concatenate([p, qq]).reshape(1, 7)).to(dev)
+        q0 = None
+        if initial_qpos is not None and len(initial_qpos):
+            (q0,) = self._single(self._vec(initial_qpos, self.nq_ext, "qpos"))
+        mask = active_qmask if active_qmask is not None and len(active_qmask) else None
+        q, ok, err = self.compute_inverse_kinematics_batched(link_index, tgt, q0, mask, eps, max_iterations, dt, damp)
+        return q[0].cpu().numpy(), bool(ok[0].item()), err[0].cpu().numpy()

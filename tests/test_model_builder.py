@@ -1,0 +1,168 @@
+"""Host-side checks that need no GPU: the product's C++ URDF model builder against the
+oracle's independent Python builder, the C-ABI exports, and the reference's error
+behaviour for orders and names."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import urdf_model as um
+from sapien_gb300 import PinocchioModel, synthetic as syn
+from sapien_gb300 import _native as N
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+DJOINT = np.dtype([("R", "<f8", 9), ("p", "<f8", 3), ("axis", "<f8", 3), ("m", "<f8"), ("h", "<f8", 3),
+                   ("I", "<f8", 6), ("parent", "<i4"), ("kind", "<i4"), ("axis_kind", "<i4"), ("flags", "<i4"),
+                   ("qcol", "<i4"), ("vcol", "<i4"), ("nv", "<i4"), ("depth", "<i4"), ("ivx", "<i4"),
+                   ("pad", "<i4", 5)])
+DLINK = np.dtype([("R", "<f8", 9), ("p", "<f8", 3), ("joint", "<i4"), ("flags", "<i4"), ("pad", "<i4", 2)])
+assert DJOINT.itemsize == 256 and DLINK.itemsize == 112
+
+
+def parse_table(raw):
+    hdr = np.frombuffer(raw, dtype="<i4", count=8)
+    nj, nv, nqe, nl = (int(x) for x in hdr[:4])
+    grav = np.frombuffer(raw, dtype="<f8", count=3, offset=32)
+    joints = np.frombuffer(raw, dtype=DJOINT, count=nj, offset=64)
+    links = np.frombuffer(raw, dtype=DLINK, count=nl, offset=64 + 256 * nj)
+    return dict(nj=nj, nv=nv, nq_ext=nqe, nlinks=nl, gravity=grav, joints=joints, links=links)
+
+
+def spatial6(m, h, I):
+    hx = np.array([[0, -h[2], h[1]], [h[2], 0, -h[0]], [-h[1], h[0], 0]])
+    Iw = np.array([[I[0], I[1], I[2]], [I[1], I[3], I[4]], [I[2], I[4], I[5]]])
+    S = np.zeros((6, 6))
+    S[:3, :3] = m * np.eye(3)
+    S[:3, 3:] = -hx
+    S[3:, :3] = hx
+    S[3:, 3:] = Iw
+    return S
+
+
+ROBOTS = {
+    "chain7": lambda: syn.serial_chain(7),
+    "arm9": lambda: syn.arm_with_fingers(),
+    "arm9_sapien": lambda: syn.arm_with_fingers(sapien_style=True),
+    "quadruped18": lambda: syn.quadruped(),
+    "humanoid": lambda: syn.humanoid(),
+    "humanoid_sapien": lambda: syn.humanoid(sapien_style=True),
+    "mixed_chain": lambda: syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                                "continuous", "prismatic"]),
+}
+
+
+def compare_with_oracle_builder(urdf, joint_order, link_order):
+    pm = PinocchioModel(urdf, [0, 0, -9.81])
+    pm.set_joint_order(joint_order)
+    pm.set_link_order(link_order)
+    t = parse_table(pm.table_bytes())
+    om = um.build_model(urdf, (0, 0, -9.81))
+    assert t["nj"] == om.njoints
+    assert t["nv"] == om.nv
+    assert pm.joint_names == om.joint_names[1:]
+    for j in range(1, om.njoints):
+        J = t["joints"][j]
+        assert J["parent"] == om.parent[j]
+        assert J["kind"] == om.jtype[j]
+        R, p = om.placement[j]
+        assert np.abs(J["R"].reshape(3, 3) - R).max() < 1e-15
+        assert np.abs(J["p"] - p).max() < 1e-15
+        if om.jtype[j] != um.JT_FREEFLYER:
+            assert np.abs(J["axis"] - om.axis[j]).max() < 1e-15
+        S = spatial6(J["m"], J["h"], J["I"])
+        assert np.abs(S - om.inertia6[j]).max() < 1e-13 * max(1, np.abs(S).max())
+    # external columns follow the joint order
+    qc, vc = 0, 0
+    for name in joint_order:
+        j = om.joint_names.index(name)
+        J = t["joints"][j]
+        assert J["qcol"] == qc and J["vcol"] == vc
+        qc += 7 if om.jtype[j] == um.JT_FREEFLYER else 1
+        vc += 6 if om.jtype[j] == um.JT_FREEFLYER else 1
+    assert t["nq_ext"] == qc
+    # link frames
+    for li, name in enumerate(link_order):
+        jid, (R, p) = om.body_frames[name]
+        L = t["links"][li]
+        assert L["joint"] == jid
+        assert np.abs(L["R"].reshape(3, 3) - R).max() < 1e-15
+        assert np.abs(L["p"] - p).max() < 1e-15
+
+
+@pytest.mark.parametrize("name", list(ROBOTS))
+def test_builder_matches_oracle_builder(name):
+    r = ROBOTS[name]()
+    compare_with_oracle_builder(r.urdf, r.joint_names, r.link_names)
+
+
+def test_builder_on_reference_assets_when_present():
+    """Panda (7R + 2P) and movo_simple (continuous joints, many fixed joints, nested
+    <transmission> joint tags) from the reference tree, when it is mounted."""
+    paths = ["/root/reference/assets/robot/panda/panda.urdf", "/root/reference/unittest/assets/movo_simple.urdf"]
+    found = [p for p in paths if os.path.exists(p)]
+    if not found:
+        pytest.skip("reference assets not mounted")
+    for path in found:
+        urdf = open(path).read()
+        om = um.build_model(urdf)
+        order = om.joint_names[1:][::-1]  # a non-trivial permutation
+        compare_with_oracle_builder(urdf, order, om.link_names_in_order)
+
+
+def test_library_exports_every_declared_symbol():
+    header = open(os.path.join(ROOT, "include", "sgdyn.h")).read()
+    declared = set(re.findall(r"^\s*(?:int|void|const char\*)\s+(sgdyn_\w+)\s*\(", header, re.M))
+    assert declared == set(N.EXPORTED)
+    L = N.load()
+    for s in declared:
+        assert hasattr(L, s), s
+
+
+def test_reference_error_behaviour():
+    r = syn.arm_with_fingers()
+    pm = PinocchioModel(r.urdf, [0, 0, -9.81])
+    with pytest.raises(RuntimeError, match="posS2P failed"):
+        pm.compute_inverse_dynamics(np.zeros(9), np.zeros(9), np.zeros(9))
+    with pytest.raises(ValueError):
+        pm.set_joint_order(r.joint_names[:-1] + ["no_such_joint"])
+    with pytest.raises(RuntimeError):
+        pm.set_joint_order(r.joint_names[:-1])  # missing DoF
+    with pytest.raises(ValueError):
+        pm.set_link_order(["no_such_link"])
+    pm.set_joint_order(r.joint_names)
+    pm.set_link_order(r.link_names)
+    with pytest.raises(RuntimeError, match="link index out of bound"):
+        pm.get_link_pose(len(r.link_names))
+    with pytest.raises(RuntimeError, match="posS2P failed"):
+        pm.compute_forward_kinematics(np.zeros(8))
+
+
+def test_bad_urdf_is_rejected():
+    with pytest.raises(RuntimeError):
+        PinocchioModel("<robot><link name='a'/>", [0, 0, -9.81])
+    planar = """<robot name="x"><link name="a"/><link name="b"/>
+      <joint name="j" type="planar"><parent link="a"/><child link="b"/></joint></robot>"""
+    with pytest.raises(RuntimeError, match="unsupported joint type"):
+        PinocchioModel(planar, [0, 0, -9.81])
+    two_roots = """<robot name="x"><link name="a"/><link name="b"/></robot>"""
+    with pytest.raises(RuntimeError, match="root"):
+        PinocchioModel(two_roots, [0, 0, -9.81])
+
+
+def test_xml_reader_tolerates_comments_and_entities():
+    urdf = """<?xml version="1.0"?>
+<!-- comment with <joint name="fake"> inside -->
+<robot name="a&amp;b">
+  <link name="base"><!-- c --></link>
+  <link name="l1"><inertial><mass value="1.5"/><inertia ixx="1" iyy="1" izz="1"/></inertial></link>
+  <joint name="j1" type="continuous"><parent link="base"/><child link="l1"/><axis xyz="0 0 1"/>
+    <![CDATA[ ignored <text> ]]>
+  </joint>
+  <transmission name="t"><joint name="j1"/></transmission>
+</robot>"""
+    pm = PinocchioModel(urdf, [0, 0, -9.81])
+    assert pm.joint_names == ["j1"]
+    assert pm.nq_ext == 1 and pm.nv == 1

@@ -1,0 +1,234 @@
+"""Pins the CPU oracle (no GPU): closed forms, dynamics identities, finite differences.
+
+The reference holds no golden vectors for this path (its only test,
+unittest/test_physx/test_articulation.py:75-97, compares against PhysX at run time), so
+the oracle is pinned here by analytic known answers and by identities every correct
+rigid-body dynamics implementation satisfies.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, se3_exp6, se3_jlog6, se3_log6
+from sapien_gb300 import synthetic as syn
+
+
+def _model(robot):
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    return o
+
+
+ROBOTS = {
+    "chain7": lambda: syn.serial_chain(7),
+    "arm9": lambda: syn.arm_with_fingers(),
+    "arm9_sapien": lambda: syn.arm_with_fingers(sapien_style=True),
+    "quadruped18": lambda: syn.quadruped(),
+    "humanoid30": lambda: syn.humanoid(),
+    "mixed_chain": lambda: syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                                "continuous", "prismatic"]),
+}
+
+
+def pendulum_urdf(m, l, Iyy, axis="0 1 0"):
+    return f"""<robot name="p">
+  <link name="base"/>
+  <link name="bob"><inertial><origin xyz="0 0 {-l}" rpy="0 0 0"/><mass value="{m}"/>
+    <inertia ixx="0.01" ixy="0" ixz="0" iyy="{Iyy}" iyz="0" izz="0.01"/></inertial></link>
+  <joint name="j" type="revolute"><origin xyz="0 0 0" rpy="0 0 0"/><axis xyz="{axis}"/>
+    <parent link="base"/><child link="bob"/><limit lower="-3" upper="3" effort="0" velocity="0"/></joint>
+</robot>"""
+
+
+def two_link_urdf(m1, m2, l1, lc1, lc2, I1, I2):
+    return f"""<robot name="two">
+  <link name="base"/>
+  <link name="l1"><inertial><origin xyz="{lc1} 0 0"/><mass value="{m1}"/>
+    <inertia ixx="0.01" ixy="0" ixz="0" iyy="0.01" iyz="0" izz="{I1}"/></inertial></link>
+  <link name="l2"><inertial><origin xyz="{lc2} 0 0"/><mass value="{m2}"/>
+    <inertia ixx="0.01" ixy="0" ixz="0" iyy="0.01" iyz="0" izz="{I2}"/></inertial></link>
+  <joint name="j1" type="revolute"><axis xyz="0 0 1"/><parent link="base"/><child link="l1"/></joint>
+  <joint name="j2" type="revolute"><origin xyz="{l1} 0 0"/><axis xyz="0 0 1"/><parent link="l1"/><child link="l2"/></joint>
+</robot>"""
+
+
+def test_pendulum_closed_form():
+    m, l, Iyy, g = 1.7, 0.6, 0.03, 9.81
+    o = Oracle(pendulum_urdf(m, l, Iyy), (0, 0, -g))
+    o.set_joint_order(["j"])
+    o.set_link_order(["base", "bob"])
+    rng = np.random.default_rng(0)
+    for _ in range(10):
+        th, thd, thdd = rng.uniform(-3, 3), rng.normal(), rng.normal()
+        tau = o.compute_inverse_dynamics([th], [thd], [thdd])[0]
+        expect = (Iyy + m * l * l) * thdd + m * g * l * math.sin(th)
+        assert abs(tau - expect) < 1e-12 * max(1, abs(expect))
+        M = o.compute_generalized_mass_matrix([th])
+        assert abs(M[0, 0] - (Iyy + m * l * l)) < 1e-14
+        a = o.compute_forward_dynamics([th], [thd], [tau])[0]
+        assert abs(a - thdd) < 1e-12
+        # link frame of the bob is the joint frame: rotation about y by th
+        T = o.link_poses([th])[1]
+        Ry = np.array([[math.cos(th), 0, math.sin(th)], [0, 1, 0], [-math.sin(th), 0, math.cos(th)]])
+        assert np.abs(T[:3, :3] - Ry).max() < 1e-15
+
+
+def test_two_link_closed_form():
+    m1, m2, l1, lc1, lc2, I1, I2, g = 1.3, 0.9, 0.5, 0.22, 0.31, 0.021, 0.013, 9.81
+    o = Oracle(two_link_urdf(m1, m2, l1, lc1, lc2, I1, I2), (0, -g, 0))
+    o.set_joint_order(["j1", "j2"])
+    o.set_link_order(["base", "l1", "l2"])
+    rng = np.random.default_rng(1)
+    for _ in range(10):
+        q = rng.uniform(-3, 3, 2)
+        qd = rng.normal(size=2)
+        c2, s2 = math.cos(q[1]), math.sin(q[1])
+        M11 = I1 + I2 + m1 * lc1 ** 2 + m2 * (l1 ** 2 + lc2 ** 2 + 2 * l1 * lc2 * c2)
+        M12 = I2 + m2 * (lc2 ** 2 + l1 * lc2 * c2)
+        M22 = I2 + m2 * lc2 ** 2
+        M = np.array([[M11, M12], [M12, M22]])
+        h = -m2 * l1 * lc2 * s2
+        C = np.array([[h * qd[1], h * (qd[0] + qd[1])], [-h * qd[0], 0.0]])
+        gv = np.array([(m1 * lc1 + m2 * l1) * g * math.cos(q[0]) + m2 * lc2 * g * math.cos(q[0] + q[1]),
+                       m2 * lc2 * g * math.cos(q[0] + q[1])])
+        assert np.abs(o.compute_generalized_mass_matrix(q) - M).max() < 1e-14
+        assert np.abs(o.compute_coriolis_matrix(q, qd) - C).max() < 1e-13
+        assert np.abs(o.compute_inverse_dynamics(q, [0, 0], [0, 0]) - gv).max() < 1e-13
+        qdd = rng.normal(size=2)
+        assert np.abs(o.compute_inverse_dynamics(q, qd, qdd) - (M @ qdd + C @ qd + gv)).max() < 1e-12
+
+
+@pytest.mark.parametrize("name", list(ROBOTS))
+def test_dynamics_identities(name):
+    robot = ROBOTS[name]()
+    o = _model(robot)
+    q, qd, qdd, tau = robot.sample(6, seed=3)
+    nv = robot.nv
+    z = np.zeros(nv)
+    for e in range(len(q)):
+        M = o.compute_generalized_mass_matrix(q[e])
+        assert np.array_equal(M, M.T)
+        assert np.linalg.eigvalsh(M).min() > 0
+        t = o.compute_inverse_dynamics(q[e], qd[e], qdd[e])
+        h = o.compute_inverse_dynamics(q[e], qd[e], z)
+        g = o.compute_inverse_dynamics(q[e], z, z)
+        scale = max(1.0, np.abs(t).max())
+        assert np.abs(M @ qdd[e] + h - t).max() < 1e-12 * scale
+        a = o.compute_forward_dynamics(q[e], qd[e], tau[e])
+        assert np.abs(o.compute_inverse_dynamics(q[e], qd[e], a) - tau[e]).max() < 1e-11 * max(1, np.abs(tau[e]).max())
+        assert np.abs(a - np.linalg.solve(M, tau[e] - h)).max() < 1e-9 * max(1, np.abs(a).max())
+        C = o.compute_coriolis_matrix(q[e], qd[e])
+        assert np.abs(C @ qd[e] - (h - g)).max() < 1e-11 * max(1, np.abs(h - g).max())
+
+
+@pytest.mark.parametrize("name", ["arm9", "humanoid30", "mixed_chain"])
+def test_coriolis_is_christoffel(name):
+    """Mdot = C + C^T (finite differences along qd) and C(q, x) y = C(q, y) x."""
+    robot = ROBOTS[name]()
+    o = _model(robot)
+    q, qd, _, _ = robot.sample(3, seed=5)
+    eps = 1e-6
+    for e in range(len(q)):
+        C = o.compute_coriolis_matrix(q[e], qd[e])
+        Mp = o.compute_generalized_mass_matrix(o.integrate(q[e], eps * qd[e]))
+        Mm = o.compute_generalized_mass_matrix(o.integrate(q[e], -eps * qd[e]))
+        Mdot = (Mp - Mm) / (2 * eps)
+        assert np.abs(Mdot - (C + C.T)).max() < 1e-6 * max(1, np.abs(Mdot).max())
+        if syn.FLOATING in robot.joint_kinds:
+            continue  # a free flyer's velocity is a body twist: no coordinate symmetry
+        x = np.random.default_rng(e).normal(size=robot.nv)
+        Cx = o.compute_coriolis_matrix(q[e], x)
+        assert np.abs(C @ x - Cx @ qd[e]).max() < 1e-10 * max(1, np.abs(C @ x).max())
+
+
+@pytest.mark.parametrize("name", ["arm9", "quadruped18", "mixed_chain"])
+def test_jacobian_matches_fk_differences(name):
+    robot = ROBOTS[name]()
+    o = _model(robot)
+    q, qd, _, _ = robot.sample(3, seed=9)
+    eps = 1e-6
+    for e in range(len(q)):
+        o.compute_full_jacobian(q[e])
+        Tp = o.link_poses(o.integrate(q[e], eps * qd[e]))
+        Tm = o.link_poses(o.integrate(q[e], -eps * qd[e]))
+        T0 = o.link_poses(q[e])
+        for li in range(o.nlinks):
+            J = o.get_link_jacobian(li, local=False)
+            v = J @ qd[e]  # spatial velocity at the world origin
+            pdot = (Tp[li, :3, 3] - Tm[li, :3, 3]) / (2 * eps)
+            Rdot = (Tp[li, :3, :3] - Tm[li, :3, :3]) / (2 * eps)
+            W = Rdot @ T0[li, :3, :3].T
+            w = np.array([W[2, 1], W[0, 2], W[1, 0]])
+            assert np.abs(w - v[3:]).max() < 1e-7
+            assert np.abs(pdot - (v[:3] + np.cross(v[3:], T0[li, :3, 3]))).max() < 1e-7
+            # local Jacobian = actInv(link pose) applied to the world one
+            Jl = o.get_link_jacobian(li, local=True)
+            R, p = T0[li, :3, :3], T0[li, :3, 3]
+            vl = np.concatenate([R.T @ (v[:3] - np.cross(p, v[3:])), R.T @ v[3:]])
+            assert np.abs(Jl @ qd[e] - vl).max() < 1e-12 * max(1, np.abs(vl).max())
+            Js = o.compute_single_link_local_jacobian(q[e], li)
+            assert np.abs(Js - Jl).max() < 1e-12 * max(1, np.abs(Jl).max())
+
+
+@pytest.mark.parametrize("name", ["arm9", "humanoid30"])
+def test_long_double_agrees(name):
+    robot = ROBOTS[name]()
+    o = _model(robot)
+    q, qd, qdd, tau = robot.sample(4, seed=13)
+    d = [o.compute_inverse_dynamics(q[e], qd[e], qdd[e]) for e in range(4)]
+    a = [o.compute_forward_dynamics(q[e], qd[e], tau[e]) for e in range(4)]
+    o.set_long_double(True)
+    for e in range(4):
+        dl = o.compute_inverse_dynamics(q[e], qd[e], qdd[e])
+        al = o.compute_forward_dynamics(q[e], qd[e], tau[e])
+        assert np.abs(d[e] - dl).max() < 1e-12 * np.abs(dl).max()
+        assert np.abs(a[e] - al).max() < 1e-10 * np.abs(al).max()
+
+
+def test_sapien_style_export_matches_plain():
+    """Fixed-joint merging and rotated joint frames leave the dynamics unchanged."""
+    plain, sap = syn.arm_with_fingers(), syn.arm_with_fingers(sapien_style=True)
+    o1, o2 = _model(plain), _model(sap)
+    q, qd, qdd, tau = plain.sample(5, seed=21)
+    r1 = o1.batch_step(q, qd, qdd, tau)
+    r2 = o2.batch_step(q, qd, qdd, tau)
+    for k in r1:
+        assert np.abs(r1[k] - r2[k]).max() < 1e-11 * max(1, np.abs(r1[k]).max()), k
+
+
+def test_se3_log_exp_and_jlog6():
+    rng = np.random.default_rng(2)
+    for scale in (1e-9, 1e-4, 0.3, 1.0, 3.0):
+        nu = rng.normal(size=6)
+        nu[3:] *= scale / np.linalg.norm(nu[3:])
+        T = se3_exp6(nu)
+        assert np.abs(se3_log6(T) - nu).max() < 1e-12
+        J = se3_jlog6(T)
+        h = 1e-6
+        Jfd = np.zeros((6, 6))
+        for k in range(6):
+            d = np.zeros(6)
+            d[k] = h
+            Jfd[:, k] = (se3_log6(T @ se3_exp6(d)) - se3_log6(T @ se3_exp6(-d))) / (2 * h)
+        assert np.abs(J - Jfd).max() < 1e-7
+
+
+def test_ik_reaches_fk_targets():
+    robot = syn.serial_chain(7)
+    o = _model(robot)
+    q, _, _, _ = robot.sample(8, seed=4)
+    ee = robot.ee_link
+    q0 = q + np.random.default_rng(0).normal(scale=0.2, size=q.shape)
+    ok_count = 0
+    for e in range(len(q)):
+        T = o.link_poses(q[e])[ee]
+        qs, ok, err = o.compute_inverse_kinematics(ee, T, initial_qpos=q0[e], eps=1e-10, max_iterations=200, damp=1e-8,
+                                                   dt=1.0)
+        if ok:
+            ok_count += 1
+            assert np.linalg.norm(err) < 1e-10
+            Ts = o.link_poses(qs)[ee]
+            assert np.abs(Ts - T).max() < 1e-9
+    assert ok_count >= 6

@@ -1,0 +1,225 @@
+"""GPU parity: the CUDA kernels (through the C ABI) against the CPU oracle.
+
+Tolerances (normwise relative, per environment: max|gpu - oracle| / max|oracle|):
+FK / Jacobian / CRBA / RNEA 1e-10, ABA 1e-8.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from sapien_gb300 import PinocchioModel, synthetic as syn
+from sapien_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"poses": 1e-10, "J": 1e-10, "M": 1e-10, "tau": 1e-10, "qdd": 1e-8}
+
+ROBOTS = {
+    "chain7": lambda: syn.serial_chain(7),
+    "arm9": lambda: syn.arm_with_fingers(),
+    "arm9_sapien": lambda: syn.arm_with_fingers(sapien_style=True),
+    "quadruped18": lambda: syn.quadruped(),
+    "humanoid": lambda: syn.humanoid(),
+    "humanoid_sapien": lambda: syn.humanoid(sapien_style=True),
+    "arm6": lambda: syn.serial_chain(6, seed=4),
+    "mixed_chain": lambda: syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                                "continuous", "prismatic"]),
+}
+
+
+def torch():
+    import torch as t
+
+    return t
+
+
+def pair(robot):
+    pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    return pm, o
+
+
+def quat_from_R(R):
+    """(w, x, y, z), Shepperd's method: same branch rule as the kernels and the oracle."""
+    t = np.trace(R)
+    q = np.zeros(4)
+    if t > 0:
+        r = np.sqrt(t + 1)
+        q[0] = 0.5 * r
+        k = 0.5 / r
+        q[1:] = [(R[2, 1] - R[1, 2]) * k, (R[0, 2] - R[2, 0]) * k, (R[1, 0] - R[0, 1]) * k]
+    else:
+        i = 0
+        if R[1, 1] > R[0, 0]:
+            i = 1
+        if R[2, 2] > R[i, i]:
+            i = 2
+        j, k_ = (i + 1) % 3, (i + 2) % 3
+        r = np.sqrt(R[i, i] - R[j, j] - R[k_, k_] + 1)
+        q[1 + i] = 0.5 * r
+        k = 0.5 / r
+        q[0] = (R[k_, j] - R[j, k_]) * k
+        q[1 + j] = (R[j, i] + R[i, j]) * k
+        q[1 + k_] = (R[k_, i] + R[i, k_]) * k
+    return q
+
+
+def oracle_pose7(poses12):
+    n, nl, _ = poses12.shape
+    out = np.zeros((n, nl, 7))
+    for e in range(n):
+        for li in range(nl):
+            out[e, li, :3] = poses12[e, li, 9:]
+            out[e, li, 3:] = quat_from_R(poses12[e, li, :9].reshape(3, 3))
+    return out
+
+
+def rel_per_env(g, o):
+    g = g.reshape(g.shape[0], -1)
+    o = o.reshape(o.shape[0], -1)
+    return (np.abs(g - o).max(axis=1) / np.maximum(np.abs(o).max(axis=1), 1e-300)).max()
+
+
+def run_step(pm, q, qd, qdd, tau):
+    T = torch()
+    dev = T.device("cuda", 0)
+    t = lambda a: T.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    out = pm.step_batched(t(q), t(qd), t(qdd), t(tau))
+    T.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+@pytest.mark.parametrize("name", list(ROBOTS))
+def test_fused_step_matches_oracle(name):
+    robot = ROBOTS[name]()
+    pm, o = pair(robot)
+    q, qd, qdd, tau = robot.sample(77, seed=101)
+    g = run_step(pm, q, qd, qdd, tau)
+    r = o.batch_step(q, qd, qdd, tau, nthreads=8)
+    errs = {
+        "poses": rel_per_env(g["link_poses"], oracle_pose7(r["poses"])),
+        "J": rel_per_env(g["jacobian"], r["J"]),
+        "M": rel_per_env(g["mass_matrix"], r["M"]),
+        "tau": rel_per_env(g["qf"], r["tau"]),
+        "qdd": rel_per_env(g["qacc"], r["qdd"]),
+    }
+    for k, v in errs.items():
+        assert v <= TOL[k], f"{name}: {k} relative error {v:.3e} > {TOL[k]:g}"
+    assert np.array_equal(g["mass_matrix"], np.swapaxes(g["mass_matrix"], 1, 2))
+
+
+@pytest.mark.parametrize("name", ["arm9", "humanoid"])
+def test_single_op_entry_points_match_fused(name):
+    robot = ROBOTS[name]()
+    pm, _ = pair(robot)
+    T = torch()
+    q, qd, qdd, tau = robot.sample(50, seed=5)
+    t = lambda a: T.from_numpy(a).cuda()  # noqa: E731
+    fused = pm.step_batched(t(q), t(qd), t(qdd), t(tau))
+    sep = {
+        "link_poses": pm.compute_forward_kinematics_batched(t(q)),
+        "jacobian": pm.compute_full_jacobian_batched(t(q)),
+        "mass_matrix": pm.compute_generalized_mass_matrix_batched(t(q)),
+        "qf": pm.compute_inverse_dynamics_batched(t(q), t(qd), t(qdd)),
+        "qacc": pm.compute_forward_dynamics_batched(t(q), t(qd), t(tau)),
+    }
+    for k, v in sep.items():
+        a, b = v.cpu().numpy(), fused[k].cpu().numpy()
+        assert rel_per_env(a, b) < 1e-13, k
+
+
+def test_drop_in_single_instance_api():
+    robot = syn.arm_with_fingers(sapien_style=True)
+    pm, o = pair(robot)
+    q, qd, qdd, tau = robot.sample(3, seed=17)
+    for e in range(3):
+        pm.compute_forward_kinematics(q[e])
+        Tref = o.link_poses(q[e])
+        for li in range(len(robot.link_names)):
+            pose = pm.get_link_pose(li)
+            assert pose.p.dtype == np.float32 and pose.q.dtype == np.float32
+            assert np.abs(pose.p - Tref[li, :3, 3]).max() < 1e-6
+            qr = quat_from_R(Tref[li, :3, :3])
+            assert min(np.abs(pose.q - qr).max(), np.abs(pose.q + qr).max()) < 1e-6
+        tt = pm.compute_inverse_dynamics(q[e], qd[e], qdd[e])
+        assert np.abs(tt - o.compute_inverse_dynamics(q[e], qd[e], qdd[e])).max() <= 1e-10 * np.abs(tt).max()
+        a = pm.compute_forward_dynamics(q[e], qd[e], tau[e])
+        assert np.abs(a - o.compute_forward_dynamics(q[e], qd[e], tau[e])).max() <= 1e-8 * np.abs(a).max()
+        M = pm.compute_generalized_mass_matrix(q[e])
+        assert np.abs(M - o.compute_generalized_mass_matrix(q[e])).max() <= 1e-10 * np.abs(M).max()
+
+
+def test_col_major_layout_through_c_abi():
+    robot = syn.arm_with_fingers()
+    pm, o = pair(robot)
+    T = torch()
+    n = 45
+    q, qd, qdd, tau = robot.sample(n, seed=8)
+    # structure-of-arrays buffers: [cols][n]
+    qT = T.from_numpy(np.ascontiguousarray(q.T)).cuda()
+    qdT = T.from_numpy(np.ascontiguousarray(qd.T)).cuda()
+    qddT = T.from_numpy(np.ascontiguousarray(qdd.T)).cuda()
+    tauT = T.from_numpy(np.ascontiguousarray(tau.T)).cuda()
+    nv = robot.nv
+    tau_o = T.empty(nv, n, dtype=T.float64, device="cuda")
+    qdd_o = T.empty(nv, n, dtype=T.float64, device="cuda")
+    M_o = T.empty(nv * nv, n, dtype=T.float64, device="cuda")
+    L = N.load()
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    pm._prepare(qT.device)
+    rc = L.sgdyn_step(pm._h, n, N.OP_INVERSE_DYNAMICS | N.OP_FORWARD_DYNAMICS | N.OP_MASS_MATRIX, p(qT), p(qdT),
+                      p(qddT), p(tauT), None, None, p(M_o), p(tau_o), p(qdd_o), N.COL_MAJOR, None)
+    assert rc == 0, N.last_error()
+    T.cuda.synchronize()
+    r = o.batch_step(q, qd, qdd, tau, ops=4 | 8 | 16)
+    assert rel_per_env(tau_o.cpu().numpy().T, r["tau"]) <= 1e-10
+    assert rel_per_env(qdd_o.cpu().numpy().T, r["qdd"]) <= 1e-8
+    assert rel_per_env(M_o.cpu().numpy().T.reshape(n, nv, nv), r["M"]) <= 1e-10
+
+
+def test_edge_cases_and_pointer_checks():
+    robot = syn.serial_chain(7)
+    pm, o = pair(robot)
+    T = torch()
+    L = N.load()
+    empty = T.empty(0, robot.nq_ext, dtype=T.float64, device="cuda")
+    assert pm.compute_inverse_dynamics_batched(empty, empty[:, :7], empty[:, :7]).shape == (0, 7)
+    # a host pointer must be rejected with an error status, never reach a kernel
+    qh = T.zeros(4, robot.nq_ext, dtype=T.float64)
+    out = T.empty(4, robot.nv, dtype=T.float64, device="cuda")
+    rc = L.sgdyn_compute_inverse_dynamics(pm._h, 4, ctypes.c_void_p(qh.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                          ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                          N.ENV_MAJOR, None)
+    assert rc == N.ERR_NULL
+    assert "not device memory" in N.last_error()
+    with pytest.raises(TypeError):
+        pm.compute_inverse_dynamics_batched(qh, qh, qh)
+    # single environment
+    q, qd, qdd, _ = robot.sample(1, seed=2)
+    t = pm.compute_inverse_dynamics(q[0], qd[0], qdd[0])
+    assert np.abs(t - o.compute_inverse_dynamics(q[0], qd[0], qdd[0])).max() <= 1e-10 * np.abs(t).max()
+
+
+def test_full_size_batch_properties_and_parity():
+    """16384 environments of the 9-DoF arm: parity on every environment plus
+    size-independent identities computed on the GPU alone."""
+    robot = syn.arm_with_fingers()
+    pm, o = pair(robot)
+    T = torch()
+    n = 16384
+    q, qd, qdd, tau = robot.sample(n, seed=1)
+    g = run_step(pm, q, qd, qdd, tau)
+    r = o.batch_step(q, qd, qdd, tau, nthreads=8)
+    assert rel_per_env(g["qf"], r["tau"]) <= 1e-10
+    assert rel_per_env(g["qacc"], r["qdd"]) <= 1e-8
+    assert rel_per_env(g["mass_matrix"], r["M"]) <= 1e-10
+    # RNEA(q, qd, ABA(q, qd, tau)) == tau, all on the GPU
+    t = lambda a: T.from_numpy(a).cuda()  # noqa: E731
+    back = pm.compute_inverse_dynamics_batched(t(q), t(qd), T.from_numpy(g["qacc"]).cuda()).cpu().numpy()
+    assert rel_per_env(back, tau) <= 1e-9
