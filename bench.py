@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of the batched articulated-body dynamics step on GB300.
+
+Workload (one "step"): the 9-DoF tree (7 revolute arm joints + 2 prismatic fingers on
+the last link), N = 16384 environments per GPU, seeded synthetic float64 inputs; every
+step computes, for every environment, forward kinematics (all link poses), the WORLD
+Jacobian, the CRBA mass matrix, RNEA inverse dynamics and ABA forward dynamics, i.e.
+the five PinocchioModel calls the reference makes per environment.
+
+Our arm: `python bench.py [--gpus N --steps K --warmup W]` (torchrun for N > 1; each rank
+owns its own N environments, no collective on the data path: weak scaling).
+Reference arm: `python bench.py --impl reference ...` times the CPU oracle (the FP64
+restatement of the reference path; the reference itself cannot be built here) on the
+same workload with all host threads, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ABA/RNEA evals/s at 16k envs; fwd+bwd rollout steps/s vs plain; err<=1e-9"
+UNIT = "env-steps/s"
+N_ENVS = 16384
+WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs per GPU, "
+            "FK (all link poses) + WORLD Jacobian + CRBA + RNEA + ABA per env per step")
+
+# FP64 (thread-level) instructions per environment-step of the fused kernel, from the ncu
+# capture summarised in profiles/step_kernel_arm9.md: 3675 DFMA + 1597 DADD/DMUL.
+FP64_INST_PER_ENV = 5272
+# DRAM bytes (read + write) per environment of one fused launch, same capture
+# (161.7 MB per 16384-environment launch).
+DRAM_BYTES_PER_ENV = 161.7e6 / 16384
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_ENVS)
+    return ap.parse_args()
+
+
+def algorithmic_bytes_per_env(nq, nv, nlinks):
+    """Compulsory FP64 traffic of one env-step: inputs q, qd, qdd, tau; outputs link poses
+    (7 per link), Jacobian 6 x nv, mass matrix nv x nv, tau, qdd."""
+    return 8 * (nq + 3 * nv) + 8 * (7 * nlinks + 6 * nv + nv * nv + 2 * nv)
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def fp64_peak_dfma_per_s():
+    from sapien_gb300.build_native import PROBE_LIB
+
+    L = ctypes.CDLL(PROBE_LIB)
+    L.sgdyn_probe_fp64_dfma_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    v = ctypes.c_double()
+    if L.sgdyn_probe_fp64_dfma_rate(5, ctypes.byref(v)) != 0:
+        return None
+    return v.value
+
+
+def make_model():
+    from sapien_gb300 import PinocchioModel, synthetic
+
+    robot = synthetic.arm_with_fingers()
+    pm = PinocchioModel(robot.urdf, [0.0, 0.0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    return robot, pm
+
+
+def run_reference(args):
+    """CPU oracle on the same workload, all host threads, rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle
+    from sapien_gb300 import synthetic
+
+    robot = synthetic.arm_with_fingers()
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    n = args.n
+    q, qd, qdd, tau = robot.sample(n, seed=0)
+    cores = host_cores()
+    for _ in range(args.warmup):
+        o.batch_step(q, qd, qdd, tau, nthreads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.batch_step(q, qd, qdd, tau, nthreads=cores)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = n / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_envs": n, "parallelism": "threads over environments"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"full workload ({n} envs) per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    from sapien_gb300 import _native as N
+
+    robot, pm = make_model()
+    n = args.n
+    q_h, qd_h, qdd_h, tau_h = robot.sample(n, seed=rank)
+    nv, nq, nl = robot.nv, robot.nq_ext, len(robot.link_names)
+    q, qd, qdd, tau = (torch.from_numpy(a).to(dev) for a in (q_h, qd_h, qdd_h, tau_h))
+    f64 = dict(dtype=torch.float64, device=dev)
+    poses, J, M = torch.empty(n, nl, 7, **f64), torch.empty(n, 6, nv, **f64), torch.empty(n, nv, nv, **f64)
+    tau_o, qdd_o = torch.empty(n, nv, **f64), torch.empty(n, nv, **f64)
+    pm._prepare(dev)
+    L = N.load()
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def step(qq, qqd, qqdd, ttau, ops=N.OP_ALL):
+        rc = L.sgdyn_step(pm._h, n, ops, P(qq), P(qqd), P(qqdd), P(ttau), P(poses), P(J), P(M), P(tau_o), P(qdd_o),
+                          N.ENV_MAJOR, sp)
+        if rc != 0:
+            raise RuntimeError(N.last_error())
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    # ---- kernel-only timing, inputs resident in HBM ---------------------------------
+    for _ in range(args.warmup):
+        flush.zero_()
+        step(q, qd, qdd, tau)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step(q, qd, qdd, tau)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers ------------------------------
+    pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
+    hq, hqd, hqdd, htau = pin(q_h), pin(qd_h), pin(qdd_h), pin(tau_h)
+    outs_d = (poses, J, M, tau_o, qdd_o)
+    outs_h = [torch.empty(o.shape, dtype=torch.float64).pin_memory() for o in outs_d]
+    h2d = sum(t.numel() * 8 for t in (hq, hqd, hqdd, htau))
+    d2h = sum(t.numel() * 8 for t in outs_h)
+
+    def e2e_step():
+        q.copy_(hq, non_blocking=True)
+        qd.copy_(hqd, non_blocking=True)
+        qdd.copy_(hqdd, non_blocking=True)
+        tau.copy_(htau, non_blocking=True)
+        step(q, qd, qdd, tau)
+        for hdst, dsrc in zip(outs_h, outs_d):
+            hdst.copy_(dsrc, non_blocking=True)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        e2e_step()
+    torch.cuda.synchronize()
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        ev2[k][0].record(stream)
+        e2e_step()
+        ev2[k][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = float(np.mean([a.elapsed_time(b) for a, b in ev2]))
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e_value = world * n / (ms_e2e * 1e-3)
+
+    # ---- per-op kernel times (same inputs) -------------------------------------------
+    per_op = {}
+    for name, ops in (("fk", N.OP_FK), ("jacobian", N.OP_JACOBIAN), ("crba", N.OP_MASS_MATRIX),
+                      ("rnea", N.OP_INVERSE_DYNAMICS), ("aba", N.OP_FORWARD_DYNAMICS),
+                      ("rnea+aba", N.OP_INVERSE_DYNAMICS | N.OP_FORWARD_DYNAMICS)):
+        ts = []
+        for k in range(10):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step(q, qd, qdd, tau, ops)
+            b.record(stream)
+            ts.append((a, b))
+        torch.cuda.synchronize()
+        t_ms = float(np.mean([a.elapsed_time(b) for a, b in ts[2:]]))
+        per_op[name] = {"evals_per_s": n / (t_ms * 1e-3), "us": t_ms * 1e3}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline -------------------------------------------------------------------
+    peaks, peak_src = measured_peaks()
+    alg = algorithmic_bytes_per_env(nq, nv, nl) * n
+    achieved_gbs = alg / (ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved_gbs / peaks["hbm_gbs"],
+                "traffic": DRAM_BYTES_PER_ENV * n if DRAM_BYTES_PER_ENV else None,
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": alg}
+    dfma = fp64_peak_dfma_per_s()
+    roofline_fp64 = None
+    if dfma:
+        roofline_fp64 = {"bound": "fp64", "peak": dfma / 1e9, "unit": "G FP64 inst/s (per lane)",
+                         "peak_source": "measured live: DFMA chain microbenchmark (csrc_probe/fp64_peak.cu)"}
+        if FP64_INST_PER_ENV:
+            ach = FP64_INST_PER_ENV * n / (ms * 1e-3) / 1e9
+            roofline_fp64.update({"achieved": ach, "frac": ach / (dfma / 1e9),
+                                  "inst_per_env_step": FP64_INST_PER_ENV})
+
+    # ---- CPU baseline on a bounded sample + parity of that sample --------------------
+    from oracle.oracle import Oracle
+
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    cores = host_cores()
+    S = min(n, 4096)
+    o.batch_step(q_h[:256], qd_h[:256], qdd_h[:256], tau_h[:256], nthreads=cores)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        ref = o.batch_step(q_h[:S], qd_h[:S], qdd_h[:S], tau_h[:S], nthreads=cores)
+        reps += 1
+        if time.perf_counter() - t0 > 2.0:
+            break
+    cpu_dt = (time.perf_counter() - t0) / reps
+    step(q, qd, qdd, tau)
+    torch.cuda.synchronize()
+
+    def rel(g, r):
+        g = g.reshape(g.shape[0], -1)
+        r = r.reshape(r.shape[0], -1)
+        return float((np.abs(g - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-300)).max())
+
+    errs = {"rnea": rel(tau_o[:S].cpu().numpy(), ref["tau"]), "aba": rel(qdd_o[:S].cpu().numpy(), ref["qdd"]),
+            "crba": rel(M[:S].cpu().numpy(), ref["M"]), "jacobian": rel(J[:S].cpu().numpy(), ref["J"]),
+            "fk_positions": rel(poses[:S, :, :3].cpu().numpy(), ref["poses"][:, :, 9:])}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_envs_per_gpu": n, "nv": nv, "links": nl,
+                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
+                   "parallelism": f"data-parallel replicas over environments x{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": ms_e2e},
+        "gpu_launches": args.steps,
+        "roofline": roofline,
+        "roofline_fp64": roofline_fp64,
+        "cpu_baseline": {"value": S / cpu_dt, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"first {S} envs of the workload, {reps} repetitions (~2 s)"},
+        "per_op_kernel": per_op,
+        "max_rel_err_vs_oracle": errs,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -70,15 +70,29 @@ def build(verbose=False, jobs=None, force=False):
     if errs:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
-    newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    _link(objs, LIB, verbose)
+    # FP64-peak microbenchmark used by bench.py (separate library, not part of the C ABI)
+    pobj, perr = _compile(PROBE_SRC, hmt, verbose)
+    if perr:
+        raise RuntimeError("nvcc failed:\n" + perr)
+    _link([pobj], PROBE_LIB, verbose)
     return LIB
+
+
+PROBE_SRC = os.path.join(HERE, "csrc_probe", "fp64_peak.cu")
+PROBE_LIB = os.path.join(LIBDIR, "libsgdyn_probe.so")
+
+
+def _link(objs, out, verbose):
+    newest = max(os.path.getmtime(o) for o in objs)
+    if os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return
+    cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", out] + objs
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":
