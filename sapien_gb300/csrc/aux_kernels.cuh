@@ -1,0 +1,401 @@
+// Link Jacobians, Coriolis matrix and CLIK inverse kinematics, one environment per thread.
+#pragma once
+#include "se3.cuh"
+#include "step_kernel.cuh"
+
+namespace sgdyn {
+
+// getLinkJacobian (pinocchio_model.cpp:167-186): WORLD columns oMi.act(S) of the joints
+// supporting the link's joint, zero elsewhere; local -> left-multiplied by the inverse
+// action of the link pose. computeSingleLinkLocalJacobian (:188-199) is the same matrix
+// (link2joint^-1 action of the joint-frame Jacobian = link2world^-1 action of the world one).
+template <int MAXJ>
+__global__ void __launch_bounds__(32) link_jacobian_kernel(const DModel* __restrict__ model, const LinkJacArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  const DJoint* __restrict__ JT = model_joints(model);
+  const DLink& L = model_links(model)[a.link];
+  const int nv = model->nv;
+  for (int r = 0; r < 6; r++)
+    for (int c = 0; c < nv; c++) stv(a.J, e, r * nv + c, 0.0);
+  int chain[MAXJ];
+  int depth = 0;
+  for (int j = L.joint; j > 0; j = JT[j].parent) chain[depth++] = j;
+  M3 oR[MAXJ];
+  V3 op[MAXJ];
+  for (int d = depth - 1; d >= 0; d--) {
+    const int i = chain[d];
+    joint_world_pose(JT[i], a.q, e, oR, op, oR[i], op[i]);
+  }
+  M3 Rl;
+#pragma unroll
+  for (int k = 0; k < 9; k++) Rl.a[k] = L.R[k];
+  M3 R;
+  V3 p;
+  if (L.joint == 0) {
+    R = Rl;
+    p = mk(L.p[0], L.p[1], L.p[2]);
+  } else {
+    R = mul(oR[L.joint], Rl);
+    p = mul_add(oR[L.joint], mk(L.p[0], L.p[1], L.p[2]), op[L.joint]);
+  }
+  for (int d = 0; d < depth; d++) {
+    const int i = chain[d];
+    const DJoint& J = JT[i];
+    for (int k = 0; k < J.nv; k++) {
+      Mot S = world_S(J, oR[i], op[i], k);
+      if (a.local) {
+        S.v = mulT(R, add_cross(S.v, S.w, p));  // R^T (v - p x w)
+        S.w = mulT(R, S.w);
+      }
+      const int c = J.vcol + k;
+      stv(a.J, e, 0 * nv + c, S.v.x);
+      stv(a.J, e, 1 * nv + c, S.v.y);
+      stv(a.J, e, 2 * nv + c, S.v.z);
+      stv(a.J, e, 3 * nv + c, S.w.x);
+      stv(a.J, e, 4 * nv + c, S.w.y);
+      stv(a.J, e, 5 * nv + c, S.w.z);
+    }
+  }
+}
+
+// Dense 6x6 of a rigid-body inertia (linear, angular ordering).
+__device__ __forceinline__ void rbi_dense(const RBI& Y, double* I6) {
+  for (int k = 0; k < 36; k++) I6[k] = 0;
+  I6[0] = I6[7] = I6[14] = Y.m;
+  // top-right -[h]x, bottom-left [h]x
+  const double h[3] = {Y.h.x, Y.h.y, Y.h.z};
+  const double H[9] = {0, -h[2], h[1], h[2], 0, -h[0], -h[1], h[0], 0};
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      I6[r * 6 + 3 + c] = -H[r * 3 + c];
+      I6[(3 + r) * 6 + c] = H[r * 3 + c];
+    }
+  const int sidx[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) I6[(3 + r) * 6 + 3 + c] = Y.I[sidx[r * 3 + c]];
+}
+__device__ __forceinline__ Mot dense_mul(const double* A, Mot x) {
+  const double xv[6] = {x.v.x, x.v.y, x.v.z, x.w.x, x.w.y, x.w.z};
+  double y[6];
+  for (int r = 0; r < 6; r++) {
+    double s = 0;
+    for (int c = 0; c < 6; c++) s = fma(A[r * 6 + c], xv[c], s);
+    y[r] = s;
+  }
+  return Mot{mk(y[0], y[1], y[2]), mk(y[3], y[4], y[5])};
+}
+__device__ __forceinline__ Mot dense_mulT(const double* A, Mot x) {
+  const double xv[6] = {x.v.x, x.v.y, x.v.z, x.w.x, x.w.y, x.w.z};
+  double y[6];
+  for (int c = 0; c < 6; c++) {
+    double s = 0;
+    for (int r = 0; r < 6; r++) s = fma(A[r * 6 + c], xv[r], s);
+    y[c] = s;
+  }
+  return Mot{mk(y[0], y[1], y[2]), mk(y[3], y[4], y[5])};
+}
+
+// computeCoriolisMatrix (pinocchio_model.cpp:208-212): the Christoffel-consistent
+// factorisation C = sum_b J_b^T (I_b Jdot_b + B_b J_b) with
+// B(I, v) = 1/2 ((v x*) I - I (v x) + (I v) xbar*), evaluated with subtree composites:
+// for a joint i with composites Ic, Bc over its subtree,
+//   C[k, l] = S_k . (Ic Sdot_l + Bc S_l)             l in joint i, k in ancestors-or-self,
+//   C[k, l] = (Ic S_k) . Sdot_l + (Bc^T S_k) . S_l   k in joint i, l in strict ancestors,
+// where Sdot = v_i x S (world frame) and all other entries vanish.
+template <int MAXJ>
+__global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__ model, const CoriolisArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = MAXJ + 5;
+  const DJoint* __restrict__ JT = model_joints(model);
+  const int nj = model->nj, nv = model->nv;
+  M3 oR[MAXJ];
+  V3 op[MAXJ];
+  Mot vel[MAXJ], Sw[MAXV], Sd[MAXV];
+  RBI Ic[MAXJ];
+  double Bc[MAXJ][36];
+  for (int r = 0; r < nv; r++)
+    for (int c = 0; c < nv; c++) stv(a.C, e, r * nv + c, 0.0);
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = JT[i];
+    const int p = J.parent, iv = J.ivx;
+    joint_world_pose(J, a.q, e, oR, op, oR[i], op[i]);
+    Mot vJ{mk(0, 0, 0), mk(0, 0, 0)};
+    for (int k = 0; k < J.nv; k++) {
+      Sw[iv + k] = world_S(J, oR[i], op[i], k);
+      vJ = axpy6(ldv(a.qd, e, J.vcol + k), Sw[iv + k], vJ);
+    }
+    const Mot v = (p == 0) ? vJ : add6(vel[p], vJ);
+    vel[i] = v;
+    const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+    for (int k = 0; k < J.nv; k++) Sd[iv + k] = add_crossm(zero, v, Sw[iv + k]);
+    RBI Yl;
+    Yl.m = J.m;
+    Yl.h = mk(J.h[0], J.h[1], J.h[2]);
+    for (int k = 0; k < 6; k++) Yl.I[k] = J.I[k];
+    const RBI Y = rbi_transport(Yl, oR[i], op[i]);
+    Ic[i] = Y;
+    // B = 1/2 (crf(v) I - I crm(v) + Hbar(I v)), column by column
+    double I6[36];
+    rbi_dense(Y, I6);
+    const Mot h = rbi_mul(Y, v);
+    for (int c = 0; c < 6; c++) {
+      Mot ec{mk(c == 0, c == 1, c == 2), mk(c == 3, c == 4, c == 5)};
+      // I6 column c
+      Mot Icol{mk(I6[0 * 6 + c], I6[1 * 6 + c], I6[2 * 6 + c]), mk(I6[3 * 6 + c], I6[4 * 6 + c], I6[5 * 6 + c])};
+      Mot t1 = add_crossf(zero, v, Icol);               // (v x*) I e_c
+      Mot t2 = rbi_mul(Y, add_crossm(zero, v, ec));     // I (v x e_c)
+      Mot t3 = add_crossf(zero, ec, h);                 // e_c x* (I v)
+      const double col[6] = {t1.v.x - t2.v.x + t3.v.x, t1.v.y - t2.v.y + t3.v.y, t1.v.z - t2.v.z + t3.v.z,
+                             t1.w.x - t2.w.x + t3.w.x, t1.w.y - t2.w.y + t3.w.y, t1.w.z - t2.w.z + t3.w.z};
+      for (int r = 0; r < 6; r++) Bc[i][r * 6 + c] = 0.5 * col[r];
+    }
+  }
+  for (int i = nj - 1; i >= 1; i--) {
+    const DJoint& J = JT[i];
+    const int p = J.parent, iv = J.ivx;
+    const RBI Y = Ic[i];
+    for (int l = 0; l < J.nv; l++) {
+      const Mot F = add6(rbi_mul(Y, Sd[iv + l]), dense_mul(Bc[i], Sw[iv + l]));
+      const int cl = J.vcol + l;
+      for (int j = i; j > 0; j = JT[j].parent) {
+        const DJoint& A = JT[j];
+        for (int k = 0; k < A.nv; k++) stv(a.C, e, (A.vcol + k) * nv + cl, dot6(Sw[A.ivx + k], F));
+      }
+    }
+    for (int k = 0; k < J.nv; k++) {
+      const Mot H = rbi_mul(Y, Sw[iv + k]);
+      const Mot K = dense_mulT(Bc[i], Sw[iv + k]);
+      const int rk = J.vcol + k;
+      for (int j = p; j > 0; j = JT[j].parent) {
+        const DJoint& A = JT[j];
+        for (int l = 0; l < A.nv; l++)
+          stv(a.C, e, rk * nv + A.vcol + l, dot6(H, Sd[A.ivx + l]) + dot6(K, Sw[A.ivx + l]));
+      }
+    }
+    if (p > 0) {
+      RBI& P = Ic[p];
+      P.m += Y.m;
+      P.h = P.h + Y.h;
+      for (int k = 0; k < 6; k++) P.I[k] += Y.I[k];
+      for (int k = 0; k < 36; k++) Bc[p][k] += Bc[i][k];
+    }
+  }
+}
+
+// computeInverseKinematics (pinocchio_model.cpp:228-300): damped-least-squares CLIK on the
+// joint-frame log6 error. Loop: FK; iMd = oMi[j]^-1 oMdes; err = log6(iMd); keep the best
+// iterate; stop when |err| < eps (success) or after max_iter updates; J = joint-frame
+// Jacobian; J = -Jlog6(iMd^-1) J diag(mask); v = -J^T (J J^T + damp 1)^-1 err;
+// q = integrate(q, v dt). Returns posP2S(best q), success, best err.
+template <int MAXJ>
+__global__ void __launch_bounds__(32) ik_kernel(const DModel* __restrict__ model, const IkArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = MAXJ + 5;
+  const DJoint* __restrict__ JT = model_joints(model);
+  const DLink& L = model_links(model)[a.link];
+  const int nj = model->nj;
+  // per-joint state in internal form: angle / slide; (cos, sin); free flyer x y z qx qy qz qw
+  double qs[MAXJ][7], best[MAXJ][7];
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = JT[i];
+    const int c0 = J.qcol;
+    switch (J.kind) {
+      case JK_CONTINUOUS: {
+        double s, c;
+        if (a.has_q0) sincos(ldv(a.q0, e, c0), &s, &c);
+        else { s = 0; c = 1; }
+        qs[i][0] = c;
+        qs[i][1] = s;
+        break;
+      }
+      case JK_FREEFLYER:
+        for (int k = 0; k < 7; k++) qs[i][k] = a.has_q0 ? ldv(a.q0, e, c0 + k) : (k == 6 ? 1.0 : 0.0);
+        break;
+      default:
+        qs[i][0] = a.has_q0 ? ldv(a.q0, e, c0) : 0.0;
+    }
+  }
+  int chain[MAXJ];
+  int depth = 0;
+  for (int j = L.joint; j > 0; j = JT[j].parent) chain[depth++] = j;
+  const int jid = L.joint;
+  // oMdes = target * l2j^-1
+  const V3 pt = mk(ldv(a.target, e, 0), ldv(a.target, e, 1), ldv(a.target, e, 2));
+  const M3 Rt = quat_to_R(ldv(a.target, e, 4), ldv(a.target, e, 5), ldv(a.target, e, 6), ldv(a.target, e, 3));
+  M3 Rl;
+  for (int k = 0; k < 9; k++) Rl.a[k] = L.R[k];
+  const M3 Rdes = mul(Rt, transpose(Rl));
+  const V3 pdes = pt - mul(Rdes, mk(L.p[0], L.p[1], L.p[2]));
+  double mk_[MAXV];
+  int ncol = 0;
+  for (int d = depth - 1; d >= 0; d--) {
+    const DJoint& J = JT[chain[d]];
+    for (int k = 0; k < J.nv; k++) mk_[ncol++] = a.has_mask ? double(a.mask[J.vcol + k]) : 1.0;
+  }
+  for (int i = 1; i < nj; i++)
+    for (int k = 0; k < 7; k++) best[i][k] = qs[i][k];
+  double minErr = 1e10;
+  Mot bestErr{mk(0, 0, 0), mk(0, 0, 0)};
+  bool ok = false;
+  M3 oR[MAXJ];
+  V3 op[MAXJ];
+  double Jc[6][MAXV];
+  for (int it = 0;; it++) {
+    // FK along the chain, root first
+    for (int d = depth - 1; d >= 0; d--) {
+      const int i = chain[d];
+      const DJoint& J = JT[i];
+      M3 Rpl;
+      for (int k = 0; k < 9; k++) Rpl.a[k] = J.R[k];
+      const V3 ppl = mk(J.p[0], J.p[1], J.p[2]);
+      const V3 ax = mk(J.axis[0], J.axis[1], J.axis[2]);
+      M3 RJ = eye3();
+      V3 pJ = mk(0, 0, 0);
+      switch (J.kind) {
+        case JK_PRISMATIC: pJ = qs[i][0] * ax; break;
+        case JK_FREEFLYER:
+          pJ = mk(qs[i][0], qs[i][1], qs[i][2]);
+          RJ = quat_to_R(qs[i][3], qs[i][4], qs[i][5], qs[i][6]);
+          break;
+        case JK_CONTINUOUS: RJ = rodrigues(ax, qs[i][1], qs[i][0]); break;
+        default: {
+          double s, c;
+          sincos(qs[i][0], &s, &c);
+          RJ = rodrigues(ax, s, c);
+        }
+      }
+      const M3 Rli = mul(Rpl, RJ);
+      const V3 pli = mul_add(Rpl, pJ, ppl);
+      if (J.parent == 0) {
+        oR[i] = Rli;
+        op[i] = pli;
+      } else {
+        oR[i] = mul(oR[J.parent], Rli);
+        op[i] = mul_add(oR[J.parent], pli, op[J.parent]);
+      }
+    }
+    M3 Ro = eye3();
+    V3 po = mk(0, 0, 0);
+    if (jid > 0) {
+      Ro = oR[jid];
+      po = op[jid];
+    }
+    // iMd = oMi^-1 oMdes
+    const M3 Re = mul(transpose(Ro), Rdes);
+    const V3 pe = mulT(Ro, pdes - po);
+    const Mot err = log6(Re, pe);
+    const double nrm = sqrt(dot6(err, err));
+    if (nrm < minErr) {
+      minErr = nrm;
+      bestErr = err;
+      for (int i = 1; i < nj; i++)
+        for (int k = 0; k < 7; k++) best[i][k] = qs[i][k];
+    }
+    if (nrm < a.eps) {
+      ok = true;
+      break;
+    }
+    if (it >= a.max_iter) break;
+    // joint-frame Jacobian of the chain columns
+    int col = 0;
+    for (int d = depth - 1; d >= 0; d--) {
+      const int i = chain[d];
+      const DJoint& J = JT[i];
+      for (int k = 0; k < J.nv; k++, col++) {
+        Mot S = world_S(J, oR[i], op[i], k);
+        const V3 v = mulT(Ro, add_cross(S.v, S.w, po));
+        const V3 w = mulT(Ro, S.w);
+        Jc[0][col] = v.x; Jc[1][col] = v.y; Jc[2][col] = v.z;
+        Jc[3][col] = w.x; Jc[4][col] = w.y; Jc[5][col] = w.z;
+      }
+    }
+    // Jlog6(iMd^-1)
+    double Jl[36];
+    const M3 Rinv = transpose(Re);
+    jlog6(Rinv, -mul(Rinv, pe), Jl);
+    // J2 = -Jl Jc diag(mask), in place column by column
+    for (int c = 0; c < ncol; c++) {
+      double t[6];
+      for (int r = 0; r < 6; r++) {
+        double s = 0;
+        for (int k = 0; k < 6; k++) s = fma(Jl[r * 6 + k], Jc[k][c], s);
+        t[r] = -s * mk_[c];
+      }
+      for (int r = 0; r < 6; r++) Jc[r][c] = t[r];
+    }
+    // (J J^T + damp) x = err, Cholesky on the packed lower triangle
+    double A[21];
+    for (int r = 0; r < 6; r++)
+      for (int c = 0; c <= r; c++) {
+        double s = (r == c) ? a.damp : 0.0;
+        for (int k = 0; k < ncol; k++) s = fma(Jc[r][k], Jc[c][k], s);
+        A[r * (r + 1) / 2 + c] = s;
+      }
+    chol6(A);
+    double x[6] = {err.v.x, err.v.y, err.v.z, err.w.x, err.w.y, err.w.z};
+    chol6_solve(A, x);
+    // v = -J^T x ; integrate the chain joints by v dt
+    col = 0;
+    for (int d = depth - 1; d >= 0; d--) {
+      const int i = chain[d];
+      const DJoint& J = JT[i];
+      double vv[6];
+      for (int k = 0; k < J.nv; k++, col++) {
+        double s = 0;
+        for (int r = 0; r < 6; r++) s = fma(Jc[r][col], x[r], s);
+        vv[k] = -s * a.dt;
+      }
+      switch (J.kind) {
+        case JK_CONTINUOUS: {
+          double sw, cw;
+          sincos(vv[0], &sw, &cw);
+          const double c = qs[i][0], s = qs[i][1];
+          const double nc = cw * c - sw * s, ns = sw * c + cw * s;
+          const double k = (3 - (nc * nc + ns * ns)) / 2;
+          qs[i][0] = nc * k;
+          qs[i][1] = ns * k;
+          break;
+        }
+        case JK_FREEFLYER: {
+          const M3 R0 = quat_to_R(qs[i][3], qs[i][4], qs[i][5], qs[i][6]);
+          M3 dR;
+          V3 dp;
+          exp6(Mot{mk(vv[0], vv[1], vv[2]), mk(vv[3], vv[4], vv[5])}, dR, dp);
+          const M3 R1 = mul(R0, dR);
+          const V3 p1 = mul_add(R0, dp, mk(qs[i][0], qs[i][1], qs[i][2]));
+          double qw[4];
+          R_to_quat(R1, qw);  // w x y z
+          const double dq = qw[1] * qs[i][3] + qw[2] * qs[i][4] + qw[3] * qs[i][5] + qw[0] * qs[i][6];
+          const double sg = dq < 0 ? -1.0 : 1.0;
+          const double n = sqrt(qw[0] * qw[0] + qw[1] * qw[1] + qw[2] * qw[2] + qw[3] * qw[3]);
+          qs[i][0] = p1.x; qs[i][1] = p1.y; qs[i][2] = p1.z;
+          qs[i][3] = sg * qw[1] / n; qs[i][4] = sg * qw[2] / n; qs[i][5] = sg * qw[3] / n; qs[i][6] = sg * qw[0] / n;
+          break;
+        }
+        default: qs[i][0] += vv[0];
+      }
+    }
+  }
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = JT[i];
+    switch (J.kind) {
+      case JK_CONTINUOUS: stv(a.q_out, e, J.qcol, atan2(best[i][1], best[i][0])); break;
+      case JK_FREEFLYER:
+        for (int k = 0; k < 7; k++) stv(a.q_out, e, J.qcol + k, best[i][k]);
+        break;
+      default: stv(a.q_out, e, J.qcol, best[i][0]);
+    }
+  }
+  a.success[e] = ok ? 1 : 0;
+  stv(a.err, e, 0, bestErr.v.x);
+  stv(a.err, e, 1, bestErr.v.y);
+  stv(a.err, e, 2, bestErr.v.z);
+  stv(a.err, e, 3, bestErr.w.x);
+  stv(a.err, e, 4, bestErr.w.y);
+  stv(a.err, e, 5, bestErr.w.z);
+}
+
+}  // namespace sgdyn

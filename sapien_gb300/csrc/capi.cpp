@@ -286,18 +286,99 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
   });
 }
 
-int sgdyn_compute_link_jacobian(const sgdyn_model*, int64_t, int, int, const double*, double*, int, void*) {
-  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+int sgdyn_compute_link_jacobian(const sgdyn_model* m, int64_t n, int link, int local, const double* q, double* J,
+                                int layout, void* stream) {
+  return guarded([&] {
+    if (int rc = check_model(m)) return rc;
+    Model& Mo = *m->impl;
+    if (link < 0 || link >= Mo.nlinks()) return fail(SGDYN_ERR_RUNTIME, "link index out of bound");
+    if (n < 0) return fail(SGDYN_ERR_RUNTIME, "negative batch size");
+    if (layout != SGDYN_ENV_MAJOR && layout != SGDYN_COL_MAJOR) return fail(SGDYN_ERR_RUNTIME, "bad layout");
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q, "q"}, {J, "J"}})) return rc;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    LinkJacArgs a;
+    a.n = n;
+    a.link = link;
+    a.local = local ? 1 : 0;
+    a.q = make_arr(q, n, Mo.nq_ext(), layout);
+    a.J = make_arr(J, n, 6 * int64_t(Mo.nv()), layout);
+    cudaError_t e = launch_link_jacobian(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+    return SGDYN_OK;
+  });
 }
-int sgdyn_compute_single_link_local_jacobian(const sgdyn_model*, int64_t, int, const double*, double*, int, void*) {
-  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+
+int sgdyn_compute_single_link_local_jacobian(const sgdyn_model* m, int64_t n, int link, const double* q, double* J,
+                                             int layout, void* stream) {
+  return sgdyn_compute_link_jacobian(m, n, link, 1, q, J, layout, stream);
 }
-int sgdyn_compute_coriolis_matrix(const sgdyn_model*, int64_t, const double*, const double*, double*, int, void*) {
-  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+
+int sgdyn_compute_coriolis_matrix(const sgdyn_model* m, int64_t n, const double* q, const double* qd, double* C,
+                                  int layout, void* stream) {
+  return guarded([&] {
+    if (int rc = check_model(m)) return rc;
+    Model& Mo = *m->impl;
+    if (n < 0) return fail(SGDYN_ERR_RUNTIME, "negative batch size");
+    if (layout != SGDYN_ENV_MAJOR && layout != SGDYN_COL_MAJOR) return fail(SGDYN_ERR_RUNTIME, "bad layout");
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q, "q"}, {qd, "qd"}, {C, "C"}})) return rc;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    CoriolisArgs a;
+    a.n = n;
+    a.q = make_arr(q, n, Mo.nq_ext(), layout);
+    a.qd = make_arr(qd, n, Mo.nv(), layout);
+    a.C = make_arr(C, n, int64_t(Mo.nv()) * Mo.nv(), layout);
+    cudaError_t e = launch_coriolis(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+    return SGDYN_OK;
+  });
 }
-int sgdyn_compute_inverse_kinematics(const sgdyn_model*, int64_t, int, const double*, const double*, const int*,
-                                     double, int, double, double, double*, int*, double*, int, void*) {
-  return fail(SGDYN_ERR_UNSUPPORTED, "not built yet");
+
+int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, const double* target,
+                                     const double* q0, const int* mask, double eps, int max_iterations, double dt,
+                                     double damp, double* q_out, int* success, double* err_out, int layout,
+                                     void* stream) {
+  return guarded([&] {
+    if (int rc = check_model(m)) return rc;
+    Model& Mo = *m->impl;
+    if (link < 0 || link >= Mo.nlinks()) return fail(SGDYN_ERR_RUNTIME, "link index out of bound");
+    if (n < 0) return fail(SGDYN_ERR_RUNTIME, "negative batch size");
+    if (max_iterations < 0) return fail(SGDYN_ERR_RUNTIME, "negative max_iterations");
+    if (layout != SGDYN_ENV_MAJOR && layout != SGDYN_COL_MAJOR) return fail(SGDYN_ERR_RUNTIME, "bad layout");
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{target, "target"}, {q_out, "q_out"}, {success, "success"}, {err_out, "err"}}))
+      return rc;
+    if (q0)
+      if (int rc = check_ptrs({{q0, "q0"}})) return rc;
+    if (mask)
+      if (int rc = check_ptrs({{mask, "mask"}})) return rc;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    IkArgs a;
+    a.n = n;
+    a.link = link;
+    a.max_iter = max_iterations;
+    a.has_q0 = q0 != nullptr;
+    a.has_mask = mask != nullptr;
+    a.eps = eps;
+    a.dt = dt;
+    a.damp = damp;
+    a.target = make_arr(target, n, 7, layout);
+    a.q0 = make_arr(q0, n, Mo.nq_ext(), layout);
+    a.q_out = make_arr(q_out, n, Mo.nq_ext(), layout);
+    a.err = make_arr(err_out, n, 6, layout);
+    a.mask = mask;
+    a.success = success;
+    cudaError_t e = launch_ik(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+    return SGDYN_OK;
+  });
 }
 
 }  // extern "C"

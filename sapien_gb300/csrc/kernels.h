@@ -23,10 +23,33 @@ struct StepArgs {
   Arr poses, J, M, tau_out, qdd_out;    // outputs (p == nullptr when not requested)
 };
 
+struct LinkJacArgs {
+  int64_t n;
+  int link, local;
+  Arr q, J;
+};
+
+struct CoriolisArgs {
+  int64_t n;
+  Arr q, qd, C;
+};
+
+struct IkArgs {
+  int64_t n;
+  int link, max_iter, has_q0, has_mask;
+  double eps, dt, damp;
+  Arr target, q0, q_out, err;
+  const int* mask;
+  int* success;
+};
+
 // Joint-count bucket for the per-thread stash (16, 32 or 64 joints incl. universe).
 int stash_bucket(int nj);
 
 // Fused world-frame sweep: any subset of {FK poses, full WORLD Jacobian, CRBA, RNEA, ABA}.
 cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_link_jacobian(const DModel* dm, int nj, const LinkJacArgs& a, cudaStream_t s);
+cudaError_t launch_coriolis(const DModel* dm, int nj, const CoriolisArgs& a, cudaStream_t s);
+cudaError_t launch_ik(const DModel* dm, int nj, const IkArgs& a, cudaStream_t s);
 
 }  // namespace sgdyn

@@ -20,3 +20,46 @@ cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cu
 }
 
 }  // namespace sgdyn
+
+#include "aux_kernels.cuh"
+
+namespace sgdyn {
+
+#define SG_DECL(J)                                                                    \
+  cudaError_t launch_link_jacobian_j##J(const DModel*, const LinkJacArgs&, cudaStream_t); \
+  cudaError_t launch_coriolis_j##J(const DModel*, const CoriolisArgs&, cudaStream_t);    \
+  cudaError_t launch_ik_j##J(const DModel*, const IkArgs&, cudaStream_t);
+SG_DECL(16)
+SG_DECL(32)
+SG_DECL(64)
+#undef SG_DECL
+
+cudaError_t launch_link_jacobian(const DModel* dm, int nj, const LinkJacArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  switch (stash_bucket(nj)) {
+    case 16: return launch_link_jacobian_j16(dm, a, s);
+    case 32: return launch_link_jacobian_j32(dm, a, s);
+    case 64: return launch_link_jacobian_j64(dm, a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+cudaError_t launch_coriolis(const DModel* dm, int nj, const CoriolisArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  switch (stash_bucket(nj)) {
+    case 16: return launch_coriolis_j16(dm, a, s);
+    case 32: return launch_coriolis_j32(dm, a, s);
+    case 64: return launch_coriolis_j64(dm, a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+cudaError_t launch_ik(const DModel* dm, int nj, const IkArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  switch (stash_bucket(nj)) {
+    case 16: return launch_ik_j16(dm, a, s);
+    case 32: return launch_ik_j32(dm, a, s);
+    case 64: return launch_ik_j64(dm, a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace sgdyn

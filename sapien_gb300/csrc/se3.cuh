@@ -1,0 +1,184 @@
+// SE(3) exponential, logarithm and the Jacobian of the logarithm, FP64 device code.
+//
+// log3 goes through the rotation's unit quaternion (Shepperd extraction, then
+// theta = 2 atan2(|v|, w) with w >= 0), which stays well conditioned up to theta = pi.
+// log6(M) = (alpha p - 1/2 w x p + beta (w.p) w, w) with beta = g(theta),
+// alpha = 1 - theta^2 g(theta), g(t) = (1 - (t/2) cot(t/2)) / t^2.
+// Jlog6(M) is the derivative for a right perturbation, log6(M exp6(d)) ~ log6(M) + J d,
+// i.e. the inverse of the SE(3) right Jacobian J_r(xi) = J_l(-xi) in Barfoot's block
+// form [[J, Q], [0, J]] (T. Barfoot, "State Estimation for Robotics", 2017, sec. 7.1.5).
+// Coefficient functions switch to their Taylor series below fixed thresholds so no
+// branch loses precision to cancellation.
+#pragma once
+#include "spatial.cuh"
+
+namespace sgdyn {
+
+__device__ __forceinline__ double se3_f_1mc(double t) {  // (1 - cos t) / t^2
+  if (t < 0.3) {
+    double t2 = t * t, r = 0, term = 0.5;
+    for (int k = 0; k < 10; k++) {
+      r += term;
+      term *= -t2 / double((2 * k + 3) * (2 * k + 4));
+    }
+    return r;
+  }
+  return (1 - cos(t)) / (t * t);
+}
+__device__ __forceinline__ double se3_f_sinc(double t) {  // sin t / t
+  if (t < 0.3) {
+    double t2 = t * t, r = 0, term = 1;
+    for (int k = 0; k < 10; k++) {
+      r += term;
+      term *= -t2 / double((2 * k + 2) * (2 * k + 3));
+    }
+    return r;
+  }
+  return sin(t) / t;
+}
+__device__ __forceinline__ double se3_f_tms(double t) {  // (t - sin t) / t^3
+  if (t < 0.3) {
+    double t2 = t * t, r = 0, term = 1.0 / 6;
+    for (int k = 0; k < 10; k++) {
+      r += term;
+      term *= -t2 / double((2 * k + 4) * (2 * k + 5));
+    }
+    return r;
+  }
+  return (t - sin(t)) / (t * t * t);
+}
+__device__ __forceinline__ double se3_f_c4(double t) {  // (t^2 + 2 cos t - 2) / (2 t^4)
+  if (t < 0.6) {
+    double t2 = t * t, r = 0, term = 1.0 / 24;
+    for (int k = 0; k < 12; k++) {
+      r += term;
+      term *= -t2 / double((2 * k + 5) * (2 * k + 6));
+    }
+    return r;
+  }
+  return (t * t + 2 * cos(t) - 2) / (2 * t * t * t * t);
+}
+__device__ __forceinline__ double se3_f_c5(double t) {  // (2t - 3 sin t + t cos t) / (2 t^5)
+  if (t < 0.9) {
+    double t2 = t * t, r = 0, fact = 120, pw = 1;
+    for (int n = 2; n < 16; n++) {
+      r += ((n % 2) ? -1.0 : 1.0) * double(n - 1) * pw / fact;
+      pw *= t2;
+      fact *= double((2 * n + 2) * (2 * n + 3));
+    }
+    return r;
+  }
+  return (2 * t - 3 * sin(t) + t * cos(t)) / (2 * t * t * t * t * t);
+}
+__device__ __forceinline__ double se3_f_g(double t) {  // (1 - (t/2) cot(t/2)) / t^2
+  if (t < 0.3) {
+    const double c[6] = {1.0 / 12, 1.0 / 720, 1.0 / 30240, 1.0 / 1209600, 1.0 / 47900160, 691.0 / 1307674368000.0};
+    double t2 = t * t, r = 0, pw = 1;
+    for (int k = 0; k < 6; k++) {
+      r += c[k] * pw;
+      pw *= t2;
+    }
+    return r;
+  }
+  double h = 0.5 * t;
+  return (1 - h * cos(h) / sin(h)) / (t * t);
+}
+
+__device__ __forceinline__ M3 skew3(V3 w) { return M3{{0, -w.z, w.y, w.z, 0, -w.x, -w.y, w.x, 0}}; }
+__device__ __forceinline__ M3 add3(const M3& A, const M3& B) {
+  M3 C;
+#pragma unroll
+  for (int k = 0; k < 9; k++) C.a[k] = A.a[k] + B.a[k];
+  return C;
+}
+
+// Rotation vector of R (theta in [0, pi]).
+__device__ __forceinline__ V3 log3(const M3& R, double* theta) {
+  double q[4];
+  R_to_quat(R, q);
+  if (q[0] < 0) {
+    q[0] = -q[0];
+    q[1] = -q[1];
+    q[2] = -q[2];
+    q[3] = -q[3];
+  }
+  double n = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  if (n == 0) {
+    *theta = 0;
+    return mk(0, 0, 0);
+  }
+  double th = 2 * atan2(n, q[0]);
+  *theta = th;
+  double k = th / n;
+  return mk(k * q[1], k * q[2], k * q[3]);
+}
+
+__device__ __forceinline__ M3 exp3(V3 w) {
+  double t = sqrt(dot(w, w));
+  M3 K = skew3(w), K2 = mul(K, K);
+  double a = se3_f_sinc(t), b = se3_f_1mc(t);
+  M3 R = eye3();
+#pragma unroll
+  for (int k = 0; k < 9; k++) R.a[k] += a * K.a[k] + b * K2.a[k];
+  return R;
+}
+
+// log6 of (R, p): linear part, angular part.
+__device__ __forceinline__ Mot log6(const M3& R, V3 p) {
+  double t;
+  V3 w = log3(R, &t);
+  double beta = se3_f_g(t);
+  double alpha = 1 - t * t * beta;
+  V3 wxp = cross(w, p);
+  double wp = dot(w, p);
+  Mot out;
+  out.v = mk(alpha * p.x - 0.5 * wxp.x + beta * wp * w.x, alpha * p.y - 0.5 * wxp.y + beta * wp * w.y,
+             alpha * p.z - 0.5 * wxp.z + beta * wp * w.z);
+  out.w = w;
+  return out;
+}
+
+// exp6 of (v, w) -> (R, p).
+__device__ __forceinline__ void exp6(Mot nu, M3& R, V3& p) {
+  V3 w = nu.w;
+  double t = sqrt(dot(w, w));
+  M3 K = skew3(w), K2 = mul(K, K);
+  double b = se3_f_1mc(t), c = se3_f_tms(t);
+  M3 V = eye3();
+#pragma unroll
+  for (int k = 0; k < 9; k++) V.a[k] += b * K.a[k] + c * K2.a[k];
+  R = exp3(w);
+  p = mul(V, nu.v);
+}
+
+// Jlog6 of (R, p) as a dense 6x6, row-major, (linear, angular) ordering.
+__device__ __forceinline__ void jlog6(const M3& R, V3 p, double* J) {
+  Mot xi = log6(R, p);
+  V3 rho = xi.v, phi = xi.w;
+  double t = sqrt(dot(phi, phi));
+  M3 K = skew3(phi), K2 = mul(K, K);
+  double g = se3_f_g(t);
+  M3 Jinv = eye3();
+#pragma unroll
+  for (int k = 0; k < 9; k++) Jinv.a[k] += 0.5 * K.a[k] + g * K2.a[k];
+  // Q_l(-rho, -phi)
+  M3 P = skew3(-phi), Rh = skew3(-rho);
+  M3 PR = mul(P, Rh), RP = mul(Rh, P), PRP = mul(PR, P);
+  M3 PPR = mul(P, PR), RPP = mul(RP, P), PRPP = mul(PRP, P), PPRP = mul(P, PRP);
+  double a = se3_f_tms(t), b = se3_f_c4(t), c = se3_f_c5(t);
+  M3 Q;
+#pragma unroll
+  for (int k = 0; k < 9; k++)
+    Q.a[k] = 0.5 * Rh.a[k] + a * (PR.a[k] + RP.a[k] + PRP.a[k]) + b * (PPR.a[k] + RPP.a[k] - 3 * PRP.a[k]) +
+             c * (PRPP.a[k] + PPRP.a[k]);
+  M3 TR = mul(mul(Jinv, Q), Jinv);
+  for (int r = 0; r < 3; r++)
+    for (int cc = 0; cc < 3; cc++) {
+      J[r * 6 + cc] = Jinv.a[r * 3 + cc];
+      J[(r + 3) * 6 + cc + 3] = Jinv.a[r * 3 + cc];
+      J[r * 6 + cc + 3] = -TR.a[r * 3 + cc];
+      J[(r + 3) * 6 + cc] = 0;
+    }
+}
+
+}  // namespace sgdyn
