@@ -131,6 +131,64 @@ int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, 
                                      const double* q0, const int* mask, double eps, int max_iterations, double dt,
                                      double damp, double* q_out, int* success, double* err, int layout, void* stream);
 
+/* ---- differentiation (additions; the reference has no derivative API, see
+ * pinocchio/cmake/pinocchio.cmake:4 which builds Pinocchio without autodiff) ----------
+ * Configuration adjoints / derivatives are tangent-space quantities with nv columns
+ * (for a free-flyer root: with respect to its body twist, as Pinocchio's derivative
+ * API defines them). Free flyers are supported only as the root joint. */
+
+/* Vector-Jacobian product of computeInverseDynamics: given tau_bar [n][nv] returns
+ * q_bar, qd_bar, qdd_bar [n][nv] (any output may be NULL). qdd_bar = M tau_bar. */
+int sgdyn_compute_inverse_dynamics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                       const double* qdd, const double* tau_bar, double* q_bar, double* qd_bar,
+                                       double* qdd_bar, int layout, void* stream);
+
+/* Vector-Jacobian product of computeForwardDynamics: given qdd_bar returns q_bar, qd_bar,
+ * tau_bar (tau_bar = M^-1 qdd_bar). */
+int sgdyn_compute_forward_dynamics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                       const double* tau, const double* qdd_bar, double* q_bar, double* qd_bar,
+                                       double* tau_bar, int layout, void* stream);
+
+/* Vector-Jacobian product of the link poses: pos_bar [n][nlinks*3] (adjoint of link
+ * positions), rot_bar [n][nlinks*9] (adjoint of row-major link rotations) or NULL ->
+ * q_bar [n][nv]. */
+int sgdyn_compute_forward_kinematics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* pos_bar,
+                                         const double* rot_bar, double* q_bar, int layout, void* stream);
+
+/* Dense derivatives of RNEA: dtau_dq, dtau_dqd, dtau_dqdd (= M; may be NULL), each
+ * [n][nv*nv] row-major (row = torque, column = input). Analogue of Pinocchio's
+ * computeRNEADerivatives, which the reference does not expose. */
+int sgdyn_compute_rnea_derivatives(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                   const double* qdd, double* dtau_dq, double* dtau_dqd, double* dtau_dqdd,
+                                   int layout, void* stream);
+
+/* Dense derivatives of ABA: dqdd_dq, dqdd_dqd, dqdd_dtau (= M^-1; may be NULL). */
+int sgdyn_compute_aba_derivatives(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                  const double* tau, double* dqdd_dq, double* dqdd_dqd, double* dqdd_dtau,
+                                  int layout, void* stream);
+
+/* Semi-implicit Euler rollout of T steps, qd += dt ABA(q, qd, tau_t); q += dt qd, for
+ * models without free flyers. Contiguous env-major arrays: q0, qT [n][nq], qd0, qdT
+ * [n][nv], tau [T][n][nv]. With q_ckpt [C][n][nq] and qd_ckpt [C][n][nv],
+ * C = ceil(T / checkpoint_every), the state at steps 0, K, 2K, ... is recorded for the
+ * backward pass (both NULL for a plain forward rollout). */
+int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, const double* q0, const double* qd0,
+                          const double* tau, int checkpoint_every, double* q_ckpt, double* qd_ckpt, double* qT,
+                          double* qdT, void* stream);
+
+/* Bytes of device scratch sgdyn_rollout_backward needs for n environments. */
+int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_every, int64_t* bytes);
+
+/* Reverse pass of sgdyn_rollout_forward: given the adjoints of the final state (either may
+ * be NULL = zero) returns q0_bar, qd0_bar and tau_bar [T][n][nv]. Each checkpoint segment
+ * is recomputed from its q / qd checkpoint, its spatial intermediates kept in `scratch`
+ * (caller-owned device memory of at least sgdyn_rollout_scratch_bytes bytes), and then
+ * reversed step by step. */
+int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, int checkpoint_every,
+                           const double* q_ckpt, const double* qd_ckpt, const double* tau, const double* qT_bar,
+                           const double* qdT_bar, double* q0_bar, double* qd0_bar, double* tau_bar, double* scratch,
+                           int64_t scratch_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,14 @@ EXPORTED = (
     "sgdyn_compute_forward_dynamics",
     "sgdyn_step",
     "sgdyn_compute_inverse_kinematics",
+    "sgdyn_compute_inverse_dynamics_vjp",
+    "sgdyn_compute_forward_dynamics_vjp",
+    "sgdyn_compute_forward_kinematics_vjp",
+    "sgdyn_compute_rnea_derivatives",
+    "sgdyn_compute_aba_derivatives",
+    "sgdyn_rollout_forward",
+    "sgdyn_rollout_scratch_bytes",
+    "sgdyn_rollout_backward",
 )
 
 _lib = None
@@ -98,6 +106,14 @@ def load():
     L.sgdyn_compute_forward_dynamics.argtypes = [vp, i64, vp, vp, vp, vp, i32, vp]
     L.sgdyn_step.argtypes = [vp, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp]
     L.sgdyn_compute_inverse_kinematics.argtypes = [vp, i64, i32, vp, vp, vp, dbl, i32, dbl, dbl, vp, vp, vp, i32, vp]
+    L.sgdyn_compute_inverse_dynamics_vjp.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, i32, vp]
+    L.sgdyn_compute_forward_dynamics_vjp.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, i32, vp]
+    L.sgdyn_compute_forward_kinematics_vjp.argtypes = [vp, i64, vp, vp, vp, vp, i32, vp]
+    L.sgdyn_compute_rnea_derivatives.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i32, vp]
+    L.sgdyn_compute_aba_derivatives.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i32, vp]
+    L.sgdyn_rollout_forward.argtypes = [vp, i64, i32, dbl, vp, vp, vp, i32, vp, vp, vp, vp, vp]
+    L.sgdyn_rollout_scratch_bytes.argtypes = [vp, i64, i32, P(i64)]
+    L.sgdyn_rollout_backward.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp]
     _lib = L
     return L
 

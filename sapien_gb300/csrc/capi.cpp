@@ -139,6 +139,27 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
   return SGDYN_OK;
 }
 
+
+// Differentiation kernels support a free flyer only as the root joint.
+int check_diff_model(const sgdyn_model* m) {
+  if (int rc = check_model(m)) return rc;
+  for (auto& J : m->impl->joints)
+    if (J.kind == JK_FREEFLYER && J.parent != 0)
+      return fail(SGDYN_ERR_UNSUPPORTED, "derivatives need the free-flyer joint at the root");
+  return SGDYN_OK;
+}
+
+int common_checks(int64_t n, int layout) {
+  if (n < 0) return fail(SGDYN_ERR_RUNTIME, "negative batch size");
+  if (layout != SGDYN_ENV_MAJOR && layout != SGDYN_COL_MAJOR) return fail(SGDYN_ERR_RUNTIME, "bad layout");
+  return SGDYN_OK;
+}
+
+int launch_status(cudaError_t e) {
+  if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  return SGDYN_OK;
+}
+
 }  // namespace
 }  // namespace sgdyn
 
@@ -378,6 +399,202 @@ int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, 
     cudaError_t e = launch_ik(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
     return SGDYN_OK;
+  });
+}
+
+int sgdyn_compute_inverse_dynamics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                       const double* qdd, const double* tau_bar, double* q_bar, double* qd_bar,
+                                       double* qdd_bar, int layout, void* stream) {
+  return guarded([&] {
+    if (int rc = check_diff_model(m)) return rc;
+    if (int rc = common_checks(n, layout)) return rc;
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q, "q"}, {qd, "qd"}, {qdd, "qdd"}, {tau_bar, "tau_bar"}})) return rc;
+    for (const void* o : {(const void*)q_bar, (const void*)qd_bar, (const void*)qdd_bar})
+      if (o && !device_accessible(o)) return fail(SGDYN_ERR_NULL, "output is not device memory");
+    Model& Mo = *m->impl;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    const int64_t nv = Mo.nv();
+    VjpArgs a;
+    a.n = n;
+    a.q = make_arr(q, n, Mo.nq_ext(), layout);
+    a.qd = make_arr(qd, n, nv, layout);
+    a.x = make_arr(qdd, n, nv, layout);
+    a.bar = make_arr(tau_bar, n, nv, layout);
+    a.o1 = make_arr(q_bar, n, nv, layout);
+    a.o2 = make_arr(qd_bar, n, nv, layout);
+    a.o3 = make_arr(qdd_bar, n, nv, layout);
+    return launch_status(launch_rnea_vjp(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
+  });
+}
+
+int sgdyn_compute_forward_dynamics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                       const double* tau, const double* qdd_bar, double* q_bar, double* qd_bar,
+                                       double* tau_bar, int layout, void* stream) {
+  return guarded([&] {
+    if (int rc = check_diff_model(m)) return rc;
+    if (int rc = common_checks(n, layout)) return rc;
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q, "q"}, {qd, "qd"}, {tau, "tau"}, {qdd_bar, "qdd_bar"}})) return rc;
+    for (const void* o : {(const void*)q_bar, (const void*)qd_bar, (const void*)tau_bar})
+      if (o && !device_accessible(o)) return fail(SGDYN_ERR_NULL, "output is not device memory");
+    Model& Mo = *m->impl;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    const int64_t nv = Mo.nv();
+    VjpArgs a;
+    a.n = n;
+    a.q = make_arr(q, n, Mo.nq_ext(), layout);
+    a.qd = make_arr(qd, n, nv, layout);
+    a.x = make_arr(tau, n, nv, layout);
+    a.bar = make_arr(qdd_bar, n, nv, layout);
+    a.o1 = make_arr(q_bar, n, nv, layout);
+    a.o2 = make_arr(qd_bar, n, nv, layout);
+    a.o3 = make_arr(tau_bar, n, nv, layout);
+    return launch_status(launch_aba_vjp(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
+  });
+}
+
+int sgdyn_compute_forward_kinematics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* pos_bar,
+                                         const double* rot_bar, double* q_bar, int layout, void* stream) {
+  return guarded([&] {
+    if (int rc = check_diff_model(m)) return rc;
+    if (int rc = common_checks(n, layout)) return rc;
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q, "q"}, {pos_bar, "pos_bar"}, {q_bar, "q_bar"}})) return rc;
+    if (rot_bar && !device_accessible(rot_bar)) return fail(SGDYN_ERR_NULL, "rot_bar is not device memory");
+    Model& Mo = *m->impl;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    FkVjpArgs a;
+    a.n = n;
+    a.q = make_arr(q, n, Mo.nq_ext(), layout);
+    a.pbar = make_arr(pos_bar, n, 3 * int64_t(Mo.nlinks()), layout);
+    a.Rbar = make_arr(rot_bar, n, 9 * int64_t(Mo.nlinks()), layout);
+    a.qbar = make_arr(q_bar, n, Mo.nv(), layout);
+    return launch_status(launch_fk_vjp(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
+  });
+}
+
+static int derivatives(bool aba, const sgdyn_model* m, int64_t n, const double* q, const double* qd, const double* x,
+                       double* d_q, double* d_qd, double* d_x, int layout, void* stream) {
+  return guarded([&] {
+    if (int rc = check_diff_model(m)) return rc;
+    if (int rc = common_checks(n, layout)) return rc;
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q, "q"}, {qd, "qd"}, {x, aba ? "tau" : "qdd"}, {d_q, "d_q"}, {d_qd, "d_qd"}}))
+      return rc;
+    if (d_x && !device_accessible(d_x)) return fail(SGDYN_ERR_NULL, "output is not device memory");
+    Model& Mo = *m->impl;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    const int64_t nv = Mo.nv();
+    DerivArgs a;
+    a.n = n;
+    a.q = make_arr(q, n, Mo.nq_ext(), layout);
+    a.qd = make_arr(qd, n, nv, layout);
+    a.x = make_arr(x, n, nv, layout);
+    a.d_q = make_arr(d_q, n, nv * nv, layout);
+    a.d_qd = make_arr(d_qd, n, nv * nv, layout);
+    a.d_x = make_arr(d_x, n, nv * nv, layout);
+    auto s = static_cast<cudaStream_t>(stream);
+    return launch_status(aba ? launch_aba_derivatives(dm, Mo.njoints(), a, s)
+                             : launch_rnea_derivatives(dm, Mo.njoints(), a, s));
+  });
+}
+
+int sgdyn_compute_rnea_derivatives(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                   const double* qdd, double* dtau_dq, double* dtau_dqd, double* dtau_dqdd,
+                                   int layout, void* stream) {
+  return derivatives(false, m, n, q, qd, qdd, dtau_dq, dtau_dqd, dtau_dqdd, layout, stream);
+}
+
+int sgdyn_compute_aba_derivatives(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
+                                  const double* tau, double* dqdd_dq, double* dqdd_dqd, double* dqdd_dtau,
+                                  int layout, void* stream) {
+  return derivatives(true, m, n, q, qd, tau, dqdd_dq, dqdd_dqd, dqdd_dtau, layout, stream);
+}
+
+static int rollout_checks(const sgdyn_model* m, int64_t n, int T, int K) {
+  if (int rc = check_diff_model(m)) return rc;
+  if (m->impl->has_free_flyer()) return fail(SGDYN_ERR_UNSUPPORTED, "rollouts do not support free-flyer joints");
+  if (n < 0 || T < 0) return fail(SGDYN_ERR_RUNTIME, "negative size");
+  if (K <= 0) return fail(SGDYN_ERR_RUNTIME, "checkpoint_every must be positive");
+  return SGDYN_OK;
+}
+
+int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, const double* q0, const double* qd0,
+                          const double* tau, int checkpoint_every, double* q_ckpt, double* qd_ckpt, double* qT,
+                          double* qdT, void* stream) {
+  return guarded([&] {
+    if (int rc = rollout_checks(m, n, T, checkpoint_every)) return rc;
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q0, "q0"}, {qd0, "qd0"}, {qT, "qT"}, {qdT, "qdT"}})) return rc;
+    if (T > 0)
+      if (int rc = check_ptrs({{tau, "tau"}})) return rc;
+    if ((q_ckpt == nullptr) != (qd_ckpt == nullptr)) return fail(SGDYN_ERR_NULL, "give both checkpoint arrays or none");
+    if (q_ckpt)
+      if (int rc = check_ptrs({{q_ckpt, "q_ckpt"}, {qd_ckpt, "qd_ckpt"}})) return rc;
+    Model& Mo = *m->impl;
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    RolloutArgs a{};
+    a.n = n;
+    a.T = T;
+    a.K = checkpoint_every;
+    a.dt = dt;
+    a.q0 = q0; a.qd0 = qd0; a.tau = tau;
+    a.qT = qT; a.qdT = qdT; a.q_ckpt = q_ckpt; a.qd_ckpt = qd_ckpt;
+    return launch_status(launch_rollout_forward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
+  });
+}
+
+int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_every, int64_t* bytes) {
+  if (!m || !bytes) return fail(SGDYN_ERR_NULL, "null argument");
+  if (checkpoint_every <= 0 || n < 0) return fail(SGDYN_ERR_RUNTIME, "bad sizes");
+  const Model& Mo = *m->impl;
+  *bytes = 8 * n * rollout_scratch_doubles_per_env(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every);
+  return SGDYN_OK;
+}
+
+int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, int checkpoint_every,
+                           const double* q_ckpt, const double* qd_ckpt, const double* tau, const double* qT_bar,
+                           const double* qdT_bar, double* q0_bar, double* qd0_bar, double* tau_bar, double* scratch,
+                           int64_t scratch_bytes, void* stream) {
+  return guarded([&] {
+    if (int rc = rollout_checks(m, n, T, checkpoint_every)) return rc;
+    if (n == 0) return SGDYN_OK;
+    if (int rc = check_ptrs({{q0_bar, "q0_bar"}, {qd0_bar, "qd0_bar"}})) return rc;
+    if (T > 0)
+      if (int rc = check_ptrs({{q_ckpt, "q_ckpt"}, {qd_ckpt, "qd_ckpt"}, {tau, "tau"}, {tau_bar, "tau_bar"},
+                               {scratch, "scratch"}}))
+        return rc;
+    for (const void* o : {(const void*)qT_bar, (const void*)qdT_bar})
+      if (o && !device_accessible(o)) return fail(SGDYN_ERR_NULL, "adjoint input is not device memory");
+    Model& Mo = *m->impl;
+    int64_t need = 8 * n * rollout_scratch_doubles_per_env(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every);
+    if (T > 0 && scratch_bytes < need)
+      return fail(SGDYN_ERR_RUNTIME, "scratch too small: need " + std::to_string(need) + " bytes");
+    int err = 0;
+    const DModel* dm = Mo.device_table(&err);
+    if (!dm) return fail(SGDYN_ERR_CUDA, "model upload failed");
+    RolloutArgs a{};
+    a.n = n;
+    a.T = T;
+    a.K = checkpoint_every;
+    a.dt = dt;
+    a.tau = tau;
+    a.q_ckpt = const_cast<double*>(q_ckpt);
+    a.qd_ckpt = const_cast<double*>(qd_ckpt);
+    a.qT_bar = qT_bar; a.qdT_bar = qdT_bar;
+    a.q0_bar = q0_bar; a.qd0_bar = qd0_bar; a.tau_bar = tau_bar; a.scratch = scratch;
+    return launch_status(launch_rollout_backward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
   });
 }
 

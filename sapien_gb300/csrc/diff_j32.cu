@@ -1,0 +1,20 @@
+// Instantiations of the differentiation kernels for trees of up to 32 joints.
+#include "diff_kernels.cuh"
+
+namespace sgdyn {
+
+#define SG_LAUNCH(kernel, Args)                                                      \
+  cudaError_t launch_##kernel##_j32(const DModel* dm, const Args& a, cudaStream_t s) { \
+    kernel##_kernel<32><<<unsigned((a.n + 31) / 32), 32, 0, s>>>(dm, a);             \
+    return cudaGetLastError();                                                      \
+  }
+SG_LAUNCH(rnea_vjp, VjpArgs)
+SG_LAUNCH(aba_vjp, VjpArgs)
+SG_LAUNCH(fk_vjp, FkVjpArgs)
+SG_LAUNCH(rnea_derivatives, DerivArgs)
+SG_LAUNCH(aba_derivatives, DerivArgs)
+SG_LAUNCH(rollout_forward, RolloutArgs)
+SG_LAUNCH(rollout_backward, RolloutArgs)
+#undef SG_LAUNCH
+
+}  // namespace sgdyn

@@ -1,0 +1,277 @@
+// Differentiation kernels: RNEA / ABA / FK adjoints, dense derivative matrices and the
+// checkpointed semi-implicit-Euler rollout (forward and reverse). One environment per
+// thread; every kernel recomputes the spatial intermediates it needs instead of reading a
+// stored tape, except the rollout backward, which recomputes one checkpoint segment at a
+// time and keeps that segment's intermediates in caller-provided scratch.
+#pragma once
+#include "diff_core.cuh"
+
+namespace sgdyn {
+
+template <int MAXJ>
+struct Ext {
+  static constexpr int MAXV = MAXJ + 5;
+  static constexpr int MAXQ = MAXJ + 6;
+};
+
+template <int MAXJ>
+__device__ __forceinline__ void load_row(const Arr& a, int64_t e, int cols, double* out) {
+  for (int c = 0; c < cols; c++) out[c] = ldv(a, e, c);
+}
+__device__ __forceinline__ void store_row(const Arr& a, int64_t e, int cols, const double* in) {
+  for (int c = 0; c < cols; c++) stv(a, e, c, in[c]);
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rnea_vjp_kernel(const DModel* __restrict__ model, const VjpArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const int nv = model->nv, nq = model->nq_ext;
+  double q[MAXQ], qd[MAXV], qdd[MAXV], tb[MAXV], o1[MAXV], o2[MAXV], o3[MAXV];
+  load_row<MAXJ>(a.q, e, nq, q);
+  load_row<MAXJ>(a.qd, e, nv, qd);
+  load_row<MAXJ>(a.x, e, nv, qdd);
+  load_row<MAXJ>(a.bar, e, nv, tb);
+  DynWork<MAXJ> W;
+  AdjScratch<MAXJ> A;
+  rnea_forward(model, q, qd, qdd, W);
+  rnea_adjoint(model, W, A, tb, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, a.o3.p ? o3 : nullptr, 1.0);
+  if (a.o1.p) store_row(a.o1, e, nv, o1);
+  if (a.o2.p) store_row(a.o2, e, nv, o2);
+  if (a.o3.p) store_row(a.o3, e, nv, o3);
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) aba_vjp_kernel(const DModel* __restrict__ model, const VjpArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const int nv = model->nv, nq = model->nq_ext;
+  double q[MAXQ], qd[MAXV], tau[MAXV], qb[MAXV], qdd[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
+  load_row<MAXJ>(a.q, e, nq, q);
+  load_row<MAXJ>(a.qd, e, nv, qd);
+  load_row<MAXJ>(a.x, e, nv, tau);
+  load_row<MAXJ>(a.bar, e, nv, qb);
+  DynWork<MAXJ> W;
+  AdjScratch<MAXJ> A;
+  aba_forward(model, q, qd, tau, qdd, W);
+  minv_solve(model, W, qb, lam);
+  rnea_adjoint(model, W, A, lam, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, nullptr, -1.0);
+  if (a.o1.p) store_row(a.o1, e, nv, o1);
+  if (a.o2.p) store_row(a.o2, e, nv, o2);
+  if (a.o3.p) store_row(a.o3, e, nv, lam);
+}
+
+// Link pose adjoint: a link at p with rotation R receives the world force
+// (pbar, p x pbar + n_R), n_R = axial part of R Rbar^T (so that tr(Rbar^T [w]x R) = w . n_R);
+// forces are summed over subtrees and projected on the world motion subspaces.
+template <int MAXJ>
+__global__ void __launch_bounds__(32) fk_vjp_kernel(const DModel* __restrict__ model, const FkVjpArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXQ = Ext<MAXJ>::MAXQ;
+  const int nj = model->nj, nq = model->nq_ext, nl = model->nlinks;
+  const DJoint* __restrict__ JT = model_joints(model);
+  const DLink* __restrict__ LT = model_links(model);
+  double q[MAXQ];
+  load_row<MAXJ>(a.q, e, nq, q);
+  DynWork<MAXJ> W;
+  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+  Mot* F = W.pA;
+  for (int i = 1; i < nj; i++) {
+    pose_and_S(JT[i], i, q, W);
+    F[i] = zero;
+  }
+  for (int l = 0; l < nl; l++) {
+    const DLink& L = LT[l];
+    const int j = L.joint;
+    if (j == 0) continue;  // links welded to the base do not move
+    M3 Rl;
+    for (int k = 0; k < 9; k++) Rl.a[k] = L.R[k];
+    const M3 R = mul(W.oR[j], Rl);
+    const V3 p = mul_add(W.oR[j], mk(L.p[0], L.p[1], L.p[2]), W.op[j]);
+    const V3 pb = mk(ldv(a.pbar, e, 3 * l), ldv(a.pbar, e, 3 * l + 1), ldv(a.pbar, e, 3 * l + 2));
+    Mot f{pb, cross(p, pb)};
+    if (a.Rbar.p) {
+      M3 Rb;
+      for (int k = 0; k < 9; k++) Rb.a[k] = ldv(a.Rbar, e, 9 * l + k);
+      const M3 A = mul(R, transpose(Rb));
+      f.w = f.w + mk(A.a[5] - A.a[7], A.a[6] - A.a[2], A.a[1] - A.a[3]);
+    }
+    F[j] = add6(F[j], f);
+  }
+  for (int i = nj - 1; i >= 1; i--) {
+    const DJoint& J = JT[i];
+    for (int k = 0; k < J.nv; k++) stv(a.qbar, e, J.vcol + k, dot6(W.Sw[J.ivx + k], F[i]));
+    if (J.parent > 0) F[J.parent] = add6(F[J.parent], F[i]);
+  }
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const int nv = model->nv, nq = model->nq_ext;
+  double q[MAXQ], qd[MAXV], qdd[MAXV], tb[MAXV], o1[MAXV], o2[MAXV], o3[MAXV];
+  load_row<MAXJ>(a.q, e, nq, q);
+  load_row<MAXJ>(a.qd, e, nv, qd);
+  load_row<MAXJ>(a.x, e, nv, qdd);
+  DynWork<MAXJ> W;
+  AdjScratch<MAXJ> A;
+  rnea_forward(model, q, qd, qdd, W);
+  for (int r = 0; r < nv; r++) {
+    for (int c = 0; c < nv; c++) tb[c] = (c == r) ? 1.0 : 0.0;
+    rnea_adjoint(model, W, A, tb, o1, o2, a.d_x.p ? o3 : nullptr, 1.0);
+    for (int c = 0; c < nv; c++) {
+      stv(a.d_q, e, r * nv + c, o1[c]);
+      stv(a.d_qd, e, r * nv + c, o2[c]);
+      if (a.d_x.p) stv(a.d_x, e, r * nv + c, o3[c]);
+    }
+  }
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const int nv = model->nv, nq = model->nq_ext;
+  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV], er[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
+  load_row<MAXJ>(a.q, e, nq, q);
+  load_row<MAXJ>(a.qd, e, nv, qd);
+  load_row<MAXJ>(a.x, e, nv, tau);
+  DynWork<MAXJ> W;
+  AdjScratch<MAXJ> A;
+  aba_forward(model, q, qd, tau, qdd, W);
+  for (int r = 0; r < nv; r++) {
+    for (int c = 0; c < nv; c++) er[c] = (c == r) ? 1.0 : 0.0;
+    minv_solve(model, W, er, lam);
+    rnea_adjoint(model, W, A, lam, o1, o2, nullptr, -1.0);
+    for (int c = 0; c < nv; c++) {
+      stv(a.d_q, e, r * nv + c, o1[c]);
+      stv(a.d_qd, e, r * nv + c, o2[c]);
+      if (a.d_x.p) stv(a.d_x, e, r * nv + c, lam[c]);
+    }
+  }
+}
+
+// ---- rollouts ---------------------------------------------------------------------
+
+// q <- q + dt qd for angle / slide coordinates (models without free flyers).
+__device__ __forceinline__ void euler_positions(const DModel* model, double* q, const double* qd, double dt) {
+  const DJoint* __restrict__ JT = model_joints(model);
+  for (int i = 1; i < model->nj; i++) q[JT[i].qcol] = fma(dt, qd[JT[i].vcol], q[JT[i].qcol]);
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rollout_forward_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const int nv = model->nv, nq = model->nq_ext;
+  const int64_t n = a.n;
+  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
+  for (int c = 0; c < nq; c++) q[c] = a.q0[e * nq + c];
+  for (int c = 0; c < nv; c++) qd[c] = a.qd0[e * nv + c];
+  DynWork<MAXJ> W;
+  for (int t = 0; t < a.T; t++) {
+    if (a.q_ckpt && t % a.K == 0) {
+      const int64_t s = t / a.K;
+      for (int c = 0; c < nq; c++) a.q_ckpt[(s * n + e) * nq + c] = q[c];
+      for (int c = 0; c < nv; c++) a.qd_ckpt[(s * n + e) * nv + c] = qd[c];
+    }
+    for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
+    aba_forward(model, q, qd, tau, qdd, W);
+    for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
+    euler_positions(model, q, qd, a.dt);
+  }
+  for (int c = 0; c < nq; c++) a.qT[e * nq + c] = q[c];
+  for (int c = 0; c < nv; c++) a.qdT[e * nv + c] = qd[c];
+}
+
+// Per step of a segment the scratch holds, structure-of-arrays over environments:
+// S (6 per velocity), U (6 per velocity), then per joint D^-1 (1), v (6), a (6), I v (6),
+// world inertia (10); plus the free-flyer factor (21).
+__host__ __device__ inline int64_t stash_doubles_per_step(int nj, int nq, int nv) {
+  (void)nq;
+  return 12 * int64_t(nv) + int64_t(nj) * 29 + 21;
+}
+
+template <int MAXJ>
+__device__ void stash_io(const DModel* __restrict__ model, DynWork<MAXJ>& W, double* base, int64_t n, int64_t e,
+                         bool store) {
+  const DJoint* __restrict__ JT = model_joints(model);
+  const int nj = model->nj, nv = model->nv;
+  int64_t f = 0;
+  auto io = [&](double& x) {
+    if (store) base[f * n + e] = x;
+    else x = base[f * n + e];
+    f++;
+  };
+  auto io6 = [&](Mot& m) {
+    io(m.v.x); io(m.v.y); io(m.v.z); io(m.w.x); io(m.w.y); io(m.w.z);
+  };
+  for (int k = 0; k < nv; k++) io6(W.Sw[k]);
+  for (int k = 0; k < nv; k++) io6(W.Uv[k]);
+  for (int i = 1; i < nj; i++) {
+    io(W.Dinv[i]);
+    io6(W.vel[i]);
+    io6(W.acc[i]);
+    io6(W.hY[i]);
+    RBI& Y = W.Iw[i];
+    io(Y.m); io(Y.h.x); io(Y.h.y); io(Y.h.z);
+    for (int k = 0; k < 6; k++) io(Y.I[k]);
+  }
+  for (int k = 0; k < 21; k++) io(W.Lff[k]);
+  (void)JT;
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rollout_backward_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const int nv = model->nv, nq = model->nq_ext, nj = model->nj;
+  const int64_t n = a.n;
+  const int64_t per_step = stash_doubles_per_step(nj, nq, nv);
+  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV], qb[MAXV], qdb[MAXV], qddb[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
+  for (int c = 0; c < nq; c++) qb[c] = a.qT_bar ? a.qT_bar[e * nq + c] : 0.0;
+  for (int c = 0; c < nv; c++) qdb[c] = a.qdT_bar ? a.qdT_bar[e * nv + c] : 0.0;
+  DynWork<MAXJ> W;
+  AdjScratch<MAXJ> A;
+  const int nseg = (a.T + a.K - 1) / a.K;
+  for (int s = nseg - 1; s >= 0; s--) {
+    const int t0 = s * a.K, t1 = min(a.T, t0 + a.K);
+    for (int c = 0; c < nq; c++) q[c] = a.q_ckpt[(int64_t(s) * n + e) * nq + c];
+    for (int c = 0; c < nv; c++) qd[c] = a.qd_ckpt[(int64_t(s) * n + e) * nv + c];
+    // recompute the segment, keeping every step's intermediates
+    for (int t = t0; t < t1; t++) {
+      double* base = a.scratch + int64_t(t - t0) * per_step * n;
+      for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
+      aba_forward(model, q, qd, tau, qdd, W);
+      stash_io(model, W, base, n, e, true);
+      for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
+      euler_positions(model, q, qd, a.dt);
+    }
+    // reverse through the segment
+    for (int t = t1 - 1; t >= t0; t--) {
+      double* base = a.scratch + int64_t(t - t0) * per_step * n;
+      // q' = q + dt qd'  and  qd' = qd + dt qdd
+      const DJoint* __restrict__ JT = model_joints(model);
+      for (int i = 1; i < nj; i++) qdb[JT[i].vcol] = fma(a.dt, qb[JT[i].qcol], qdb[JT[i].vcol]);
+      for (int c = 0; c < nv; c++) qddb[c] = a.dt * qdb[c];
+      stash_io(model, W, base, n, e, false);
+      minv_solve(model, W, qddb, lam);
+      for (int c = 0; c < nv; c++) a.tau_bar[(int64_t(t) * n + e) * nv + c] = lam[c];
+      rnea_adjoint(model, W, A, lam, o1, o2, nullptr, -1.0);
+      for (int i = 1; i < nj; i++) qb[JT[i].qcol] += o1[JT[i].vcol];
+      for (int c = 0; c < nv; c++) qdb[c] += o2[c];
+    }
+  }
+  for (int c = 0; c < nq; c++) a.q0_bar[e * nq + c] = qb[c];
+  for (int c = 0; c < nv; c++) a.qd0_bar[e * nv + c] = qdb[c];
+}
+
+}  // namespace sgdyn

@@ -43,6 +43,42 @@ struct IkArgs {
   int* success;
 };
 
+// Adjoint (vector-Jacobian product) of RNEA or ABA.
+//   RNEA: x = qdd, bar = taubar -> o1 = qbar, o2 = qdbar, o3 = qddbar
+//   ABA:  x = tau, bar = qddbar -> o1 = qbar, o2 = qdbar, o3 = taubar
+struct VjpArgs {
+  int64_t n;
+  Arr q, qd, x, bar, o1, o2, o3;
+};
+
+// Adjoint of link positions (pbar, n x nlinks*3) and rotations (Rbar, nlinks*9, optional).
+struct FkVjpArgs {
+  int64_t n;
+  Arr q, pbar, Rbar, qbar;
+};
+
+// Dense derivative matrices, rows = outputs, columns = tangent inputs.
+//   RNEA: x = qdd -> d_q = dtau/dq, d_qd = dtau/dqd, d_x = dtau/dqdd (= M)
+//   ABA:  x = tau -> d_q = dqdd/dq, d_qd = dqdd/dqd, d_x = dqdd/dtau (= M^-1)
+struct DerivArgs {
+  int64_t n;
+  Arr q, qd, x, d_q, d_qd, d_x;
+};
+
+// Semi-implicit Euler rollout qd += dt ABA(q, qd, tau_t); q += dt qd, with q / qd
+// checkpoints every K steps (segment s starts at step s K). Contiguous env-major arrays:
+// q0 [n][nq], qd0 [n][nv], tau [T][n][nv], q_ckpt [C][n][nq], qd_ckpt [C][n][nv].
+struct RolloutArgs {
+  int64_t n;
+  int T, K;
+  double dt;
+  const double *q0, *qd0, *tau;
+  double *qT, *qdT, *q_ckpt, *qd_ckpt;
+  // backward
+  const double *qT_bar, *qdT_bar;
+  double *q0_bar, *qd0_bar, *tau_bar, *scratch;
+};
+
 // Joint-count bucket for the per-thread stash (16, 32 or 64 joints incl. universe).
 int stash_bucket(int nj);
 
@@ -51,5 +87,14 @@ cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cu
 cudaError_t launch_link_jacobian(const DModel* dm, int nj, const LinkJacArgs& a, cudaStream_t s);
 cudaError_t launch_coriolis(const DModel* dm, int nj, const CoriolisArgs& a, cudaStream_t s);
 cudaError_t launch_ik(const DModel* dm, int nj, const IkArgs& a, cudaStream_t s);
+cudaError_t launch_rnea_vjp(const DModel* dm, int nj, const VjpArgs& a, cudaStream_t s);
+cudaError_t launch_aba_vjp(const DModel* dm, int nj, const VjpArgs& a, cudaStream_t s);
+cudaError_t launch_fk_vjp(const DModel* dm, int nj, const FkVjpArgs& a, cudaStream_t s);
+cudaError_t launch_rnea_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
+cudaError_t launch_aba_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
+cudaError_t launch_rollout_forward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
+cudaError_t launch_rollout_backward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
+// doubles of rollout-backward scratch per environment
+int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K);
 
 }  // namespace sgdyn

@@ -63,3 +63,35 @@ cudaError_t launch_ik(const DModel* dm, int nj, const IkArgs& a, cudaStream_t s)
 }
 
 }  // namespace sgdyn
+
+#include "diff_kernels.cuh"
+
+namespace sgdyn {
+
+#define SG_DISPATCH(kernel, Args)                                                        \
+  cudaError_t launch_##kernel##_j16(const DModel*, const Args&, cudaStream_t);            \
+  cudaError_t launch_##kernel##_j32(const DModel*, const Args&, cudaStream_t);            \
+  cudaError_t launch_##kernel##_j64(const DModel*, const Args&, cudaStream_t);            \
+  cudaError_t launch_##kernel(const DModel* dm, int nj, const Args& a, cudaStream_t s) {  \
+    if (a.n <= 0) return cudaSuccess;                                                    \
+    switch (stash_bucket(nj)) {                                                          \
+      case 16: return launch_##kernel##_j16(dm, a, s);                                   \
+      case 32: return launch_##kernel##_j32(dm, a, s);                                   \
+      case 64: return launch_##kernel##_j64(dm, a, s);                                   \
+      default: return cudaErrorInvalidValue;                                             \
+    }                                                                                    \
+  }
+SG_DISPATCH(rnea_vjp, VjpArgs)
+SG_DISPATCH(aba_vjp, VjpArgs)
+SG_DISPATCH(fk_vjp, FkVjpArgs)
+SG_DISPATCH(rnea_derivatives, DerivArgs)
+SG_DISPATCH(aba_derivatives, DerivArgs)
+SG_DISPATCH(rollout_forward, RolloutArgs)
+SG_DISPATCH(rollout_backward, RolloutArgs)
+#undef SG_DISPATCH
+
+int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K) {
+  return int64_t(K) * stash_doubles_per_step(nj, nq, nv);
+}
+
+}  // namespace sgdyn

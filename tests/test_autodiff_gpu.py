@@ -1,0 +1,216 @@
+"""GPU adjoint kernels against FP64 central finite differences of the CPU oracle.
+
+Gradient tolerance: 1e-6 relative (normwise per environment) for FD with h = 1e-6;
+exact identities (dtau/dqdd = M, dqdd/dtau = M^-1, VJP = row combination of the dense
+derivatives, checkpoint-interval invariance) at 1e-10 or tighter.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from sapien_gb300 import PinocchioModel, autodiff as ad, synthetic as syn
+
+pytestmark = pytest.mark.gpu
+H = 1e-6
+
+
+def T():
+    import torch
+
+    return torch
+
+
+def pair(robot):
+    pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    return pm, o
+
+
+def cu(a):
+    return T().from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def rel(g, r):
+    return np.abs(g - r).max() / max(np.abs(r).max(), 1e-300)
+
+
+FIXED = {
+    "arm9": lambda: syn.arm_with_fingers(),
+    "arm9_sapien": lambda: syn.arm_with_fingers(sapien_style=True),
+    "mixed_chain": lambda: syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                                "continuous", "prismatic"]),
+}
+
+
+def fd_grad(f, x, w):
+    """w . d f / d x by central differences (x, w 1-D)."""
+    g = np.zeros(x.size)
+    for k in range(x.size):
+        e = np.zeros(x.size)
+        e[k] = H
+        g[k] = (w @ f(x + e) - w @ f(x - e)) / (2 * H)
+    return g
+
+
+@pytest.mark.parametrize("name", list(FIXED))
+def test_rnea_and_aba_vjp_match_finite_differences(name):
+    robot = FIXED[name]()
+    pm, o = pair(robot)
+    n = 6
+    q, qd, qdd, tau = robot.sample(n, seed=81)
+    w = np.random.default_rng(2).normal(size=(n, robot.nv))
+    qb, qdb, qddb = (x.cpu().numpy() for x in ad.inverse_dynamics_vjp(pm, cu(q), cu(qd), cu(qdd), cu(w)))
+    ab = [x.cpu().numpy() for x in ad.forward_dynamics_vjp(pm, cu(q), cu(qd), cu(tau), cu(w))]
+    for e in range(n):
+        assert rel(qb[e], fd_grad(lambda x: o.compute_inverse_dynamics(x, qd[e], qdd[e]), q[e], w[e])) < 1e-6
+        assert rel(qdb[e], fd_grad(lambda x: o.compute_inverse_dynamics(q[e], x, qdd[e]), qd[e], w[e])) < 1e-6
+        assert rel(qddb[e], fd_grad(lambda x: o.compute_inverse_dynamics(q[e], qd[e], x), qdd[e], w[e])) < 1e-6
+        assert rel(ab[0][e], fd_grad(lambda x: o.compute_forward_dynamics(x, qd[e], tau[e]), q[e], w[e])) < 1e-6
+        assert rel(ab[1][e], fd_grad(lambda x: o.compute_forward_dynamics(q[e], x, tau[e]), qd[e], w[e])) < 1e-6
+        assert rel(ab[2][e], fd_grad(lambda x: o.compute_forward_dynamics(q[e], qd[e], x), tau[e], w[e])) < 1e-6
+
+
+def test_fk_vjp_matches_finite_differences():
+    robot = syn.arm_with_fingers(sapien_style=True)
+    pm, o = pair(robot)
+    n, L = 4, len(robot.link_names)
+    q, _, _, _ = robot.sample(n, seed=91)
+    rng = np.random.default_rng(3)
+    pb = rng.normal(size=(n, L, 3))
+    rb = rng.normal(size=(n, L, 3, 3))
+    qb = ad.forward_kinematics_vjp(pm, cu(q), cu(pb), cu(rb)).cpu().numpy()
+    for e in range(n):
+        def f(x):
+            Tm = o.link_poses(x)
+            return np.concatenate([Tm[:, :3, 3].ravel(), Tm[:, :3, :3].ravel()])
+        wv = np.concatenate([pb[e].ravel(), rb[e].ravel()])
+        assert rel(qb[e], fd_grad(f, q[e], wv)) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["humanoid", "quadruped18", "arm9"])
+def test_dense_derivatives_match_finite_differences(name):
+    robot = {"humanoid": syn.humanoid, "quadruped18": syn.quadruped, "arm9": syn.arm_with_fingers}[name]()
+    pm, o = pair(robot)
+    n, nv = 3, robot.nv
+    q, qd, qdd, tau = robot.sample(n, seed=97)
+    dq, dqd, M = (x.cpu().numpy() for x in ad.rnea_derivatives(pm, cu(q), cu(qd), cu(qdd)))
+    aq, aqd, Minv = (x.cpu().numpy() for x in ad.aba_derivatives(pm, cu(q), cu(qd), cu(tau)))
+    for e in range(n):
+        # q derivatives in the tangent space: perturb with integrate(q, +-h e_k)
+        fdq_t = np.zeros((nv, nv))
+        fdq_a = np.zeros((nv, nv))
+        for k in range(nv):
+            d = np.zeros(nv)
+            d[k] = H
+            qp, qm = o.integrate(q[e], d), o.integrate(q[e], -d)
+            fdq_t[:, k] = (o.compute_inverse_dynamics(qp, qd[e], qdd[e]) - o.compute_inverse_dynamics(qm, qd[e], qdd[e])) / (2 * H)
+            fdq_a[:, k] = (o.compute_forward_dynamics(qp, qd[e], tau[e]) - o.compute_forward_dynamics(qm, qd[e], tau[e])) / (2 * H)
+        fdqd_t = np.stack([(o.compute_inverse_dynamics(q[e], qd[e] + H * np.eye(nv)[k], qdd[e])
+                            - o.compute_inverse_dynamics(q[e], qd[e] - H * np.eye(nv)[k], qdd[e])) / (2 * H)
+                           for k in range(nv)], axis=1)
+        fdqd_a = np.stack([(o.compute_forward_dynamics(q[e], qd[e] + H * np.eye(nv)[k], tau[e])
+                            - o.compute_forward_dynamics(q[e], qd[e] - H * np.eye(nv)[k], tau[e])) / (2 * H)
+                           for k in range(nv)], axis=1)
+        assert rel(dq[e], fdq_t) < 1e-6
+        assert rel(dqd[e], fdqd_t) < 1e-6
+        assert rel(aq[e], fdq_a) < 1e-6
+        assert rel(aqd[e], fdqd_a) < 1e-6
+        Mref = o.compute_generalized_mass_matrix(q[e])
+        assert rel(M[e], Mref) < 1e-10
+        assert rel(Minv[e], np.linalg.inv(Mref)) < 1e-8
+
+
+def test_vjp_equals_dense_rows():
+    robot = syn.arm_with_fingers()
+    pm, _ = pair(robot)
+    q, qd, qdd, tau = robot.sample(16, seed=7)
+    w = np.random.default_rng(5).normal(size=(16, robot.nv))
+    dq, dqd, M = (x.cpu().numpy() for x in ad.rnea_derivatives(pm, cu(q), cu(qd), cu(qdd)))
+    qb, qdb, qddb = (x.cpu().numpy() for x in ad.inverse_dynamics_vjp(pm, cu(q), cu(qd), cu(qdd), cu(w)))
+    assert rel(qb, np.einsum("er,erc->ec", w, dq)) < 1e-12
+    assert rel(qdb, np.einsum("er,erc->ec", w, dqd)) < 1e-12
+    assert rel(qddb, np.einsum("er,erc->ec", w, M)) < 1e-12
+
+
+def test_autograd_functions():
+    torch = T()
+    robot = syn.arm_with_fingers()
+    pm, o = pair(robot)
+    q, qd, qdd, tau = robot.sample(5, seed=11)
+    qt, qdt, qddt = (cu(x).requires_grad_() for x in (q, qd, qdd))
+    out = ad.inverse_dynamics(pm, qt, qdt, qddt)
+    out.pow(2).sum().backward()
+    tb = 2 * out.detach()
+    ref = ad.inverse_dynamics_vjp(pm, cu(q), cu(qd), cu(qdd), tb)
+    for g, r in zip((qt.grad, qdt.grad, qddt.grad), ref):
+        assert torch.equal(g, r)
+    qt2 = cu(q).requires_grad_()
+    pos = ad.link_positions(pm, qt2)
+    pos[:, robot.ee_link].sum().backward()
+    pb = np.zeros((5, len(robot.link_names), 3))
+    pb[:, robot.ee_link] = 1
+    assert rel(qt2.grad.cpu().numpy(), ad.forward_kinematics_vjp(pm, cu(q), cu(pb)).cpu().numpy()) < 1e-14
+
+
+def _rollout_setup(n=16, T=200, seed=123):
+    robot = syn.arm_with_fingers()
+    pm, o = pair(robot)
+    q0, qd0, _, _ = robot.sample(n, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    tau = rng.normal(scale=5.0, size=(T, n, robot.nv))
+    targets = rng.uniform(-0.5, 0.5, size=(n, 3))
+    return robot, pm, o, q0, qd0, tau, targets
+
+
+def test_rollout_forward_matches_oracle():
+    robot, pm, o, q0, qd0, tau, targets = _rollout_setup()
+    qT, qdT, _, _ = ad.rollout_forward(pm, cu(q0), cu(qd0), cu(tau), 1.0 / 500)
+    rq, rqd, _ = o.rollout(q0, qd0, tau, 1.0 / 500, robot.ee_link, targets)
+    assert rel(qT.cpu().numpy(), rq) < 1e-9
+    assert rel(qdT.cpu().numpy(), rqd) < 1e-9
+
+
+def test_rollout_gradient_matches_finite_differences():
+    """Config: 9-DoF arm, T = 200 steps at dt = 1/500, tau ~ N(0, 5) per step, q/qd
+    checkpoints every 20 steps, loss = sum |p_ee(q_T) - target|^2, 16 environments."""
+    torch = T()
+    robot, pm, o, q0, qd0, tau, targets = _rollout_setup()
+    dt, ee = 1.0 / 500, robot.ee_link
+    q0t, qd0t, taut = cu(q0).requires_grad_(), cu(qd0).requires_grad_(), cu(tau).requires_grad_()
+    qT, _ = ad.rollout(pm, q0t, qd0t, taut, dt, checkpoint_every=20)
+    pos = ad.link_positions(pm, qT)[:, ee]
+    loss = ((pos - cu(targets)) ** 2).sum()
+    loss.backward()
+    g_q0, g_qd0, g_tau = q0t.grad.cpu().numpy(), qd0t.grad.cpu().numpy(), taut.grad.cpu().numpy()
+
+    def L(q0_, qd0_, tau_):
+        return o.rollout(q0_, qd0_, tau_, dt, ee, targets)[2]  # per-env losses
+
+    n, nv = q0.shape
+    fq, fqd = np.zeros_like(q0), np.zeros_like(qd0)
+    for k in range(nv):
+        e = np.zeros(nv)
+        e[k] = H
+        fq[:, k] = (L(q0 + e, qd0, tau) - L(q0 - e, qd0, tau)) / (2 * H)
+        fqd[:, k] = (L(q0, qd0 + e, tau) - L(q0, qd0 - e, tau)) / (2 * H)
+    for env in range(n):
+        assert rel(g_q0[env], fq[env]) < 1e-6
+        assert rel(g_qd0[env], fqd[env]) < 1e-6
+    rng = np.random.default_rng(9)
+    for _ in range(12):
+        t, k = int(rng.integers(0, tau.shape[0])), int(rng.integers(0, nv))
+        d = np.zeros_like(tau)
+        d[t, :, k] = H
+        fd = (L(q0, qd0, tau + d) - L(q0, qd0, tau - d)) / (2 * H)
+        assert np.abs(g_tau[t, :, k] - fd).max() <= 1e-6 * max(np.abs(g_tau[:, :, k]).max(), 1e-12)
+    # checkpoint interval does not change the result
+    q0b1, qd0b1, tb1 = ad.rollout_backward(pm, *ad.rollout_forward(pm, cu(q0), cu(qd0), cu(tau), dt, 1)[2:], cu(tau),
+                                           dt, 1, qT_bar=torch.ones_like(qT))
+    q0b2, qd0b2, tb2 = ad.rollout_backward(pm, *ad.rollout_forward(pm, cu(q0), cu(qd0), cu(tau), dt, 200)[2:],
+                                           cu(tau), dt, 200, qT_bar=torch.ones_like(qT))
+    assert rel(q0b1.cpu().numpy(), q0b2.cpu().numpy()) < 1e-12
+    assert rel(tb1.cpu().numpy(), tb2.cpu().numpy()) < 1e-12
