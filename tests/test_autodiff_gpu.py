@@ -200,13 +200,14 @@ def test_rollout_gradient_matches_finite_differences():
     for env in range(n):
         assert rel(g_q0[env], fq[env]) < 1e-6
         assert rel(g_qd0[env], fqd[env]) < 1e-6
+    # tau: each entry moves the loss by O(dt^2), below central-difference noise, so compare
+    # directional derivatives along random directions of the whole [T, nv] control sequence
     rng = np.random.default_rng(9)
-    for _ in range(12):
-        t, k = int(rng.integers(0, tau.shape[0])), int(rng.integers(0, nv))
-        d = np.zeros_like(tau)
-        d[t, :, k] = H
-        fd = (L(q0, qd0, tau + d) - L(q0, qd0, tau - d)) / (2 * H)
-        assert np.abs(g_tau[t, :, k] - fd).max() <= 1e-6 * max(np.abs(g_tau[:, :, k]).max(), 1e-12)
+    for _ in range(4):
+        D = rng.normal(size=tau.shape)
+        fd = (L(q0, qd0, tau + H * D) - L(q0, qd0, tau - H * D)) / (2 * H)
+        dd = np.einsum("tek,tek->e", g_tau, D)
+        assert np.abs(dd - fd).max() <= 1e-6 * np.abs(fd).max()
     # checkpoint interval does not change the result
     q0b1, qd0b1, tb1 = ad.rollout_backward(pm, *ad.rollout_forward(pm, cu(q0), cu(qd0), cu(tau), dt, 1)[2:], cu(tau),
                                            dt, 1, qT_bar=torch.ones_like(qT))
