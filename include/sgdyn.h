@@ -189,6 +189,20 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
                            const double* qdT_bar, double* q0_bar, double* qd0_bar, double* tau_bar, double* scratch,
                            int64_t scratch_bytes, void* stream);
 
+/* Same reverse pass as sgdyn_rollout_backward for callers that must not allocate device
+ * memory while they run (real-time loops that reserve everything at start-up, plug-ins
+ * whose host owns the memory budget). No counterpart in the reference. Its scratch is a
+ * fixed SGDYN_NOALLOC_SCRATCH_BYTES device array that the library holds on every GPU that
+ * loads it, until exit; calls needing more (sgdyn_rollout_scratch_bytes) fail with
+ * SGDYN_ERR_RUNTIME. It calls no allocator: the model must already be on the device
+ * (sgdyn_model_upload). The first call on a device looks the array up (make it before any
+ * stream capture). All calls share the array: calls that overlap on the GPU race. */
+#define SGDYN_NOALLOC_SCRATCH_BYTES (64LL << 20)
+int sgdyn_rollout_backward_noalloc(const sgdyn_model* m, int64_t n, int T, double dt, int checkpoint_every,
+                                   const double* q_ckpt, const double* qd_ckpt, const double* tau,
+                                   const double* qT_bar, const double* qdT_bar, double* q0_bar, double* qd0_bar,
+                                   double* tau_bar, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,7 @@ EXPORTED = (
     "sgdyn_rollout_forward",
     "sgdyn_rollout_scratch_bytes",
     "sgdyn_rollout_backward",
+    "sgdyn_rollout_backward_noalloc",
 )
 
 _lib = None
@@ -114,6 +115,7 @@ def load():
     L.sgdyn_rollout_forward.argtypes = [vp, i64, i32, dbl, vp, vp, vp, i32, vp, vp, vp, vp, vp]
     L.sgdyn_rollout_scratch_bytes.argtypes = [vp, i64, i32, P(i64)]
     L.sgdyn_rollout_backward.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp]
+    L.sgdyn_rollout_backward_noalloc.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -163,6 +163,11 @@ int launch_status(cudaError_t e) {
 }  // namespace
 }  // namespace sgdyn
 
+namespace sgdyn {
+// Records a message for sgdyn_last_error() from entry points defined in other files.
+int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace sgdyn
+
 using namespace sgdyn;
 
 extern "C" {

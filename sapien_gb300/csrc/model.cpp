@@ -421,6 +421,14 @@ const DModel* Model::device_table(int* err) {
   return static_cast<const DModel*>(p);
 }
 
+const DModel* Model::find_device_table() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = dev_.find(dev);
+  return it == dev_.end() ? nullptr : static_cast<const DModel*>(it->second);
+}
+
 Model::~Model() {
   for (auto& kv : dev_) {
     int cur;

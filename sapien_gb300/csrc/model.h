@@ -57,6 +57,9 @@ class Model {
 
   // Device table for the current CUDA device (uploaded on first use).
   const DModel* device_table(int* err);
+  // Device table for the current CUDA device if it was already uploaded, else null;
+  // never allocates.
+  const DModel* find_device_table();
   // Host copy of the packed table (for tests and for the heterogeneous packer).
   const std::vector<unsigned char>& host_table() const { return table_; }
 

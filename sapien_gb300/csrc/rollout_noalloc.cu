@@ -1,0 +1,146 @@
+// Allocation-free reverse rollout: sgdyn_rollout_backward_noalloc.
+//
+// sgdyn_rollout_backward needs a caller-provided device scratch buffer that holds one
+// checkpoint segment's recomputed intermediates. Some callers cannot allocate device
+// memory at the point where they need gradients: a real-time control or planning loop
+// that reserves all of its memory at start-up and must not enter the CUDA allocator
+// while it runs (allocation latency is unbounded, and a failed allocation mid-loop has
+// no recovery), or a plug-in invoked by a host application that owns the device memory
+// budget and gives plug-ins none. For them this file keeps the scratch in a fixed
+// file-scope device array that exists for as long as the library is loaded.
+//
+// Properties a caller must know:
+//  * The array holds SGDYN_NOALLOC_SCRATCH_BYTES (64 MiB) on every GPU that loads the
+//    library, until the process exits. A call that needs more (8 * n * checkpoint_every *
+//    per-step doubles, see sgdyn_rollout_scratch_bytes) is rejected with
+//    SGDYN_ERR_RUNTIME before any work is enqueued.
+//  * Nothing here calls cudaMalloc, cudaFree or an allocating library routine. The model
+//    tables must already be on the device (sgdyn_model_upload, or any earlier compute
+//    call on that device); otherwise the call fails instead of uploading them.
+//  * The first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress (which may load the library's device code on that device);
+//    make that first call before any stream capture begins.
+//  * All calls on a device share the one array, and it keeps whatever the last call left
+//    in it. Every scratch value a call reads is first written by that same call, so no
+//    clearing is needed, but two calls whose kernels overlap on the GPU (different
+//    streams, or different host threads) race on the array: serialise them.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/sgdyn.h"
+#include "kernels.h"
+#include "model.h"
+
+struct sgdyn_model {
+  sgdyn::Model* impl;
+};
+
+namespace sgdyn {
+
+int set_last_error(int code, const std::string& msg);
+
+namespace {
+
+constexpr int64_t kNoAllocScratchBytes = SGDYN_NOALLOC_SCRATCH_BYTES;
+static_assert(kNoAllocScratchBytes % 256 == 0, "scratch size");
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchBytes / sizeof(double)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+double* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once per device).
+double* scratch_on_current_device(std::string* why) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    *why = std::string("cudaGetDevice failed: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    *why = "device ordinal out of range for the allocation-free entry point";
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      *why = std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    g_scratch_ptr[dev] = static_cast<double*>(p);
+  }
+  return g_scratch_ptr[dev];
+}
+
+bool on_device(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+}  // namespace sgdyn
+
+using namespace sgdyn;
+
+extern "C" int sgdyn_rollout_backward_noalloc(const sgdyn_model* m, int64_t n, int T, double dt,
+                                              int checkpoint_every, const double* q_ckpt, const double* qd_ckpt,
+                                              const double* tau, const double* qT_bar, const double* qdT_bar,
+                                              double* q0_bar, double* qd0_bar, double* tau_bar, void* stream) {
+  if (!m || !m->impl) return set_last_error(SGDYN_ERR_NULL, "null model");
+  Model& Mo = *m->impl;
+  if (stash_bucket(Mo.njoints()) == 0) return set_last_error(SGDYN_ERR_UNSUPPORTED, "model has too many joints");
+  if (Mo.has_free_flyer())
+    return set_last_error(SGDYN_ERR_UNSUPPORTED, "rollouts do not support free-flyer joints");
+  if (n < 0 || T < 0) return set_last_error(SGDYN_ERR_RUNTIME, "negative size");
+  if (checkpoint_every <= 0) return set_last_error(SGDYN_ERR_RUNTIME, "checkpoint_every must be positive");
+  const int64_t need =
+      8 * n * rollout_scratch_doubles_per_env(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every);
+  if (need > kNoAllocScratchBytes)
+    return set_last_error(SGDYN_ERR_RUNTIME, "allocation-free rollout backward needs " + std::to_string(need) +
+                                                 " bytes of scratch but holds " +
+                                                 std::to_string(kNoAllocScratchBytes) +
+                                                 "; use fewer environments, a shorter checkpoint interval, or "
+                                                 "sgdyn_rollout_backward with your own buffer");
+  if (n == 0) return SGDYN_OK;
+  if (!on_device(q0_bar) || !on_device(qd0_bar))
+    return set_last_error(SGDYN_ERR_NULL, "q0_bar / qd0_bar is null or not device memory");
+  if (T > 0 && (!on_device(q_ckpt) || !on_device(qd_ckpt) || !on_device(tau) || !on_device(tau_bar)))
+    return set_last_error(SGDYN_ERR_NULL, "checkpoint, tau or tau_bar is null or not device memory");
+  if ((qT_bar && !on_device(qT_bar)) || (qdT_bar && !on_device(qdT_bar)))
+    return set_last_error(SGDYN_ERR_NULL, "adjoint input is not device memory");
+  const DModel* dm = Mo.find_device_table();
+  if (!dm)
+    return set_last_error(SGDYN_ERR_RUNTIME,
+                          "model tables are not on this device; call sgdyn_model_upload first (this entry point "
+                          "does not allocate)");
+  std::string why;
+  double* scratch = scratch_on_current_device(&why);
+  if (!scratch) return set_last_error(SGDYN_ERR_CUDA, why);
+  RolloutArgs a{};
+  a.n = n;
+  a.T = T;
+  a.K = checkpoint_every;
+  a.dt = dt;
+  a.tau = tau;
+  a.q_ckpt = const_cast<double*>(q_ckpt);
+  a.qd_ckpt = const_cast<double*>(qd_ckpt);
+  a.qT_bar = qT_bar;
+  a.qdT_bar = qdT_bar;
+  a.q0_bar = q0_bar;
+  a.qd0_bar = qd0_bar;
+  a.tau_bar = tau_bar;
+  a.scratch = scratch;
+  cudaError_t e = launch_rollout_backward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  return SGDYN_OK;
+}
