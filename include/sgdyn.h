@@ -131,6 +131,27 @@ int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, 
                                      const double* q0, const int* mask, double eps, int max_iterations, double dt,
                                      double damp, double* q_out, int* success, double* err, int layout, void* stream);
 
+/* ---- heterogeneous batches (addition: the reference evaluates one robot per call) ------
+ * Robots of different size and topology in one persistent launch. A batch is planned once
+ * (tables packed, environments grouped per model into tiles of up to 32, tiles ordered by
+ * descending velocity dimension) and stepped many times; a step allocates nothing, so it
+ * can be recorded into a CUDA graph. Arrays are row-major and padded to the batch maxima:
+ * q [n][max_nq], qd / qdd / tau / tau_out / qdd_out [n][max_nv], M [n][max_nv*max_nv]
+ * (environment e's nv x nv matrix packed at the start of its row), J [n][6*max_nv],
+ * link_poses [n][max_nlinks*7]. Supported op sets: MASS_MATRIX|INVERSE_DYNAMICS|
+ * FORWARD_DYNAMICS, INVERSE_DYNAMICS|FORWARD_DYNAMICS, all five, or one of the three. */
+typedef struct sgdyn_batch sgdyn_batch;
+/* model_of_env: host array [n] of indices into models[] (models must outlive the batch). */
+int sgdyn_batch_create(const sgdyn_model* const* models, int nmodels, const int* model_of_env, int64_t n,
+                       sgdyn_batch** out);
+void sgdyn_batch_free(sgdyn_batch* b);
+int sgdyn_batch_info(const sgdyn_batch* b, int64_t* n, int* max_nq, int* max_nv, int* max_nlinks);
+/* Launch shape: persistent CTAs per SM, warps per CTA, tile order (0 = descending DoF, 1 =
+ * input order). Chosen by sapien_gb300.autotune. */
+int sgdyn_batch_set_launch(sgdyn_batch* b, int ctas_per_sm, int warps_per_cta, int order);
+int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
+                     double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream);
+
 /* ---- differentiation (additions; the reference has no derivative API, see
  * pinocchio/cmake/pinocchio.cmake:4 which builds Pinocchio without autodiff) ----------
  * Configuration adjoints / derivatives are tangent-space quantities with nv columns

@@ -61,6 +61,11 @@ EXPORTED = (
     "sgdyn_rollout_scratch_bytes",
     "sgdyn_rollout_backward",
     "sgdyn_rollout_backward_noalloc",
+    "sgdyn_batch_create",
+    "sgdyn_batch_free",
+    "sgdyn_batch_info",
+    "sgdyn_batch_set_launch",
+    "sgdyn_batch_step",
 )
 
 _lib = None
@@ -115,6 +120,12 @@ def load():
     L.sgdyn_rollout_forward.argtypes = [vp, i64, i32, dbl, vp, vp, vp, i32, vp, vp, vp, vp, vp]
     L.sgdyn_rollout_scratch_bytes.argtypes = [vp, i64, i32, P(i64)]
     L.sgdyn_rollout_backward.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp]
+    L.sgdyn_batch_create.argtypes = [P(vp), i32, P(i32), i64, P(vp)]
+    L.sgdyn_batch_free.argtypes = [vp]
+    L.sgdyn_batch_free.restype = None
+    L.sgdyn_batch_info.argtypes = [vp, P(i64), P(i32), P(i32), P(i32)]
+    L.sgdyn_batch_set_launch.argtypes = [vp, i32, i32, i32]
+    L.sgdyn_batch_step.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.sgdyn_rollout_backward_noalloc.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L

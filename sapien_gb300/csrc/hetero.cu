@@ -1,0 +1,301 @@
+// Heterogeneous batches: robots of different size and topology in one persistent launch.
+//
+// Plan (host, once per batch): the models' tables are packed into one device buffer;
+// environments are grouped per model into tiles of up to 32 (one warp each); tiles are
+// ordered by descending velocity dimension (longest work first), so the largest trees
+// start first and small ones fill in behind them.
+// Step (device): a persistent grid of warps pulls tile indices from a global counter with
+// atomicAdd until the queue is exhausted; each lane runs the fused sweep for one
+// environment with its own model's table. No warp ever waits on another, so there is no
+// spin loop to bound. The counter is reset with cudaMemsetAsync on the same stream before
+// every launch, which keeps a step stream-ordered and capturable into a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sgdyn.h"
+#include "model.h"
+#include "step_kernel.cuh"
+
+struct sgdyn_model {
+  sgdyn::Model* impl;
+};
+
+namespace sgdyn {
+
+int set_last_error(int code, const std::string& msg);
+
+struct HeteroArgs {
+  const unsigned char* tables;
+  const int64_t* table_offset;
+  const int* perm;
+  const int4* tiles;  // (model, start, count, 0)
+  int ntiles;
+  unsigned int* head;
+  StepArgs io;
+};
+
+template <int MAXJ, int OPS>
+__global__ void hetero_kernel(const HeteroArgs a) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(a.head, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= unsigned(a.ntiles)) break;
+    const int4 tile = a.tiles[t];
+    const DModel* m = reinterpret_cast<const DModel*>(a.tables + a.table_offset[tile.x]);
+    if (lane < tile.z) step_env<MAXJ, OPS>(m, a.io, int64_t(a.perm[tile.y + lane]));
+    __syncwarp();
+  }
+}
+
+template <int MAXJ>
+cudaError_t launch_hetero_bucket(int ops, const HeteroArgs& a, dim3 grid, dim3 block, cudaStream_t s) {
+  switch (ops) {
+#define SG_CASE(O) \
+  case O: hetero_kernel<MAXJ, O><<<grid, block, 0, s>>>(a); break;
+    SG_CASE(OP_CRBA | OP_RNEA | OP_ABA)
+    SG_CASE(OP_RNEA | OP_ABA)
+    SG_CASE(OP_ALL)
+    SG_CASE(OP_RNEA)
+    SG_CASE(OP_ABA)
+    SG_CASE(OP_CRBA)
+#undef SG_CASE
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace sgdyn
+
+using namespace sgdyn;
+
+struct sgdyn_batch {
+  std::vector<const sgdyn_model*> models;
+  int64_t n = 0;
+  int max_nq = 0, max_nv = 0, max_nlinks = 0, max_nj = 0;
+  std::vector<int> model_of_env;
+  // device
+  unsigned char* tables = nullptr;
+  int64_t* offsets = nullptr;
+  int* perm = nullptr;
+  int4* tiles = nullptr;
+  int ntiles = 0;
+  unsigned int* head = nullptr;
+  int device = -1;
+  // launch shape (autotuned)
+  int ctas_per_sm = 4, warps_per_cta = 1, order = 0;
+  int sms = 0;
+};
+
+namespace {
+
+void free_device(sgdyn_batch* b) {
+  cudaFree(b->tables);
+  cudaFree(b->offsets);
+  cudaFree(b->perm);
+  cudaFree(b->tiles);
+  cudaFree(b->head);
+  b->tables = nullptr;
+  b->offsets = nullptr;
+  b->perm = nullptr;
+  b->tiles = nullptr;
+  b->head = nullptr;
+}
+
+// Builds the permutation and tile list for the current order and uploads them.
+int upload_plan(sgdyn_batch* b) {
+  const int nm = int(b->models.size());
+  std::vector<std::vector<int>> envs(nm);
+  for (int64_t e = 0; e < b->n; e++) envs[b->model_of_env[e]].push_back(int(e));
+  std::vector<int> mo(nm);
+  std::iota(mo.begin(), mo.end(), 0);
+  if (b->order == 0)
+    std::stable_sort(mo.begin(), mo.end(),
+                     [&](int x, int y) { return b->models[x]->impl->nv() > b->models[y]->impl->nv(); });
+  std::vector<int> perm;
+  std::vector<int4> tiles;
+  if (b->order == 0) {
+    for (int m : mo)
+      for (size_t s = 0; s < envs[m].size(); s += 32) {
+        int cnt = int(std::min<size_t>(32, envs[m].size() - s));
+        tiles.push_back(make_int4(m, int(perm.size()), cnt, 0));
+        for (int k = 0; k < cnt; k++) perm.push_back(envs[m][s + k]);
+      }
+  } else {
+    // input order: consecutive environments of the same model share a tile
+    int64_t e = 0;
+    while (e < b->n) {
+      int m = b->model_of_env[e];
+      int cnt = 0;
+      int start = int(perm.size());
+      while (e < b->n && cnt < 32 && b->model_of_env[e] == m) {
+        perm.push_back(int(e));
+        e++;
+        cnt++;
+      }
+      tiles.push_back(make_int4(m, start, cnt, 0));
+    }
+  }
+  cudaFree(b->perm);
+  cudaFree(b->tiles);
+  b->perm = nullptr;
+  b->tiles = nullptr;
+  if (cudaMalloc(&b->perm, sizeof(int) * std::max<size_t>(perm.size(), 1)) != cudaSuccess ||
+      cudaMalloc(&b->tiles, sizeof(int4) * std::max<size_t>(tiles.size(), 1)) != cudaSuccess)
+    return SGDYN_ERR_CUDA;
+  if (!perm.empty() && cudaMemcpy(b->perm, perm.data(), sizeof(int) * perm.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return SGDYN_ERR_CUDA;
+  if (!tiles.empty() &&
+      cudaMemcpy(b->tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return SGDYN_ERR_CUDA;
+  b->ntiles = int(tiles.size());
+  return SGDYN_OK;
+}
+
+bool dev_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+Arr env_major(const void* p, int64_t cols) { return Arr{static_cast<double*>(const_cast<void*>(p)), cols, 1}; }
+
+}  // namespace
+
+extern "C" {
+
+int sgdyn_batch_create(const sgdyn_model* const* models, int nmodels, const int* model_of_env, int64_t n,
+                       sgdyn_batch** out) {
+  if (!models || nmodels <= 0 || !out || (n > 0 && !model_of_env))
+    return set_last_error(SGDYN_ERR_NULL, "null argument");
+  if (n < 0 || n > int64_t(1) << 31) return set_last_error(SGDYN_ERR_RUNTIME, "bad batch size");
+  auto* b = new sgdyn_batch;
+  b->n = n;
+  for (int k = 0; k < nmodels; k++) {
+    if (!models[k] || !models[k]->impl) {
+      delete b;
+      return set_last_error(SGDYN_ERR_NULL, "null model in batch");
+    }
+    const Model& M = *models[k]->impl;
+    int nff = 0;
+    for (auto& J : M.joints) nff += J.kind == JK_FREEFLYER;
+    if (nff > 1 || stash_bucket(M.njoints()) == 0 || M.njoints() > 32) {
+      delete b;
+      return set_last_error(SGDYN_ERR_UNSUPPORTED, "batch models need at most 31 moving joints and one free flyer");
+    }
+    b->models.push_back(models[k]);
+    b->max_nq = std::max(b->max_nq, M.nq_ext());
+    b->max_nv = std::max(b->max_nv, M.nv());
+    b->max_nlinks = std::max(b->max_nlinks, M.nlinks());
+    b->max_nj = std::max(b->max_nj, M.njoints());
+  }
+  b->model_of_env.assign(model_of_env, model_of_env + n);
+  for (int m : b->model_of_env)
+    if (m < 0 || m >= nmodels) {
+      delete b;
+      return set_last_error(SGDYN_ERR_RUNTIME, "model index out of range");
+    }
+  cudaGetDevice(&b->device);
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+  // pack tables (16-byte aligned offsets)
+  std::vector<unsigned char> packed;
+  std::vector<int64_t> offs;
+  for (auto* m : b->models) {
+    const auto& t = m->impl->host_table();
+    offs.push_back(int64_t(packed.size()));
+    packed.insert(packed.end(), t.begin(), t.end());
+    while (packed.size() % 256) packed.push_back(0);
+  }
+  if (cudaMalloc(&b->tables, packed.size()) != cudaSuccess ||
+      cudaMalloc(&b->offsets, sizeof(int64_t) * offs.size()) != cudaSuccess ||
+      cudaMalloc(&b->head, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemcpy(b->tables, packed.data(), packed.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->offsets, offs.data(), sizeof(int64_t) * offs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      upload_plan(b) != SGDYN_OK) {
+    free_device(b);
+    delete b;
+    return set_last_error(SGDYN_ERR_CUDA, "batch upload failed");
+  }
+  *out = b;
+  return SGDYN_OK;
+}
+
+void sgdyn_batch_free(sgdyn_batch* b) {
+  if (!b) return;
+  free_device(b);
+  delete b;
+}
+
+int sgdyn_batch_info(const sgdyn_batch* b, int64_t* n, int* max_nq, int* max_nv, int* max_nlinks) {
+  if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
+  if (n) *n = b->n;
+  if (max_nq) *max_nq = b->max_nq;
+  if (max_nv) *max_nv = b->max_nv;
+  if (max_nlinks) *max_nlinks = b->max_nlinks;
+  return SGDYN_OK;
+}
+
+int sgdyn_batch_set_launch(sgdyn_batch* b, int ctas_per_sm, int warps_per_cta, int order) {
+  if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
+  if (ctas_per_sm < 1 || ctas_per_sm > 32 || warps_per_cta < 1 || warps_per_cta > 8 || order < 0 || order > 1)
+    return set_last_error(SGDYN_ERR_RUNTIME, "bad launch shape");
+  b->ctas_per_sm = ctas_per_sm;
+  b->warps_per_cta = warps_per_cta;
+  if (order != b->order) {
+    b->order = order;
+    if (upload_plan(b) != SGDYN_OK) return set_last_error(SGDYN_ERR_CUDA, "plan upload failed");
+  }
+  return SGDYN_OK;
+}
+
+int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
+                     double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream) {
+  if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
+  if (b->n == 0) return SGDYN_OK;
+  if (!dev_ptr(q)) return set_last_error(SGDYN_ERR_NULL, "q is null or not device memory");
+  if ((ops & (OP_RNEA | OP_ABA)) && !dev_ptr(qd)) return set_last_error(SGDYN_ERR_NULL, "qd missing");
+  if ((ops & OP_RNEA) && (!dev_ptr(qdd) || !dev_ptr(tau_out))) return set_last_error(SGDYN_ERR_NULL, "qdd / tau_out missing");
+  if ((ops & OP_ABA) && (!dev_ptr(tau) || !dev_ptr(qdd_out))) return set_last_error(SGDYN_ERR_NULL, "tau / qdd_out missing");
+  if ((ops & OP_CRBA) && !dev_ptr(M)) return set_last_error(SGDYN_ERR_NULL, "M missing");
+  if ((ops & OP_FK) && !dev_ptr(link_poses)) return set_last_error(SGDYN_ERR_NULL, "link_poses missing");
+  if ((ops & OP_JAC) && !dev_ptr(J)) return set_last_error(SGDYN_ERR_NULL, "J missing");
+  const int64_t nv = b->max_nv;
+  HeteroArgs a;
+  a.tables = b->tables;
+  a.table_offset = b->offsets;
+  a.perm = b->perm;
+  a.tiles = b->tiles;
+  a.ntiles = b->ntiles;
+  a.head = b->head;
+  a.io.n = b->n;
+  a.io.q = env_major(q, b->max_nq);
+  a.io.qd = env_major(qd, nv);
+  a.io.qdd = env_major(qdd, nv);
+  a.io.tau = env_major(tau, nv);
+  a.io.poses = env_major(link_poses, int64_t(b->max_nlinks) * 7);
+  a.io.J = env_major(J, 6 * nv);
+  a.io.M = env_major(M, nv * nv);
+  a.io.tau_out = env_major(tau_out, nv);
+  a.io.qdd_out = env_major(qdd_out, nv);
+  auto s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(b->head, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("memset failed: ") + cudaGetErrorString(e));
+  dim3 grid(unsigned(b->sms * b->ctas_per_sm)), block(unsigned(32 * b->warps_per_cta));
+  e = (b->max_nj <= 16) ? launch_hetero_bucket<16>(ops, a, grid, block, s)
+                        : launch_hetero_bucket<32>(ops, a, grid, block, s);
+  if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  return SGDYN_OK;
+}
+
+}  // extern "C"

@@ -129,10 +129,9 @@ __device__ __forceinline__ void chol6_solve(const double* L, double* b) {
 #undef LI
 }
 
+// The whole fused sweep for environment e (rows of the StepArgs arrays).
 template <int MAXJ, int OPS>
-__global__ void __launch_bounds__(32) step_kernel(const DModel* __restrict__ model, const StepArgs args) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= args.n) return;
+__device__ __forceinline__ void step_env(const DModel* __restrict__ model, const StepArgs& args, const int64_t e) {
   constexpr int MAXV = MAXJ + 5;
   constexpr bool kFK = OPS & OP_FK, kJAC = OPS & OP_JAC, kCRBA = OPS & OP_CRBA, kRNEA = OPS & OP_RNEA,
                  kABA = OPS & OP_ABA;
@@ -400,6 +399,13 @@ __global__ void __launch_bounds__(32) step_kernel(const DModel* __restrict__ mod
       acc[i] = a;
     }
   }
+}
+
+template <int MAXJ, int OPS>
+__global__ void __launch_bounds__(32) step_kernel(const DModel* __restrict__ model, const StepArgs args) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= args.n) return;
+  step_env<MAXJ, OPS>(model, args, e);
 }
 
 }  // namespace sgdyn

@@ -278,3 +278,15 @@ def by_name(name, **kw):
         "quadruped18": lambda: quadruped(**kw),
         "humanoid30": lambda: humanoid(**kw),
     }[name]()
+
+
+def hetero_mix(n, seed=0, fractions=(0.5, 0.3, 0.2)):
+    """Seeded mix of 6-DoF arms, floating-base quadrupeds and floating-base humanoids:
+    returns (robots, model_of_env) with robots = [arm6, quadruped18, humanoid]."""
+    robots = [serial_chain(6, seed=4), quadruped(), humanoid()]
+    rng = np.random.default_rng(seed)
+    counts = [int(round(f * n)) for f in fractions[:-1]]
+    counts.append(n - sum(counts))
+    model_of_env = np.concatenate([np.full(c, k, dtype=np.int32) for k, c in enumerate(counts)])
+    rng.shuffle(model_of_env)
+    return robots, model_of_env
