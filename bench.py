@@ -50,6 +50,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_ENVS)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the secondary workloads (rollout, heterogeneous batch, IK, derivatives)")
     return ap.parse_args()
 
 
@@ -142,6 +144,84 @@ def make_model():
     return robot, pm
 
 
+def _event_ms(torch, fn, reps=5, warm=2):
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def secondary_workloads(dev):
+    """The other workloads of the benchmark spec, timed with CUDA events on rank 0:
+    differentiable rollout (9-DoF arm, 4096 envs, 200 steps, dt 1/500, q/qd checkpoints
+    every 20 steps), heterogeneous batch (8192 mixed robots, RNEA + ABA + CRBA, CUDA-graph
+    replay, autotuned launch), batched CLIK (65536 targets, 100 iterations, damping 1e-3)
+    and dense derivatives on the floating-base humanoid (8192 envs)."""
+    import torch
+
+    from sapien_gb300 import PinocchioModel, autodiff as ad, autotune, synthetic
+    from sapien_gb300.hetero import OPS_DYNAMICS, HeteroBatch
+
+    def model_of(r):
+        m = PinocchioModel(r.urdf, [0.0, 0.0, -9.81])
+        m.set_joint_order(r.joint_names)
+        m.set_link_order(r.link_names)
+        return m
+
+    out = {}
+    arm = synthetic.arm_with_fingers()
+    pm = model_of(arm)
+    n, T, K, dt = 4096, 200, 20, 1.0 / 500
+    q0, qd0, _, _ = (torch.from_numpy(a).to(dev) for a in arm.sample(n, seed=0))
+    tau = torch.from_numpy(np.random.default_rng(1).normal(scale=5.0, size=(T, n, arm.nv))).to(dev)
+    fwd = _event_ms(torch, lambda: ad.rollout_forward(pm, q0, qd0, tau, dt))
+    fwd_ck = _event_ms(torch, lambda: ad.rollout_forward(pm, q0, qd0, tau, dt, K))
+    _, _, qc, qdc = ad.rollout_forward(pm, q0, qd0, tau, dt, K)
+    ones = torch.ones_like(q0)
+    bwd = _event_ms(torch, lambda: ad.rollout_backward(pm, qc, qdc, tau, dt, K, qT_bar=ones))
+    out["rollout"] = {"workload": "arm9, 4096 envs, T=200, dt=1/500, checkpoints every 20 steps",
+                      "plain_env_steps_per_s": n * T / (fwd * 1e-3),
+                      "fwd_bwd_env_steps_per_s": n * T / ((fwd_ck + bwd) * 1e-3),
+                      "fwd_ms": fwd, "fwd_with_checkpoints_ms": fwd_ck, "bwd_ms": bwd,
+                      "fwd_bwd_over_plain": (fwd_ck + bwd) / fwd}
+    robots, moe = synthetic.hetero_mix(8192, seed=0)
+    models = [model_of(r) for r in robots]
+    ins = [r.sample(int((moe == k).sum()), seed=k) for k, r in enumerate(robots)]
+    hb = HeteroBatch(models, moe, device=dev)
+    hq, hqd, hqdd, htau = (hb.pad_q([x[0] for x in ins]), hb.pad_v([x[1] for x in ins]),
+                           hb.pad_v([x[2] for x in ins]), hb.pad_v([x[3] for x in ins]))
+    shape, _ = autotune.tune_batch(hb, hq, hqd, hqdd, htau, OPS_DYNAMICS)
+    g = hb.capture(hq, hqd, hqdd, htau, steps=10)
+    hms = _event_ms(torch, g.replay, reps=5, warm=1) / 10
+    out["hetero"] = {"workload": "8192 envs: 50% 6-DoF arms, 30% 18-DoF quadrupeds, 20% 35-DoF humanoids; "
+                                 "RNEA+ABA+CRBA; CUDA-graph replay of 10 steps",
+                     "env_steps_per_s": 8192 / (hms * 1e-3), "ms_per_step": hms, "launch_shape": list(shape)}
+    nik = 65536
+    qik, _, _, _ = arm.sample(nik, seed=3)
+    tgt = pm.compute_forward_kinematics_batched(torch.from_numpy(qik).to(dev))[:, arm.ee_link].contiguous()
+    ik_ms = _event_ms(torch, lambda: pm.compute_inverse_kinematics_batched(arm.ee_link, tgt, None, None, eps=0.0,
+                                                                           max_iterations=100, dt=0.1, damp=1e-3),
+                      reps=3, warm=1)
+    out["ik"] = {"workload": "arm9 CLIK, 65536 FK targets, 100 iterations, damping 1e-3",
+                 "solves_per_s": nik / (ik_ms * 1e-3), "ms": ik_ms}
+    hum = synthetic.humanoid()
+    hm = model_of(hum)
+    hq2, hqd2, hqdd2, htau2 = (torch.from_numpy(a).to(dev) for a in hum.sample(8192, seed=0))
+    rd = _event_ms(torch, lambda: ad.rnea_derivatives(hm, hq2, hqd2, hqdd2), reps=3, warm=1)
+    adr = _event_ms(torch, lambda: ad.aba_derivatives(hm, hq2, hqd2, htau2), reps=3, warm=1)
+    out["derivatives"] = {"workload": "humanoid (35 DoF, floating base), 8192 envs, dense dtau/d(q,qd,qdd) and "
+                                      "dqdd/d(q,qd,tau)",
+                          "rnea_derivatives_evals_per_s": 8192 / (rd * 1e-3),
+                          "aba_derivatives_evals_per_s": 8192 / (adr * 1e-3)}
+    return out
+
+
 def run_reference(args):
     """CPU oracle on the same workload, all host threads, rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
@@ -199,6 +279,7 @@ def main():
             dist.barrier()
 
     from sapien_gb300 import _native as N
+    from sapien_gb300.sharding import aggregate_throughput, max_across_ranks
 
     robot, pm = make_model()
     n = args.n
@@ -240,12 +321,8 @@ def main():
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n / (ms * 1e-3)
+    ms = max_across_ranks(float(np.mean([a.elapsed_time(b) for a, b in ev])), dist, dev)
+    value = aggregate_throughput(n, world, ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ------------------------------
     pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
@@ -278,12 +355,8 @@ def main():
         ev2[k][1].record(stream)
     torch.cuda.synchronize()
     barrier()
-    ms_e2e = float(np.mean([a.elapsed_time(b) for a, b in ev2]))
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
-    e2e_value = world * n / (ms_e2e * 1e-3)
+    ms_e2e = max_across_ranks(float(np.mean([a.elapsed_time(b) for a, b in ev2])), dist, dev)
+    e2e_value = aggregate_throughput(n, world, ms_e2e * 1e-3)
 
     # ---- per-op kernel times (same inputs) -------------------------------------------
     per_op = {}
@@ -302,6 +375,10 @@ def main():
         t_ms = float(np.mean([a.elapsed_time(b) for a, b in ts[2:]]))
         per_op[name] = {"evals_per_s": n / (t_ms * 1e-3), "us": t_ms * 1e3}
 
+    extras = None
+    if rank == 0 and not args.no_extras:
+        extras = secondary_workloads(dev)
+    barrier()
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -372,6 +449,7 @@ def main():
         "per_op_kernel": per_op,
         "max_rel_err_vs_oracle": errs,
         "clocks": clk,
+        "secondary": extras,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
