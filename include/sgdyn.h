@@ -122,6 +122,18 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
                const double* tau, double* link_poses, double* J, double* M, double* tau_out, double* qdd_out,
                int layout, void* stream);
 
+/* Run-time specialisation (addition). The fused sweep behind sgdyn_step and the five
+ * single-op entry points is compiled per model with NVRTC on first use (tables baked in as
+ * constants; same arithmetic, bitwise-equal results) when enabled and n >= min_n; otherwise,
+ * or if the run-time compiler or the driver library is unavailable, the generic kernel runs.
+ * enable / min_n < 0 leave a setting unchanged; the current values are returned. Defaults:
+ * enabled unless SGDYN_JIT=0, min_n = 2048 (SGDYN_JIT_MIN_N). Compile ahead with
+ * sgdyn_jit_prepare (needed before capturing launches into a CUDA graph). */
+int sgdyn_jit_config(int enable, int64_t min_n, int* enabled, int64_t* min_n_out);
+int sgdyn_jit_prepare(const sgdyn_model* m, int ops);
+/* The generated translation unit for (model, ops); valid until the next call on this thread. */
+int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source);
+
 /* PinocchioModel::computeInverseKinematics (CLIK, pinocchio_model.cpp:228-300), one solve per
  * environment. target [n][7] = link pose (x y z qw qx qy qz) in the base frame, FP64.
  * q0 [n][nq_ext] or NULL (neutral start), mask [nv] int (1 active, 0 frozen) or NULL (all

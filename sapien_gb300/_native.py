@@ -66,6 +66,9 @@ EXPORTED = (
     "sgdyn_batch_info",
     "sgdyn_batch_set_launch",
     "sgdyn_batch_step",
+    "sgdyn_jit_config",
+    "sgdyn_jit_prepare",
+    "sgdyn_jit_source",
 )
 
 _lib = None
@@ -126,6 +129,9 @@ def load():
     L.sgdyn_batch_info.argtypes = [vp, P(i64), P(i32), P(i32), P(i32)]
     L.sgdyn_batch_set_launch.argtypes = [vp, i32, i32, i32]
     L.sgdyn_batch_step.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.sgdyn_jit_config.argtypes = [i32, i64, P(i32), P(i64)]
+    L.sgdyn_jit_prepare.argtypes = [vp, i32]
+    L.sgdyn_jit_source.argtypes = [vp, i32, P(ctypes.c_char_p)]
     L.sgdyn_rollout_backward_noalloc.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L

@@ -54,6 +54,28 @@ def _compile(src, hmt, verbose):
     return obj, None
 
 
+JIT_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
+
+
+def _write_jit_headers():
+    """Embed the device headers the run-time compiler needs into a generated C++ file."""
+    out = os.path.join(BUILD, "jit_headers.cpp")
+    parts = ["// generated by build_native.py: device headers for run-time compilation",
+             "namespace sgdyn {",
+             "extern const char* const kJitHeaderNames[] = {" + ", ".join(f'"{h}"' for h in JIT_HEADERS) + "};",
+             "extern const char* const kJitHeaderSources[] = {"]
+    for h in JIT_HEADERS:
+        text = open(os.path.join(CSRC, h)).read()
+        assert ")SGJIT\"" not in text
+        parts.append('R"SGJIT(' + text + ')SGJIT",')
+    parts += ["};", f"extern const int kJitHeaderCount = {len(JIT_HEADERS)};", "}  // namespace sgdyn", ""]
+    text = "\n".join(parts)
+    if not os.path.exists(out) or open(out).read() != text:
+        with open(out, "w") as f:
+            f.write(text)
+    return out
+
+
 def build(verbose=False, jobs=None, force=False):
     """Compile all translation units and link libsgdyn.so; returns the library path."""
     os.makedirs(BUILD, exist_ok=True)
@@ -62,7 +84,7 @@ def build(verbose=False, jobs=None, force=False):
         for o in glob.glob(os.path.join(BUILD, "*.o")):
             os.remove(o)
     hmt = _headers_mtime()
-    srcs = sources()
+    srcs = sources() + [_write_jit_headers()]
     jobs = jobs or min(len(srcs), max(2, os.cpu_count() or 2))
     with ThreadPoolExecutor(jobs) as ex:
         results = list(ex.map(lambda s: _compile(s, hmt, verbose), srcs))
@@ -87,7 +109,7 @@ def _link(objs, out, verbose):
     newest = max(os.path.getmtime(o) for o in objs)
     if os.path.exists(out) and os.path.getmtime(out) >= newest:
         return
-    cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", out] + objs
+    cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", out] + objs + ["-ldl"]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/sgdyn.h"
+#include "jit.h"
 #include "kernels.h"
 #include "model.h"
 
@@ -133,6 +134,8 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
   for (int b = 1; b <= OP_ABA; b <<= 1)
     if (rest & b) launches.push_back(b);
   for (int o : launches) {
+    std::string why;
+    if (launch_step_jit(Mo, o, a, s, &why)) continue;  // model-specialised kernel
     cudaError_t e = launch_step(dm, Mo.njoints(), o, a, s);
     if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   }
@@ -264,6 +267,28 @@ int sgdyn_model_table(const sgdyn_model* m, const void** data, int64_t* bytes) {
   if (!m || !data || !bytes) return fail(SGDYN_ERR_NULL, "null argument");
   *data = m->impl->host_table().data();
   *bytes = int64_t(m->impl->host_table().size());
+  return SGDYN_OK;
+}
+
+int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n_out) {
+  set_jit_config(enable, min_n);
+  get_jit_config(enabled_out, min_n_out);
+  return SGDYN_OK;
+}
+
+int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
+  if (!m) return fail(SGDYN_ERR_NULL, "null model");
+  if (ops <= 0 || ops > OP_ALL) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
+  std::string why;
+  if (!prepare_step_jit(*m->impl, ops, &why)) return fail(SGDYN_ERR_UNSUPPORTED, "run-time compilation unavailable: " + why);
+  return SGDYN_OK;
+}
+
+int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
+  if (!m || !source) return fail(SGDYN_ERR_NULL, "null argument");
+  thread_local std::string buf;
+  buf = step_jit_source(*m->impl, ops);
+  *source = buf.c_str();
   return SGDYN_OK;
 }
 

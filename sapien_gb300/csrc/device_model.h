@@ -3,7 +3,14 @@
 // Every environment of a batch reads the same table, so all lanes of a warp load the
 // same address (a broadcast through L1).
 #pragma once
+#ifdef __CUDACC_RTC__
+// run-time compilation: no standard headers
+typedef long long int64_t;
+typedef unsigned long size_t;
+#else
+#include <cstddef>
 #include <cstdint>
+#endif
 
 #ifdef __CUDACC__
 #define SG_HD __host__ __device__ __forceinline__

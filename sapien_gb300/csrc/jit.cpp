@@ -1,0 +1,311 @@
+// Run-time specialisation of the fused sweep (NVRTC).
+//
+// For a given model and op set the generated translation unit holds the model's kernel
+// tables as compile-time constants and instantiates step_env_t with StaticTab, so every
+// joint loop unrolls into straight-line code with constant parents, axes, placements and
+// inertias: no dynamic local-memory indexing, no branches on joint kind, and one large
+// basic block in which the scheduler can fill the FP64 pipe's issue shadow. The arithmetic
+// is the same sequence of operations as the generic kernel (results are bitwise equal).
+//
+// libnvrtc and the driver library are opened with dlopen on first use, so the package
+// loads on machines without them; compiled cubins are cached in memory per (source,
+// device) and on disk under $SGDYN_JIT_CACHE (default ~/.cache/sapien_gb300/jit).
+#include "jit.h"
+
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <vector>
+
+#include "model.h"
+
+namespace sgdyn {
+
+extern const char* const kJitHeaderNames[];
+extern const char* const kJitHeaderSources[];
+extern const int kJitHeaderCount;
+
+namespace {
+
+struct Api {
+  bool loaded = false;
+  std::string why;
+  decltype(&nvrtcCreateProgram) createProgram = nullptr;
+  decltype(&nvrtcCompileProgram) compileProgram = nullptr;
+  decltype(&nvrtcGetCUBINSize) getCUBINSize = nullptr;
+  decltype(&nvrtcGetCUBIN) getCUBIN = nullptr;
+  decltype(&nvrtcGetProgramLogSize) getLogSize = nullptr;
+  decltype(&nvrtcGetProgramLog) getLog = nullptr;
+  decltype(&nvrtcDestroyProgram) destroyProgram = nullptr;
+  decltype(&nvrtcVersion) version = nullptr;
+  decltype(&cuModuleLoadData) moduleLoadData = nullptr;
+  decltype(&cuModuleGetFunction) moduleGetFunction = nullptr;
+  decltype(&cuLaunchKernel) launchKernel = nullptr;
+};
+
+Api load_api() {
+  Api a;
+  void* nv = dlopen("libnvrtc.so.13", RTLD_NOW | RTLD_LOCAL);
+  if (!nv) nv = dlopen("libnvrtc.so", RTLD_NOW | RTLD_LOCAL);
+  void* cu = dlopen("libcuda.so.1", RTLD_NOW | RTLD_LOCAL);
+  if (!nv || !cu) {
+    a.why = !nv ? "libnvrtc not found" : "libcuda.so.1 not found";
+    return a;
+  }
+#define SG_SYM(lib, field, name)                                  \
+  a.field = reinterpret_cast<decltype(a.field)>(dlsym(lib, name)); \
+  if (!a.field) {                                                 \
+    a.why = std::string("missing symbol ") + name;                \
+    return a;                                                     \
+  }
+  SG_SYM(nv, createProgram, "nvrtcCreateProgram")
+  SG_SYM(nv, compileProgram, "nvrtcCompileProgram")
+  SG_SYM(nv, getCUBINSize, "nvrtcGetCUBINSize")
+  SG_SYM(nv, getCUBIN, "nvrtcGetCUBIN")
+  SG_SYM(nv, getLogSize, "nvrtcGetProgramLogSize")
+  SG_SYM(nv, getLog, "nvrtcGetProgramLog")
+  SG_SYM(nv, destroyProgram, "nvrtcDestroyProgram")
+  SG_SYM(nv, version, "nvrtcVersion")
+  SG_SYM(cu, moduleLoadData, "cuModuleLoadData")
+  SG_SYM(cu, moduleGetFunction, "cuModuleGetFunction")
+  SG_SYM(cu, launchKernel, "cuLaunchKernel")
+#undef SG_SYM
+  a.loaded = true;
+  return a;
+}
+
+Api& api() {
+  static Api a = load_api();
+  return a;
+}
+
+std::mutex g_mu;
+int g_enable = -1;  // -1: read SGDYN_JIT on first use
+int64_t g_min_n = 2048;
+std::map<std::string, CUfunction> g_functions;  // key: source hash + device
+std::map<std::string, std::string> g_failed;    // key -> reason
+
+void read_env_config() {
+  if (g_enable >= 0) return;
+  const char* e = std::getenv("SGDYN_JIT");
+  g_enable = (e && std::strcmp(e, "0") == 0) ? 0 : 1;
+  if (const char* m = std::getenv("SGDYN_JIT_MIN_N")) g_min_n = std::atoll(m);
+}
+
+uint64_t fnv1a(const std::string& s) {
+  uint64_t h = 1469598103934665603ull;
+  for (unsigned char c : s) {
+    h ^= c;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+std::string num(double x) {
+  char b[40];
+  std::snprintf(b, sizeof b, "%.17g", x);
+  return b;
+}
+
+template <class It>
+std::string list(It b, It e) {
+  std::string s;
+  for (It i = b; i != e; ++i) s += (i == b ? "" : ", ") + num(*i);
+  return s;
+}
+
+std::string generate_source(const Model& M, int ops) {
+  const auto& t = M.host_table();
+  const auto* hdr = reinterpret_cast<const DModel*>(t.data());
+  const DJoint* J = model_joints(hdr);
+  const DLink* L = model_links(hdr);
+  const int nj = hdr->nj, nl = hdr->nlinks;
+  std::ostringstream o;
+  o << "#include \"step_kernel.cuh\"\nnamespace sgjit {\n";
+  o << "__device__ constexpr sgdyn::DModel kM = {" << hdr->nj << ", " << hdr->nv << ", " << hdr->nq_ext << ", "
+    << hdr->nlinks << ", " << hdr->max_depth << ", " << hdr->n_free_flyer << ", {0, 0}, {"
+    << list(hdr->gravity, hdr->gravity + 3) << "}, 0.0};\n";
+  o << "__device__ constexpr sgdyn::DJoint kJT[" << nj << "] = {\n";
+  for (int j = 0; j < nj; j++) {
+    const DJoint& d = J[j];
+    o << " {{" << list(d.R, d.R + 9) << "}, {" << list(d.p, d.p + 3) << "}, {" << list(d.axis, d.axis + 3) << "}, "
+      << num(d.m) << ", {" << list(d.h, d.h + 3) << "}, {" << list(d.I, d.I + 6) << "}, " << d.parent << ", " << d.kind
+      << ", " << d.axis_kind << ", " << d.flags << ", " << d.qcol << ", " << d.vcol << ", " << d.nv << ", " << d.depth
+      << ", " << d.ivx << ", {0, 0, 0, 0, 0}},\n";
+  }
+  o << "};\n";
+  o << "__device__ constexpr sgdyn::DLink kLT[" << (nl > 0 ? nl : 1) << "] = {\n";
+  for (int l = 0; l < nl; l++)
+    o << " {{" << list(L[l].R, L[l].R + 9) << "}, {" << list(L[l].p, L[l].p + 3) << "}, " << L[l].joint << ", "
+      << L[l].flags << ", {0, 0}},\n";
+  if (nl == 0) o << " {{1,0,0,0,1,0,0,0,1}, {0,0,0}, 0, 1, {0, 0}},\n";
+  o << "};\n}  // namespace sgjit\n";
+  o << "extern \"C\" __global__ void __launch_bounds__(32) sgjit_step(const sgdyn::StepArgs a) {\n"
+    << "  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
+    << "  if (e >= a.n) return;\n"
+    << "  sgdyn::step_env_t<" << nj << ", " << ops << ">(sgdyn::StaticTab<" << nj << ", " << hdr->nv << ", " << nl
+    << ", sgjit::kJT, sgjit::kLT, &sgjit::kM>(), a, e);\n}\n";
+  return o.str();
+}
+
+std::string cache_dir() {
+  if (const char* d = std::getenv("SGDYN_JIT_CACHE")) return d;
+  const char* home = std::getenv("HOME");
+  return std::string(home ? home : "/tmp") + "/.cache/sapien_gb300/jit";
+}
+
+void mkdirs(const std::string& path) {
+  std::string cur;
+  for (size_t i = 0; i < path.size(); i++) {
+    cur += path[i];
+    if (path[i] == '/' && cur.size() > 1) mkdir(cur.c_str(), 0755);
+  }
+  mkdir(path.c_str(), 0755);
+}
+
+bool compile_cubin(const std::string& src, std::vector<char>* cubin, std::string* why) {
+  Api& A = api();
+  nvrtcProgram prog;
+  if (A.createProgram(&prog, src.c_str(), "sgjit_step.cu", kJitHeaderCount, kJitHeaderSources, kJitHeaderNames) !=
+      NVRTC_SUCCESS) {
+    *why = "nvrtcCreateProgram failed";
+    return false;
+  }
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
+  nvrtcResult rc = A.compileProgram(prog, 3, opts);
+  if (rc != NVRTC_SUCCESS) {
+    size_t n = 0;
+    A.getLogSize(prog, &n);
+    std::string log(n, '\0');
+    A.getLog(prog, &log[0]);
+    *why = "nvrtc compile failed: " + log.substr(0, 2000);
+    A.destroyProgram(&prog);
+    return false;
+  }
+  size_t n = 0;
+  A.getCUBINSize(prog, &n);
+  cubin->resize(n);
+  A.getCUBIN(prog, cubin->data());
+  A.destroyProgram(&prog);
+  return true;
+}
+
+// Returns the specialised kernel for (M, ops) on the current device, compiling if needed.
+CUfunction get_function(const Model& M, int ops, std::string* why) {
+  Api& A = api();
+  if (!A.loaded) {
+    *why = A.why;
+    return nullptr;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    *why = "no CUDA device";
+    return nullptr;
+  }
+  const std::string src = generate_source(M, ops);
+  int major = 0, minor = 0;
+  A.version(&major, &minor);
+  char hx[40];
+  std::snprintf(hx, sizeof hx, "%016llx-%d.%d", static_cast<unsigned long long>(fnv1a(src)), major, minor);
+  const std::string key = std::string(hx) + "@" + std::to_string(dev);
+  auto it = g_functions.find(key);
+  if (it != g_functions.end()) return it->second;
+  auto f = g_failed.find(key);
+  if (f != g_failed.end()) {
+    *why = f->second;
+    return nullptr;
+  }
+  std::vector<char> cubin;
+  const std::string dir = cache_dir();
+  const std::string path = dir + "/" + hx + ".cubin";
+  {
+    std::ifstream in(path, std::ios::binary);
+    if (in) cubin.assign(std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>());
+  }
+  if (cubin.empty()) {
+    if (!compile_cubin(src, &cubin, why)) {
+      g_failed[key] = *why;
+      return nullptr;
+    }
+    mkdirs(dir);
+    const std::string tmp = path + ".tmp" + std::to_string(getpid());
+    {
+      std::ofstream out(tmp, std::ios::binary);
+      out.write(cubin.data(), std::streamsize(cubin.size()));
+    }
+    std::rename(tmp.c_str(), path.c_str());
+  }
+  cudaFree(nullptr);  // make sure the runtime's primary context is current
+  CUmodule mod;
+  CUfunction fn;
+  if (A.moduleLoadData(&mod, cubin.data()) != CUDA_SUCCESS || A.moduleGetFunction(&fn, mod, "sgjit_step") != CUDA_SUCCESS) {
+    *why = "loading the compiled module failed";
+    g_failed[key] = *why;
+    return nullptr;
+  }
+  g_functions[key] = fn;
+  return fn;
+}
+
+}  // namespace
+
+std::string step_jit_source(const Model& M, int ops) { return generate_source(M, ops); }
+
+void set_jit_config(int enable, int64_t min_n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  if (enable >= 0) g_enable = enable ? 1 : 0;
+  if (min_n >= 0) g_min_n = min_n;
+}
+
+void get_jit_config(int* enable, int64_t* min_n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  if (enable) *enable = g_enable;
+  if (min_n) *min_n = g_min_n;
+}
+
+bool prepare_step_jit(Model& M, int ops, std::string* why) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  return get_function(M, ops, why) != nullptr;
+}
+
+bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why) {
+  CUfunction fn;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    read_env_config();
+    if (!g_enable) {
+      *why = "disabled";
+      return false;
+    }
+    if (a.n < g_min_n) {
+      *why = "batch below the run-time compilation threshold";
+      return false;
+    }
+    fn = get_function(M, ops, why);
+  }
+  if (!fn) return false;
+  StepArgs args = a;
+  void* params[] = {&args};
+  const unsigned blocks = unsigned((a.n + 31) / 32);
+  if (api().launchKernel(fn, blocks, 1, 1, 32, 1, 1, 0, reinterpret_cast<CUstream>(s), params, nullptr) !=
+      CUDA_SUCCESS) {
+    *why = "cuLaunchKernel failed";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace sgdyn

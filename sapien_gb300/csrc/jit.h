@@ -1,0 +1,25 @@
+// Run-time specialisation of the fused sweep per model (NVRTC).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "kernels.h"
+
+namespace sgdyn {
+
+class Model;
+
+// Launches the model-specialised sweep if run-time compilation is enabled, available and
+// the batch is large enough; returns false (with the reason) when the caller should use the
+// generic kernel. Compiles and caches on first use of (model tables, ops, device).
+bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why);
+// Compiles (or loads from the cache) now; false with the reason if not possible.
+bool prepare_step_jit(Model& M, int ops, std::string* why);
+void set_jit_config(int enable, int64_t min_n);
+// The generated translation unit (for inspection and tests).
+std::string step_jit_source(const Model& M, int ops);
+void get_jit_config(int* enable, int64_t* min_n);
+
+}  // namespace sgdyn

@@ -1,8 +1,10 @@
 // Launcher interface between the C-ABI layer and the CUDA kernels.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#endif
 
 #include "device_model.h"
 
@@ -79,6 +81,7 @@ struct RolloutArgs {
   double *q0_bar, *qd0_bar, *tau_bar, *scratch;
 };
 
+#ifndef __CUDACC_RTC__
 // Joint-count bucket for the per-thread stash (16, 32 or 64 joints incl. universe).
 int stash_bucket(int nj);
 
@@ -96,5 +99,6 @@ cudaError_t launch_rollout_forward(const DModel* dm, int nj, const RolloutArgs& 
 cudaError_t launch_rollout_backward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 // doubles of rollout-backward scratch per environment
 int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K);
+#endif  // __CUDACC_RTC__
 
 }  // namespace sgdyn

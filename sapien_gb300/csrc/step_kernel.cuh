@@ -22,6 +22,28 @@
 
 namespace sgdyn {
 
+// Table policies for the sweep: a table read through a device pointer at run time, or a
+// table whose contents are compile-time constants (run-time-compiled per model, so every
+// joint loop unrolls into straight-line code with constant parents, axes and inertias).
+struct RuntimeTab {
+  const DModel* m;
+  __device__ __forceinline__ int nj() const { return m->nj; }
+  __device__ __forceinline__ int nv() const { return m->nv; }
+  __device__ __forceinline__ int nlinks() const { return m->nlinks; }
+  __device__ __forceinline__ double gravity(int k) const { return m->gravity[k]; }
+  __device__ __forceinline__ const DJoint& joint(int i) const { return model_joints(m)[i]; }
+  __device__ __forceinline__ const DLink& link(int l) const { return model_links(m)[l]; }
+};
+template <int NJ, int NV, int NL, const DJoint* JT, const DLink* LT, const DModel* M>
+struct StaticTab {
+  __device__ __forceinline__ static constexpr int nj() { return NJ; }
+  __device__ __forceinline__ static constexpr int nv() { return NV; }
+  __device__ __forceinline__ static constexpr int nlinks() { return NL; }
+  __device__ __forceinline__ double gravity(int k) const { return M->gravity[k]; }
+  __device__ __forceinline__ const DJoint& joint(int i) const { return JT[i]; }
+  __device__ __forceinline__ const DLink& link(int l) const { return LT[l]; }
+};
+
 __device__ __forceinline__ double ldv(const Arr& a, int64_t e, int c) { return a.p[e * a.es + int64_t(c) * a.cs]; }
 __device__ __forceinline__ void stv(const Arr& a, int64_t e, int c, double v) { a.p[e * a.es + int64_t(c) * a.cs] = v; }
 
@@ -130,15 +152,14 @@ __device__ __forceinline__ void chol6_solve(const double* L, double* b) {
 }
 
 // The whole fused sweep for environment e (rows of the StepArgs arrays).
-template <int MAXJ, int OPS>
-__device__ __forceinline__ void step_env(const DModel* __restrict__ model, const StepArgs& args, const int64_t e) {
+template <int MAXJ, int OPS, class Tab>
+__device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, const int64_t e) {
   constexpr int MAXV = MAXJ + 5;
   constexpr bool kFK = OPS & OP_FK, kJAC = OPS & OP_JAC, kCRBA = OPS & OP_CRBA, kRNEA = OPS & OP_RNEA,
                  kABA = OPS & OP_ABA;
   constexpr bool kVel = kRNEA || kABA;
   constexpr bool kInertia = kCRBA || kRNEA || kABA;
-  const int nj = model->nj;
-  const DJoint* __restrict__ JT = model_joints(model);
+  const int nj = T.nj();
 
   M3 oR[MAXJ];
   V3 op[MAXJ];
@@ -152,17 +173,18 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
   double uv[kABA ? MAXV : 1], Dinv[kABA ? MAXJ : 1];
   double Lff[kABA ? 21 : 1];  // Cholesky factor of D for the (single) free-flyer joint
 
-  const Mot a0{mk(-model->gravity[0], -model->gravity[1], -model->gravity[2]), mk(0, 0, 0)};
+  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
 
   if constexpr (kCRBA) {
-    const int nv = model->nv;
+    const int nv = T.nv();
     for (int r = 0; r < nv; r++)
       for (int c = 0; c < nv; c++) stv(args.M, e, r * nv + c, 0.0);
   }
 
   // ---------------- pass 1: root to leaves ----------------
+#pragma unroll
   for (int i = 1; i < nj; i++) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent;
     M3 Ro;
     V3 po;
@@ -172,7 +194,7 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
     const int nvi = J.nv, iv = J.ivx, vc = J.vcol;
     for (int k = 0; k < nvi; k++) Sw[iv + k] = world_S(J, Ro, po, k);
     if constexpr (kJAC) {
-      const int nv = model->nv;
+      const int nv = T.nv();
       for (int k = 0; k < nvi; k++) {
         const Mot S = Sw[iv + k];
         stv(args.J, e, 0 * nv + vc + k, S.v.x);
@@ -216,10 +238,10 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
   }
 
   if constexpr (kFK) {
-    const DLink* __restrict__ LT = model_links(model);
-    const int nl = model->nlinks;
+    const int nl = T.nlinks();
+#pragma unroll
     for (int l = 0; l < nl; l++) {
-      const DLink& L = LT[l];
+      const DLink& L = T.link(l);
       const int j = L.joint;
       M3 R;
       V3 pp;
@@ -248,8 +270,9 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
 
   if constexpr (kCRBA || kRNEA || kABA) {
     // ---------------- pass 2: leaves to root ----------------
+#pragma unroll
     for (int i = nj - 1; i >= 1; i--) {
-      const DJoint& J = JT[i];
+      const DJoint& J = T.joint(i);
       const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
       if constexpr (kRNEA) {
         const Mot f = frc[i];
@@ -257,7 +280,7 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
         if (p > 0) frc[p] = add6(frc[p], f);
       }
       if constexpr (kCRBA) {
-        const int nv = model->nv;
+        const int nv = T.nv();
         const RBI Y = Ic[i];
         for (int k = 0; k < nvi; k++) {
           const Mot F = rbi_mul(Y, Sw[iv + k]);
@@ -266,8 +289,9 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
             stv(args.M, e, (vc + l) * nv + vc + k, m);
             stv(args.M, e, (vc + k) * nv + vc + l, m);
           }
-          for (int j = p; j > 0; j = JT[j].parent) {
-            const int jv = JT[j].ivx, jc = JT[j].vcol, nvj = JT[j].nv;
+#pragma unroll
+          for (int j = p; j > 0; j = T.joint(j).parent) {
+            const int jv = T.joint(j).ivx, jc = T.joint(j).vcol, nvj = T.joint(j).nv;
             for (int l = 0; l < nvj; l++) {
               const double m = dot6(Sw[jv + l], F);
               stv(args.M, e, (jc + l) * nv + vc + k, m);
@@ -379,8 +403,9 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
 
   if constexpr (kABA) {
     // ---------------- pass 3: root to leaves ----------------
+#pragma unroll
     for (int i = 1; i < nj; i++) {
-      const DJoint& J = JT[i];
+      const DJoint& J = T.joint(i);
       const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
       Mot a = add6((p == 0) ? a0 : acc[p], cb[i]);
       if (nvi == 1) {
@@ -399,6 +424,11 @@ __device__ __forceinline__ void step_env(const DModel* __restrict__ model, const
       acc[i] = a;
     }
   }
+}
+
+template <int MAXJ, int OPS>
+__device__ __forceinline__ void step_env(const DModel* __restrict__ model, const StepArgs& args, const int64_t e) {
+  step_env_t<MAXJ, OPS>(RuntimeTab{model}, args, e);
 }
 
 template <int MAXJ, int OPS>

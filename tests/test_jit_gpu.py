@@ -1,0 +1,58 @@
+"""The model-specialised (run-time compiled) sweep against the generic kernel and the
+oracle. Tolerances as in test_parity_gpu.py; specialised vs generic within 1e-13."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from sapien_gb300 import PinocchioModel, synthetic as syn
+from sapien_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def jit_config(enable, min_n):
+    e, m = ctypes.c_int(), ctypes.c_int64()
+    N.check(N.load().sgdyn_jit_config(enable, min_n, ctypes.byref(e), ctypes.byref(m)))
+    return e.value, m.value
+
+
+def rel_per_env(g, o):
+    g = g.reshape(g.shape[0], -1)
+    o = o.reshape(o.shape[0], -1)
+    return (np.abs(g - o).max(axis=1) / np.maximum(np.abs(o).max(axis=1), 1e-300)).max()
+
+
+@pytest.mark.parametrize("name", ["arm9", "arm9_sapien", "humanoid", "quadruped", "mixed"])
+def test_specialised_sweep_matches_generic_and_oracle(name):
+    import torch
+
+    robot = {"arm9": syn.arm_with_fingers(), "arm9_sapien": syn.arm_with_fingers(sapien_style=True),
+             "humanoid": syn.humanoid(), "quadruped": syn.quadruped(),
+             "mixed": syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                          "continuous", "prismatic"])}[name]
+    pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    q, qd, qdd, tau = (torch.from_numpy(a).cuda() for a in robot.sample(100, seed=23))
+    old = jit_config(-1, -1)
+    try:
+        jit_config(0, -1)
+        gen = {k: v.cpu().numpy() for k, v in pm.step_batched(q, qd, qdd, tau).items()}
+        jit_config(1, 0)
+        assert N.load().sgdyn_jit_prepare(pm._h, N.OP_ALL) == 0, N.last_error()
+        spec = {k: v.cpu().numpy() for k, v in pm.step_batched(q, qd, qdd, tau).items()}
+        single = pm.compute_forward_dynamics_batched(q, qd, tau).cpu().numpy()
+    finally:
+        jit_config(*old)
+    for k in gen:
+        assert rel_per_env(spec[k], gen[k]) <= 1e-13, k
+    assert rel_per_env(single, gen["qacc"]) <= 1e-13
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    r = o.batch_step(*(x.cpu().numpy() for x in (q, qd, qdd, tau)), ops=4 | 8 | 16)
+    assert rel_per_env(spec["qf"], r["tau"]) <= 1e-10
+    assert rel_per_env(spec["qacc"], r["qdd"]) <= 1e-8
+    assert rel_per_env(spec["mass_matrix"], r["M"]) <= 1e-10

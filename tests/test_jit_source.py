@@ -1,0 +1,55 @@
+"""The run-time-specialised sweep's generated source compiles with NVRTC for sm_103a (CPU
+test: NVRTC needs no GPU). GPU parity of the specialised kernel is in test_parity_gpu.py."""
+import ctypes
+import ctypes.util
+
+import pytest
+
+from sapien_gb300 import PinocchioModel, synthetic as syn
+from sapien_gb300 import _native as N
+
+
+def _nvrtc():
+    for name in ("libnvrtc.so.13", "libnvrtc.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    pytest.skip("libnvrtc not available")
+
+
+def _headers():
+    import os
+
+    from sapien_gb300.build_native import CSRC, JIT_HEADERS
+
+    return [h.encode() for h in JIT_HEADERS], [open(os.path.join(CSRC, h)).read().encode() for h in JIT_HEADERS]
+
+
+@pytest.mark.parametrize("name,ops", [("arm9", 31), ("humanoid", 28), ("mixed", 8)])
+def test_generated_source_compiles(name, ops):
+    robot = {"arm9": syn.arm_with_fingers(), "humanoid": syn.humanoid(),
+             "mixed": syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                          "continuous", "prismatic"])}[name]
+    pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    src = ctypes.c_char_p()
+    assert N.load().sgdyn_jit_source(pm._h, ops, ctypes.byref(src)) == 0
+    nv = _nvrtc()
+    names, texts = _headers()
+    prog = ctypes.c_void_p()
+    arr = lambda xs: (ctypes.c_char_p * len(xs))(*xs)  # noqa: E731
+    assert nv.nvrtcCreateProgram(ctypes.byref(prog), src.value, b"sgjit_step.cu", len(names), arr(texts),
+                                 arr(names)) == 0
+    opts = [b"--gpu-architecture=sm_103a", b"-std=c++17", b"-lineinfo"]
+    rc = nv.nvrtcCompileProgram(prog, len(opts), arr(opts))
+    if rc != 0:
+        n = ctypes.c_size_t()
+        nv.nvrtcGetProgramLogSize(prog, ctypes.byref(n))
+        log = ctypes.create_string_buffer(n.value)
+        nv.nvrtcGetProgramLog(prog, log)
+        pytest.fail(log.value.decode()[:3000])
+    size = ctypes.c_size_t()
+    assert nv.nvrtcGetCUBINSize(prog, ctypes.byref(size)) == 0 and size.value > 1000
+    nv.nvrtcDestroyProgram(ctypes.byref(prog))
