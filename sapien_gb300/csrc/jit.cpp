@@ -23,6 +23,7 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <sstream>
 #include <vector>
@@ -94,6 +95,9 @@ int g_enable = -1;  // -1: read SGDYN_JIT on first use
 int64_t g_min_n = 2048;
 std::map<std::string, CUfunction> g_functions;  // key: source hash + device
 std::map<std::string, std::string> g_failed;    // key -> reason
+// fast path: (model uid, table version, ops, device) -> kernel, so a launch does no string work
+std::map<std::tuple<uint64_t, uint64_t, int, int>, CUfunction> g_by_model;
+std::map<std::tuple<uint64_t, uint64_t, int, int>, std::string> g_failed_by_model;
 
 void read_env_config() {
   if (g_enable >= 0) return;
@@ -200,6 +204,8 @@ bool compile_cubin(const std::string& src, std::vector<char>* cubin, std::string
   return true;
 }
 
+CUfunction get_function_slow(const Model& M, int ops, int dev, std::string* why);
+
 // Returns the specialised kernel for (M, ops) on the current device, compiling if needed.
 CUfunction get_function(const Model& M, int ops, std::string* why) {
   Api& A = api();
@@ -212,6 +218,22 @@ CUfunction get_function(const Model& M, int ops, std::string* why) {
     *why = "no CUDA device";
     return nullptr;
   }
+  const auto fast = std::make_tuple(M.uid(), M.table_version(), ops, dev);
+  auto it = g_by_model.find(fast);
+  if (it != g_by_model.end()) return it->second;
+  auto bad = g_failed_by_model.find(fast);
+  if (bad != g_failed_by_model.end()) {
+    *why = bad->second;
+    return nullptr;
+  }
+  CUfunction fn = get_function_slow(M, ops, dev, why);
+  if (fn) g_by_model[fast] = fn;
+  else g_failed_by_model[fast] = *why;
+  return fn;
+}
+
+CUfunction get_function_slow(const Model& M, int ops, int dev, std::string* why) {
+  Api& A = api();
   const std::string src = generate_source(M, ops);
   int major = 0, minor = 0;
   A.version(&major, &minor);

@@ -17,6 +17,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <charconv>
 #include <cmath>
 #include <cstring>
@@ -341,7 +342,13 @@ bool Model::has_free_flyer() const {
   return false;
 }
 
+uint64_t Model::next_uid() {
+  static std::atomic<uint64_t> counter{1};
+  return counter++;
+}
+
 void Model::rebuild_table() {
+  version_++;
   int nj = njoints(), nl = int(link_bodies_.size());
   table_.assign(model_table_bytes(nj, nl), 0);
   auto* hdr = reinterpret_cast<DModel*>(table_.data());

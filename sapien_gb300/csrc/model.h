@@ -72,6 +72,11 @@ class Model {
 
   ~Model();
 
+  // Identity of this model and of the current contents of its tables (bumped whenever
+  // the tables are rebuilt), for caches keyed on the table contents.
+  uint64_t uid() const { return uid_; }
+  uint64_t table_version() const { return version_; }
+
  private:
   void rebuild_table();
   int nq_ext_ = 0, nv_ = 0, nq_int_ = 0;
@@ -80,6 +85,9 @@ class Model {
   std::vector<unsigned char> table_;
   std::map<int, void*> dev_;       // device ordinal -> device copy of table_
   std::mutex mu_;
+  uint64_t uid_ = next_uid();
+  uint64_t version_ = 0;
+  static uint64_t next_uid();
 };
 
 }  // namespace sgdyn
