@@ -35,12 +35,13 @@ N_ENVS = 16384
 WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs per GPU, "
             "FK (all link poses) + WORLD Jacobian + CRBA + RNEA + ABA per env per step")
 
-# FP64 (thread-level) instructions per environment-step of the fused kernel, from the ncu
-# capture summarised in profiles/step_kernel_arm9.md: 3675 DFMA + 1597 DADD/DMUL.
-FP64_INST_PER_ENV = 5272
-# DRAM bytes (read + write) per environment of one fused launch, same capture
-# (161.7 MB per 16384-environment launch).
-DRAM_BYTES_PER_ENV = 161.7e6 / 16384
+# FP64 thread-instructions per environment-step and DRAM bytes per environment of one
+# fused launch, from the ncu captures summarised in profiles/step_kernel_arm9.md, for the
+# model-specialised kernel (run-time compiled) and the generic one.
+KERNEL_COUNTERS = {
+    "specialised": {"fp64_inst_per_env": 5209, "dram_bytes_per_env": 35.68e6 / 16384},
+    "generic": {"fp64_inst_per_env": 5272, "dram_bytes_per_env": 161.7e6 / 16384},
+}
 
 
 def parse_args():
@@ -291,6 +292,8 @@ def main():
     tau_o, qdd_o = torch.empty(n, nv, **f64), torch.empty(n, nv, **f64)
     pm._prepare(dev)
     L = N.load()
+    kernel = "specialised" if L.sgdyn_jit_prepare(pm._h, N.OP_ALL) == 0 else "generic"
+    counters = KERNEL_COUNTERS[kernel]
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
@@ -390,7 +393,7 @@ def main():
     achieved_gbs = alg / (ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved_gbs / peaks["hbm_gbs"],
-                "traffic": DRAM_BYTES_PER_ENV * n if DRAM_BYTES_PER_ENV else None,
+                "traffic": counters["dram_bytes_per_env"] * n,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": alg}
     dfma = fp64_peak_dfma_per_s()
@@ -398,10 +401,9 @@ def main():
     if dfma:
         roofline_fp64 = {"bound": "fp64", "peak": dfma / 1e9, "unit": "G FP64 inst/s (per lane)",
                          "peak_source": "measured live: DFMA chain microbenchmark (csrc_probe/fp64_peak.cu)"}
-        if FP64_INST_PER_ENV:
-            ach = FP64_INST_PER_ENV * n / (ms * 1e-3) / 1e9
-            roofline_fp64.update({"achieved": ach, "frac": ach / (dfma / 1e9),
-                                  "inst_per_env_step": FP64_INST_PER_ENV})
+        ach = counters["fp64_inst_per_env"] * n / (ms * 1e-3) / 1e9
+        roofline_fp64.update({"achieved": ach, "frac": ach / (dfma / 1e9),
+                              "inst_per_env_step": counters["fp64_inst_per_env"]})
 
     # ---- CPU baseline on a bounded sample + parity of that sample --------------------
     from oracle.oracle import Oracle
@@ -438,7 +440,8 @@ def main():
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n_envs_per_gpu": n, "nv": nv, "links": nl,
                    "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
-                   "parallelism": f"data-parallel replicas over environments x{world}"},
+                   "parallelism": f"data-parallel replicas over environments x{world}",
+                   "kernel": kernel},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e},
         "gpu_launches": args.steps,
