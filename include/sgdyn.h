@@ -60,6 +60,29 @@ const char* sgdyn_last_error(void);
 int sgdyn_model_from_urdf(const char* urdf_xml, const double gravity[3], sgdyn_model** out);
 void sgdyn_model_free(sgdyn_model* m);
 
+/* Native model source (addition): the articulation SAPIEN's create_pinocchio_model exports
+ * (python/py_package/wrapper/pinocchio_model.py:317-326 with urdf_exporter.py:21-152), built
+ * without the URDF text. Poses are (x y z qw qx qy qz). Joint types: 0 fixed, 1 revolute
+ * (continuous when lower < -1e5 and upper > 1e5), 2 prismatic, 3 free (root only; becomes
+ * fixed when force_fix_root). parent = -1 marks the root joint. Link i is named link_i,
+ * the joint whose child is link i joint_i; the joint order is set to the non-fixed joints
+ * in the given order and the link order to link_0 .. link_{nlinks-1}. */
+typedef struct {
+  double mass;
+  double cmass_pose[7]; /* centre-of-mass frame in the link frame */
+  double inertia[3];    /* principal moments in the centre-of-mass frame */
+} sgdyn_link_desc;
+typedef struct {
+  int type;
+  int parent;
+  int child;
+  double pose_in_parent[7];
+  double pose_in_child[7];
+  double lower, upper;
+} sgdyn_joint_desc;
+int sgdyn_model_from_articulation(const sgdyn_link_desc* links, int nlinks, const sgdyn_joint_desc* joints,
+                                  int njoints, const double gravity[3], int force_fix_root, sgdyn_model** out);
+
 /* PinocchioModel::setJointOrder (pinocchio_model.cpp:99-128). */
 int sgdyn_model_set_joint_order(sgdyn_model* m, const char* const* names, int n);
 /* PinocchioModel::setLinkOrder (pinocchio_model.cpp:130-140). */
@@ -114,6 +137,14 @@ int sgdyn_compute_inverse_dynamics(const sgdyn_model* m, int64_t n, const double
 /* PinocchioModel::computeForwardDynamics (ABA, pinocchio_model.cpp:221-226): qdd [n][nv]. */
 int sgdyn_compute_forward_dynamics(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                    const double* tau, double* qdd, int layout, void* stream);
+
+/* PhysxArticulation::computePassiveForce (src/physx/articulation.cpp:400-418) on SAPIEN's
+ * batched GPU state buffers (src/physx/physx_system.cpp:1074-1081): qpos / qvel float32
+ * [n][in_stride] (in_stride = maxDof), result float32 into qf [n][out_stride]. Computed in
+ * FP64 as RNEA(q, qd, 0) with the gravity and / or velocity terms selected. */
+int sgdyn_compute_passive_force_f32(const sgdyn_model* m, int64_t n, const float* qpos, const float* qvel,
+                                    int64_t in_stride, int gravity, int coriolis_and_centrifugal, float* qf,
+                                    int64_t out_stride, void* stream);
 
 /* One fused sweep computing any subset (ops = SGDYN_OP_* bits) of the five calls above
  * on the same q / qd: outputs for unrequested ops may be NULL. No reference counterpart

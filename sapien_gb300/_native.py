@@ -69,6 +69,8 @@ EXPORTED = (
     "sgdyn_jit_config",
     "sgdyn_jit_prepare",
     "sgdyn_jit_source",
+    "sgdyn_model_from_articulation",
+    "sgdyn_compute_passive_force_f32",
 )
 
 _lib = None
@@ -129,6 +131,8 @@ def load():
     L.sgdyn_batch_info.argtypes = [vp, P(i64), P(i32), P(i32), P(i32)]
     L.sgdyn_batch_set_launch.argtypes = [vp, i32, i32, i32]
     L.sgdyn_batch_step.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.sgdyn_model_from_articulation.argtypes = [vp, i32, vp, i32, P(dbl), i32, P(vp)]
+    L.sgdyn_compute_passive_force_f32.argtypes = [vp, i64, vp, vp, i64, i32, i32, vp, i64, vp]
     L.sgdyn_jit_config.argtypes = [i32, i64, P(i32), P(i64)]
     L.sgdyn_jit_prepare.argtypes = [vp, i32]
     L.sgdyn_jit_source.argtypes = [vp, i32, P(ctypes.c_char_p)]

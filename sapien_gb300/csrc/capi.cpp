@@ -187,6 +187,21 @@ int sgdyn_model_from_urdf(const char* urdf_xml, const double gravity[3], sgdyn_m
   });
 }
 
+int sgdyn_model_from_articulation(const sgdyn_link_desc* links, int nlinks, const sgdyn_joint_desc* joints,
+                                  int njoints, const double gravity[3], int force_fix_root, sgdyn_model** out) {
+  if (!links || (!joints && njoints > 0) || !gravity || !out) return fail(SGDYN_ERR_NULL, "null argument");
+  static_assert(sizeof(sgdyn_link_desc) == sizeof(ArtLink), "link layout");
+  static_assert(sizeof(sgdyn_joint_desc) == sizeof(ArtJoint), "joint layout");
+  return guarded([&] {
+    *out = nullptr;
+    Model* M = Model::from_articulation(reinterpret_cast<const ArtLink*>(links), nlinks,
+                                        reinterpret_cast<const ArtJoint*>(joints), njoints, gravity,
+                                        force_fix_root != 0);
+    *out = new sgdyn_model{M};
+    return SGDYN_OK;
+  });
+}
+
 void sgdyn_model_free(sgdyn_model* m) {
   if (!m) return;
   delete m->impl;

@@ -174,48 +174,17 @@ bool is_identity(const double* R) {
 
 }  // namespace
 
-Model* Model::from_urdf(const std::string& xml, const double g[3]) {
-  auto root = parse_xml(xml);
-  if (root->name != "robot") throw std::runtime_error("URDF: root element is not <robot>");
-  struct JointDesc {
-    std::string type, parent, child;
-    Placement origin;
-    double axis[3];
-  };
-  std::map<std::string, const XmlNode*> links;
-  std::map<std::string, JointDesc> jdesc;  // std::map: byte-wise name order
+// Builds the depth-first tree from link inertias (origin form, link frame) and joint
+// descriptions keyed by name (std::map: byte-wise name order for siblings).
+Model* Model::build_tree(const std::map<std::string, BodyInertia>& links, const std::map<std::string, JointSpec>& jdesc,
+                         const double g[3]) {
   std::map<std::string, std::string> parent_joint_of;  // child link -> joint name
-  for (auto& c : root->children) {
-    if (c->name == "link") {
-      auto* n = c->attr("name");
-      if (!n) throw std::runtime_error("URDF: link without name");
-      if (links.count(*n)) throw std::runtime_error("URDF: duplicate link " + *n);
-      links[*n] = c.get();
-    } else if (c->name == "joint") {
-      auto* n = c->attr("name");
-      auto* t = c->attr("type");
-      if (!n || !t) throw std::runtime_error("URDF: joint without name or type");
-      const XmlNode* pe = c->child("parent");
-      const XmlNode* ce = c->child("child");
-      if (!pe || !ce || !pe->attr("link") || !ce->attr("link"))
-        throw std::runtime_error("URDF: joint " + *n + " lacks parent/child");
-      JointDesc d;
-      d.type = *t;
-      d.parent = *pe->attr("link");
-      d.child = *ce->attr("link");
-      d.origin = origin_of(c.get());
-      d.axis[0] = 1; d.axis[1] = 0; d.axis[2] = 0;
-      if (auto* ax = c->child("axis"))
-        if (auto* a = ax->attr("xyz")) parse_doubles(*a, d.axis, 3);
-      if (jdesc.count(*n)) throw std::runtime_error("URDF: duplicate joint " + *n);
-      if (parent_joint_of.count(d.child)) throw std::runtime_error("URDF: link " + d.child + " has two parents");
-      parent_joint_of[d.child] = *n;
-      jdesc[*n] = d;
-    }
-  }
   for (auto& kv : jdesc) {
-    if (!links.count(kv.second.parent) || !links.count(kv.second.child))
+    const JointSpec& d = kv.second;
+    if (!links.count(d.parent) || !links.count(d.child))
       throw std::runtime_error("URDF: joint " + kv.first + " references an unknown link");
+    if (parent_joint_of.count(d.child)) throw std::runtime_error("URDF: link " + d.child + " has two parents");
+    parent_joint_of[d.child] = kv.first;
   }
   std::vector<std::string> roots;
   for (auto& kv : links)
@@ -230,14 +199,14 @@ Model* Model::from_urdf(const std::string& xml, const double g[3]) {
   uni.name = "universe";
   uni.placement = identity();
   M->joints.push_back(uni);
-  M->joints[0].inertia = link_inertia(links[roots[0]]);
+  M->joints[0].inertia = links.at(roots[0]);
   M->bodies.push_back({roots[0], 0, identity()});
   std::function<void(const std::string&, int)> visit = [&](const std::string& link, int body_idx) {
     const HostBody pb = M->bodies[body_idx];
     for (auto& jn : children[link]) {
-      const JointDesc& d = jdesc[jn];
+      const JointSpec& d = jdesc.at(jn);
       Placement P = compose(pb.placement, d.origin);
-      BodyInertia Yc = link_inertia(links[d.child]);
+      BodyInertia Yc = links.at(d.child);
       if (d.type == "fixed") {
         add_inertia(M->joints[pb.joint].inertia, transport(Yc, P));
         M->bodies.push_back({d.child, pb.joint, P});
@@ -285,6 +254,142 @@ Model* Model::from_urdf(const std::string& xml, const double g[3]) {
   for (auto& b : M->bodies) ln.push_back(b.name);
   M->set_joint_order(jn);
   M->set_link_order(ln);
+  return M;
+}
+
+Model* Model::from_urdf(const std::string& xml, const double g[3]) {
+  auto root = parse_xml(xml);
+  if (root->name != "robot") throw std::runtime_error("URDF: root element is not <robot>");
+  std::map<std::string, BodyInertia> links;
+  std::map<std::string, JointSpec> jdesc;
+  for (auto& c : root->children) {
+    if (c->name == "link") {
+      auto* n = c->attr("name");
+      if (!n) throw std::runtime_error("URDF: link without name");
+      if (links.count(*n)) throw std::runtime_error("URDF: duplicate link " + *n);
+      links[*n] = link_inertia(c.get());
+    } else if (c->name == "joint") {
+      auto* n = c->attr("name");
+      auto* t = c->attr("type");
+      if (!n || !t) throw std::runtime_error("URDF: joint without name or type");
+      const XmlNode* pe = c->child("parent");
+      const XmlNode* ce = c->child("child");
+      if (!pe || !ce || !pe->attr("link") || !ce->attr("link"))
+        throw std::runtime_error("URDF: joint " + *n + " lacks parent/child");
+      JointSpec d;
+      d.type = *t;
+      d.parent = *pe->attr("link");
+      d.child = *ce->attr("link");
+      d.origin = origin_of(c.get());
+      d.axis[0] = 1; d.axis[1] = 0; d.axis[2] = 0;
+      if (auto* ax = c->child("axis"))
+        if (auto* a = ax->attr("xyz")) parse_doubles(*a, d.axis, 3);
+      if (jdesc.count(*n)) throw std::runtime_error("URDF: duplicate joint " + *n);
+      jdesc[*n] = d;
+    }
+  }
+  return build_tree(links, jdesc, g);
+}
+
+namespace {
+Placement pose7(const double* p) {
+  Placement P;
+  const double w = p[3], x = p[4], y = p[5], z = p[6];
+  P.R[0] = 1 - 2 * (y * y + z * z); P.R[1] = 2 * (x * y - w * z);     P.R[2] = 2 * (x * z + w * y);
+  P.R[3] = 2 * (x * y + w * z);     P.R[4] = 1 - 2 * (x * x + z * z); P.R[5] = 2 * (y * z - w * x);
+  P.R[6] = 2 * (x * z - w * y);     P.R[7] = 2 * (y * z + w * x);     P.R[8] = 1 - 2 * (x * x + y * y);
+  P.p[0] = p[0]; P.p[1] = p[1]; P.p[2] = p[2];
+  return P;
+}
+Placement inverse(const Placement& a) {
+  Placement b;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) b.R[i * 3 + j] = a.R[j * 3 + i];
+  double t[3];
+  mat_vec(b.R, a.p, t);
+  for (int k = 0; k < 3; k++) b.p[k] = -t[k];
+  return b;
+}
+}  // namespace
+
+// Restates python/py_package/wrapper/urdf_exporter.py:21-152 (export_link, export_joint,
+// export_kinematic_chain_urdf with force_fix_root) and create_pinocchio_model
+// (python/py_package/wrapper/pinocchio_model.py:317-326) without the XML round trip.
+Model* Model::from_articulation(const ArtLink* links, int nlinks, const ArtJoint* joints, int njoints,
+                                const double g[3], bool force_fix_root) {
+  if (nlinks <= 0) throw std::runtime_error("articulation without links");
+  std::map<std::string, BodyInertia> L;
+  std::map<std::string, JointSpec> J;
+  L["world"] = BodyInertia();
+  for (int i = 0; i < nlinks; i++) {
+    // inertial: origin = c.o.m. pose, diagonal principal inertia in that frame
+    const Placement o = pose7(links[i].cmass_pose);
+    double Ic[9], T[9], Rt[9];
+    const double Id[9] = {links[i].inertia[0], 0, 0, 0, links[i].inertia[1], 0, 0, 0, links[i].inertia[2]};
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) Rt[r * 3 + c] = o.R[c * 3 + r];
+    mat_mul(o.R, Id, T);
+    mat_mul(T, Rt, Ic);
+    BodyInertia B;
+    const double m = links[i].mass, *c = o.p;
+    const double cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+    B.m = m;
+    for (int k = 0; k < 3; k++) B.h[k] = m * c[k];
+    B.I[0] = Ic[0] + m * (cc - c[0] * c[0]);
+    B.I[1] = Ic[1] - m * c[0] * c[1];
+    B.I[2] = Ic[2] - m * c[0] * c[2];
+    B.I[3] = Ic[4] + m * (cc - c[1] * c[1]);
+    B.I[4] = Ic[5] - m * c[1] * c[2];
+    B.I[5] = Ic[8] + m * (cc - c[2] * c[2]);
+    L["link_" + std::to_string(i)] = B;
+  }
+  std::vector<std::string> active;
+  for (int k = 0; k < njoints; k++) {
+    const ArtJoint& a = joints[k];
+    if (a.child < 0 || a.child >= nlinks || a.parent >= nlinks)
+      throw std::runtime_error("articulation joint references an unknown link");
+    const std::string ci = std::to_string(a.child), name = "joint_" + ci;
+    JointSpec js;
+    js.axis[0] = 1; js.axis[1] = 0; js.axis[2] = 0;
+    if (a.parent < 0) {
+      js.type = (a.type == ART_FIXED || force_fix_root) ? "fixed" : "floating";
+      js.parent = "world";
+      js.child = "link_" + ci;
+      js.origin = identity();
+      J[name] = js;
+      if (js.type != "fixed") active.push_back(name);
+      continue;
+    }
+    switch (a.type) {
+      case ART_FIXED: js.type = "fixed"; break;
+      case ART_PRISMATIC: js.type = "prismatic"; break;
+      case ART_REVOLUTE: js.type = (a.lower < -1e5 && a.upper > 1e5) ? "continuous" : "revolute"; break;
+      default: throw std::runtime_error("invalid joint type for a non-root joint");
+    }
+    js.parent = "link_" + std::to_string(a.parent);
+    js.child = "link_dummy_" + ci;
+    js.origin = pose7(a.pose_in_parent);
+    J[name] = js;
+    JointSpec dj;
+    dj.type = "fixed";
+    dj.parent = "link_dummy_" + ci;
+    dj.child = "link_" + ci;
+    dj.origin = inverse(pose7(a.pose_in_child));
+    dj.axis[0] = 0; dj.axis[1] = 0; dj.axis[2] = 0;
+    J["joint_dummy_" + ci] = dj;
+    L["link_dummy_" + ci] = BodyInertia();
+    if (js.type != "fixed") active.push_back(name);
+  }
+  Model* M = build_tree(L, J, g);
+  try {
+    std::vector<std::string> lo;
+    for (int i = 0; i < nlinks; i++) lo.push_back("link_" + std::to_string(i));
+    M->set_joint_order(active);
+    M->set_link_order(lo);
+  } catch (...) {
+    delete M;
+    throw;
+  }
   return M;
 }
 

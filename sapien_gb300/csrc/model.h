@@ -33,6 +33,29 @@ struct HostJoint {
   int idx_q = 0, idx_v = 0, nq = 0, nv = 0, depth = 0;
 };
 
+struct JointSpec {  // a URDF joint before tree building
+  std::string type, parent, child;
+  Placement origin;
+  double axis[3];
+};
+
+// An articulation as SAPIEN describes it (PhysxArticulationLinkComponent / Joint getters):
+// poses are (x y z qw qx qy qz); inertia are principal moments in the c.o.m. frame.
+struct ArtLink {
+  double mass;
+  double cmass_pose[7];
+  double inertia[3];
+};
+enum ArtJointType : int { ART_FIXED = 0, ART_REVOLUTE = 1, ART_PRISMATIC = 2, ART_FREE = 3 };
+struct ArtJoint {
+  int type;    // ArtJointType
+  int parent;  // parent link index, -1 for the root joint
+  int child;   // child link index
+  double pose_in_parent[7];
+  double pose_in_child[7];
+  double lower, upper;  // limits of the joint's single coordinate
+};
+
 struct HostBody {  // a BODY frame (one per URDF link)
   std::string name;
   int joint;
@@ -43,6 +66,16 @@ class Model {
  public:
   // Builds from URDF XML; the root link is welded to the universe (joint 0).
   static Model* from_urdf(const std::string& xml, const double gravity[3]);
+  // Builds the tree SAPIEN's URDF exporter would describe for this articulation
+  // (link_{i} / joint_{child} names, a dummy link per moving joint, joint axis x), then
+  // sets the joint order to the active joints in articulation order and the link order to
+  // the articulation's links, as create_pinocchio_model does.
+  static Model* from_articulation(const ArtLink* links, int nlinks, const ArtJoint* joints, int njoints,
+                                  const double gravity[3], bool force_fix_root);
+  // Builds from link inertias (origin form, in the link frame) and joint descriptions,
+  // both keyed by name; the root link is welded to the universe.
+  static Model* build_tree(const std::map<std::string, BodyInertia>& links,
+                           const std::map<std::string, JointSpec>& joints, const double gravity[3]);
 
   void set_joint_order(const std::vector<std::string>& names);
   void set_link_order(const std::vector<std::string>& names);

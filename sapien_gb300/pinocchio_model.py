@@ -83,6 +83,19 @@ class PinocchioModel:
         self._device = None
         self._refresh()
 
+    @classmethod
+    def _from_handle(cls, h, joint_order_set=False, link_order_set=False):
+        """Wrap a model handle created through another C-ABI constructor."""
+        self = cls.__new__(cls)
+        self._h = h
+        self._joint_order_set = joint_order_set
+        self._link_order_set = link_order_set
+        self._fk_cache = None
+        self._jac_q = None
+        self._device = None
+        self._refresh()
+        return self
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -322,6 +335,30 @@ class PinocchioModel:
                 self._h, n, int(link_index), _ptr(tgt), _ptr(q0), _ptr(mask), float(eps), int(max_iterations),
                 float(dt), float(damp), _ptr(q), _ptr(ok), _ptr(err), N.ENV_MAJOR, self._stream(dev)))
         return q, ok.bool(), err
+
+    def compute_passive_force_batched(self, qpos, qvel=None, gravity=True, coriolis_and_centrifugal=True, out=None):
+        """PhysxArticulation.compute_passive_force for a whole batch, read straight from
+        SAPIEN-style float32 state buffers: qpos / qvel [N, maxDof] (maxDof >= dof, padded
+        rows as SAPIEN's GPU system exports them). Returns (or fills `out`) a float32
+        [N, maxDof] tensor whose first dof columns hold RNEA(q, qd, 0) with the selected terms,
+        computed in FP64."""
+        torch = _torch()
+        self._require_order()
+        if qpos.dtype != torch.float32 or not qpos.is_cuda or qpos.dim() != 2 or qpos.stride(1) != 1:
+            raise TypeError("qpos must be a float32 CUDA tensor [N, maxDof] with unit column stride")
+        if coriolis_and_centrifugal:
+            if qvel is None or qvel.shape != qpos.shape or qvel.stride() != qpos.stride() or qvel.dtype != torch.float32:
+                raise TypeError("qvel must be a float32 CUDA tensor laid out like qpos")
+        n, width = qpos.shape
+        if out is None:
+            out = torch.zeros(n, width, dtype=torch.float32, device=qpos.device)
+        dev = qpos.device
+        self._prepare(dev)
+        with torch.cuda.device(dev):
+            N.check(N.load().sgdyn_compute_passive_force_f32(
+                self._h, n, _ptr(qpos), _ptr(qvel) if coriolis_and_centrifugal else None, qpos.stride(0),
+                int(bool(gravity)), int(bool(coriolis_and_centrifugal)), _ptr(out), out.stride(0), self._stream(dev)))
+        return out
 
     # ---- reference single-instance API -----------------------------------
     def compute_forward_kinematics(self, qpos):
