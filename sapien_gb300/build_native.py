@@ -54,7 +54,7 @@ def _compile(src, hmt, verbose):
     return obj, None
 
 
-JIT_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
+JIT_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh", "diff_core.cuh", "diff_kernels.cuh")
 
 
 def _write_jit_headers():

@@ -302,7 +302,8 @@ int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
 int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
   if (!m || !source) return fail(SGDYN_ERR_NULL, "null argument");
   thread_local std::string buf;
-  buf = step_jit_source(*m->impl, ops);
+  // ops > 0: fused sweep with that op set; -1 / -2: rollout forward / backward
+  buf = ops > 0 ? step_jit_source(*m->impl, ops) : rollout_jit_source(*m->impl, ops == -2);
   *source = buf.c_str();
   return SGDYN_OK;
 }
@@ -596,6 +597,8 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
     a.dt = dt;
     a.q0 = q0; a.qd0 = qd0; a.tau = tau;
     a.qT = qT; a.qdT = qdT; a.q_ckpt = q_ckpt; a.qd_ckpt = qd_ckpt;
+    std::string why;
+    if (launch_rollout_jit(Mo, false, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
     return launch_status(launch_rollout_forward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
   });
 }
@@ -639,6 +642,8 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
     a.qd_ckpt = const_cast<double*>(qd_ckpt);
     a.qT_bar = qT_bar; a.qdT_bar = qdT_bar;
     a.q0_bar = q0_bar; a.qd0_bar = qd0_bar; a.tau_bar = tau_bar; a.scratch = scratch;
+    std::string why;
+    if (launch_rollout_jit(Mo, true, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
     return launch_status(launch_rollout_backward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
   });
 }

@@ -58,14 +58,14 @@ __device__ __forceinline__ RBI local_rbi(const DJoint& J) {
 
 // ABA in the world frame; fills W (acc = world accelerations incl. gravity) and qdd
 // (external order).
-template <int MAXJ>
-__device__ void aba_forward(const DModel* __restrict__ model, const double* q, const double* qd, const double* tau,
+template <int MAXJ, class Tab>
+__device__ void aba_forward(const Tab& T, const double* q, const double* qd, const double* tau,
                             double* qdd, DynWork<MAXJ>& W) {
-  const DJoint* __restrict__ JT = model_joints(model);
-  const int nj = model->nj;
+  const int nj = T.nj();
   const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+#pragma unroll
   for (int i = 1; i < nj; i++) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent, iv = J.ivx;
     pose_and_S(J, i, q, W);
     const RBI Y = rbi_transport(local_rbi(J), W.oR[i], W.op[i]);
@@ -80,8 +80,9 @@ __device__ void aba_forward(const DModel* __restrict__ model, const double* q, c
     W.IA[i] = sym6_from_rbi(Y);
     W.pA[i] = add_crossf(zero, v, h);
   }
+#pragma unroll
   for (int i = nj - 1; i >= 1; i--) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent, iv = J.ivx;
     if (J.nv == 1) {
       const Mot S = W.Sw[iv];
@@ -131,9 +132,10 @@ __device__ void aba_forward(const DModel* __restrict__ model, const double* q, c
       chol6(W.Lff);
     }
   }
-  const Mot a0{mk(-model->gravity[0], -model->gravity[1], -model->gravity[2]), mk(0, 0, 0)};
+  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
+#pragma unroll
   for (int i = 1; i < nj; i++) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent, iv = J.ivx;
     Mot a = add6((p == 0) ? a0 : W.acc[p], W.cb[i]);
     if (J.nv == 1) {
@@ -155,16 +157,16 @@ __device__ void aba_forward(const DModel* __restrict__ model, const double* q, c
 
 // y = M^-1 x (external order) from ABA's stored U, D^-1, S: the ABA recursion with zero
 // velocity and zero gravity.
-template <int MAXJ>
-__device__ void minv_solve(const DModel* __restrict__ model, DynWork<MAXJ>& W, const double* x, double* y) {
-  const DJoint* __restrict__ JT = model_joints(model);
-  const int nj = model->nj;
+template <int MAXJ, class Tab>
+__device__ void minv_solve(const Tab& T, DynWork<MAXJ>& W, const double* x, double* y) {
+  const int nj = T.nj();
   const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
   Mot* pAs = W.pA;  // reused as scratch: ABA's bias forces are no longer needed
   double* us = W.uv;
   for (int i = 1; i < nj; i++) pAs[i] = zero;
+#pragma unroll
   for (int i = nj - 1; i >= 1; i--) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent, iv = J.ivx;
     if (J.nv == 1) {
       const double u = x[J.vcol] - dot6(W.Sw[iv], pAs[i]);
@@ -175,8 +177,9 @@ __device__ void minv_solve(const DModel* __restrict__ model, DynWork<MAXJ>& W, c
     }
   }
   Mot* as = W.cb;  // scratch accelerations
+#pragma unroll
   for (int i = 1; i < nj; i++) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent, iv = J.ivx;
     Mot a = (p == 0) ? zero : as[p];
     if (J.nv == 1) {
@@ -197,15 +200,15 @@ __device__ void minv_solve(const DModel* __restrict__ model, DynWork<MAXJ>& W, c
 }
 
 // RNEA forward quantities (pose, S, v, a, I, I v) for given qdd.
-template <int MAXJ>
-__device__ void rnea_forward(const DModel* __restrict__ model, const double* q, const double* qd, const double* qdd,
+template <int MAXJ, class Tab>
+__device__ void rnea_forward(const Tab& T, const double* q, const double* qd, const double* qdd,
                              DynWork<MAXJ>& W) {
-  const DJoint* __restrict__ JT = model_joints(model);
-  const int nj = model->nj;
+  const int nj = T.nj();
   const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
-  const Mot a0{mk(-model->gravity[0], -model->gravity[1], -model->gravity[2]), mk(0, 0, 0)};
+  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
+#pragma unroll
   for (int i = 1; i < nj; i++) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent, iv = J.ivx;
     pose_and_S(J, i, q, W);
     const RBI Y = rbi_transport(local_rbi(J), W.oR[i], W.op[i]);
@@ -231,15 +234,15 @@ struct AdjScratch {
 // Reverse-mode RNEA sweep over the forward quantities in W (acc must be the world
 // accelerations the torques were computed with). taubar and the outputs are external
 // order; any output pointer may be null; outputs are scaled by `sign`. W is not modified.
-template <int MAXJ>
-__device__ void rnea_adjoint(const DModel* __restrict__ model, const DynWork<MAXJ>& W, AdjScratch<MAXJ>& A,
+template <int MAXJ, class Tab>
+__device__ void rnea_adjoint(const Tab& T, const DynWork<MAXJ>& W, AdjScratch<MAXJ>& A,
                              const double* taubar, double* qbar, double* qdbar, double* qddbar, double sign) {
-  const DJoint* __restrict__ JT = model_joints(model);
-  const int nj = model->nj;
+  const int nj = T.nj();
   const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
-  const Mot a0{mk(-model->gravity[0], -model->gravity[1], -model->gravity[2]), mk(0, 0, 0)};
+  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
+#pragma unroll
   for (int i = 1; i < nj; i++) {
-    const DJoint& J = JT[i];
+    const DJoint& J = T.joint(i);
     const int p = J.parent, iv = J.ivx;
     Mot wi = (p == 0) ? zero : A.w[p];
     for (int k = 0; k < J.nv; k++) wi = axpy6(taubar[J.vcol + k], W.Sw[iv + k], wi);
@@ -253,8 +256,9 @@ __device__ void rnea_adjoint(const DModel* __restrict__ model, const DynWork<MAX
     A.R[i] = add_crossf(zero, wi, W.hY[i]);
     A.T[i] = rbi_mul(Y, add_crossm(zero, v, wi));
   }
+#pragma unroll
   for (int j = nj - 1; j >= 1; j--) {
-    const DJoint& J = JT[j];
+    const DJoint& J = T.joint(j);
     const int p = J.parent, iv = J.ivx;
     const Mot P = A.P[j], Q = A.Q[j], R = A.R[j], T = A.T[j], Fj = A.F[j];
     const Mot vl = (p == 0) ? zero : W.vel[p];

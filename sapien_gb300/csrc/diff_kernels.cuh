@@ -27,7 +27,8 @@ __global__ void __launch_bounds__(32) rnea_vjp_kernel(const DModel* __restrict__
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const int nv = model->nv, nq = model->nq_ext;
+  const RuntimeTab T{model};
+  const int nv = T.nv(), nq = T.nq_ext();
   double q[MAXQ], qd[MAXV], qdd[MAXV], tb[MAXV], o1[MAXV], o2[MAXV], o3[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
@@ -35,8 +36,8 @@ __global__ void __launch_bounds__(32) rnea_vjp_kernel(const DModel* __restrict__
   load_row<MAXJ>(a.bar, e, nv, tb);
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
-  rnea_forward(model, q, qd, qdd, W);
-  rnea_adjoint(model, W, A, tb, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, a.o3.p ? o3 : nullptr, 1.0);
+  rnea_forward<MAXJ>(T, q, qd, qdd, W);
+  rnea_adjoint<MAXJ>(T, W, A, tb, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, a.o3.p ? o3 : nullptr, 1.0);
   if (a.o1.p) store_row(a.o1, e, nv, o1);
   if (a.o2.p) store_row(a.o2, e, nv, o2);
   if (a.o3.p) store_row(a.o3, e, nv, o3);
@@ -47,7 +48,8 @@ __global__ void __launch_bounds__(32) aba_vjp_kernel(const DModel* __restrict__ 
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const int nv = model->nv, nq = model->nq_ext;
+  const RuntimeTab T{model};
+  const int nv = T.nv(), nq = T.nq_ext();
   double q[MAXQ], qd[MAXV], tau[MAXV], qb[MAXV], qdd[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
@@ -55,9 +57,9 @@ __global__ void __launch_bounds__(32) aba_vjp_kernel(const DModel* __restrict__ 
   load_row<MAXJ>(a.bar, e, nv, qb);
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
-  aba_forward(model, q, qd, tau, qdd, W);
-  minv_solve(model, W, qb, lam);
-  rnea_adjoint(model, W, A, lam, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, nullptr, -1.0);
+  aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
+  minv_solve<MAXJ>(T, W, qb, lam);
+  rnea_adjoint<MAXJ>(T, W, A, lam, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, nullptr, -1.0);
   if (a.o1.p) store_row(a.o1, e, nv, o1);
   if (a.o2.p) store_row(a.o2, e, nv, o2);
   if (a.o3.p) store_row(a.o3, e, nv, lam);
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(32) fk_vjp_kernel(const DModel* __restrict__ m
   const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
   Mot* F = W.pA;
   for (int i = 1; i < nj; i++) {
-    pose_and_S(JT[i], i, q, W);
+    pose_and_S<MAXJ>(JT[i], i, q, W);
     F[i] = zero;
   }
   for (int l = 0; l < nl; l++) {
@@ -113,17 +115,18 @@ __global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __re
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const int nv = model->nv, nq = model->nq_ext;
+  const RuntimeTab T{model};
+  const int nv = T.nv(), nq = T.nq_ext();
   double q[MAXQ], qd[MAXV], qdd[MAXV], tb[MAXV], o1[MAXV], o2[MAXV], o3[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
   load_row<MAXJ>(a.x, e, nv, qdd);
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
-  rnea_forward(model, q, qd, qdd, W);
+  rnea_forward<MAXJ>(T, q, qd, qdd, W);
   for (int r = 0; r < nv; r++) {
     for (int c = 0; c < nv; c++) tb[c] = (c == r) ? 1.0 : 0.0;
-    rnea_adjoint(model, W, A, tb, o1, o2, a.d_x.p ? o3 : nullptr, 1.0);
+    rnea_adjoint<MAXJ>(T, W, A, tb, o1, o2, a.d_x.p ? o3 : nullptr, 1.0);
     for (int c = 0; c < nv; c++) {
       stv(a.d_q, e, r * nv + c, o1[c]);
       stv(a.d_qd, e, r * nv + c, o2[c]);
@@ -137,18 +140,19 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const int nv = model->nv, nq = model->nq_ext;
+  const RuntimeTab T{model};
+  const int nv = T.nv(), nq = T.nq_ext();
   double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV], er[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
   load_row<MAXJ>(a.x, e, nv, tau);
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
-  aba_forward(model, q, qd, tau, qdd, W);
+  aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
   for (int r = 0; r < nv; r++) {
     for (int c = 0; c < nv; c++) er[c] = (c == r) ? 1.0 : 0.0;
-    minv_solve(model, W, er, lam);
-    rnea_adjoint(model, W, A, lam, o1, o2, nullptr, -1.0);
+    minv_solve<MAXJ>(T, W, er, lam);
+    rnea_adjoint<MAXJ>(T, W, A, lam, o1, o2, nullptr, -1.0);
     for (int c = 0; c < nv; c++) {
       stv(a.d_q, e, r * nv + c, o1[c]);
       stv(a.d_qd, e, r * nv + c, o2[c]);
@@ -160,17 +164,19 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
 // ---- rollouts ---------------------------------------------------------------------
 
 // q <- q + dt qd for angle / slide coordinates (models without free flyers).
-__device__ __forceinline__ void euler_positions(const DModel* model, double* q, const double* qd, double dt) {
-  const DJoint* __restrict__ JT = model_joints(model);
-  for (int i = 1; i < model->nj; i++) q[JT[i].qcol] = fma(dt, qd[JT[i].vcol], q[JT[i].qcol]);
+template <class Tab>
+__device__ __forceinline__ void euler_positions(const Tab& T, double* q, const double* qd, double dt) {
+#pragma unroll
+  for (int i = 1; i < T.nj(); i++) {
+    const DJoint& J = T.joint(i);
+    q[J.qcol] = fma(dt, qd[J.vcol], q[J.qcol]);
+  }
 }
 
-template <int MAXJ>
-__global__ void __launch_bounds__(32) rollout_forward_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void rollout_forward_env(const Tab& T, const RolloutArgs& a, const int64_t e) {
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const int nv = model->nv, nq = model->nq_ext;
+  const int nv = T.nv(), nq = T.nq_ext();
   const int64_t n = a.n;
   double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
   for (int c = 0; c < nq; c++) q[c] = a.q0[e * nq + c];
@@ -183,12 +189,19 @@ __global__ void __launch_bounds__(32) rollout_forward_kernel(const DModel* __res
       for (int c = 0; c < nv; c++) a.qd_ckpt[(s * n + e) * nv + c] = qd[c];
     }
     for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
-    aba_forward(model, q, qd, tau, qdd, W);
+    aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
     for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
-    euler_positions(model, q, qd, a.dt);
+    euler_positions(T, q, qd, a.dt);
   }
   for (int c = 0; c < nq; c++) a.qT[e * nq + c] = q[c];
   for (int c = 0; c < nv; c++) a.qdT[e * nv + c] = qd[c];
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rollout_forward_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  rollout_forward_env<MAXJ>(RuntimeTab{model}, a, e);
 }
 
 // Per step of a segment the scratch holds, structure-of-arrays over environments:
@@ -199,11 +212,10 @@ __host__ __device__ inline int64_t stash_doubles_per_step(int nj, int nq, int nv
   return 12 * int64_t(nv) + int64_t(nj) * 29 + 21;
 }
 
-template <int MAXJ>
-__device__ void stash_io(const DModel* __restrict__ model, DynWork<MAXJ>& W, double* base, int64_t n, int64_t e,
-                         bool store) {
-  const DJoint* __restrict__ JT = model_joints(model);
-  const int nj = model->nj, nv = model->nv;
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, double* base, int64_t n, int64_t e,
+                                         bool store) {
+  const int nj = T.nj(), nv = T.nv();
   int64_t f = 0;
   auto io = [&](double& x) {
     if (store) base[f * n + e] = x;
@@ -213,8 +225,11 @@ __device__ void stash_io(const DModel* __restrict__ model, DynWork<MAXJ>& W, dou
   auto io6 = [&](Mot& m) {
     io(m.v.x); io(m.v.y); io(m.v.z); io(m.w.x); io(m.w.y); io(m.w.z);
   };
+#pragma unroll
   for (int k = 0; k < nv; k++) io6(W.Sw[k]);
+#pragma unroll
   for (int k = 0; k < nv; k++) io6(W.Uv[k]);
+#pragma unroll
   for (int i = 1; i < nj; i++) {
     io(W.Dinv[i]);
     io6(W.vel[i]);
@@ -225,15 +240,12 @@ __device__ void stash_io(const DModel* __restrict__ model, DynWork<MAXJ>& W, dou
     for (int k = 0; k < 6; k++) io(Y.I[k]);
   }
   for (int k = 0; k < 21; k++) io(W.Lff[k]);
-  (void)JT;
 }
 
-template <int MAXJ>
-__global__ void __launch_bounds__(32) rollout_backward_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void rollout_backward_env(const Tab& T, const RolloutArgs& a, const int64_t e) {
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const int nv = model->nv, nq = model->nq_ext, nj = model->nj;
+  const int nv = T.nv(), nq = T.nq_ext(), nj = T.nj();
   const int64_t n = a.n;
   const int64_t per_step = stash_doubles_per_step(nj, nq, nv);
   double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV], qb[MAXV], qdb[MAXV], qddb[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
@@ -250,28 +262,41 @@ __global__ void __launch_bounds__(32) rollout_backward_kernel(const DModel* __re
     for (int t = t0; t < t1; t++) {
       double* base = a.scratch + int64_t(t - t0) * per_step * n;
       for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
-      aba_forward(model, q, qd, tau, qdd, W);
-      stash_io(model, W, base, n, e, true);
+      aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
+      stash_io<MAXJ>(T, W, base, n, e, true);
       for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
-      euler_positions(model, q, qd, a.dt);
+      euler_positions(T, q, qd, a.dt);
     }
-    // reverse through the segment
+    // reverse through the segment: q' = q + dt qd' and qd' = qd + dt qdd
     for (int t = t1 - 1; t >= t0; t--) {
       double* base = a.scratch + int64_t(t - t0) * per_step * n;
-      // q' = q + dt qd'  and  qd' = qd + dt qdd
-      const DJoint* __restrict__ JT = model_joints(model);
-      for (int i = 1; i < nj; i++) qdb[JT[i].vcol] = fma(a.dt, qb[JT[i].qcol], qdb[JT[i].vcol]);
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+        qdb[J.vcol] = fma(a.dt, qb[J.qcol], qdb[J.vcol]);
+      }
       for (int c = 0; c < nv; c++) qddb[c] = a.dt * qdb[c];
-      stash_io(model, W, base, n, e, false);
-      minv_solve(model, W, qddb, lam);
+      stash_io<MAXJ>(T, W, base, n, e, false);
+      minv_solve<MAXJ>(T, W, qddb, lam);
       for (int c = 0; c < nv; c++) a.tau_bar[(int64_t(t) * n + e) * nv + c] = lam[c];
-      rnea_adjoint(model, W, A, lam, o1, o2, nullptr, -1.0);
-      for (int i = 1; i < nj; i++) qb[JT[i].qcol] += o1[JT[i].vcol];
+      rnea_adjoint<MAXJ>(T, W, A, lam, o1, o2, nullptr, -1.0);
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+        qb[J.qcol] += o1[J.vcol];
+      }
       for (int c = 0; c < nv; c++) qdb[c] += o2[c];
     }
   }
   for (int c = 0; c < nq; c++) a.q0_bar[e * nq + c] = qb[c];
   for (int c = 0; c < nv; c++) a.qd0_bar[e * nv + c] = qdb[c];
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rollout_backward_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  rollout_backward_env<MAXJ>(RuntimeTab{model}, a, e);
 }
 
 }  // namespace sgdyn

@@ -96,8 +96,8 @@ int64_t g_min_n = 2048;
 std::map<std::string, CUfunction> g_functions;  // key: source hash + device
 std::map<std::string, std::string> g_failed;    // key -> reason
 // fast path: (model uid, table version, ops, device) -> kernel, so a launch does no string work
-std::map<std::tuple<uint64_t, uint64_t, int, int>, CUfunction> g_by_model;
-std::map<std::tuple<uint64_t, uint64_t, int, int>, std::string> g_failed_by_model;
+std::map<std::tuple<uint64_t, uint64_t, int, int, int>, CUfunction> g_by_model;
+std::map<std::tuple<uint64_t, uint64_t, int, int, int>, std::string> g_failed_by_model;
 
 void read_env_config() {
   if (g_enable >= 0) return;
@@ -128,14 +128,17 @@ std::string list(It b, It e) {
   return s;
 }
 
-std::string generate_source(const Model& M, int ops) {
+enum JitKind { JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_ROLLOUT_BWD = 2 };
+
+std::string generate_source(const Model& M, int kind, int ops) {
   const auto& t = M.host_table();
   const auto* hdr = reinterpret_cast<const DModel*>(t.data());
   const DJoint* J = model_joints(hdr);
   const DLink* L = model_links(hdr);
   const int nj = hdr->nj, nl = hdr->nlinks;
   std::ostringstream o;
-  o << "#include \"step_kernel.cuh\"\nnamespace sgjit {\n";
+  o << (kind == JIT_STEP ? "#include \"step_kernel.cuh\"\n" : "#include \"diff_kernels.cuh\"\n");
+  o << "namespace sgjit {\n";
   o << "__device__ constexpr sgdyn::DModel kM = {" << hdr->nj << ", " << hdr->nv << ", " << hdr->nq_ext << ", "
     << hdr->nlinks << ", " << hdr->max_depth << ", " << hdr->n_free_flyer << ", {0, 0}, {"
     << list(hdr->gravity, hdr->gravity + 3) << "}, 0.0};\n";
@@ -154,11 +157,15 @@ std::string generate_source(const Model& M, int ops) {
       << L[l].flags << ", {0, 0}},\n";
   if (nl == 0) o << " {{1,0,0,0,1,0,0,0,1}, {0,0,0}, 0, 1, {0, 0}},\n";
   o << "};\n}  // namespace sgjit\n";
-  o << "extern \"C\" __global__ void __launch_bounds__(32) sgjit_step(const sgdyn::StepArgs a) {\n"
+  const std::string tab = "sgdyn::StaticTab<" + std::to_string(nj) + ", " + std::to_string(hdr->nv) + ", " +
+                          std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM>()";
+  const char* args = kind == JIT_STEP ? "sgdyn::StepArgs" : "sgdyn::RolloutArgs";
+  o << "extern \"C\" __global__ void __launch_bounds__(32) sgjit_kernel(const " << args << " a) {\n"
     << "  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
-    << "  if (e >= a.n) return;\n"
-    << "  sgdyn::step_env_t<" << nj << ", " << ops << ">(sgdyn::StaticTab<" << nj << ", " << hdr->nv << ", " << nl
-    << ", sgjit::kJT, sgjit::kLT, &sgjit::kM>(), a, e);\n}\n";
+    << "  if (e >= a.n) return;\n";
+  if (kind == JIT_STEP) o << "  sgdyn::step_env_t<" << nj << ", " << ops << ">(" << tab << ", a, e);\n}\n";
+  else if (kind == JIT_ROLLOUT_FWD) o << "  sgdyn::rollout_forward_env<" << nj << ">(" << tab << ", a, e);\n}\n";
+  else o << "  sgdyn::rollout_backward_env<" << nj << ">(" << tab << ", a, e);\n}\n";
   return o.str();
 }
 
@@ -180,7 +187,7 @@ void mkdirs(const std::string& path) {
 bool compile_cubin(const std::string& src, std::vector<char>* cubin, std::string* why) {
   Api& A = api();
   nvrtcProgram prog;
-  if (A.createProgram(&prog, src.c_str(), "sgjit_step.cu", kJitHeaderCount, kJitHeaderSources, kJitHeaderNames) !=
+  if (A.createProgram(&prog, src.c_str(), "sgjit_kernel.cu", kJitHeaderCount, kJitHeaderSources, kJitHeaderNames) !=
       NVRTC_SUCCESS) {
     *why = "nvrtcCreateProgram failed";
     return false;
@@ -204,10 +211,10 @@ bool compile_cubin(const std::string& src, std::vector<char>* cubin, std::string
   return true;
 }
 
-CUfunction get_function_slow(const Model& M, int ops, int dev, std::string* why);
+CUfunction get_function_slow(const Model& M, int kind, int ops, int dev, std::string* why);
 
-// Returns the specialised kernel for (M, ops) on the current device, compiling if needed.
-CUfunction get_function(const Model& M, int ops, std::string* why) {
+// Returns the specialised kernel for (M, kind, ops) on the current device, compiling if needed.
+CUfunction get_function(const Model& M, int kind, int ops, std::string* why) {
   Api& A = api();
   if (!A.loaded) {
     *why = A.why;
@@ -218,7 +225,7 @@ CUfunction get_function(const Model& M, int ops, std::string* why) {
     *why = "no CUDA device";
     return nullptr;
   }
-  const auto fast = std::make_tuple(M.uid(), M.table_version(), ops, dev);
+  const auto fast = std::make_tuple(M.uid(), M.table_version(), kind, ops, dev);
   auto it = g_by_model.find(fast);
   if (it != g_by_model.end()) return it->second;
   auto bad = g_failed_by_model.find(fast);
@@ -226,15 +233,15 @@ CUfunction get_function(const Model& M, int ops, std::string* why) {
     *why = bad->second;
     return nullptr;
   }
-  CUfunction fn = get_function_slow(M, ops, dev, why);
+  CUfunction fn = get_function_slow(M, kind, ops, dev, why);
   if (fn) g_by_model[fast] = fn;
   else g_failed_by_model[fast] = *why;
   return fn;
 }
 
-CUfunction get_function_slow(const Model& M, int ops, int dev, std::string* why) {
+CUfunction get_function_slow(const Model& M, int kind, int ops, int dev, std::string* why) {
   Api& A = api();
-  const std::string src = generate_source(M, ops);
+  const std::string src = generate_source(M, kind, ops);
   int major = 0, minor = 0;
   A.version(&major, &minor);
   char hx[40];
@@ -270,7 +277,7 @@ CUfunction get_function_slow(const Model& M, int ops, int dev, std::string* why)
   cudaFree(nullptr);  // make sure the runtime's primary context is current
   CUmodule mod;
   CUfunction fn;
-  if (A.moduleLoadData(&mod, cubin.data()) != CUDA_SUCCESS || A.moduleGetFunction(&fn, mod, "sgjit_step") != CUDA_SUCCESS) {
+  if (A.moduleLoadData(&mod, cubin.data()) != CUDA_SUCCESS || A.moduleGetFunction(&fn, mod, "sgjit_kernel") != CUDA_SUCCESS) {
     *why = "loading the compiled module failed";
     g_failed[key] = *why;
     return nullptr;
@@ -281,7 +288,10 @@ CUfunction get_function_slow(const Model& M, int ops, int dev, std::string* why)
 
 }  // namespace
 
-std::string step_jit_source(const Model& M, int ops) { return generate_source(M, ops); }
+std::string step_jit_source(const Model& M, int ops) { return generate_source(M, JIT_STEP, ops); }
+std::string rollout_jit_source(const Model& M, bool backward) {
+  return generate_source(M, backward ? JIT_ROLLOUT_BWD : JIT_ROLLOUT_FWD, 0);
+}
 
 void set_jit_config(int enable, int64_t min_n) {
   std::lock_guard<std::mutex> lk(g_mu);
@@ -300,10 +310,12 @@ void get_jit_config(int* enable, int64_t* min_n) {
 bool prepare_step_jit(Model& M, int ops, std::string* why) {
   std::lock_guard<std::mutex> lk(g_mu);
   read_env_config();
-  return get_function(M, ops, why) != nullptr;
+  return get_function(M, JIT_STEP, ops, why) != nullptr;
 }
 
-bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why) {
+namespace {
+template <class Args>
+bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std::string* why) {
   CUfunction fn;
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -316,10 +328,10 @@ bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::
       *why = "batch below the run-time compilation threshold";
       return false;
     }
-    fn = get_function(M, ops, why);
+    fn = get_function(M, kind, ops, why);
   }
   if (!fn) return false;
-  StepArgs args = a;
+  Args args = a;
   void* params[] = {&args};
   const unsigned blocks = unsigned((a.n + 31) / 32);
   if (api().launchKernel(fn, blocks, 1, 1, 32, 1, 1, 0, reinterpret_cast<CUstream>(s), params, nullptr) !=
@@ -328,6 +340,15 @@ bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::
     return false;
   }
   return true;
+}
+}  // namespace
+
+bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why) {
+  return launch_jit(M, JIT_STEP, ops, a, s, why);
+}
+
+bool launch_rollout_jit(Model& M, bool backward, const RolloutArgs& a, cudaStream_t s, std::string* why) {
+  return launch_jit(M, backward ? JIT_ROLLOUT_BWD : JIT_ROLLOUT_FWD, 0, a, s, why);
 }
 
 }  // namespace sgdyn

@@ -29,6 +29,7 @@ struct RuntimeTab {
   const DModel* m;
   __device__ __forceinline__ int nj() const { return m->nj; }
   __device__ __forceinline__ int nv() const { return m->nv; }
+  __device__ __forceinline__ int nq_ext() const { return m->nq_ext; }
   __device__ __forceinline__ int nlinks() const { return m->nlinks; }
   __device__ __forceinline__ double gravity(int k) const { return m->gravity[k]; }
   __device__ __forceinline__ const DJoint& joint(int i) const { return model_joints(m)[i]; }
@@ -38,6 +39,7 @@ template <int NJ, int NV, int NL, const DJoint* JT, const DLink* LT, const DMode
 struct StaticTab {
   __device__ __forceinline__ static constexpr int nj() { return NJ; }
   __device__ __forceinline__ static constexpr int nv() { return NV; }
+  __device__ __forceinline__ int nq_ext() const { return M->nq_ext; }
   __device__ __forceinline__ static constexpr int nlinks() { return NL; }
   __device__ __forceinline__ double gravity(int k) const { return M->gravity[k]; }
   __device__ __forceinline__ const DJoint& joint(int i) const { return JT[i]; }

@@ -56,3 +56,42 @@ def test_specialised_sweep_matches_generic_and_oracle(name):
     assert rel_per_env(spec["qf"], r["tau"]) <= 1e-10
     assert rel_per_env(spec["qacc"], r["qdd"]) <= 1e-8
     assert rel_per_env(spec["mass_matrix"], r["M"]) <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["arm9", "mixed"])
+def test_specialised_rollout_matches_generic(name):
+    """Checkpointed rollout forward and backward: the model-specialised kernels reproduce the
+    generic ones (same operation order, tables folded to constants) to 1e-12 relative."""
+    import torch
+
+    from sapien_gb300 import autodiff as AD
+
+    robot = {"arm9": syn.arm_with_fingers(),
+             "mixed": syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                          "continuous", "prismatic"])}[name]
+    pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    n, T, K, dt = 96, 30, 7, 2e-3
+    q, qd, _, tau = (torch.from_numpy(a).cuda() for a in robot.sample(n, seed=5))
+    taus = (0.2 * tau).unsqueeze(0).repeat(T, 1, 1).contiguous()
+    g = torch.Generator(device="cpu").manual_seed(3)
+    qTb = torch.randn(n, pm.nq_ext, generator=g, dtype=torch.float64).cuda()
+    qdTb = torch.randn(n, pm.nv, generator=g, dtype=torch.float64).cuda()
+
+    def run():
+        qT, qdT, qc, qdc = AD.rollout_forward(pm, q, qd, taus, dt, K)
+        q0b, qd0b, taub = AD.rollout_backward(pm, qc, qdc, taus, dt, K, qTb, qdTb)
+        return [x.cpu().numpy() for x in (qT, qdT, qc, qdc, q0b, qd0b, taub)]
+
+    old = jit_config(-1, -1)
+    try:
+        jit_config(0, -1)
+        gen = run()
+        jit_config(1, 0)
+        spec = run()
+    finally:
+        jit_config(*old)
+    for a, b in zip(spec, gen):
+        a2, b2 = a.reshape(-1, a.shape[-1]), b.reshape(-1, b.shape[-1])
+        assert rel_per_env(a2, b2) <= 1e-12

@@ -1,5 +1,7 @@
-"""The run-time-specialised sweep's generated source compiles with NVRTC for sm_103a (CPU
-test: NVRTC needs no GPU). GPU parity of the specialised kernel is in test_parity_gpu.py."""
+"""The run-time-specialised kernels' generated source compiles with NVRTC for sm_103a (CPU
+test: NVRTC needs no GPU). ``ops`` > 0 selects the fused sweep with that op set, -1 / -2 the
+rollout forward / backward kernel. GPU parity of the specialised kernels is in
+test_jit_gpu.py."""
 import ctypes
 import ctypes.util
 
@@ -26,7 +28,8 @@ def _headers():
     return [h.encode() for h in JIT_HEADERS], [open(os.path.join(CSRC, h)).read().encode() for h in JIT_HEADERS]
 
 
-@pytest.mark.parametrize("name,ops", [("arm9", 31), ("humanoid", 28), ("mixed", 8)])
+@pytest.mark.parametrize("name,ops", [("arm9", 31), ("humanoid", 28), ("mixed", 8), ("arm9", -1), ("arm9", -2),
+                                      ("mixed", -2)])
 def test_generated_source_compiles(name, ops):
     robot = {"arm9": syn.arm_with_fingers(), "humanoid": syn.humanoid(),
              "mixed": syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
@@ -40,7 +43,7 @@ def test_generated_source_compiles(name, ops):
     names, texts = _headers()
     prog = ctypes.c_void_p()
     arr = lambda xs: (ctypes.c_char_p * len(xs))(*xs)  # noqa: E731
-    assert nv.nvrtcCreateProgram(ctypes.byref(prog), src.value, b"sgjit_step.cu", len(names), arr(texts),
+    assert nv.nvrtcCreateProgram(ctypes.byref(prog), src.value, b"sgjit_kernel.cu", len(names), arr(texts),
                                  arr(names)) == 0
     opts = [b"--gpu-architecture=sm_103a", b"-std=c++17", b"-lineinfo"]
     rc = nv.nvrtcCompileProgram(prog, len(opts), arr(opts))
