@@ -154,12 +154,13 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
                int layout, void* stream);
 
 /* Run-time specialisation (addition). The fused sweep behind sgdyn_step and the five
- * single-op entry points is compiled per model with NVRTC on first use (tables baked in as
- * constants; same arithmetic, bitwise-equal results) when enabled and n >= min_n; otherwise,
- * or if the run-time compiler or the driver library is unavailable, the generic kernel runs.
- * enable / min_n < 0 leave a setting unchanged; the current values are returned. Defaults:
- * enabled unless SGDYN_JIT=0, min_n = 2048 (SGDYN_JIT_MIN_N). Compile ahead with
- * sgdyn_jit_prepare (needed before capturing launches into a CUDA graph). */
+ * single-op entry points, and the forward rollout kernel, are compiled per model with NVRTC on
+ * first use (tables baked in as constants; same arithmetic) when enabled and n >= min_n;
+ * otherwise, or if the run-time compiler or the driver library is unavailable, the generic
+ * kernel runs. enable / min_n < 0 leave a setting unchanged; the current values are
+ * returned. Defaults: enabled unless SGDYN_JIT=0, min_n = 2048 (SGDYN_JIT_MIN_N). Compile
+ * ahead with sgdyn_jit_prepare (needed before capturing launches into a CUDA graph).
+ * `ops`: an SGDYN_OP_* mask for the fused sweep, or -1 for the forward rollout kernel. */
 int sgdyn_jit_config(int enable, int64_t min_n, int* enabled, int64_t* min_n_out);
 int sgdyn_jit_prepare(const sgdyn_model* m, int ops);
 /* The generated translation unit for (model, ops); valid until the next call on this thread. */
@@ -240,14 +241,17 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
                           const double* tau, int checkpoint_every, double* q_ckpt, double* qd_ckpt, double* qT,
                           double* qdT, void* stream);
 
-/* Bytes of device scratch sgdyn_rollout_backward needs for n environments. */
+/* Bytes of device scratch sgdyn_rollout_backward needs for n environments: the
+ * intermediates of one checkpoint segment. */
 int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_every, int64_t* bytes);
 
 /* Reverse pass of sgdyn_rollout_forward: given the adjoints of the final state (either may
- * be NULL = zero) returns q0_bar, qd0_bar and tau_bar [T][n][nv]. Each checkpoint segment
- * is recomputed from its q / qd checkpoint, its spatial intermediates kept in `scratch`
+ * be NULL = zero) returns q0_bar, qd0_bar and tau_bar [T][n][nv]. Checkpoint segments are
+ * recomputed from their q / qd checkpoints, their spatial intermediates kept in `scratch`
  * (caller-owned device memory of at least sgdyn_rollout_scratch_bytes bytes), and then
- * reversed step by step. */
+ * reversed step by step. A scratch of k times the minimum lets k segments recompute at
+ * once (one thread per segment and environment), which fills the GPU at small n;
+ * ceil(T / checkpoint_every) times the minimum recomputes all segments in one launch. */
 int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, int checkpoint_every,
                            const double* q_ckpt, const double* qd_ckpt, const double* tau, const double* qT_bar,
                            const double* qdT_bar, double* q0_bar, double* qd0_bar, double* tau_bar, double* scratch,

@@ -214,14 +214,20 @@ def rollout_forward(model, q0, qd0, tau, dt, checkpoint_every=None):
     return qT, qdT, qc, qdc
 
 
-def rollout_backward(model, q_ckpt, qd_ckpt, tau, dt, checkpoint_every, qT_bar=None, qdT_bar=None):
-    """Reverse pass: returns (q0_bar, qd0_bar, tau_bar [T, N, nv])."""
+def rollout_backward(model, q_ckpt, qd_ckpt, tau, dt, checkpoint_every, qT_bar=None, qdT_bar=None,
+                     max_scratch_bytes=4 << 30):
+    """Reverse pass: returns (q0_bar, qd0_bar, tau_bar [T, N, nv]).
+
+    The scratch holds as many checkpoint segments' intermediates as fit in
+    ``max_scratch_bytes`` (at least one): that many segments are recomputed in parallel."""
     n, dev = q_ckpt.shape[1], q_ckpt.device
     T = tau.shape[0]
     nb = ctypes.c_int64()
     L = N.load()
     N.check(L.sgdyn_rollout_scratch_bytes(model._h, n, int(checkpoint_every), ctypes.byref(nb)))
-    scratch = torch.empty(max(nb.value // 8, 1), dtype=torch.float64, device=dev)
+    nseg = (T + int(checkpoint_every) - 1) // int(checkpoint_every)
+    segs = max(1, min(nseg, int(max_scratch_bytes) // max(nb.value, 1)))
+    scratch = torch.empty(max(segs * nb.value // 8, 1), dtype=torch.float64, device=dev)
     q0b = torch.empty(n, model.nq_ext, dtype=torch.float64, device=dev)
     qd0b = torch.empty(n, model.nv, dtype=torch.float64, device=dev)
     taub = torch.empty_like(tau)

@@ -291,19 +291,23 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
   return SGDYN_OK;
 }
 
+// ops > 0: the fused sweep with that op set; -1: the forward rollout kernel
+static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || ops == -1; }
+
 int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
   if (!m) return fail(SGDYN_ERR_NULL, "null model");
-  if (ops <= 0 || ops > OP_ALL) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
+  if (!jit_kind_ok(ops)) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
   std::string why;
-  if (!prepare_step_jit(*m->impl, ops, &why)) return fail(SGDYN_ERR_UNSUPPORTED, "run-time compilation unavailable: " + why);
+  const bool ok = ops > 0 ? prepare_step_jit(*m->impl, ops, &why) : prepare_rollout_jit(*m->impl, &why);
+  if (!ok) return fail(SGDYN_ERR_UNSUPPORTED, "run-time compilation unavailable: " + why);
   return SGDYN_OK;
 }
 
 int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
   if (!m || !source) return fail(SGDYN_ERR_NULL, "null argument");
+  if (!jit_kind_ok(ops)) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
   thread_local std::string buf;
-  // ops > 0: fused sweep with that op set; -1 / -2: rollout forward / backward
-  buf = ops > 0 ? step_jit_source(*m->impl, ops) : rollout_jit_source(*m->impl, ops == -2);
+  buf = ops > 0 ? step_jit_source(*m->impl, ops) : rollout_jit_source(*m->impl);
   *source = buf.c_str();
   return SGDYN_OK;
 }
@@ -598,7 +602,7 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
     a.q0 = q0; a.qd0 = qd0; a.tau = tau;
     a.qT = qT; a.qdT = qdT; a.q_ckpt = q_ckpt; a.qd_ckpt = qd_ckpt;
     std::string why;
-    if (launch_rollout_jit(Mo, false, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
+    if (launch_rollout_jit(Mo, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
     return launch_status(launch_rollout_forward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
   });
 }
@@ -642,9 +646,11 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
     a.qd_ckpt = const_cast<double*>(qd_ckpt);
     a.qT_bar = qT_bar; a.qdT_bar = qdT_bar;
     a.q0_bar = q0_bar; a.qd0_bar = qd0_bar; a.tau_bar = tau_bar; a.scratch = scratch;
-    std::string why;
-    if (launch_rollout_jit(Mo, true, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
-    return launch_status(launch_rollout_backward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nj = Mo.njoints();
+    return launch_status(rollout_backward_grouped(
+        a, need / 8, scratch_bytes / 8, [&](const RolloutArgs& g) { return launch_rollout_recompute(dm, nj, g, st); },
+        [&](const RolloutArgs& g) { return launch_rollout_reverse(dm, nj, g, st); }));
   });
 }
 

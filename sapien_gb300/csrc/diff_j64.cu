@@ -14,7 +14,12 @@ SG_LAUNCH(fk_vjp, FkVjpArgs)
 SG_LAUNCH(rnea_derivatives, DerivArgs)
 SG_LAUNCH(aba_derivatives, DerivArgs)
 SG_LAUNCH(rollout_forward, RolloutArgs)
-SG_LAUNCH(rollout_backward, RolloutArgs)
+SG_LAUNCH(rollout_reverse, RolloutArgs)
 #undef SG_LAUNCH
+
+cudaError_t launch_rollout_recompute_j64(const DModel* dm, const RolloutArgs& a, cudaStream_t s) {
+  rollout_recompute_kernel<64><<<unsigned((a.n * a.s_cnt + 31) / 32), 32, 0, s>>>(dm, a);
+  return cudaGetLastError();
+}
 
 }  // namespace sgdyn

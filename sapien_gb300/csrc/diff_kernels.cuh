@@ -242,34 +242,56 @@ __device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, double*
   for (int k = 0; k < 21; k++) io(W.Lff[k]);
 }
 
+// Backward, part 1. Segments are independent given their checkpoints, so one thread per
+// (segment of the group, environment) re-runs its segment and keeps every step's
+// intermediates in the scratch: [segment of group][step of segment][field][env].
 template <int MAXJ, class Tab>
-__device__ __forceinline__ void rollout_backward_env(const Tab& T, const RolloutArgs& a, const int64_t e) {
+__device__ __forceinline__ void rollout_recompute_env(const Tab& T, const RolloutArgs& a, const int64_t idx) {
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const int nv = T.nv(), nq = T.nq_ext(), nj = T.nj();
+  const int64_t n = a.n;
+  const int64_t e = idx % n;
+  const int g = int(idx / n), s = a.s_lo + g;
+  const int64_t per_step = stash_doubles_per_step(nj, nq, nv);
+  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
+  for (int c = 0; c < nq; c++) q[c] = a.q_ckpt[(int64_t(s) * n + e) * nq + c];
+  for (int c = 0; c < nv; c++) qd[c] = a.qd_ckpt[(int64_t(s) * n + e) * nv + c];
+  DynWork<MAXJ> W;
+  const int t0 = s * a.K, t1 = min(a.T, t0 + a.K);
+  for (int t = t0; t < t1; t++) {
+    double* base = a.scratch + (int64_t(g) * a.K + (t - t0)) * per_step * n;
+    for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
+    aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
+    stash_io<MAXJ>(T, W, base, n, e, true);
+    for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
+    euler_positions(T, q, qd, a.dt);
+  }
+}
+
+// Backward, part 2: one thread per environment walks the group's steps in reverse from
+// the stored intermediates. The adjoint of the state enters from qT_bar / qdT_bar for the
+// last group and from q0_bar / qd0_bar (the previous group's result) otherwise, and
+// leaves through q0_bar / qd0_bar.
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void rollout_reverse_env(const Tab& T, const RolloutArgs& a, const int64_t e) {
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
   const int nv = T.nv(), nq = T.nq_ext(), nj = T.nj();
   const int64_t n = a.n;
   const int64_t per_step = stash_doubles_per_step(nj, nq, nv);
-  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV], qb[MAXV], qdb[MAXV], qddb[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
-  for (int c = 0; c < nq; c++) qb[c] = a.qT_bar ? a.qT_bar[e * nq + c] : 0.0;
-  for (int c = 0; c < nv; c++) qdb[c] = a.qdT_bar ? a.qdT_bar[e * nv + c] : 0.0;
+  const int nseg = (a.T + a.K - 1) / a.K;
+  const bool last = a.s_lo + a.s_cnt == nseg;
+  const double* qin = last ? a.qT_bar : a.q0_bar;
+  const double* qdin = last ? a.qdT_bar : a.qd0_bar;
+  double qb[MAXQ], qdb[MAXV], qddb[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
+  for (int c = 0; c < nq; c++) qb[c] = qin ? qin[e * nq + c] : 0.0;
+  for (int c = 0; c < nv; c++) qdb[c] = qdin ? qdin[e * nv + c] : 0.0;
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
-  const int nseg = (a.T + a.K - 1) / a.K;
-  for (int s = nseg - 1; s >= 0; s--) {
+  for (int s = a.s_lo + a.s_cnt - 1; s >= a.s_lo; s--) {
     const int t0 = s * a.K, t1 = min(a.T, t0 + a.K);
-    for (int c = 0; c < nq; c++) q[c] = a.q_ckpt[(int64_t(s) * n + e) * nq + c];
-    for (int c = 0; c < nv; c++) qd[c] = a.qd_ckpt[(int64_t(s) * n + e) * nv + c];
-    // recompute the segment, keeping every step's intermediates
-    for (int t = t0; t < t1; t++) {
-      double* base = a.scratch + int64_t(t - t0) * per_step * n;
-      for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
-      aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
-      stash_io<MAXJ>(T, W, base, n, e, true);
-      for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
-      euler_positions(T, q, qd, a.dt);
-    }
-    // reverse through the segment: q' = q + dt qd' and qd' = qd + dt qdd
+    // q' = q + dt qd' and qd' = qd + dt qdd, reversed
     for (int t = t1 - 1; t >= t0; t--) {
-      double* base = a.scratch + int64_t(t - t0) * per_step * n;
+      double* base = a.scratch + (int64_t(s - a.s_lo) * a.K + (t - t0)) * per_step * n;
 #pragma unroll
       for (int i = 1; i < nj; i++) {
         const DJoint& J = T.joint(i);
@@ -293,10 +315,17 @@ __device__ __forceinline__ void rollout_backward_env(const Tab& T, const Rollout
 }
 
 template <int MAXJ>
-__global__ void __launch_bounds__(32) rollout_backward_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+__global__ void __launch_bounds__(32) rollout_recompute_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= a.n * a.s_cnt) return;
+  rollout_recompute_env<MAXJ>(RuntimeTab{model}, a, idx);
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rollout_reverse_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
-  rollout_backward_env<MAXJ>(RuntimeTab{model}, a, e);
+  rollout_reverse_env<MAXJ>(RuntimeTab{model}, a, e);
 }
 
 }  // namespace sgdyn

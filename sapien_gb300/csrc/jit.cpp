@@ -128,7 +128,9 @@ std::string list(It b, It e) {
   return s;
 }
 
-enum JitKind { JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_ROLLOUT_BWD = 2 };
+// The rollout's backward kernels stay generic: specialised, they came out slower (the
+// fully unrolled reverse sweep spills heavily).
+enum JitKind { JIT_STEP = 0, JIT_ROLLOUT_FWD = 1 };
 
 std::string generate_source(const Model& M, int kind, int ops) {
   const auto& t = M.host_table();
@@ -164,8 +166,7 @@ std::string generate_source(const Model& M, int kind, int ops) {
     << "  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
     << "  if (e >= a.n) return;\n";
   if (kind == JIT_STEP) o << "  sgdyn::step_env_t<" << nj << ", " << ops << ">(" << tab << ", a, e);\n}\n";
-  else if (kind == JIT_ROLLOUT_FWD) o << "  sgdyn::rollout_forward_env<" << nj << ">(" << tab << ", a, e);\n}\n";
-  else o << "  sgdyn::rollout_backward_env<" << nj << ">(" << tab << ", a, e);\n}\n";
+  else o << "  sgdyn::rollout_forward_env<" << nj << ">(" << tab << ", a, e);\n}\n";
   return o.str();
 }
 
@@ -289,8 +290,8 @@ CUfunction get_function_slow(const Model& M, int kind, int ops, int dev, std::st
 }  // namespace
 
 std::string step_jit_source(const Model& M, int ops) { return generate_source(M, JIT_STEP, ops); }
-std::string rollout_jit_source(const Model& M, bool backward) {
-  return generate_source(M, backward ? JIT_ROLLOUT_BWD : JIT_ROLLOUT_FWD, 0);
+std::string rollout_jit_source(const Model& M) {
+  return generate_source(M, JIT_ROLLOUT_FWD, 0);
 }
 
 void set_jit_config(int enable, int64_t min_n) {
@@ -311,6 +312,12 @@ bool prepare_step_jit(Model& M, int ops, std::string* why) {
   std::lock_guard<std::mutex> lk(g_mu);
   read_env_config();
   return get_function(M, JIT_STEP, ops, why) != nullptr;
+}
+
+bool prepare_rollout_jit(Model& M, std::string* why) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  return get_function(M, JIT_ROLLOUT_FWD, 0, why) != nullptr;
 }
 
 namespace {
@@ -347,8 +354,8 @@ bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::
   return launch_jit(M, JIT_STEP, ops, a, s, why);
 }
 
-bool launch_rollout_jit(Model& M, bool backward, const RolloutArgs& a, cudaStream_t s, std::string* why) {
-  return launch_jit(M, backward ? JIT_ROLLOUT_BWD : JIT_ROLLOUT_FWD, 0, a, s, why);
+bool launch_rollout_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why) {
+  return launch_jit(M, JIT_ROLLOUT_FWD, 0, a, s, why);
 }
 
 }  // namespace sgdyn

@@ -15,9 +15,10 @@ class Model;
 // the batch is large enough; returns false (with the reason) when the caller should use the
 // generic kernel. Compiles and caches on first use of (model tables, ops, device).
 bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why);
-// Same for the rollout forward / backward kernels.
-bool launch_rollout_jit(Model& M, bool backward, const RolloutArgs& a, cudaStream_t s, std::string* why);
-std::string rollout_jit_source(const Model& M, bool backward);
+// Same for the forward rollout kernel.
+bool launch_rollout_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why);
+std::string rollout_jit_source(const Model& M);
+bool prepare_rollout_jit(Model& M, std::string* why);
 // Compiles (or loads from the cache) now; false with the reason if not possible.
 bool prepare_step_jit(Model& M, int ops, std::string* why);
 void set_jit_config(int enable, int64_t min_n);

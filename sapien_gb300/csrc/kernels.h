@@ -70,9 +70,11 @@ struct DerivArgs {
 // Semi-implicit Euler rollout qd += dt ABA(q, qd, tau_t); q += dt qd, with q / qd
 // checkpoints every K steps (segment s starts at step s K). Contiguous env-major arrays:
 // q0 [n][nq], qd0 [n][nv], tau [T][n][nv], q_ckpt [C][n][nq], qd_ckpt [C][n][nv].
+// The backward runs in groups of segments [s_lo, s_lo + s_cnt), latest group first.
 struct RolloutArgs {
   int64_t n;
   int T, K;
+  int s_lo, s_cnt;
   double dt;
   const double *q0, *qd0, *tau;
   double *qT, *qdT, *q_ckpt, *qd_ckpt;
@@ -96,9 +98,35 @@ cudaError_t launch_fk_vjp(const DModel* dm, int nj, const FkVjpArgs& a, cudaStre
 cudaError_t launch_rnea_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
 cudaError_t launch_aba_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_forward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
-cudaError_t launch_rollout_backward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
-// doubles of rollout-backward scratch per environment
+cudaError_t launch_rollout_recompute(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
+cudaError_t launch_rollout_reverse(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
+// doubles of rollout-backward scratch per environment and segment (the minimum scratch is
+// one segment for all environments; k segments' worth lets k segments recompute at once)
 int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K);
+
+// Whole rollout backward: groups of as many segments as the scratch holds, latest first;
+// per group one recompute launch over (segment, env) and one reverse launch over envs.
+// `recompute` / `reverse` launch one group (RolloutArgs with s_lo / s_cnt set).
+template <class Recompute, class Reverse>
+cudaError_t rollout_backward_grouped(RolloutArgs a, int64_t seg_doubles, int64_t scratch_doubles,
+                                     Recompute recompute, Reverse reverse) {
+  const int nseg = (a.T + a.K - 1) / a.K;
+  const int64_t fit = seg_doubles > 0 ? scratch_doubles / seg_doubles : 0;
+  const int G = int(fit < nseg ? fit : nseg);
+  if (nseg == 0) {  // no steps: the adjoint passes through
+    a.s_lo = 0;
+    a.s_cnt = 0;
+    return reverse(a);
+  }
+  if (G <= 0) return cudaErrorInvalidValue;
+  for (int hi = nseg; hi > 0; hi -= G) {
+    a.s_lo = hi - G > 0 ? hi - G : 0;
+    a.s_cnt = hi - a.s_lo;
+    if (cudaError_t e = recompute(a)) return e;
+    if (cudaError_t e = reverse(a)) return e;
+  }
+  return cudaSuccess;
+}
 #endif  // __CUDACC_RTC__
 
 }  // namespace sgdyn

@@ -87,7 +87,8 @@ SG_DISPATCH(fk_vjp, FkVjpArgs)
 SG_DISPATCH(rnea_derivatives, DerivArgs)
 SG_DISPATCH(aba_derivatives, DerivArgs)
 SG_DISPATCH(rollout_forward, RolloutArgs)
-SG_DISPATCH(rollout_backward, RolloutArgs)
+SG_DISPATCH(rollout_recompute, RolloutArgs)
+SG_DISPATCH(rollout_reverse, RolloutArgs)
 #undef SG_DISPATCH
 
 int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K) {

@@ -140,7 +140,12 @@ extern "C" int sgdyn_rollout_backward_noalloc(const sgdyn_model* m, int64_t n, i
   a.qd0_bar = qd0_bar;
   a.tau_bar = tau_bar;
   a.scratch = scratch;
-  cudaError_t e = launch_rollout_backward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream));
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int nj = Mo.njoints();
+  cudaError_t e = rollout_backward_grouped(
+      a, need / 8, kNoAllocScratchBytes / 8,
+      [&](const RolloutArgs& g) { return launch_rollout_recompute(dm, nj, g, st); },
+      [&](const RolloutArgs& g) { return launch_rollout_reverse(dm, nj, g, st); });
   if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   return SGDYN_OK;
 }

@@ -215,3 +215,39 @@ def test_rollout_gradient_matches_finite_differences():
                                            cu(tau), dt, 200, qT_bar=torch.ones_like(qT))
     assert rel(q0b1.cpu().numpy(), q0b2.cpu().numpy()) < 1e-12
     assert rel(tb1.cpu().numpy(), tb2.cpu().numpy()) < 1e-12
+
+
+@pytest.mark.parametrize("T,K", [(50, 7), (20, 20), (0, 5)])
+def test_rollout_backward_segment_groups_agree(T, K):
+    """The backward recomputes as many checkpoint segments at once as the scratch holds; one
+    segment at a time, three at a time and all at once give bitwise-equal gradients (every
+    environment runs the same operations in the same order)."""
+    import ctypes
+
+    import torch
+
+    from sapien_gb300 import _native as N
+
+    r = syn.arm_with_fingers()
+    pm = PinocchioModel(r.urdf, [0, 0, -9.81])
+    pm.set_joint_order(r.joint_names)
+    pm.set_link_order(r.link_names)
+    n, dt = 40, 2e-3
+    q0, qd0, _, tau1 = (torch.from_numpy(a).cuda() for a in r.sample(n, seed=8))
+    tau = (0.3 * tau1).unsqueeze(0).repeat(T, 1, 1).contiguous()
+    _, _, qc, qdc = ad.rollout_forward(pm, q0, qd0, tau, dt, K)
+    if qc is None or qc.numel() == 0:
+        qc = torch.empty(0, n, pm.nq_ext, dtype=torch.float64, device="cuda")
+        qdc = torch.empty(0, n, pm.nv, dtype=torch.float64, device="cuda")
+    g = torch.Generator(device="cpu").manual_seed(1)
+    qTb = torch.randn(n, pm.nq_ext, generator=g, dtype=torch.float64).cuda()
+    qdTb = torch.randn(n, pm.nv, generator=g, dtype=torch.float64).cuda()
+    nb = ctypes.c_int64()
+    assert N.load().sgdyn_rollout_scratch_bytes(pm._h, n, K, ctypes.byref(nb)) == 0
+    outs = [ad.rollout_backward(pm, qc, qdc, tau, dt, K, qTb, qdTb, max_scratch_bytes=k * nb.value)
+            for k in (1, 3, 1000)]
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert torch.equal(a, b)
+    if T == 0:
+        assert torch.equal(outs[0][0], qTb) and torch.equal(outs[0][1], qdTb)

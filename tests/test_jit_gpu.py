@@ -60,8 +60,9 @@ def test_specialised_sweep_matches_generic_and_oracle(name):
 
 @pytest.mark.parametrize("name", ["arm9", "mixed"])
 def test_specialised_rollout_matches_generic(name):
-    """Checkpointed rollout forward and backward: the model-specialised kernels reproduce the
-    generic ones (same operation order, tables folded to constants) to 1e-12 relative."""
+    """Checkpointed rollout: the model-specialised forward kernel reproduces the generic one
+    (same operation order, tables folded to constants) to 1e-12 relative, and so do the
+    gradients the (generic) backward computes from its checkpoints."""
     import torch
 
     from sapien_gb300 import autodiff as AD
