@@ -69,6 +69,34 @@ def host_cores():
         return os.cpu_count() or 1
 
 
+def cpu_model():
+    """Host CPU name from /proc/cpuinfo (x86 "model name"; Arm implementer / part ids)."""
+    try:
+        info = open("/proc/cpuinfo").read().splitlines()
+    except OSError:
+        return "unknown"
+    kv = {}
+    for line in info:
+        if ":" in line:
+            k, v = line.split(":", 1)
+            kv.setdefault(k.strip(), v.strip())
+    if "model name" in kv:
+        return kv["model name"]
+    if "CPU part" in kv:
+        return f"arm implementer {kv.get('CPU implementer', '?')} part {kv['CPU part']}"
+    return "unknown"
+
+
+def time_median(fn, min_reps=5, min_seconds=2.0):
+    """Median wall time of fn() over at least min_reps runs and min_seconds."""
+    ts, t_start = [], time.perf_counter()
+    while len(ts) < min_reps or time.perf_counter() - t_start < min_seconds:
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts)), len(ts)
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -414,14 +442,11 @@ def main():
     cores = host_cores()
     S = min(n, 4096)
     o.batch_step(q_h[:256], qd_h[:256], qdd_h[:256], tau_h[:256], nthreads=cores)
-    t0 = time.perf_counter()
-    reps = 0
-    while True:
-        ref = o.batch_step(q_h[:S], qd_h[:S], qdd_h[:S], tau_h[:S], nthreads=cores)
-        reps += 1
-        if time.perf_counter() - t0 > 2.0:
-            break
-    cpu_dt = (time.perf_counter() - t0) / reps
+    cpu_dt, reps = time_median(lambda: o.batch_step(q_h[:S], qd_h[:S], qdd_h[:S], tau_h[:S], nthreads=cores))
+    ref = o.batch_step(q_h[:S], qd_h[:S], qdd_h[:S], tau_h[:S], nthreads=cores)
+    S1 = min(n, 512)
+    cpu1_dt, _ = time_median(lambda: o.batch_step(q_h[:S1], qd_h[:S1], qdd_h[:S1], tau_h[:S1], nthreads=1),
+                             min_seconds=1.0)
     step(q, qd, qdd, tau)
     torch.cuda.synchronize()
 
@@ -448,7 +473,8 @@ def main():
         "roofline": roofline,
         "roofline_fp64": roofline_fp64,
         "cpu_baseline": {"value": S / cpu_dt, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"first {S} envs of the workload, {reps} repetitions (~2 s)"},
+                         "sample": f"first {S} envs of the workload, median of {reps} repetitions (>= 2 s)",
+                         "single_thread_value": S1 / cpu1_dt, "nproc": os.cpu_count(), "cpu_model": cpu_model()},
         "per_op_kernel": per_op,
         "max_rel_err_vs_oracle": errs,
         "clocks": clk,
