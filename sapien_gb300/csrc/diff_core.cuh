@@ -231,9 +231,26 @@ struct AdjScratch {
   Mot w[MAXJ], F[MAXJ], P[MAXJ], Q[MAXJ], R[MAXJ], T[MAXJ];
 };
 
+// Subtree sums of the RNEA body forces f = I a + v x* I v (world frame) into F[1..nj-1].
+// They do not depend on the adjoint, so one evaluation serves any number of
+// rnea_adjoint calls on the same forward quantities.
+template <int MAXJ, class Tab>
+__device__ void rnea_subtree_forces(const Tab& T, const DynWork<MAXJ>& W, Mot* F) {
+  const int nj = T.nj();
+  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+#pragma unroll
+  for (int i = 1; i < nj; i++) F[i] = rbi_mul_add(W.Iw[i], W.acc[i], add_crossf(zero, W.vel[i], W.hY[i]));
+#pragma unroll
+  for (int j = nj - 1; j >= 1; j--) {
+    const int p = T.joint(j).parent;
+    if (p > 0) F[p] = add6(F[p], F[j]);
+  }
+}
+
 // Reverse-mode RNEA sweep over the forward quantities in W (acc must be the world
-// accelerations the torques were computed with). taubar and the outputs are external
-// order; any output pointer may be null; outputs are scaled by `sign`. W is not modified.
+// accelerations the torques were computed with) and the subtree forces in A.F (from
+// rnea_subtree_forces; read only). taubar and the outputs are external order; any output
+// pointer may be null; outputs are scaled by `sign`. W is not modified.
 template <int MAXJ, class Tab>
 __device__ void rnea_adjoint(const Tab& T, const DynWork<MAXJ>& W, AdjScratch<MAXJ>& A,
                              const double* taubar, double* qbar, double* qdbar, double* qddbar, double sign) {
@@ -249,7 +266,6 @@ __device__ void rnea_adjoint(const Tab& T, const DynWork<MAXJ>& W, AdjScratch<MA
     A.w[i] = wi;
     const RBI& Y = W.Iw[i];
     const Mot v = W.vel[i];
-    A.F[i] = rbi_mul_add(Y, W.acc[i], add_crossf(zero, v, W.hY[i]));  // f = I a + v x* I v
     const Mot Pw = rbi_mul(Y, wi);
     A.P[i] = Pw;
     A.Q[i] = add_crossf(zero, v, Pw);
@@ -280,7 +296,6 @@ __device__ void rnea_adjoint(const Tab& T, const DynWork<MAXJ>& W, AdjScratch<MA
     if (qddbar)
       for (int k = 0; k < J.nv; k++) qddbar[J.vcol + k] = sign * dot6(W.Sw[iv + k], P);
     if (p > 0) {
-      A.F[p] = add6(A.F[p], Fj);
       A.P[p] = add6(A.P[p], P);
       A.Q[p] = add6(A.Q[p], Q);
       A.R[p] = add6(A.R[p], R);

@@ -37,6 +37,7 @@ __global__ void __launch_bounds__(32) rnea_vjp_kernel(const DModel* __restrict__
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
   rnea_forward<MAXJ>(T, q, qd, qdd, W);
+  rnea_subtree_forces<MAXJ>(T, W, A.F);
   rnea_adjoint<MAXJ>(T, W, A, tb, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, a.o3.p ? o3 : nullptr, 1.0);
   if (a.o1.p) store_row(a.o1, e, nv, o1);
   if (a.o2.p) store_row(a.o2, e, nv, o2);
@@ -58,6 +59,7 @@ __global__ void __launch_bounds__(32) aba_vjp_kernel(const DModel* __restrict__ 
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
   aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
+  rnea_subtree_forces<MAXJ>(T, W, A.F);
   minv_solve<MAXJ>(T, W, qb, lam);
   rnea_adjoint<MAXJ>(T, W, A, lam, a.o1.p ? o1 : nullptr, a.o2.p ? o2 : nullptr, nullptr, -1.0);
   if (a.o1.p) store_row(a.o1, e, nv, o1);
@@ -124,6 +126,7 @@ __global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __re
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
   rnea_forward<MAXJ>(T, q, qd, qdd, W);
+  rnea_subtree_forces<MAXJ>(T, W, A.F);
   for (int r = 0; r < nv; r++) {
     for (int c = 0; c < nv; c++) tb[c] = (c == r) ? 1.0 : 0.0;
     rnea_adjoint<MAXJ>(T, W, A, tb, o1, o2, a.d_x.p ? o3 : nullptr, 1.0);
@@ -149,6 +152,7 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
   aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
+  rnea_subtree_forces<MAXJ>(T, W, A.F);
   for (int r = 0; r < nv; r++) {
     for (int c = 0; c < nv; c++) er[c] = (c == r) ? 1.0 : 0.0;
     minv_solve<MAXJ>(T, W, er, lam);
@@ -206,15 +210,15 @@ __global__ void __launch_bounds__(32) rollout_forward_kernel(const DModel* __res
 
 // Per step of a segment the scratch holds, structure-of-arrays over environments:
 // S (6 per velocity), U (6 per velocity), then per joint D^-1 (1), v (6), a (6), I v (6),
-// world inertia (10); plus the free-flyer factor (21).
+// world inertia (10), subtree force (6); plus the free-flyer factor (21).
 __host__ __device__ inline int64_t stash_doubles_per_step(int nj, int nq, int nv) {
   (void)nq;
-  return 12 * int64_t(nv) + int64_t(nj) * 29 + 21;
+  return 12 * int64_t(nv) + int64_t(nj) * 35 + 21;
 }
 
 template <int MAXJ, class Tab>
-__device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, double* base, int64_t n, int64_t e,
-                                         bool store) {
+__device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, Mot* F, double* base, int64_t n,
+                                         int64_t e, bool store) {
   const int nj = T.nj(), nv = T.nv();
   int64_t f = 0;
   auto io = [&](double& x) {
@@ -238,6 +242,7 @@ __device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, double*
     RBI& Y = W.Iw[i];
     io(Y.m); io(Y.h.x); io(Y.h.y); io(Y.h.z);
     for (int k = 0; k < 6; k++) io(Y.I[k]);
+    io6(F[i]);
   }
   for (int k = 0; k < 21; k++) io(W.Lff[k]);
 }
@@ -262,7 +267,8 @@ __device__ __forceinline__ void rollout_recompute_env(const Tab& T, const Rollou
     double* base = a.scratch + (int64_t(g) * a.K + (t - t0)) * per_step * n;
     for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
     aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
-    stash_io<MAXJ>(T, W, base, n, e, true);
+    rnea_subtree_forces<MAXJ>(T, W, W.pA);  // ABA's bias forces are no longer needed
+    stash_io<MAXJ>(T, W, W.pA, base, n, e, true);
     for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
     euler_positions(T, q, qd, a.dt);
   }
@@ -298,7 +304,7 @@ __device__ __forceinline__ void rollout_reverse_env(const Tab& T, const RolloutA
         qdb[J.vcol] = fma(a.dt, qb[J.qcol], qdb[J.vcol]);
       }
       for (int c = 0; c < nv; c++) qddb[c] = a.dt * qdb[c];
-      stash_io<MAXJ>(T, W, base, n, e, false);
+      stash_io<MAXJ>(T, W, A.F, base, n, e, false);
       minv_solve<MAXJ>(T, W, qddb, lam);
       for (int c = 0; c < nv; c++) a.tau_bar[(int64_t(t) * n + e) * nv + c] = lam[c];
       rnea_adjoint<MAXJ>(T, W, A, lam, o1, o2, nullptr, -1.0);

@@ -131,6 +131,7 @@ std::string list(It b, It e) {
 // The rollout's backward kernels stay generic: specialised, they came out slower (the
 // fully unrolled reverse sweep spills heavily).
 enum JitKind { JIT_STEP = 0, JIT_ROLLOUT_FWD = 1 };
+const char* kernel_name(int kind) { return kind == JIT_STEP ? "sgjit_step" : "sgjit_rollout_forward"; }
 
 std::string generate_source(const Model& M, int kind, int ops) {
   const auto& t = M.host_table();
@@ -162,7 +163,7 @@ std::string generate_source(const Model& M, int kind, int ops) {
   const std::string tab = "sgdyn::StaticTab<" + std::to_string(nj) + ", " + std::to_string(hdr->nv) + ", " +
                           std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM>()";
   const char* args = kind == JIT_STEP ? "sgdyn::StepArgs" : "sgdyn::RolloutArgs";
-  o << "extern \"C\" __global__ void __launch_bounds__(32) sgjit_kernel(const " << args << " a) {\n"
+  o << "extern \"C\" __global__ void __launch_bounds__(32) " << kernel_name(kind) << "(const " << args << " a) {\n"
     << "  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
     << "  if (e >= a.n) return;\n";
   if (kind == JIT_STEP) o << "  sgdyn::step_env_t<" << nj << ", " << ops << ">(" << tab << ", a, e);\n}\n";
@@ -278,7 +279,7 @@ CUfunction get_function_slow(const Model& M, int kind, int ops, int dev, std::st
   cudaFree(nullptr);  // make sure the runtime's primary context is current
   CUmodule mod;
   CUfunction fn;
-  if (A.moduleLoadData(&mod, cubin.data()) != CUDA_SUCCESS || A.moduleGetFunction(&fn, mod, "sgjit_kernel") != CUDA_SUCCESS) {
+  if (A.moduleLoadData(&mod, cubin.data()) != CUDA_SUCCESS || A.moduleGetFunction(&fn, mod, kernel_name(kind)) != CUDA_SUCCESS) {
     *why = "loading the compiled module failed";
     g_failed[key] = *why;
     return nullptr;
