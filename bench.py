@@ -35,12 +35,13 @@ N_ENVS = 16384
 WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs per GPU, "
             "FK (all link poses) + WORLD Jacobian + CRBA + RNEA + ABA per env per step")
 
-# FP64 thread-instructions per environment-step and DRAM bytes per environment of one
-# fused launch, from the ncu captures summarised in profiles/step_kernel_arm9.md, for the
-# model-specialised kernel (run-time compiled) and the generic one.
+# FP64 thread-instructions (DFMA + DMUL + DADD) per environment-step and DRAM bytes per
+# environment of one fused launch (structure-of-arrays buffers), from the ncu captures
+# summarised in profiles/step_kernel_arm9.md, for the model-specialised kernel (run-time
+# compiled) and the generic one.
 KERNEL_COUNTERS = {
-    "specialised": {"fp64_inst_per_env": 5209, "dram_bytes_per_env": 35.68e6 / 16384},
-    "generic": {"fp64_inst_per_env": 5272, "dram_bytes_per_env": 161.7e6 / 16384},
+    "specialised": {"fp64_inst_per_env": 5215, "dram_bytes_per_env": 25.66e6 / 16384},
+    "generic": {"fp64_inst_per_env": 5272, "dram_bytes_per_env": 155.1e6 / 16384},
 }
 
 
@@ -314,10 +315,11 @@ def main():
     n = args.n
     q_h, qd_h, qdd_h, tau_h = robot.sample(n, seed=rank)
     nv, nq, nl = robot.nv, robot.nq_ext, len(robot.link_names)
-    q, qd, qdd, tau = (torch.from_numpy(a).to(dev) for a in (q_h, qd_h, qdd_h, tau_h))
-    f64 = dict(dtype=torch.float64, device=dev)
-    poses, J, M = torch.empty(n, nl, 7, **f64), torch.empty(n, 6, nv, **f64), torch.empty(n, nv, nv, **f64)
-    tau_o, qdd_o = torch.empty(n, nv, **f64), torch.empty(n, nv, **f64)
+    # structure-of-arrays buffers ([cols][n], SGDYN_COL_MAJOR): every column coalesced
+    soa = lambda a: np.ascontiguousarray(a.reshape(n, -1).T)  # noqa: E731
+    q, qd, qdd, tau = (torch.from_numpy(soa(a)).to(dev) for a in (q_h, qd_h, qdd_h, tau_h))
+    out_cols = (nl * 7, 6 * nv, nv * nv, nv, nv)
+    poses, J, M, tau_o, qdd_o = (torch.empty(c, n, dtype=torch.float64, device=dev) for c in out_cols)
     pm._prepare(dev)
     L = N.load()
     kernel = "specialised" if L.sgdyn_jit_prepare(pm._h, N.OP_ALL) == 0 else "generic"
@@ -327,8 +329,10 @@ def main():
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
 
     def step(qq, qqd, qqdd, ttau, ops=N.OP_ALL):
-        rc = L.sgdyn_step(pm._h, n, ops, P(qq), P(qqd), P(qqdd), P(ttau), P(poses), P(J), P(M), P(tau_o), P(qdd_o),
-                          N.ENV_MAJOR, sp)
+        call(ops, (qq, qqd, qqdd, ttau), (poses, J, M, tau_o, qdd_o))
+
+    def call(ops, ins, outs):
+        rc = L.sgdyn_step(pm._h, n, ops, *[P(t) for t in ins], *[P(t) for t in outs], N.COL_MAJOR, sp)
         if rc != 0:
             raise RuntimeError(N.last_error())
 
@@ -356,38 +360,54 @@ def main():
     value = aggregate_throughput(n, world, ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ------------------------------
-    pin = lambda a: torch.from_numpy(a).pin_memory()  # noqa: E731
-    hq, hqd, hqdd, htau = pin(q_h), pin(qd_h), pin(qdd_h), pin(tau_h)
+    # Inputs and outputs live in pinned host memory. The C ABI accepts mapped pinned host
+    # pointers: the kernel reads the inputs and writes the results in host memory over the
+    # host link, so every step's bytes cross it inside the timed region. The same step with
+    # explicit cudaMemcpyAsync staging through device buffers is timed beside it.
+    pin = lambda a: torch.from_numpy(soa(a)).pin_memory()  # noqa: E731
+    ins_h = [pin(q_h), pin(qd_h), pin(qdd_h), pin(tau_h)]
+    ins_d = (q, qd, qdd, tau)
     outs_d = (poses, J, M, tau_o, qdd_o)
     outs_h = [torch.empty(o.shape, dtype=torch.float64).pin_memory() for o in outs_d]
-    h2d = sum(t.numel() * 8 for t in (hq, hqd, hqdd, htau))
+    h2d = sum(t.numel() * 8 for t in ins_h)
     d2h = sum(t.numel() * 8 for t in outs_h)
 
-    def e2e_step():
-        q.copy_(hq, non_blocking=True)
-        qd.copy_(hqd, non_blocking=True)
-        qdd.copy_(hqdd, non_blocking=True)
-        tau.copy_(htau, non_blocking=True)
-        step(q, qd, qdd, tau)
-        for hdst, dsrc in zip(outs_h, outs_d):
-            hdst.copy_(dsrc, non_blocking=True)
+    def e2e_mapped():
+        call(N.OP_ALL, ins_h, outs_h)
 
-    for _ in range(args.warmup):
-        flush.zero_()
-        e2e_step()
-    torch.cuda.synchronize()
-    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier()
-    torch.cuda.synchronize()
-    for k in range(args.steps):
-        flush.zero_()
-        ev2[k][0].record(stream)
-        e2e_step()
-        ev2[k][1].record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    ms_e2e = max_across_ranks(float(np.mean([a.elapsed_time(b) for a, b in ev2])), dist, dev)
+    def e2e_staged():
+        for d, h in zip(ins_d, ins_h):
+            d.copy_(h, non_blocking=True)
+        step(q, qd, qdd, tau)
+        for h, d in zip(outs_h, outs_d):
+            h.copy_(d, non_blocking=True)
+
+    def time_e2e(fn):
+        for _ in range(args.warmup):
+            flush.zero_()
+            fn()
+        torch.cuda.synchronize()
+        ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        barrier()
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.zero_()
+            ev2[k][0].record(stream)
+            fn()
+            ev2[k][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return max_across_ranks(float(np.mean([a.elapsed_time(b) for a, b in ev2])), dist, dev)
+
+    ms_e2e = time_e2e(e2e_mapped)
     e2e_value = aggregate_throughput(n, world, ms_e2e * 1e-3)
+    ms_e2e_staged = time_e2e(e2e_staged)
+    # the mapped-host run must give the device run's results bit for bit
+    step(q, qd, qdd, tau)
+    e2e_mapped()
+    torch.cuda.synchronize()
+    e2e_identical = all(torch.equal(h, d.cpu()) for h, d in zip(outs_h, outs_d))
 
     # ---- per-op kernel times (same inputs) -------------------------------------------
     per_op = {}
@@ -455,20 +475,28 @@ def main():
         r = r.reshape(r.shape[0], -1)
         return float((np.abs(g - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-300)).max())
 
-    errs = {"rnea": rel(tau_o[:S].cpu().numpy(), ref["tau"]), "aba": rel(qdd_o[:S].cpu().numpy(), ref["qdd"]),
-            "crba": rel(M[:S].cpu().numpy(), ref["M"]), "jacobian": rel(J[:S].cpu().numpy(), ref["J"]),
-            "fk_positions": rel(poses[:S, :, :3].cpu().numpy(), ref["poses"][:, :, 9:])}
+    first = lambda t, *shape: t[:, :S].T.reshape(S, *shape).cpu().numpy()  # noqa: E731  SoA -> [S, ...]
+    errs = {"rnea": rel(first(tau_o, nv), ref["tau"]), "aba": rel(first(qdd_o, nv), ref["qdd"]),
+            "crba": rel(first(M, nv, nv), ref["M"]), "jacobian": rel(first(J, 6, nv), ref["J"]),
+            "fk_positions": rel(first(poses, nl, 7)[:, :, :3], ref["poses"][:, :, 9:])}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n_envs_per_gpu": n, "nv": nv, "links": nl,
+                   "layout": "structure of arrays ([cols][n], SGDYN_COL_MAJOR)",
                    "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
                    "parallelism": f"data-parallel replicas over environments x{world}",
                    "kernel": kernel},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": ms_e2e},
+                "ms_per_step": ms_e2e,
+                "transfer": "sgdyn_step on mapped pinned host buffers (SoA): the kernel reads inputs from and "
+                            "writes results to host memory over the host link",
+                "results_identical_to_device_run": e2e_identical,
+                "staged_copies": {"value": aggregate_throughput(n, world, ms_e2e_staged * 1e-3),
+                                  "ms_per_step": ms_e2e_staged,
+                                  "transfer": "cudaMemcpyAsync host->device, kernel, device->host on one stream"}},
         "gpu_launches": args.steps,
         "roofline": roofline,
         "roofline_fp64": roofline_fp64,

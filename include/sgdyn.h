@@ -9,7 +9,12 @@
  * Conventions
  *  - All compute functions take DEVICE pointers (or managed memory) to FP64 arrays and
  *    enqueue work on `stream` (a cudaStream_t; NULL = legacy default stream). They return
- *    after the launch; results are ready when the stream reaches that point.
+ *    after the launch; results are ready when the stream reaches that point. Pinned host
+ *    memory that is mapped at the same address on the device (cudaHostAlloc, or
+ *    cudaHostRegister with mapping, under unified addressing) is accepted as well: the
+ *    kernels then read inputs from and write results to host memory directly over the
+ *    host link, with no staging copy (SGDYN_COL_MAJOR keeps those accesses coalesced).
+ *    Pageable host memory is rejected with SGDYN_ERR_NULL.
  *  - Arrays are batched over n environments. layout SGDYN_ENV_MAJOR: [n][cols] row-major
  *    (a torch tensor of shape [n, cols]); SGDYN_COL_MAJOR: [cols][n] (structure of arrays).
  *  - q is in external (SAPIEN) joint order, one coordinate per revolute / continuous /

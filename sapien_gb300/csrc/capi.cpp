@@ -18,6 +18,21 @@ struct sgdyn_model {
 };
 
 namespace sgdyn {
+
+// Rejects pageable host pointers before they reach a kernel.
+bool device_accessible(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return true;
+  // pinned host memory mapped at the same address in the device's space: kernels read and
+  // write it directly over the host link (no staging copy)
+  return at.type == cudaMemoryTypeHost && at.devicePointer == p;
+}
+
 namespace {
 
 thread_local std::string g_err;
@@ -40,16 +55,6 @@ int guarded(F&& f) {
   }
 }
 
-// Rejects host pointers before they reach a kernel.
-bool device_accessible(const void* p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
 
 Arr make_arr(const void* p, int64_t n, int64_t cols, int layout) {
   Arr a;

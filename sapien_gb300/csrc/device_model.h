@@ -40,7 +40,8 @@ struct alignas(16) DJoint {
   int nv;        // 1, or 6 for a free flyer
   int depth;     // 1 for children of the universe
   int ivx;       // first velocity index in depth-first (tree) order
-  int pad_[5];
+  int subtree_end;  // one past the last joint of this joint's subtree (depth-first order)
+  int pad_[4];
 };
 static_assert(sizeof(DJoint) == 256, "DJoint layout");
 

@@ -151,7 +151,7 @@ std::string generate_source(const Model& M, int kind, int ops) {
     o << " {{" << list(d.R, d.R + 9) << "}, {" << list(d.p, d.p + 3) << "}, {" << list(d.axis, d.axis + 3) << "}, "
       << num(d.m) << ", {" << list(d.h, d.h + 3) << "}, {" << list(d.I, d.I + 6) << "}, " << d.parent << ", " << d.kind
       << ", " << d.axis_kind << ", " << d.flags << ", " << d.qcol << ", " << d.vcol << ", " << d.nv << ", " << d.depth
-      << ", " << d.ivx << ", {0, 0, 0, 0, 0}},\n";
+      << ", " << d.ivx << ", " << d.subtree_end << ", {0, 0, 0, 0}},\n";
   }
   o << "};\n";
   o << "__device__ constexpr sgdyn::DLink kLT[" << (nl > 0 ? nl : 1) << "] = {\n";

@@ -84,6 +84,9 @@ struct RolloutArgs {
 };
 
 #ifndef __CUDACC_RTC__
+// Device, managed, or mapped pinned host memory (usable by a kernel at this address).
+bool device_accessible(const void* p);
+
 // Joint-count bucket for the per-thread stash (16, 32 or 64 joints incl. universe).
 int stash_bucket(int nj);
 

@@ -489,7 +489,12 @@ void Model::rebuild_table() {
     D.nv = J.nv;
     D.depth = J.depth;
     D.ivx = J.idx_v;
+    D.subtree_end = j + 1;
   }
+  // subtrees are contiguous in depth-first order: extend each parent's end to its children's
+  for (int j = nj - 1; j >= 1; j--)
+    if (dj[j].parent > 0 && dj[dj[j].parent].subtree_end < dj[j].subtree_end)
+      dj[dj[j].parent].subtree_end = dj[j].subtree_end;
   auto* dl = const_cast<DLink*>(model_links(hdr));
   for (int l = 0; l < nl; l++) {
     const HostBody& B = bodies[link_bodies_[l]];

@@ -33,6 +33,7 @@ struct GravityTab {
   double g[3];
   __device__ __forceinline__ int nj() const { return m->nj; }
   __device__ __forceinline__ int nv() const { return m->nv; }
+  __device__ __forceinline__ int nq_ext() const { return m->nq_ext; }
   __device__ __forceinline__ int nlinks() const { return m->nlinks; }
   __device__ __forceinline__ double gravity(int k) const { return g[k]; }
   __device__ __forceinline__ const DJoint& joint(int i) const { return model_joints(m)[i]; }
@@ -73,16 +74,6 @@ __global__ void __launch_bounds__(32) passive_force_kernel(const DModel* __restr
   for (int c = 0; c < nv; c++) a.qf[e * a.out_stride + c] = float(tau[c]);
 }
 
-bool on_device(const void* p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
 }  // namespace
 }  // namespace sgdyn
 
@@ -99,7 +90,7 @@ extern "C" int sgdyn_compute_passive_force_f32(const sgdyn_model* m, int64_t n, 
   if (in_stride < Mo.nq_ext() || out_stride < Mo.nv())
     return set_last_error(SGDYN_ERR_RUNTIME, "row stride smaller than the model's dof");
   if (n == 0) return SGDYN_OK;
-  if (!on_device(qpos) || !on_device(qf) || (coriolis_and_centrifugal && !on_device(qvel)))
+  if (!device_accessible(qpos) || !device_accessible(qf) || (coriolis_and_centrifugal && !device_accessible(qvel)))
     return set_last_error(SGDYN_ERR_NULL, "qpos / qvel / qf is null or not device memory");
   int err = 0;
   const DModel* dm = Mo.device_table(&err);

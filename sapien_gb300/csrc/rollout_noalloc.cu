@@ -77,16 +77,6 @@ double* scratch_on_current_device(std::string* why) {
   return g_scratch_ptr[dev];
 }
 
-bool on_device(const void* p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
 }  // namespace
 }  // namespace sgdyn
 
@@ -112,11 +102,11 @@ extern "C" int sgdyn_rollout_backward_noalloc(const sgdyn_model* m, int64_t n, i
                                                  "; use fewer environments, a shorter checkpoint interval, or "
                                                  "sgdyn_rollout_backward with your own buffer");
   if (n == 0) return SGDYN_OK;
-  if (!on_device(q0_bar) || !on_device(qd0_bar))
+  if (!device_accessible(q0_bar) || !device_accessible(qd0_bar))
     return set_last_error(SGDYN_ERR_NULL, "q0_bar / qd0_bar is null or not device memory");
-  if (T > 0 && (!on_device(q_ckpt) || !on_device(qd_ckpt) || !on_device(tau) || !on_device(tau_bar)))
+  if (T > 0 && (!device_accessible(q_ckpt) || !device_accessible(qd_ckpt) || !device_accessible(tau) || !device_accessible(tau_bar)))
     return set_last_error(SGDYN_ERR_NULL, "checkpoint, tau or tau_bar is null or not device memory");
-  if ((qT_bar && !on_device(qT_bar)) || (qdT_bar && !on_device(qdT_bar)))
+  if ((qT_bar && !device_accessible(qT_bar)) || (qdT_bar && !device_accessible(qdT_bar)))
     return set_last_error(SGDYN_ERR_NULL, "adjoint input is not device memory");
   const DModel* dm = Mo.find_device_table();
   if (!dm)

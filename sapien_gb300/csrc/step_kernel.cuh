@@ -177,11 +177,24 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
 
   const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
 
-  if constexpr (kCRBA) {
-    const int nv = T.nv();
-    for (int r = 0; r < nv; r++)
-      for (int c = 0; c < nv; c++) stv(args.M, e, r * nv + c, 0.0);
+  // Each pass reads its inputs in one batch before it starts, so their memory latency is
+  // paid once per pass instead of once per joint (most of all when they live in host memory).
+  double qin[MAXJ + 6], qdin[kVel ? MAXV : 1], qddin[kRNEA ? MAXV : 1], tauin[kABA ? MAXV : 1];
+  {
+    const int nq = T.nq_ext(), nv = T.nv();
+#pragma unroll
+    for (int c = 0; c < nq; c++) qin[c] = ldv(args.q, e, c);
+    if constexpr (kVel) {
+#pragma unroll
+      for (int c = 0; c < nv; c++) qdin[c] = ldv(args.qd, e, c);
+    }
+    if constexpr (kRNEA) {
+#pragma unroll
+      for (int c = 0; c < nv; c++) qddin[c] = ldv(args.qdd, e, c);
+    }
   }
+  const Arr qa{qin, 0, 1};
+
 
   // ---------------- pass 1: root to leaves ----------------
 #pragma unroll
@@ -190,7 +203,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
     const int p = J.parent;
     M3 Ro;
     V3 po;
-    joint_world_pose(J, args.q, e, oR, op, Ro, po);
+    joint_world_pose(J, qa, 0, oR, op, Ro, po);
     oR[i] = Ro;
     op[i] = po;
     const int nvi = J.nv, iv = J.ivx, vc = J.vcol;
@@ -217,7 +230,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
       if constexpr (kCRBA) Ic[i] = Y;
       if constexpr (kVel) {
         Mot vJ{mk(0, 0, 0), mk(0, 0, 0)};
-        for (int k = 0; k < nvi; k++) vJ = axpy6(ldv(args.qd, e, vc + k), Sw[iv + k], vJ);
+        for (int k = 0; k < nvi; k++) vJ = axpy6(qdin[vc + k], Sw[iv + k], vJ);
         const Mot v = (p == 0) ? vJ : add6(vel[p], vJ);
         vel[i] = v;
         const Mot hY = rbi_mul(Y, v);  // momentum I v
@@ -225,7 +238,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
         const Mot bias = add_crossf(zero, v, hY);  // v x* I v
         if constexpr (kRNEA) {
           Mot a = (p == 0) ? a0 : acc[p];
-          for (int k = 0; k < nvi; k++) a = axpy6(ldv(args.qdd, e, vc + k), Sw[iv + k], a);
+          for (int k = 0; k < nvi; k++) a = axpy6(qddin[vc + k], Sw[iv + k], a);
           a = add_crossm(a, v, vJ);
           acc[i] = a;
           frc[i] = rbi_mul_add(Y, a, bias);
@@ -270,6 +283,12 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
     }
   }
 
+  if constexpr (kABA) {
+    const int nv = T.nv();
+#pragma unroll
+    for (int c = 0; c < nv; c++) tauin[c] = ldv(args.tau, e, c);
+  }
+
   if constexpr (kCRBA || kRNEA || kABA) {
     // ---------------- pass 2: leaves to root ----------------
 #pragma unroll
@@ -301,6 +320,17 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
             }
           }
         }
+        // entries between this joint and the joints after its subtree (neither ancestors
+        // nor descendants) are structurally zero; every other entry is written above
+#pragma unroll
+        for (int j = J.subtree_end; j < nj; j++) {
+          const int jc = T.joint(j).vcol, nvj = T.joint(j).nv;
+          for (int k = 0; k < nvi; k++)
+            for (int l = 0; l < nvj; l++) {
+              stv(args.M, e, (jc + l) * nv + vc + k, 0.0);
+              stv(args.M, e, (vc + k) * nv + jc + l, 0.0);
+            }
+        }
         if (p > 0) {
           RBI& P = Ic[p];
           P.m += Y.m;
@@ -315,7 +345,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
           const Mot U = sym6_mul(IA[i], S);
           const double D = dot6(S, U);
           const double di = 1.0 / D;
-          const double u = ldv(args.tau, e, vc) - dot6(S, pA[i]);
+          const double u = tauin[vc] - dot6(S, pA[i]);
           Uv[iv] = U;
           uv[iv] = u;
           Dinv[i] = di;
@@ -353,7 +383,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
           // free flyer: 6x6 D = S^T IA S, Cholesky-factored
           for (int k = 0; k < 6; k++) {
             Uv[iv + k] = sym6_mul(IA[i], Sw[iv + k]);
-            uv[iv + k] = ldv(args.tau, e, vc + k) - dot6(Sw[iv + k], pA[i]);
+            uv[iv + k] = tauin[vc + k] - dot6(Sw[iv + k], pA[i]);
           }
           for (int r = 0; r < 6; r++)
             for (int c = 0; c <= r; c++) Lff[r * (r + 1) / 2 + c] = dot6(Sw[iv + r], Uv[iv + c]);

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DJOINT = np.dtype([("R", "<f8", 9), ("p", "<f8", 3), ("axis", "<f8", 3), ("m", "<f8"), ("h", "<f8", 3),
                    ("I", "<f8", 6), ("parent", "<i4"), ("kind", "<i4"), ("axis_kind", "<i4"), ("flags", "<i4"),
                    ("qcol", "<i4"), ("vcol", "<i4"), ("nv", "<i4"), ("depth", "<i4"), ("ivx", "<i4"),
-                   ("pad", "<i4", 5)])
+                   ("subtree_end", "<i4"), ("pad", "<i4", 4)])
 DLINK = np.dtype([("R", "<f8", 9), ("p", "<f8", 3), ("joint", "<i4"), ("flags", "<i4"), ("pad", "<i4", 2)])
 assert DJOINT.itemsize == 256 and DLINK.itemsize == 112
 
@@ -74,6 +74,13 @@ def compare_with_oracle_builder(urdf, joint_order, link_order):
             assert np.abs(J["axis"] - om.axis[j]).max() < 1e-15
         S = spatial6(J["m"], J["h"], J["I"])
         assert np.abs(S - om.inertia6[j]).max() < 1e-13 * max(1, np.abs(S).max())
+        # subtree = the contiguous depth-first range [j, subtree_end)
+        def is_desc(k):
+            while k > 0 and k != j:
+                k = om.parent[k]
+            return k == j
+        assert all(is_desc(k) for k in range(j, J["subtree_end"]))
+        assert not any(is_desc(k) for k in range(J["subtree_end"], om.njoints))
     # external columns follow the joint order
     qc, vc = 0, 0
     for name in joint_order:

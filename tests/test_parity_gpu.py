@@ -183,6 +183,40 @@ def test_col_major_layout_through_c_abi():
     assert rel_per_env(M_o.cpu().numpy().T.reshape(n, nv, nv), r["M"]) <= 1e-10
 
 
+@pytest.mark.parametrize("layout", ["env_major", "col_major"])
+def test_pinned_host_buffers_read_and_written_in_place(layout):
+    """Mapped pinned host memory is accepted at the C ABI: the kernel reads the inputs and
+    writes every output straight in host memory, bitwise equal to the device-buffer run."""
+    robot = syn.arm_with_fingers()
+    pm, _ = pair(robot)
+    T = torch()
+    n, nv, nl = 77, robot.nv, len(robot.link_names)
+    q, qd, qdd, tau = robot.sample(n, seed=12)
+    lay = N.ENV_MAJOR if layout == "env_major" else N.COL_MAJOR
+    arr = (lambda a: a) if layout == "env_major" else (lambda a: a.reshape(n, -1).T)  # noqa: E731
+    ins = [np.ascontiguousarray(arr(x)) for x in (q, qd, qdd, tau)]
+    shapes = [(n, nl * 7), (n, 6 * nv), (n, nv * nv), (n, nv), (n, nv)]
+    shapes = shapes if layout == "env_major" else [(c, r) for r, c in shapes]
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    L = N.load()
+    res = {}
+    for where in ("device", "host"):
+        if where == "device":
+            tin = [T.from_numpy(x).cuda() for x in ins]
+            tout = [T.full(sh, float("nan"), dtype=T.float64, device="cuda") for sh in shapes]
+        else:
+            tin = [T.from_numpy(x).pin_memory() for x in ins]
+            tout = [T.full(sh, float("nan"), dtype=T.float64).pin_memory() for sh in shapes]
+        pm._prepare(T.device("cuda", 0))
+        rc = L.sgdyn_step(pm._h, n, N.OP_ALL, *[p(x) for x in tin], *[p(x) for x in tout], lay, None)
+        assert rc == 0, N.last_error()
+        T.cuda.synchronize()
+        res[where] = [x.cpu() for x in tout]
+    for a, b in zip(res["device"], res["host"]):
+        assert not T.isnan(b).any()
+        assert T.equal(a, b)
+
+
 def test_edge_cases_and_pointer_checks():
     robot = syn.serial_chain(7)
     pm, o = pair(robot)
