@@ -105,27 +105,38 @@ __device__ __forceinline__ M3 quat_to_R(double x, double y, double z, double w) 
   return M3{{1 - (yy + zz), xy - wz, xz + wy, xy + wz, 1 - (xx + zz), yz - wx, xz - wy, yz + wx, 1 - (xx + yy)}};
 }
 // Rotation -> unit quaternion (w, x, y, z), Shepperd's method (largest component first).
+// Case rule: the trace branch when the trace is positive, else the largest diagonal entry
+// (first of equals). Written without a branch on the case: lanes of a warp hold different
+// rotations, and a divergent branch would run the square root and the division once per
+// case taken in the warp. The case only selects operands; the arithmetic per case is
+// unchanged.
 __device__ __forceinline__ void R_to_quat(const M3& R, double* q) {
-  double t = R.a[0] + R.a[4] + R.a[8];
-  if (t > 0) {
-    double r = sqrt(t + 1.0);
-    q[0] = 0.5 * r;
-    double k = 0.5 / r;
-    q[1] = (R.a[7] - R.a[5]) * k;
-    q[2] = (R.a[2] - R.a[6]) * k;
-    q[3] = (R.a[3] - R.a[1]) * k;
-  } else {
+  const double* a = R.a;
+  const double t = a[0] + a[4] + a[8];
+  int c = 0;  // 0: trace, 1 + i: diagonal entry i
+  if (!(t > 0)) {
     int i = 0;
-    if (R.a[4] > R.a[0]) i = 1;
-    if (R.a[8] > R.a[i * 4]) i = 2;
-    int j = (i + 1) % 3, k = (j + 1) % 3;
-    double r = sqrt(R.a[i * 4] - R.a[j * 4] - R.a[k * 4] + 1.0);
-    double kk = 0.5 / r;
-    q[1 + i] = 0.5 * r;
-    q[0] = (R.a[k * 3 + j] - R.a[j * 3 + k]) * kk;
-    q[1 + j] = (R.a[j * 3 + i] + R.a[i * 3 + j]) * kk;
-    q[1 + k] = (R.a[k * 3 + i] + R.a[i * 3 + k]) * kk;
+    if (a[4] > a[0]) i = 1;
+    if (a[8] > a[i * 4]) i = 2;
+    c = 1 + i;
   }
+  // sqrt argument: t + 1, or R_ii - R_jj - R_kk + 1 with (i, j, k) cyclic
+  const int i = c > 0 ? c - 1 : 0, j = i == 2 ? 0 : i + 1, k = j == 2 ? 0 : j + 1;
+  const double diag = a[i * 4] - a[j * 4] - a[k * 4] + 1.0;
+  const double r = sqrt(c == 0 ? t + 1.0 : diag);
+  const double kk = 0.5 / r;
+  const double d1 = a[7] - a[5], d2 = a[2] - a[6], d3 = a[3] - a[1];
+  const double s01 = a[1] + a[3], s02 = a[2] + a[6], s12 = a[5] + a[7];
+  // numerators of the components not fixed to r / 2, per case (w x y z)
+  const double n0 = c == 1 ? d1 : c == 2 ? d2 : d3;
+  const double n1 = c == 0 ? d1 : c == 2 ? s01 : s02;
+  const double n2 = c == 0 ? d2 : c == 1 ? s01 : s12;
+  const double n3 = c == 0 ? d3 : c == 1 ? s02 : s12;
+  const double h = 0.5 * r;
+  q[0] = c == 0 ? h : n0 * kk;
+  q[1] = c == 1 ? h : n1 * kk;
+  q[2] = c == 2 ? h : n2 * kk;
+  q[3] = c == 3 ? h : n3 * kk;
 }
 
 // Motion cross motion: a x b = (a.w x b.v + a.v x b.w, a.w x b.w); acc + a x b.
