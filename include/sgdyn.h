@@ -103,8 +103,10 @@ int sgdyn_model_body_count(const sgdyn_model* m, int* nbodies);
 int sgdyn_model_body_name(const sgdyn_model* m, int b, const char** name);
 /* Upload the model tables to the current device (done lazily by the first launch). */
 int sgdyn_model_upload(sgdyn_model* m);
-/* Host copy of the packed kernel tables (DModel header, DJoint[njoints], DLink[nlinks];
- * layout in sapien_gb300/csrc/device_model.h). Valid until the model changes. */
+/* Host copy of the packed kernel tables (DModel header, DJoint[njoints], DLink[nlinks],
+ * DFrame[njoints]; layout in sapien_gb300/csrc/device_model.h). Joint frames in the table
+ * may be rotated so that the joint axis is +z (DFrame holds the rotation back to the
+ * model's joint frame). Valid until the model changes. */
 int sgdyn_model_table(const sgdyn_model* m, const void** data, int64_t* bytes);
 
 /* PinocchioModel::computeForwardKinematics + getLinkPose for every link

@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(32) ik_kernel(const DModel* __restrict__ model
       M3 Rpl;
       for (int k = 0; k < 9; k++) Rpl.a[k] = J.R[k];
       const V3 ppl = mk(J.p[0], J.p[1], J.p[2]);
-      const V3 ax = mk(J.axis[0], J.axis[1], J.axis[2]);
+      const V3 ax = mk(J.axis[0], J.axis[1], J.axis[2]);  // +z in a canonical frame
       M3 RJ = eye3();
       V3 pJ = mk(0, 0, 0);
       switch (J.kind) {
@@ -260,11 +260,13 @@ __global__ void __launch_bounds__(32) ik_kernel(const DModel* __restrict__ model
           pJ = mk(qs[i][0], qs[i][1], qs[i][2]);
           RJ = quat_to_R(qs[i][3], qs[i][4], qs[i][5], qs[i][6]);
           break;
-        case JK_CONTINUOUS: RJ = rodrigues(ax, qs[i][1], qs[i][0]); break;
+        case JK_CONTINUOUS:
+          RJ = J.axis_kind == AX_Z ? rot_z(qs[i][1], qs[i][0]) : rodrigues(ax, qs[i][1], qs[i][0]);
+          break;
         default: {
           double s, c;
           sincos(qs[i][0], &s, &c);
-          RJ = rodrigues(ax, s, c);
+          RJ = J.axis_kind == AX_Z ? rot_z(s, c) : rodrigues(ax, s, c);
         }
       }
       const M3 Rli = mul(Rpl, RJ);
@@ -390,6 +392,13 @@ __global__ void __launch_bounds__(32) ik_kernel(const DModel* __restrict__ model
     }
   }
   a.success[e] = ok ? 1 : 0;
+  // the error lives in the table's canonical joint frame F' = F C: report it in F
+  if (jid > 0) {
+    M3 C;
+    for (int k = 0; k < 9; k++) C.a[k] = model_frames(model)[jid].C[k];
+    bestErr.v = mul(C, bestErr.v);
+    bestErr.w = mul(C, bestErr.w);
+  }
   stv(a.err, e, 0, bestErr.v.x);
   stv(a.err, e, 1, bestErr.v.y);
   stv(a.err, e, 2, bestErr.v.z);

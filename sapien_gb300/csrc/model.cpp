@@ -172,6 +172,43 @@ bool is_identity(const double* R) {
          R[7] == 0;
 }
 
+// Rotation C (row-major) with C e_z = a for a unit axis a. Coordinate axes get exact
+// integer rotations; other axes the orthonormal basis of Duff et al., "Building an
+// Orthonormal Basis, Revisited" (JCGT 2017), with a as the third column.
+void rotation_to_axis(const double a[3], double C[9]) {
+  const double ex[9] = {0, 0, 1, 0, 1, 0, -1, 0, 0}, nex[9] = {0, 0, -1, 0, 1, 0, 1, 0, 0};
+  const double ey[9] = {1, 0, 0, 0, 0, 1, 0, -1, 0}, ney[9] = {1, 0, 0, 0, 0, -1, 0, 1, 0};
+  const double ez[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, nez[9] = {1, 0, 0, 0, -1, 0, 0, 0, -1};
+  const double* exact = nullptr;
+  if (a[1] == 0 && a[2] == 0) exact = a[0] > 0 ? ex : nex;
+  else if (a[0] == 0 && a[2] == 0) exact = a[1] > 0 ? ey : ney;
+  else if (a[0] == 0 && a[1] == 0) exact = a[2] > 0 ? ez : nez;
+  if (exact) {
+    std::memcpy(C, exact, 9 * sizeof(double));
+    return;
+  }
+  const double sg = std::copysign(1.0, a[2]);
+  const double k = -1.0 / (sg + a[2]);
+  const double b = a[0] * a[1] * k;
+  const double b1[3] = {1.0 + sg * a[0] * a[0] * k, sg * b, -sg * a[0]};
+  const double b2[3] = {b, sg + a[1] * a[1] * k, -a[1]};
+  for (int r = 0; r < 3; r++) {
+    C[r * 3 + 0] = b1[r];
+    C[r * 3 + 1] = b2[r];
+    C[r * 3 + 2] = a[r];
+  }
+}
+
+// out = A^T B (3x3 row-major)
+void mat_tmul(const double* A, const double* B, double* out) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) out[i * 3 + j] = A[0 * 3 + i] * B[0 * 3 + j] + A[1 * 3 + i] * B[1 * 3 + j] + A[2 * 3 + i] * B[2 * 3 + j];
+}
+// out = A^T x
+void mat_tvec(const double* A, const double* x, double* out) {
+  for (int i = 0; i < 3; i++) out[i] = A[0 * 3 + i] * x[0] + A[1 * 3 + i] * x[1] + A[2 * 3 + i] * x[2];
+}
+
 }  // namespace
 
 // Builds the depth-first tree from link inertias (origin form, link frame) and joint
@@ -467,23 +504,62 @@ void Model::rebuild_table() {
   hdr->n_free_flyer = nff;
   std::memcpy(hdr->gravity, gravity, sizeof(double) * 3);
   auto* dj = const_cast<DJoint*>(model_joints(hdr));
+  auto* df = const_cast<DFrame*>(model_frames(hdr));
+  // Canonical frames: C_j with C_j e_z = axis_j for 1-DoF joints. A joint keeps its own
+  // frame (C_j = 1, general axis) when its placement, seen from its parent's table frame,
+  // and some link frame on it are both unrotated: there the axis products cost less than
+  // the rotation C_j would add to that link's pose. Parents come first in depth-first order.
+  std::vector<char> canon(nj, 0), bare_link(nj, 0);
+  for (int l = 0; l < nl; l++) {
+    const HostBody& B = bodies[link_bodies_[l]];
+    if (is_identity(B.placement.R)) bare_link[B.joint] = 1;
+  }
+  const double I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  std::memcpy(df[0].C, I3, sizeof I3);
+  for (int j = 1; j < nj; j++) {
+    const HostJoint& J = joints[j];
+    const bool axial = J.kind == JK_REVOLUTE || J.kind == JK_CONTINUOUS || J.kind == JK_PRISMATIC;
+    double Reff[9];
+    mat_tmul(df[J.parent].C, J.placement.R, Reff);
+    canon[j] = axial && !(is_identity(Reff) && bare_link[j]);
+    if (canon[j]) rotation_to_axis(J.axis, df[j].C);
+    else std::memcpy(df[j].C, I3, sizeof I3);
+  }
   for (int j = 0; j < nj; j++) {
     const HostJoint& J = joints[j];
     DJoint& D = dj[j];
-    std::memcpy(D.R, J.placement.R, sizeof D.R);
-    std::memcpy(D.p, J.placement.p, sizeof D.p);
-    std::memcpy(D.axis, J.axis, sizeof D.axis);
+    const double* Cj = df[j].C;
+    const double* Cp = df[j > 0 ? J.parent : 0].C;
+    // placement in canonical frames: R' = Cp^T R Cj, p' = Cp^T p
+    double T[9];
+    mat_tmul(Cp, J.placement.R, T);
+    mat_mul(T, Cj, D.R);
+    mat_tvec(Cp, J.placement.p, D.p);
+    if (canon[j]) {
+      D.axis[0] = 0;
+      D.axis[1] = 0;
+      D.axis[2] = 1.0;
+    } else {
+      std::memcpy(D.axis, J.axis, sizeof D.axis);
+    }
+    // body inertia in the canonical frame: h' = Cj^T h, I' = Cj^T I Cj
     D.m = J.inertia.m;
-    std::memcpy(D.h, J.inertia.h, sizeof D.h);
-    std::memcpy(D.I, J.inertia.I, sizeof D.I);
+    mat_tvec(Cj, J.inertia.h, D.h);
+    const double* I = J.inertia.I;
+    const double Im[9] = {I[0], I[1], I[2], I[1], I[3], I[4], I[2], I[4], I[5]};
+    double Ir[9];
+    mat_tmul(Cj, Im, T);
+    mat_mul(T, Cj, Ir);
+    D.I[0] = Ir[0];
+    D.I[1] = 0.5 * (Ir[1] + Ir[3]);
+    D.I[2] = 0.5 * (Ir[2] + Ir[6]);
+    D.I[3] = Ir[4];
+    D.I[4] = 0.5 * (Ir[5] + Ir[7]);
+    D.I[5] = Ir[8];
     D.parent = J.parent;
     D.kind = J.kind;
-    D.axis_kind = AX_GENERAL;
-    if (J.kind != JK_FREEFLYER) {
-      for (int a = 0; a < 3; a++)
-        if (J.axis[a] == 1.0 && J.axis[(a + 1) % 3] == 0.0 && J.axis[(a + 2) % 3] == 0.0) D.axis_kind = a;
-    }
-    D.flags = is_identity(J.placement.R) ? JF_ROT_IDENTITY : 0;
+    D.axis_kind = canon[j] ? AX_Z : AX_GENERAL;
+    D.flags = is_identity(D.R) ? JF_ROT_IDENTITY : 0;
     D.qcol = j < int(qcol_.size()) ? qcol_[j] : -1;
     D.vcol = j < int(vcol_.size()) ? vcol_[j] : -1;
     D.nv = J.nv;
@@ -498,10 +574,12 @@ void Model::rebuild_table() {
   auto* dl = const_cast<DLink*>(model_links(hdr));
   for (int l = 0; l < nl; l++) {
     const HostBody& B = bodies[link_bodies_[l]];
-    std::memcpy(dl[l].R, B.placement.R, sizeof dl[l].R);
-    std::memcpy(dl[l].p, B.placement.p, sizeof dl[l].p);
+    // link frame relative to its joint's canonical frame: Cj^T (R, p)
+    const double* Cj = df[B.joint].C;
+    mat_tmul(Cj, B.placement.R, dl[l].R);
+    mat_tvec(Cj, B.placement.p, dl[l].p);
     dl[l].joint = B.joint;
-    dl[l].flags = is_identity(B.placement.R) ? JF_ROT_IDENTITY : 0;
+    dl[l].flags = is_identity(dl[l].R) ? JF_ROT_IDENTITY : 0;
   }
   // device copies are stale now
   for (auto& kv : dev_) {

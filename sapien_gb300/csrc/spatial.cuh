@@ -81,6 +81,8 @@ __device__ __forceinline__ V3 sym_mul_add(const double* S, V3 w, V3 acc) {
             fma(S[5], w.z, fma(S[4], w.y, fma(S[2], w.x, acc.z)))};
 }
 
+// Rotation about z with (s, c) = (sin, cos) of the angle.
+__device__ __forceinline__ M3 rot_z(double s, double c) { return M3{{c, -s, 0, s, c, 0, 0, 0, 1}}; }
 // Rotation about unit axis a by angle with (s, c) = (sin, cos): c 1 + s [a]x + (1-c) a a^T.
 __device__ __forceinline__ M3 rodrigues(V3 a, double s, double c) {
   double t = 1.0 - c;
@@ -214,6 +216,33 @@ __device__ __forceinline__ Sym6 sym6_from_rbi(const RBI& Y) {
 #pragma unroll
   for (int k = 0; k < 6; k++) S.C[k] = Y.I[k];
   return S;
+}
+// sym6_from_rbi(Y) + S, adding only where Y's matrix has non-zero entries
+__device__ __forceinline__ Sym6 sym6_rbi_add(const RBI& Y, const Sym6& S) {
+  Sym6 R = S;
+  R.A[0] += Y.m; R.A[3] += Y.m; R.A[5] += Y.m;
+  R.B[1] += Y.h.z; R.B[2] -= Y.h.y; R.B[3] -= Y.h.z;
+  R.B[5] += Y.h.x; R.B[6] += Y.h.y; R.B[7] -= Y.h.x;
+#pragma unroll
+  for (int k = 0; k < 6; k++) R.C[k] += Y.I[k];
+  return R;
+}
+__device__ __forceinline__ void sym6_acc(Sym6& P, const Sym6& S) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    P.A[k] += S.A[k];
+    P.C[k] += S.C[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) P.B[k] += S.B[k];
+}
+__device__ __forceinline__ RBI rbi_add(const RBI& a, const RBI& b) {
+  RBI r;
+  r.m = a.m + b.m;
+  r.h = a.h + b.h;
+#pragma unroll
+  for (int k = 0; k < 6; k++) r.I[k] = a.I[k] + b.I[k];
+  return r;
 }
 // acc + S x  (x a 6-vector)
 __device__ __forceinline__ Mot sym6_mul_add(const Sym6& S, Mot x, Mot acc) {

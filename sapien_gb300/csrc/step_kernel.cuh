@@ -55,42 +55,64 @@ struct JointFrame {
   V3 p;
 };
 
-// Local joint transform liMi = placement * M_J(q); returns the world pose given the parent's.
+// World pose of joint J from its parent's: (Ro, po) = oMi[parent] * placement * M_J(q).
+// A joint in a canonical frame (axis_kind AX_Z) rotates about / slides along z: with
+// B = R_parent R_placement, Ro = B Rz(q) mixes two columns of B and keeps the third. Other
+// 1-DoF joints keep their axis (Rodrigues), which is cheaper when both the placement and the
+// link frames on the joint are unrotated (the table builder decides per joint).
 __device__ __forceinline__ void joint_world_pose(const DJoint& J, const Arr& q, int64_t e, const M3* oR, const V3* op,
                                                  M3& Ro, V3& po) {
+  const int p = J.parent;
+  const bool rot_id = (J.flags & JF_ROT_IDENTITY) != 0;
   M3 Rpl;
 #pragma unroll
   for (int k = 0; k < 9; k++) Rpl.a[k] = J.R[k];
   const V3 ppl = mk(J.p[0], J.p[1], J.p[2]);
+  if (J.kind == JK_FREEFLYER) {
+    const int c0 = J.qcol;
+    const V3 t = mk(ldv(q, e, c0), ldv(q, e, c0 + 1), ldv(q, e, c0 + 2));
+    const M3 RJ = quat_to_R(ldv(q, e, c0 + 3), ldv(q, e, c0 + 4), ldv(q, e, c0 + 5), ldv(q, e, c0 + 6));
+    const M3 Rli = rot_id ? RJ : mul(Rpl, RJ);
+    const V3 pli = rot_id ? t + ppl : mul_add(Rpl, t, ppl);
+    Ro = (p == 0) ? Rli : mul(oR[p], Rli);
+    po = (p == 0) ? pli : mul_add(oR[p], pli, op[p]);
+    return;
+  }
+  if (J.axis_kind == AX_Z) {
+    // placement origin in the world
+    const V3 o = (p == 0) ? ppl : mul_add(oR[p], ppl, op[p]);
+    const M3 B = (p == 0) ? Rpl : (rot_id ? oR[p] : mul(oR[p], Rpl));
+    if (J.kind == JK_PRISMATIC) {
+      Ro = B;
+      po = axpy(ldv(q, e, J.qcol), mk(B.a[2], B.a[5], B.a[8]), o);
+    } else {  // revolute and continuous
+      double s, c;
+      sincos(ldv(q, e, J.qcol), &s, &c);
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        const double b0 = B.a[r * 3], b1 = B.a[r * 3 + 1];
+        Ro.a[r * 3 + 0] = fma(c, b0, s * b1);
+        Ro.a[r * 3 + 1] = fma(c, b1, -s * b0);
+        Ro.a[r * 3 + 2] = B.a[r * 3 + 2];
+      }
+      po = o;
+    }
+    return;
+  }
   const V3 ax = mk(J.axis[0], J.axis[1], J.axis[2]);
   M3 Rli;
   V3 pli;
-  const bool rot_id = (J.flags & JF_ROT_IDENTITY) != 0;
-  switch (J.kind) {
-    case JK_PRISMATIC: {
-      double d = ldv(q, e, J.qcol);
-      Rli = Rpl;
-      pli = rot_id ? axpy(d, ax, ppl) : mul_add(Rpl, d * ax, ppl);
-      break;
-    }
-    case JK_FREEFLYER: {
-      const int c0 = J.qcol;
-      V3 t = mk(ldv(q, e, c0), ldv(q, e, c0 + 1), ldv(q, e, c0 + 2));
-      M3 RJ = quat_to_R(ldv(q, e, c0 + 3), ldv(q, e, c0 + 4), ldv(q, e, c0 + 5), ldv(q, e, c0 + 6));
-      Rli = rot_id ? RJ : mul(Rpl, RJ);
-      pli = rot_id ? (t + ppl) : mul_add(Rpl, t, ppl);
-      break;
-    }
-    default: {  // revolute and continuous: rotation about the axis
-      double s, c;
-      sincos(ldv(q, e, J.qcol), &s, &c);
-      M3 RJ = rodrigues(ax, s, c);
-      Rli = rot_id ? RJ : mul(Rpl, RJ);
-      pli = ppl;
-      break;
-    }
+  if (J.kind == JK_PRISMATIC) {
+    const double d = ldv(q, e, J.qcol);
+    Rli = Rpl;
+    pli = rot_id ? axpy(d, ax, ppl) : mul_add(Rpl, d * ax, ppl);
+  } else {
+    double s, c;
+    sincos(ldv(q, e, J.qcol), &s, &c);
+    const M3 RJ = rodrigues(ax, s, c);
+    Rli = rot_id ? RJ : mul(Rpl, RJ);
+    pli = ppl;
   }
-  const int p = J.parent;
   if (p == 0) {
     Ro = Rli;
     po = pli;
@@ -100,7 +122,8 @@ __device__ __forceinline__ void joint_world_pose(const DJoint& J, const Arr& q, 
   }
 }
 
-// World-frame motion subspace column k of joint J (pose Ro, po).
+// World-frame motion subspace column k of joint J (pose Ro, po): for a joint in a
+// canonical frame the z column of Ro, else Ro times the axis.
 __device__ __forceinline__ Mot world_S(const DJoint& J, const M3& Ro, V3 po, int k) {
   Mot S;
   if (J.kind == JK_FREEFLYER) {
@@ -112,12 +135,15 @@ __device__ __forceinline__ Mot world_S(const DJoint& J, const M3& Ro, V3 po, int
       S.v = cross(po, r);
       S.w = r;
     }
-  } else if (J.kind == JK_PRISMATIC) {
-    S.v = mul(Ro, mk(J.axis[0], J.axis[1], J.axis[2]));
+    return S;
+  }
+  const V3 u = (J.axis_kind == AX_Z) ? mk(Ro.a[2], Ro.a[5], Ro.a[8]) : mul(Ro, mk(J.axis[0], J.axis[1], J.axis[2]));
+  if (J.kind == JK_PRISMATIC) {
+    S.v = u;
     S.w = mk(0, 0, 0);
   } else {
-    S.w = mul(Ro, mk(J.axis[0], J.axis[1], J.axis[2]));
-    S.v = cross(po, S.w);
+    S.w = u;
+    S.v = cross(po, u);
   }
   return S;
 }
@@ -169,8 +195,13 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
   Mot vel[kVel ? MAXJ : 1];
   Mot acc[(kRNEA || kABA) ? MAXJ : 1];
   Mot frc[kRNEA ? MAXJ : 1];
-  RBI Ic[kCRBA ? MAXJ : 1];
-  Sym6 IA[kABA ? MAXJ : 1];
+  // Pass 2 rebuilds each joint's composite (CRBA) and articulated (ABA) inertia as its own
+  // body inertia Yb plus what its children passed up (CC, AC). The last child in
+  // depth-first order is processed first and initialises its parent's slot, so no slot is
+  // zero-filled and only joints with children carry one.
+  RBI Yb[(kCRBA || kABA) ? MAXJ : 1];
+  RBI CC[kCRBA ? MAXJ : 1];
+  Sym6 AC[kABA ? MAXJ : 1];
   Mot pA[kABA ? MAXJ : 1], cb[kABA ? MAXJ : 1], Uv[kABA ? MAXV : 1];
   double uv[kABA ? MAXV : 1], Dinv[kABA ? MAXJ : 1];
   double Lff[kABA ? 21 : 1];  // Cholesky factor of D for the (single) free-flyer joint
@@ -227,7 +258,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
 #pragma unroll
       for (int k = 0; k < 6; k++) Yl.I[k] = J.I[k];
       const RBI Y = rbi_transport(Yl, Ro, po);
-      if constexpr (kCRBA) Ic[i] = Y;
+      if constexpr (kCRBA || kABA) Yb[i] = Y;
       if constexpr (kVel) {
         Mot vJ{mk(0, 0, 0), mk(0, 0, 0)};
         for (int k = 0; k < nvi; k++) vJ = axpy6(qdin[vc + k], Sw[iv + k], vJ);
@@ -245,7 +276,6 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
         }
         if constexpr (kABA) {
           cb[i] = add_crossm(zero, v, vJ);
-          IA[i] = sym6_from_rbi(Y);
           pA[i] = bias;
         }
       }
@@ -295,6 +325,9 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
     for (int i = nj - 1; i >= 1; i--) {
       const DJoint& J = T.joint(i);
       const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
+      const bool has_children = J.subtree_end > i + 1;
+      // the last child of p in depth-first order ends where p's subtree ends
+      const bool first_of_parent = p > 0 && J.subtree_end == T.joint(p).subtree_end;
       if constexpr (kRNEA) {
         const Mot f = frc[i];
         for (int k = 0; k < nvi; k++) stv(args.tau_out, e, vc + k, dot6(Sw[iv + k], f));
@@ -302,7 +335,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
       }
       if constexpr (kCRBA) {
         const int nv = T.nv();
-        const RBI Y = Ic[i];
+        const RBI Y = has_children ? rbi_add(Yb[i], CC[i]) : Yb[i];
         for (int k = 0; k < nvi; k++) {
           const Mot F = rbi_mul(Y, Sw[iv + k]);
           for (int l = 0; l <= k; l++) {  // own block, upper triangle mirrored
@@ -331,18 +364,13 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
               stv(args.M, e, (vc + k) * nv + jc + l, 0.0);
             }
         }
-        if (p > 0) {
-          RBI& P = Ic[p];
-          P.m += Y.m;
-          P.h = P.h + Y.h;
-#pragma unroll
-          for (int k = 0; k < 6; k++) P.I[k] += Y.I[k];
-        }
+        if (p > 0) CC[p] = first_of_parent ? Y : rbi_add(CC[p], Y);
       }
       if constexpr (kABA) {
+        const Sym6 IAi = has_children ? sym6_rbi_add(Yb[i], AC[i]) : sym6_from_rbi(Yb[i]);
         if (nvi == 1) {
           const Mot S = Sw[iv];
-          const Mot U = sym6_mul(IA[i], S);
+          const Mot U = sym6_mul(IAi, S);
           const double D = dot6(S, U);
           const double di = 1.0 / D;
           const double u = tauin[vc] - dot6(S, pA[i]);
@@ -351,7 +379,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
           Dinv[i] = di;
           if (p > 0) {
             const Mot Ud = scale6(di, U);
-            Sym6 Ia = IA[i];
+            Sym6 Ia = IAi;
             const double ud[6] = {Ud.v.x, Ud.v.y, Ud.v.z, Ud.w.x, Ud.w.y, Ud.w.z};
             const double uu[6] = {U.v.x, U.v.y, U.v.z, U.w.x, U.w.y, U.w.z};
             // A -= ud_lin u_lin^T (sym), B -= ud_lin u_ang^T, C -= ud_ang u_ang^T (sym)
@@ -369,20 +397,14 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
               for (int c = 0; c < 3; c++) Ia.B[r * 3 + c] = fma(-ud[r], uu[3 + c], Ia.B[r * 3 + c]);
             Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
             pa = axpy6(u, Ud, pa);
-            Sym6& P = IA[p];
-#pragma unroll
-            for (int k = 0; k < 6; k++) {
-              P.A[k] += Ia.A[k];
-              P.C[k] += Ia.C[k];
-            }
-#pragma unroll
-            for (int k = 0; k < 9; k++) P.B[k] += Ia.B[k];
+            if (first_of_parent) AC[p] = Ia;
+            else sym6_acc(AC[p], Ia);
             pA[p] = add6(pA[p], pa);
           }
         } else {
           // free flyer: 6x6 D = S^T IA S, Cholesky-factored
           for (int k = 0; k < 6; k++) {
-            Uv[iv + k] = sym6_mul(IA[i], Sw[iv + k]);
+            Uv[iv + k] = sym6_mul(IAi, Sw[iv + k]);
             uv[iv + k] = tauin[vc + k] - dot6(Sw[iv + k], pA[i]);
           }
           for (int r = 0; r < 6; r++)
@@ -390,7 +412,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
           chol6(Lff);
           if (p > 0) {
             // Ia = IA - U D^-1 U^T ; pa = pA + Ia c + U D^-1 u, with D^-1 applied by solves
-            Sym6 Ia = IA[i];
+            Sym6 Ia = IAi;
             double W[6][6];  // W[:, k] = D^-1 e_k
             for (int k = 0; k < 6; k++) {
               for (int r = 0; r < 6; r++) W[r][k] = (r == k) ? 1.0 : 0.0;
@@ -420,12 +442,8 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
             }
             Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
             for (int k = 0; k < 6; k++) pa = axpy6(uv[iv + k], UD[k], pa);
-            Sym6& P = IA[p];
-            for (int k = 0; k < 6; k++) {
-              P.A[k] += Ia.A[k];
-              P.C[k] += Ia.C[k];
-            }
-            for (int k = 0; k < 9; k++) P.B[k] += Ia.B[k];
+            if (first_of_parent) AC[p] = Ia;
+            else sym6_acc(AC[p], Ia);
             pA[p] = add6(pA[p], pa);
           }
         }

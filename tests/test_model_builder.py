@@ -19,7 +19,8 @@ DJOINT = np.dtype([("R", "<f8", 9), ("p", "<f8", 3), ("axis", "<f8", 3), ("m", "
                    ("qcol", "<i4"), ("vcol", "<i4"), ("nv", "<i4"), ("depth", "<i4"), ("ivx", "<i4"),
                    ("subtree_end", "<i4"), ("pad", "<i4", 4)])
 DLINK = np.dtype([("R", "<f8", 9), ("p", "<f8", 3), ("joint", "<i4"), ("flags", "<i4"), ("pad", "<i4", 2)])
-assert DJOINT.itemsize == 256 and DLINK.itemsize == 112
+DFRAME = np.dtype([("C", "<f8", 9), ("pad", "<f8")])
+assert DJOINT.itemsize == 256 and DLINK.itemsize == 112 and DFRAME.itemsize == 80
 
 
 def parse_table(raw):
@@ -28,7 +29,26 @@ def parse_table(raw):
     grav = np.frombuffer(raw, dtype="<f8", count=3, offset=32)
     joints = np.frombuffer(raw, dtype=DJOINT, count=nj, offset=64)
     links = np.frombuffer(raw, dtype=DLINK, count=nl, offset=64 + 256 * nj)
-    return dict(nj=nj, nv=nv, nq_ext=nqe, nlinks=nl, gravity=grav, joints=joints, links=links)
+    frames = np.frombuffer(raw, dtype=DFRAME, count=nj, offset=64 + 256 * nj + 112 * nl)
+    assert len(raw) == 64 + 256 * nj + 112 * nl + 80 * nj
+    return dict(nj=nj, nv=nv, nq_ext=nqe, nlinks=nl, gravity=grav, joints=joints, links=links, frames=frames)
+
+
+def model_frame_quantities(t):
+    """Undo the table's canonical joint frames (F' = F C, axis +z): per joint the placement
+    (R, p), axis, first moment and rotational inertia in the model's joint frames, and per
+    link its (R, p) in its joint's model frame."""
+    C = [f["C"].reshape(3, 3) for f in t["frames"]]
+    out = []
+    for j in range(t["nj"]):
+        J = t["joints"][j]
+        Cj, Cp = C[j], C[J["parent"]] if j > 0 else np.eye(3)
+        I = J["I"]
+        Im = np.array([[I[0], I[1], I[2]], [I[1], I[3], I[4]], [I[2], I[4], I[5]]])
+        out.append(dict(R=Cp @ J["R"].reshape(3, 3) @ Cj.T, p=Cp @ J["p"], axis=Cj @ J["axis"], h=Cj @ J["h"],
+                        I=Cj @ Im @ Cj.T))
+    links = [dict(R=C[L["joint"]] @ L["R"].reshape(3, 3), p=C[L["joint"]] @ L["p"]) for L in t["links"]]
+    return out, links
 
 
 def spatial6(m, h, I):
@@ -63,16 +83,26 @@ def compare_with_oracle_builder(urdf, joint_order, link_order):
     assert t["nj"] == om.njoints
     assert t["nv"] == om.nv
     assert pm.joint_names == om.joint_names[1:]
+    mj, ml = model_frame_quantities(t)
     for j in range(1, om.njoints):
-        J = t["joints"][j]
+        J, G = t["joints"][j], mj[j]
         assert J["parent"] == om.parent[j]
         assert J["kind"] == om.jtype[j]
+        C = t["frames"][j]["C"].reshape(3, 3)
+        assert np.abs(C @ C.T - np.eye(3)).max() < 1e-15 and abs(np.linalg.det(C) - 1) < 1e-15
         R, p = om.placement[j]
-        assert np.abs(J["R"].reshape(3, 3) - R).max() < 1e-15
-        assert np.abs(J["p"] - p).max() < 1e-15
+        assert np.abs(G["R"] - R).max() < 1e-15
+        assert np.abs(G["p"] - p).max() < 1e-15
         if om.jtype[j] != um.JT_FREEFLYER:
-            assert np.abs(J["axis"] - om.axis[j]).max() < 1e-15
-        S = spatial6(J["m"], J["h"], J["I"])
+            if J["axis_kind"] == 2:  # canonical frame: axis +z
+                assert np.array_equal(J["axis"], [0.0, 0.0, 1.0])
+            else:  # own frame kept
+                assert np.array_equal(C, np.eye(3))
+            assert np.abs(G["axis"] - om.axis[j]).max() < 1e-15
+        else:
+            assert np.array_equal(C, np.eye(3))
+        Ig = G["I"]
+        S = spatial6(J["m"], G["h"], [Ig[0, 0], Ig[0, 1], Ig[0, 2], Ig[1, 1], Ig[1, 2], Ig[2, 2]])
         assert np.abs(S - om.inertia6[j]).max() < 1e-13 * max(1, np.abs(S).max())
         # subtree = the contiguous depth-first range [j, subtree_end)
         def is_desc(k):
@@ -95,8 +125,8 @@ def compare_with_oracle_builder(urdf, joint_order, link_order):
         jid, (R, p) = om.body_frames[name]
         L = t["links"][li]
         assert L["joint"] == jid
-        assert np.abs(L["R"].reshape(3, 3) - R).max() < 1e-15
-        assert np.abs(L["p"] - p).max() < 1e-15
+        assert np.abs(ml[li]["R"] - R).max() < 1e-15
+        assert np.abs(ml[li]["p"] - p).max() < 1e-15
 
 
 @pytest.mark.parametrize("name", list(ROBOTS))

