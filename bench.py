@@ -231,7 +231,8 @@ def secondary_workloads(dev):
     hms = _event_ms(torch, g.replay, reps=5, warm=1) / 10
     out["hetero"] = {"workload": "8192 envs: 50% 6-DoF arms, 30% 18-DoF quadrupeds, 20% 35-DoF humanoids; "
                                  "RNEA+ABA+CRBA; CUDA-graph replay of 10 steps",
-                     "env_steps_per_s": 8192 / (hms * 1e-3), "ms_per_step": hms, "launch_shape": list(shape)}
+                     "env_steps_per_s": 8192 / (hms * 1e-3), "ms_per_step": hms, "launch_shape": list(shape),
+                     "lanes_per_env": list(hb.lanes)}
     nik = 65536
     qik, _, _, _ = arm.sample(nik, seed=3)
     tgt = pm.compute_forward_kinematics_batched(torch.from_numpy(qik).to(dev))[:, arm.ee_link].contiguous()

@@ -1,12 +1,17 @@
-"""Launch-shape autotuner.
+"""Launch-shape and threads-per-environment autotuner.
 
-For a heterogeneous batch the tuner times every candidate of
-  persistent CTAs per SM  x  warps per CTA  x  tile order (descending DoF / input order)
-with CUDA events (median of a few launches after warm-up) and keeps the fastest. Results
-are cached in a JSON file keyed by GPU name, the batch signature (velocity dimension and
-count of every model) and the op set, so a process pays for the search once per tree mix.
-One environment runs per thread in every candidate (the per-lane work of the sweep is
-sequential along the tree); the tile is one warp of environments of one model.
+For a heterogeneous batch the tuner times, with CUDA events (median of a few launches
+after warm-up):
+  1. every launch shape: persistent CTAs per SM x warps per CTA x tile order (descending
+     DoF / input order), one lane per environment;
+  2. lanes per environment (1, 2, 4, 8) for each model in turn, largest tree first, each
+     count with every launch shape, keeping the best pair (coordinate descent over the
+     models): a team of L lanes shares one environment, the joints near the root on every
+     lane and the subtrees off them split among the lanes, which shortens a wide tree's
+     sequential sweep but needs more warps, hence the joint search with the shape.
+The choice is cached in a JSON file keyed by GPU name, the batch signature (velocity
+dimension, joint count and environment count of every model) and the op set, so a process
+pays for the search once per tree mix.
 """
 from __future__ import annotations
 
@@ -46,9 +51,10 @@ def _time(fn, reps=5):
     return float(np.median(ts))
 
 
-def tune_batch(batch, q, qd, qdd, tau, ops, use_cache=True, candidates=None):
-    """Pick the fastest launch shape for `batch` on these inputs; returns (shape, table)."""
-    key = f"{torch.cuda.get_device_name(batch.device)}|{batch_signature(batch, ops)}"
+def tune_batch(batch, q, qd, qdd, tau, ops, use_cache=True, candidates=None, lane_candidates=(1, 2, 4, 8)):
+    """Pick the fastest launch shape and lanes per environment for `batch` on these inputs,
+    apply them to the batch and return (shape, table); the lanes are in batch.lanes."""
+    key = f"{torch.cuda.get_device_name(batch.device)}|{batch_signature(batch, ops)}|lanes{tuple(lane_candidates)}"
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -59,19 +65,36 @@ def tune_batch(batch, q, qd, qdd, tau, ops, use_cache=True, candidates=None):
     if use_cache and key in cache:
         shape = tuple(cache[key]["shape"])
         batch.set_launch(*shape)
+        batch.set_lanes(cache[key].get("lanes", [1] * len(batch.models)))
         return shape, cache[key]["table"]
     out = batch.alloc_outputs(ops)
+    shapes = list(candidates or CANDIDATES)
     table = []
-    for shape in candidates or CANDIDATES:
+
+    def measure(shape, lanes):
         batch.set_launch(*shape)
+        batch.set_lanes(lanes)
         ms = _time(lambda: batch.step(q, qd, qdd, tau, ops, out))
-        table.append({"shape": list(shape), "ms": ms})
-    best = min(table, key=lambda r: r["ms"])
-    batch.set_launch(*best["shape"])
-    cache[key] = {"shape": best["shape"], "table": table, "when": time.time()}
+        table.append({"shape": list(shape), "lanes": list(lanes), "ms": ms})
+        return ms
+
+    lanes = [1] * len(batch.models)
+    best_ms, best_shape = min((measure(sh, lanes), sh) for sh in shapes)
+    if len(lane_candidates) > 1:
+        for m in sorted(range(len(batch.models)), key=lambda k: -batch.models[k].nv):
+            for L in lane_candidates:
+                if L == lanes[m]:
+                    continue
+                trial = lanes[:m] + [L] + lanes[m + 1:]
+                ms, sh = min((measure(sh, trial), sh) for sh in shapes)
+                if ms < best_ms:
+                    best_ms, best_shape, lanes = ms, sh, trial
+    batch.set_launch(*best_shape)
+    batch.set_lanes(lanes)
+    cache[key] = {"shape": list(best_shape), "lanes": lanes, "table": table, "when": time.time()}
     if use_cache:
         tmp = path + ".tmp"
         with open(tmp, "w") as f:
             json.dump(cache, f, indent=1)
         os.replace(tmp, path)
-    return tuple(best["shape"]), table
+    return tuple(best_shape), table

@@ -12,7 +12,9 @@ cudaError_t launch_coriolis_j32(const DModel* dm, const CoriolisArgs& a, cudaStr
   return cudaGetLastError();
 }
 cudaError_t launch_ik_j32(const DModel* dm, const IkArgs& a, cudaStream_t s) {
-  ik_kernel<32><<<unsigned((a.n + 31) / 32), 32, 0, s>>>(dm, a);
+  static int occ = 0;
+  if (occ == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ik_kernel<32>, 32, 0) != cudaSuccess) occ = 1;
+  ik_kernel<32><<<balanced_grid(a.n, occ), 32, 0, s>>>(dm, a);
   return cudaGetLastError();
 }
 

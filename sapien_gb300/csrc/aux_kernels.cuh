@@ -184,15 +184,32 @@ __global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__
   }
 }
 
+#ifndef __CUDACC_RTC__
+// Grid for a grid-stride kernel of one-warp blocks: as few rounds as the resident capacity
+// (occupancy x SMs) allows, with the environments spread evenly over the rounds. Without
+// it, a batch slightly above one wave (65536 CLIK solves: 2048 warps for ~1800 resident)
+// runs a second, nearly empty wave at full per-warp latency.
+inline unsigned balanced_grid(int64_t n, int blocks_per_sm) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const int64_t blocks = (n + 31) / 32, cap = int64_t(sms) * (blocks_per_sm > 0 ? blocks_per_sm : 1);
+  const int64_t rounds = (blocks + cap - 1) / cap;
+  return unsigned(rounds > 0 ? (blocks + rounds - 1) / rounds : 1);
+}
+#endif
+
 // computeInverseKinematics (pinocchio_model.cpp:228-300): damped-least-squares CLIK on the
 // joint-frame log6 error. Loop: FK; iMd = oMi[j]^-1 oMdes; err = log6(iMd); keep the best
 // iterate; stop when |err| < eps (success) or after max_iter updates; J = joint-frame
 // Jacobian; J = -Jlog6(iMd^-1) J diag(mask); v = -J^T (J J^T + damp 1)^-1 err;
 // q = integrate(q, v dt). Returns posP2S(best q), success, best err.
 template <int MAXJ>
-__global__ void __launch_bounds__(32) ik_kernel(const DModel* __restrict__ model, const IkArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+__device__ __forceinline__ void ik_env(const DModel* __restrict__ model, const IkArgs& a, const int64_t e) {
   constexpr int MAXV = MAXJ + 5;
   const DJoint* __restrict__ JT = model_joints(model);
   const DLink& L = model_links(model)[a.link];
@@ -405,6 +422,12 @@ __global__ void __launch_bounds__(32) ik_kernel(const DModel* __restrict__ model
   stv(a.err, e, 3, bestErr.w.x);
   stv(a.err, e, 4, bestErr.w.y);
   stv(a.err, e, 5, bestErr.w.z);
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) ik_kernel(const DModel* __restrict__ model, const IkArgs a) {
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < a.n; e += int64_t(gridDim.x) * blockDim.x)
+    ik_env<MAXJ>(model, a, e);
 }
 
 }  // namespace sgdyn

@@ -6,7 +6,9 @@
 // start first and small ones fill in behind them.
 // Step (device): a persistent grid of warps pulls tile indices from a global counter with
 // atomicAdd until the queue is exhausted; each lane runs the fused sweep for one
-// environment with its own model's table. No warp ever waits on another, so there is no
+// environment with its own model's table, or, for a model given L lanes per environment,
+// each team of L lanes shares one environment (trunk + branches, see step_kernel.cuh) and
+// a tile holds 32 / L environments. No warp ever waits on another, so there is no
 // spin loop to bound. The counter is reset with cudaMemsetAsync on the same stream before
 // every launch, which keeps a step stream-ordered and capturable into a CUDA graph.
 #include <cuda_runtime.h>
@@ -33,8 +35,10 @@ int set_last_error(int code, const std::string& msg);
 struct HeteroArgs {
   const unsigned char* tables;
   const int64_t* table_offset;
+  const int* teams;             // team tables of the models run with L > 1
+  const int64_t* team_offset;   // per model (-1: one lane per environment)
   const int* perm;
-  const int4* tiles;  // (model, start, count, 0)
+  const int4* tiles;  // (model, start, count, lanes per environment)
   int ntiles;
   unsigned int* head;
   StepArgs io;
@@ -50,7 +54,16 @@ __global__ void hetero_kernel(const HeteroArgs a) {
     if (t >= unsigned(a.ntiles)) break;
     const int4 tile = a.tiles[t];
     const DModel* m = reinterpret_cast<const DModel*>(a.tables + a.table_offset[tile.x]);
-    if (lane < tile.z) step_env<MAXJ, OPS>(m, a.io, int64_t(a.perm[tile.y + lane]));
+    if (tile.w <= 1) {
+      if (lane < tile.z) step_env<MAXJ, OPS>(m, a.io, int64_t(a.perm[tile.y + lane]));
+    } else {
+      // every lane takes part (the team sums are warp shuffles); lanes of an empty tail
+      // slot repeat the tile's first environment and store nothing
+      const int slot = lane / tile.w;
+      const bool valid = slot < tile.z;
+      const TeamLanes tm{a.teams + a.team_offset[tile.x], lane % tile.w, valid};
+      step_env_t<MAXJ, OPS>(RuntimeTab{m}, a.io, int64_t(a.perm[tile.y + (valid ? slot : 0)]), tm);
+    }
     __syncwarp();
   }
 }
@@ -81,9 +94,12 @@ struct sgdyn_batch {
   int64_t n = 0;
   int max_nq = 0, max_nv = 0, max_nlinks = 0, max_nj = 0;
   std::vector<int> model_of_env;
+  std::vector<int> lanes;  // lanes per environment, per model
   // device
   unsigned char* tables = nullptr;
   int64_t* offsets = nullptr;
+  int* teams = nullptr;
+  int64_t* team_offsets = nullptr;
   int* perm = nullptr;
   int4* tiles = nullptr;
   int ntiles = 0;
@@ -99,6 +115,10 @@ namespace {
 void free_device(sgdyn_batch* b) {
   cudaFree(b->tables);
   cudaFree(b->offsets);
+  cudaFree(b->teams);
+  cudaFree(b->team_offsets);
+  b->teams = nullptr;
+  b->team_offsets = nullptr;
   cudaFree(b->perm);
   cudaFree(b->tiles);
   cudaFree(b->head);
@@ -122,25 +142,28 @@ int upload_plan(sgdyn_batch* b) {
   std::vector<int> perm;
   std::vector<int4> tiles;
   if (b->order == 0) {
-    for (int m : mo)
-      for (size_t s = 0; s < envs[m].size(); s += 32) {
-        int cnt = int(std::min<size_t>(32, envs[m].size() - s));
-        tiles.push_back(make_int4(m, int(perm.size()), cnt, 0));
+    for (int m : mo) {
+      const size_t per_tile = size_t(32 / b->lanes[m]);
+      for (size_t s = 0; s < envs[m].size(); s += per_tile) {
+        int cnt = int(std::min<size_t>(per_tile, envs[m].size() - s));
+        tiles.push_back(make_int4(m, int(perm.size()), cnt, b->lanes[m]));
         for (int k = 0; k < cnt; k++) perm.push_back(envs[m][s + k]);
       }
+    }
   } else {
     // input order: consecutive environments of the same model share a tile
     int64_t e = 0;
     while (e < b->n) {
       int m = b->model_of_env[e];
+      const int per_tile = 32 / b->lanes[m];
       int cnt = 0;
       int start = int(perm.size());
-      while (e < b->n && cnt < 32 && b->model_of_env[e] == m) {
+      while (e < b->n && cnt < per_tile && b->model_of_env[e] == m) {
         perm.push_back(int(e));
         e++;
         cnt++;
       }
-      tiles.push_back(make_int4(m, start, cnt, 0));
+      tiles.push_back(make_int4(m, start, cnt, b->lanes[m]));
     }
   }
   cudaFree(b->perm);
@@ -156,6 +179,104 @@ int upload_plan(sgdyn_batch* b) {
       cudaMemcpy(b->tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return SGDYN_ERR_CUDA;
   b->ntiles = int(tiles.size());
+  return SGDYN_OK;
+}
+
+// Team table for L lanes per environment (layout in step_kernel.cuh). The trunk starts
+// empty with the root subtrees as branches; the heaviest branch's root is moved into the
+// trunk (its children become branches) while that lowers trunk cost + the heaviest lane's
+// cost, lanes being filled longest-branch-first. Joint cost: 1, a free flyer 4.
+std::vector<int> build_team_table(const Model& M, int L) {
+  const auto* hdr = reinterpret_cast<const DModel*>(M.host_table().data());
+  const DJoint* J = model_joints(hdr);
+  const int nj = hdr->nj;
+  std::vector<std::vector<int>> kids(nj);
+  for (int j = 1; j < nj; j++) kids[J[j].parent].push_back(j);
+  std::vector<int> cost(nj, 0), sub(nj, 0);
+  for (int j = 1; j < nj; j++) cost[j] = J[j].nv == 6 ? 4 : 1;
+  for (int j = nj - 1; j >= 1; j--) {
+    sub[j] += cost[j];
+    if (J[j].parent > 0) sub[J[j].parent] += sub[j];
+  }
+  std::vector<int> trunk, branches = kids[0];
+  int trunk_cost = 0;
+  int best = 1 << 30;
+  std::vector<int> best_trunk, best_owner;
+  for (;;) {
+    std::vector<int> order = branches;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sub[x] > sub[y]; });
+    std::vector<int> load(L, 0), role_of(nj, -1);
+    for (int r : order) {
+      const int lane = int(std::min_element(load.begin(), load.end()) - load.begin());
+      load[lane] += sub[r];
+      role_of[r] = lane;
+    }
+    const int cp = trunk_cost + *std::max_element(load.begin(), load.end());
+    if (cp < best) {
+      best = cp;
+      best_trunk = trunk;
+      best_owner.assign(nj, -1);
+      for (int j = 1; j < nj; j++) {  // a branch joint belongs to its branch root's lane
+        int r = j;
+        while (r > 0 && role_of[r] < 0 && std::find(trunk.begin(), trunk.end(), r) == trunk.end()) r = J[r].parent;
+        if (r > 0 && role_of[r] >= 0) best_owner[j] = role_of[r];
+      }
+    }
+    if (branches.empty()) break;
+    const int h = *std::max_element(branches.begin(), branches.end(), [&](int x, int y) { return sub[x] < sub[y]; });
+    if (kids[h].empty()) break;
+    branches.erase(std::find(branches.begin(), branches.end(), h));
+    trunk.push_back(h);
+    trunk_cost += cost[h];
+    for (int c : kids[h]) branches.push_back(c);
+  }
+  std::sort(best_trunk.begin(), best_trunk.end());
+  std::vector<std::vector<int>> lanes(L);
+  for (int j = 1; j < nj; j++)
+    if (best_owner[j] >= 0) lanes[best_owner[j]].push_back(j);
+  size_t smax = 0;
+  for (auto& l : lanes) smax = std::max(smax, l.size());
+  std::vector<int> attach;
+  for (int t : best_trunk)
+    for (int c : kids[t])
+      if (best_owner[c] >= 0) {
+        attach.push_back(t);
+        break;
+      }
+  std::vector<int> tab = {L, int(best_trunk.size()), int(smax), int(attach.size())};
+  tab.insert(tab.end(), best_trunk.begin(), best_trunk.end());
+  for (auto& l : lanes) {
+    tab.insert(tab.end(), l.begin(), l.end());
+    tab.insert(tab.end(), smax - l.size(), 0);
+  }
+  tab.insert(tab.end(), attach.begin(), attach.end());
+  tab.insert(tab.end(), best_owner.begin(), best_owner.end());
+  return tab;
+}
+
+int upload_teams(sgdyn_batch* b) {
+  std::vector<int> all;
+  std::vector<int64_t> offs;
+  for (size_t m = 0; m < b->models.size(); m++) {
+    if (b->lanes[m] <= 1) {
+      offs.push_back(-1);
+      continue;
+    }
+    offs.push_back(int64_t(all.size()));
+    const auto t = build_team_table(*b->models[m]->impl, b->lanes[m]);
+    all.insert(all.end(), t.begin(), t.end());
+  }
+  cudaFree(b->teams);
+  cudaFree(b->team_offsets);
+  b->teams = nullptr;
+  b->team_offsets = nullptr;
+  if (cudaMalloc(&b->teams, sizeof(int) * std::max<size_t>(all.size(), 1)) != cudaSuccess ||
+      cudaMalloc(&b->team_offsets, sizeof(int64_t) * offs.size()) != cudaSuccess)
+    return SGDYN_ERR_CUDA;
+  if (!all.empty() && cudaMemcpy(b->teams, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return SGDYN_ERR_CUDA;
+  if (cudaMemcpy(b->team_offsets, offs.data(), sizeof(int64_t) * offs.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return SGDYN_ERR_CUDA;
   return SGDYN_OK;
 }
 
@@ -201,6 +322,7 @@ int sgdyn_batch_create(const sgdyn_model* const* models, int nmodels, const int*
     b->max_nj = std::max(b->max_nj, M.njoints());
   }
   b->model_of_env.assign(model_of_env, model_of_env + n);
+  b->lanes.assign(b->models.size(), 1);
   for (int m : b->model_of_env)
     if (m < 0 || m >= nmodels) {
       delete b;
@@ -222,7 +344,7 @@ int sgdyn_batch_create(const sgdyn_model* const* models, int nmodels, const int*
       cudaMalloc(&b->head, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemcpy(b->tables, packed.data(), packed.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->offsets, offs.data(), sizeof(int64_t) * offs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-      upload_plan(b) != SGDYN_OK) {
+      upload_teams(b) != SGDYN_OK || upload_plan(b) != SGDYN_OK) {
     free_device(b);
     delete b;
     return set_last_error(SGDYN_ERR_CUDA, "batch upload failed");
@@ -259,6 +381,18 @@ int sgdyn_batch_set_launch(sgdyn_batch* b, int ctas_per_sm, int warps_per_cta, i
   return SGDYN_OK;
 }
 
+int sgdyn_batch_set_lanes(sgdyn_batch* b, const int* lanes_per_model) {
+  if (!b || !lanes_per_model) return set_last_error(SGDYN_ERR_NULL, "null argument");
+  for (size_t m = 0; m < b->models.size(); m++) {
+    const int L = lanes_per_model[m];
+    if (L != 1 && L != 2 && L != 4 && L != 8) return set_last_error(SGDYN_ERR_RUNTIME, "lanes must be 1, 2, 4 or 8");
+  }
+  b->lanes.assign(lanes_per_model, lanes_per_model + b->models.size());
+  if (upload_teams(b) != SGDYN_OK || upload_plan(b) != SGDYN_OK)
+    return set_last_error(SGDYN_ERR_CUDA, "team / plan upload failed");
+  return SGDYN_OK;
+}
+
 int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
                      double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream) {
   if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
@@ -274,6 +408,8 @@ int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd,
   HeteroArgs a;
   a.tables = b->tables;
   a.table_offset = b->offsets;
+  a.teams = b->teams;
+  a.team_offset = b->team_offsets;
   a.perm = b->perm;
   a.tiles = b->tiles;
   a.ntiles = b->ntiles;

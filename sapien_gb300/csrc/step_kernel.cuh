@@ -179,14 +179,55 @@ __device__ __forceinline__ void chol6_solve(const double* L, double* b) {
 #undef LI
 }
 
+// Several lanes per environment ("team"): L consecutive lanes of a warp share one
+// environment. The tree is split into a trunk (a root-connected set of joints that every
+// lane of the team computes, identically) and branches (whole subtrees hanging off the
+// trunk), each branch owned by one lane. Pass 1 runs the trunk, then each lane its own
+// branches side by side; pass 2 runs the branches, sums what they pass up to the trunk
+// joints they hang from with a butterfly of warp shuffles (every lane ends with the same
+// bits), then runs the trunk; pass 3 runs the trunk, then the branches. The critical path
+// per step shrinks from all joints to trunk + heaviest lane. Results are written by a
+// joint's owner: the branch's lane, or role 0 for trunk joints.
+//
+// Team table (ints, per model and L, built on the host):
+//   [0] L  [1] ntrunk  [2] smax (longest lane list)  [3] nattach
+//   trunk joints [ntrunk] in depth-first order
+//   per role, smax joints in depth-first order (0 = idle step)
+//   attach joints [nattach]: trunk joints with a child on a branch
+//   owner [nj]: -1 for trunk joints, else the owning role
+struct NoTeam {
+  static constexpr bool kOn = false;
+};
+struct TeamLanes {
+  static constexpr bool kOn = true;
+  const int* t;
+  int role;
+  bool valid;  // false for the lanes of an empty tail slot: they compute but store nothing
+  __device__ __forceinline__ int L() const { return t[0]; }
+  __device__ __forceinline__ int ntrunk() const { return t[1]; }
+  __device__ __forceinline__ int smax() const { return t[2]; }
+  __device__ __forceinline__ int nattach() const { return t[3]; }
+  __device__ __forceinline__ int trunk(int k) const { return t[4 + k]; }
+  __device__ __forceinline__ int sched(int k) const { return t[4 + ntrunk() + role * smax() + k]; }
+  __device__ __forceinline__ int attach(int k) const { return t[4 + ntrunk() + L() * smax() + k]; }
+  __device__ __forceinline__ int owner(int j) const { return t[4 + ntrunk() + L() * smax() + nattach() + j]; }
+};
+
+// Sum over the L lanes of a team (L a power of two, teams aligned in the warp).
+__device__ __forceinline__ double team_sum(double v, int L) {
+  for (int m = 1; m < L; m <<= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+  return v;
+}
+
 // The whole fused sweep for environment e (rows of the StepArgs arrays).
-template <int MAXJ, int OPS, class Tab>
-__device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, const int64_t e) {
+template <int MAXJ, int OPS, class Tab, class Team = NoTeam>
+__device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const Team& tm = Team{}) {
   constexpr int MAXV = MAXJ + 5;
   constexpr bool kFK = OPS & OP_FK, kJAC = OPS & OP_JAC, kCRBA = OPS & OP_CRBA, kRNEA = OPS & OP_RNEA,
                  kABA = OPS & OP_ABA;
   constexpr bool kVel = kRNEA || kABA;
   constexpr bool kInertia = kCRBA || kRNEA || kABA;
+  constexpr bool kTeam = Team::kOn;
   const int nj = T.nj();
 
   M3 oR[MAXJ];
@@ -198,7 +239,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
   // Pass 2 rebuilds each joint's composite (CRBA) and articulated (ABA) inertia as its own
   // body inertia Yb plus what its children passed up (CC, AC). The last child in
   // depth-first order is processed first and initialises its parent's slot, so no slot is
-  // zero-filled and only joints with children carry one.
+  // zero-filled and only joints with children carry one (teams zero their trunk's slots).
   RBI Yb[(kCRBA || kABA) ? MAXJ : 1];
   RBI CC[kCRBA ? MAXJ : 1];
   Sym6 AC[kABA ? MAXJ : 1];
@@ -226,10 +267,18 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
   }
   const Arr qa{qin, 0, 1};
 
+  // whether this lane writes joint i's results
+  auto writes = [&](int i) -> bool {
+    if constexpr (kTeam) return tm.valid && (tm.owner(i) < 0 ? tm.role == 0 : tm.owner(i) == tm.role);
+    else return true;
+  };
+  auto in_trunk = [&](int i) -> bool {
+    if constexpr (kTeam) return i > 0 && tm.owner(i) < 0;
+    else return false;
+  };
 
   // ---------------- pass 1: root to leaves ----------------
-#pragma unroll
-  for (int i = 1; i < nj; i++) {
+  auto pass1 = [&](int i) {
     const DJoint& J = T.joint(i);
     const int p = J.parent;
     M3 Ro;
@@ -240,15 +289,17 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
     const int nvi = J.nv, iv = J.ivx, vc = J.vcol;
     for (int k = 0; k < nvi; k++) Sw[iv + k] = world_S(J, Ro, po, k);
     if constexpr (kJAC) {
-      const int nv = T.nv();
-      for (int k = 0; k < nvi; k++) {
-        const Mot S = Sw[iv + k];
-        stv(args.J, e, 0 * nv + vc + k, S.v.x);
-        stv(args.J, e, 1 * nv + vc + k, S.v.y);
-        stv(args.J, e, 2 * nv + vc + k, S.v.z);
-        stv(args.J, e, 3 * nv + vc + k, S.w.x);
-        stv(args.J, e, 4 * nv + vc + k, S.w.y);
-        stv(args.J, e, 5 * nv + vc + k, S.w.z);
+      if (writes(i)) {
+        const int nv = T.nv();
+        for (int k = 0; k < nvi; k++) {
+          const Mot S = Sw[iv + k];
+          stv(args.J, e, 0 * nv + vc + k, S.v.x);
+          stv(args.J, e, 1 * nv + vc + k, S.v.y);
+          stv(args.J, e, 2 * nv + vc + k, S.v.z);
+          stv(args.J, e, 3 * nv + vc + k, S.w.x);
+          stv(args.J, e, 4 * nv + vc + k, S.w.y);
+          stv(args.J, e, 5 * nv + vc + k, S.w.z);
+        }
       }
     }
     if constexpr (kInertia) {
@@ -280,62 +331,27 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
         }
       }
     }
-  }
+  };
 
-  if constexpr (kFK) {
-    const int nl = T.nlinks();
-#pragma unroll
-    for (int l = 0; l < nl; l++) {
-      const DLink& L = T.link(l);
-      const int j = L.joint;
-      M3 R;
-      V3 pp;
-      M3 Rl;
-#pragma unroll
-      for (int k = 0; k < 9; k++) Rl.a[k] = L.R[k];
-      const V3 pl = mk(L.p[0], L.p[1], L.p[2]);
-      if (j == 0) {
-        R = Rl;
-        pp = pl;
-      } else {
-        R = (L.flags & JF_ROT_IDENTITY) ? oR[j] : mul(oR[j], Rl);
-        pp = mul_add(oR[j], pl, op[j]);
-      }
-      double qt[4];
-      R_to_quat(R, qt);
-      stv(args.poses, e, l * 7 + 0, pp.x);
-      stv(args.poses, e, l * 7 + 1, pp.y);
-      stv(args.poses, e, l * 7 + 2, pp.z);
-      stv(args.poses, e, l * 7 + 3, qt[0]);
-      stv(args.poses, e, l * 7 + 4, qt[1]);
-      stv(args.poses, e, l * 7 + 5, qt[2]);
-      stv(args.poses, e, l * 7 + 6, qt[3]);
-    }
-  }
-
-  if constexpr (kABA) {
-    const int nv = T.nv();
-#pragma unroll
-    for (int c = 0; c < nv; c++) tauin[c] = ldv(args.tau, e, c);
-  }
-
-  if constexpr (kCRBA || kRNEA || kABA) {
-    // ---------------- pass 2: leaves to root ----------------
-#pragma unroll
-    for (int i = nj - 1; i >= 1; i--) {
-      const DJoint& J = T.joint(i);
-      const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
-      const bool has_children = J.subtree_end > i + 1;
-      // the last child of p in depth-first order ends where p's subtree ends
-      const bool first_of_parent = p > 0 && J.subtree_end == T.joint(p).subtree_end;
-      if constexpr (kRNEA) {
-        const Mot f = frc[i];
+  // ---------------- pass 2: leaves to root ----------------
+  auto pass2 = [&](int i) {
+    const DJoint& J = T.joint(i);
+    const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
+    // a team's trunk joints always carry (zeroed) slots; elsewhere only joints with children
+    const bool has_children = in_trunk(i) || J.subtree_end > i + 1;
+    // the last child of p in depth-first order ends where p's subtree ends
+    const bool first_of_parent = p > 0 && !in_trunk(p) && J.subtree_end == T.joint(p).subtree_end;
+    const bool out = writes(i);
+    if constexpr (kRNEA) {
+      const Mot f = frc[i];
+      if (out)
         for (int k = 0; k < nvi; k++) stv(args.tau_out, e, vc + k, dot6(Sw[iv + k], f));
-        if (p > 0) frc[p] = add6(frc[p], f);
-      }
-      if constexpr (kCRBA) {
-        const int nv = T.nv();
-        const RBI Y = has_children ? rbi_add(Yb[i], CC[i]) : Yb[i];
+      if (p > 0) frc[p] = add6(frc[p], f);
+    }
+    if constexpr (kCRBA) {
+      const int nv = T.nv();
+      const RBI Y = has_children ? rbi_add(Yb[i], CC[i]) : Yb[i];
+      if (out) {
         for (int k = 0; k < nvi; k++) {
           const Mot F = rbi_mul(Y, Sw[iv + k]);
           for (int l = 0; l <= k; l++) {  // own block, upper triangle mirrored
@@ -364,114 +380,239 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
               stv(args.M, e, (vc + k) * nv + jc + l, 0.0);
             }
         }
-        if (p > 0) CC[p] = first_of_parent ? Y : rbi_add(CC[p], Y);
       }
-      if constexpr (kABA) {
-        const Sym6 IAi = has_children ? sym6_rbi_add(Yb[i], AC[i]) : sym6_from_rbi(Yb[i]);
-        if (nvi == 1) {
-          const Mot S = Sw[iv];
-          const Mot U = sym6_mul(IAi, S);
-          const double D = dot6(S, U);
-          const double di = 1.0 / D;
-          const double u = tauin[vc] - dot6(S, pA[i]);
-          Uv[iv] = U;
-          uv[iv] = u;
-          Dinv[i] = di;
-          if (p > 0) {
-            const Mot Ud = scale6(di, U);
-            Sym6 Ia = IAi;
-            const double ud[6] = {Ud.v.x, Ud.v.y, Ud.v.z, Ud.w.x, Ud.w.y, Ud.w.z};
-            const double uu[6] = {U.v.x, U.v.y, U.v.z, U.w.x, U.w.y, U.w.z};
-            // A -= ud_lin u_lin^T (sym), B -= ud_lin u_ang^T, C -= ud_ang u_ang^T (sym)
+      if (p > 0) CC[p] = first_of_parent ? Y : rbi_add(CC[p], Y);
+    }
+    if constexpr (kABA) {
+      const Sym6 IAi = has_children ? sym6_rbi_add(Yb[i], AC[i]) : sym6_from_rbi(Yb[i]);
+      if (nvi == 1) {
+        const Mot S = Sw[iv];
+        const Mot U = sym6_mul(IAi, S);
+        const double D = dot6(S, U);
+        const double di = 1.0 / D;
+        const double u = tauin[vc] - dot6(S, pA[i]);
+        Uv[iv] = U;
+        uv[iv] = u;
+        Dinv[i] = di;
+        if (p > 0) {
+          const Mot Ud = scale6(di, U);
+          Sym6 Ia = IAi;
+          const double ud[6] = {Ud.v.x, Ud.v.y, Ud.v.z, Ud.w.x, Ud.w.y, Ud.w.z};
+          const double uu[6] = {U.v.x, U.v.y, U.v.z, U.w.x, U.w.y, U.w.z};
+          // A -= ud_lin u_lin^T (sym), B -= ud_lin u_ang^T, C -= ud_ang u_ang^T (sym)
+          int t = 0;
+#pragma unroll
+          for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = r; c < 3; c++, t++) {
+              Ia.A[t] = fma(-ud[r], uu[c], Ia.A[t]);
+              Ia.C[t] = fma(-ud[3 + r], uu[3 + c], Ia.C[t]);
+            }
+#pragma unroll
+          for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) Ia.B[r * 3 + c] = fma(-ud[r], uu[3 + c], Ia.B[r * 3 + c]);
+          Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
+          pa = axpy6(u, Ud, pa);
+          if (first_of_parent) AC[p] = Ia;
+          else sym6_acc(AC[p], Ia);
+          pA[p] = add6(pA[p], pa);
+        }
+      } else {
+        // free flyer: 6x6 D = S^T IA S, Cholesky-factored
+        for (int k = 0; k < 6; k++) {
+          Uv[iv + k] = sym6_mul(IAi, Sw[iv + k]);
+          uv[iv + k] = tauin[vc + k] - dot6(Sw[iv + k], pA[i]);
+        }
+        for (int r = 0; r < 6; r++)
+          for (int c = 0; c <= r; c++) Lff[r * (r + 1) / 2 + c] = dot6(Sw[iv + r], Uv[iv + c]);
+        chol6(Lff);
+        if (p > 0) {
+          // Ia = IA - U D^-1 U^T ; pa = pA + Ia c + U D^-1 u, with D^-1 applied by solves
+          Sym6 Ia = IAi;
+          double W[6][6];  // W[:, k] = D^-1 e_k
+          for (int k = 0; k < 6; k++) {
+            for (int r = 0; r < 6; r++) W[r][k] = (r == k) ? 1.0 : 0.0;
+            double col[6];
+            for (int r = 0; r < 6; r++) col[r] = W[r][k];
+            chol6_solve(Lff, col);
+            for (int r = 0; r < 6; r++) W[r][k] = col[r];
+          }
+          Mot UD[6];
+          for (int k = 0; k < 6; k++) {
+            Mot s{mk(0, 0, 0), mk(0, 0, 0)};
+            for (int l = 0; l < 6; l++) s = axpy6(W[l][k], Uv[iv + l], s);
+            UD[k] = s;
+          }
+          for (int k = 0; k < 6; k++) {
+            const Mot a = UD[k], b = Uv[iv + k];
+            const double ud[6] = {a.v.x, a.v.y, a.v.z, a.w.x, a.w.y, a.w.z};
+            const double uu[6] = {b.v.x, b.v.y, b.v.z, b.w.x, b.w.y, b.w.z};
             int t = 0;
-#pragma unroll
             for (int r = 0; r < 3; r++)
-#pragma unroll
               for (int c = r; c < 3; c++, t++) {
                 Ia.A[t] = fma(-ud[r], uu[c], Ia.A[t]);
                 Ia.C[t] = fma(-ud[3 + r], uu[3 + c], Ia.C[t]);
               }
-#pragma unroll
             for (int r = 0; r < 3; r++)
-#pragma unroll
               for (int c = 0; c < 3; c++) Ia.B[r * 3 + c] = fma(-ud[r], uu[3 + c], Ia.B[r * 3 + c]);
-            Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
-            pa = axpy6(u, Ud, pa);
-            if (first_of_parent) AC[p] = Ia;
-            else sym6_acc(AC[p], Ia);
-            pA[p] = add6(pA[p], pa);
           }
-        } else {
-          // free flyer: 6x6 D = S^T IA S, Cholesky-factored
-          for (int k = 0; k < 6; k++) {
-            Uv[iv + k] = sym6_mul(IAi, Sw[iv + k]);
-            uv[iv + k] = tauin[vc + k] - dot6(Sw[iv + k], pA[i]);
-          }
-          for (int r = 0; r < 6; r++)
-            for (int c = 0; c <= r; c++) Lff[r * (r + 1) / 2 + c] = dot6(Sw[iv + r], Uv[iv + c]);
-          chol6(Lff);
-          if (p > 0) {
-            // Ia = IA - U D^-1 U^T ; pa = pA + Ia c + U D^-1 u, with D^-1 applied by solves
-            Sym6 Ia = IAi;
-            double W[6][6];  // W[:, k] = D^-1 e_k
-            for (int k = 0; k < 6; k++) {
-              for (int r = 0; r < 6; r++) W[r][k] = (r == k) ? 1.0 : 0.0;
-              double col[6];
-              for (int r = 0; r < 6; r++) col[r] = W[r][k];
-              chol6_solve(Lff, col);
-              for (int r = 0; r < 6; r++) W[r][k] = col[r];
-            }
-            Mot UD[6];
-            for (int k = 0; k < 6; k++) {
-              Mot s{mk(0, 0, 0), mk(0, 0, 0)};
-              for (int l = 0; l < 6; l++) s = axpy6(W[l][k], Uv[iv + l], s);
-              UD[k] = s;
-            }
-            for (int k = 0; k < 6; k++) {
-              const Mot a = UD[k], b = Uv[iv + k];
-              const double ud[6] = {a.v.x, a.v.y, a.v.z, a.w.x, a.w.y, a.w.z};
-              const double uu[6] = {b.v.x, b.v.y, b.v.z, b.w.x, b.w.y, b.w.z};
-              int t = 0;
-              for (int r = 0; r < 3; r++)
-                for (int c = r; c < 3; c++, t++) {
-                  Ia.A[t] = fma(-ud[r], uu[c], Ia.A[t]);
-                  Ia.C[t] = fma(-ud[3 + r], uu[3 + c], Ia.C[t]);
-                }
-              for (int r = 0; r < 3; r++)
-                for (int c = 0; c < 3; c++) Ia.B[r * 3 + c] = fma(-ud[r], uu[3 + c], Ia.B[r * 3 + c]);
-            }
-            Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
-            for (int k = 0; k < 6; k++) pa = axpy6(uv[iv + k], UD[k], pa);
-            if (first_of_parent) AC[p] = Ia;
-            else sym6_acc(AC[p], Ia);
-            pA[p] = add6(pA[p], pa);
-          }
+          Mot pa = sym6_mul_add(Ia, cb[i], pA[i]);
+          for (int k = 0; k < 6; k++) pa = axpy6(uv[iv + k], UD[k], pa);
+          if (first_of_parent) AC[p] = Ia;
+          else sym6_acc(AC[p], Ia);
+          pA[p] = add6(pA[p], pa);
         }
       }
     }
-  }
+  };
 
-  if constexpr (kABA) {
-    // ---------------- pass 3: root to leaves ----------------
+  // ---------------- pass 3: root to leaves ----------------
+  auto pass3 = [&](int i) {
+    const DJoint& J = T.joint(i);
+    const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
+    const bool out = writes(i);
+    Mot a = add6((p == 0) ? a0 : acc[p], cb[i]);
+    if (nvi == 1) {
+      const double qdd = Dinv[i] * (uv[iv] - dot6(Uv[iv], a));
+      a = axpy6(qdd, Sw[iv], a);
+      if (out) stv(args.qdd_out, e, vc, qdd);
+    } else {
+      double b[6];
+      for (int k = 0; k < 6; k++) b[k] = uv[iv + k] - dot6(Uv[iv + k], a);
+      chol6_solve(Lff, b);
+      for (int k = 0; k < 6; k++) {
+        a = axpy6(b[k], Sw[iv + k], a);
+        if (out) stv(args.qdd_out, e, vc + k, b[k]);
+      }
+    }
+    acc[i] = a;
+  };
+
+  auto link_poses = [&]() {
+    const int nl = T.nlinks();
 #pragma unroll
-    for (int i = 1; i < nj; i++) {
-      const DJoint& J = T.joint(i);
-      const int p = J.parent, nvi = J.nv, iv = J.ivx, vc = J.vcol;
-      Mot a = add6((p == 0) ? a0 : acc[p], cb[i]);
-      if (nvi == 1) {
-        const double qdd = Dinv[i] * (uv[iv] - dot6(Uv[iv], a));
-        a = axpy6(qdd, Sw[iv], a);
-        stv(args.qdd_out, e, vc, qdd);
+    for (int l = 0; l < nl; l++) {
+      const DLink& L = T.link(l);
+      const int j = L.joint;
+      if constexpr (kTeam) {
+        if (!writes(j)) continue;  // another lane holds this joint's pose
+      }
+      M3 R;
+      V3 pp;
+      M3 Rl;
+#pragma unroll
+      for (int k = 0; k < 9; k++) Rl.a[k] = L.R[k];
+      const V3 pl = mk(L.p[0], L.p[1], L.p[2]);
+      if (j == 0) {
+        R = Rl;
+        pp = pl;
       } else {
-        double b[6];
-        for (int k = 0; k < 6; k++) b[k] = uv[iv + k] - dot6(Uv[iv + k], a);
-        chol6_solve(Lff, b);
-        for (int k = 0; k < 6; k++) {
-          a = axpy6(b[k], Sw[iv + k], a);
-          stv(args.qdd_out, e, vc + k, b[k]);
+        R = (L.flags & JF_ROT_IDENTITY) ? oR[j] : mul(oR[j], Rl);
+        pp = mul_add(oR[j], pl, op[j]);
+      }
+      double qt[4];
+      R_to_quat(R, qt);
+      stv(args.poses, e, l * 7 + 0, pp.x);
+      stv(args.poses, e, l * 7 + 1, pp.y);
+      stv(args.poses, e, l * 7 + 2, pp.z);
+      stv(args.poses, e, l * 7 + 3, qt[0]);
+      stv(args.poses, e, l * 7 + 4, qt[1]);
+      stv(args.poses, e, l * 7 + 5, qt[2]);
+      stv(args.poses, e, l * 7 + 6, qt[3]);
+    }
+  };
+
+  auto load_tau = [&]() {
+    if constexpr (kABA) {
+      const int nv = T.nv();
+#pragma unroll
+      for (int c = 0; c < nv; c++) tauin[c] = ldv(args.tau, e, c);
+    }
+  };
+
+  if constexpr (!kTeam) {
+#pragma unroll
+    for (int i = 1; i < nj; i++) pass1(i);
+    if constexpr (kFK) link_poses();
+    load_tau();
+    if constexpr (kCRBA || kRNEA || kABA) {
+#pragma unroll
+      for (int i = nj - 1; i >= 1; i--) pass2(i);
+    }
+    if constexpr (kABA) {
+#pragma unroll
+      for (int i = 1; i < nj; i++) pass3(i);
+    }
+  } else {
+    const int nt = tm.ntrunk(), sm = tm.smax(), na = tm.nattach(), L = tm.L();
+    for (int k = 0; k < nt; k++) pass1(tm.trunk(k));
+    for (int k = 0; k < sm; k++) {
+      const int j = tm.sched(k);
+      if (j > 0) pass1(j);
+    }
+    if constexpr (kFK) link_poses();
+    load_tau();
+    if constexpr (kCRBA || kRNEA || kABA) {
+      // trunk slots start at zero; attach joints keep their own force / bias aside so that
+      // the branch contributions alone are summed across the team
+      Mot fbase[kRNEA ? MAXJ : 1], pbase[kABA ? MAXJ : 1];
+      for (int k = 0; k < nt; k++) {
+        const int t = tm.trunk(k);
+        if constexpr (kCRBA) CC[t] = RBI{0.0, mk(0, 0, 0), {0, 0, 0, 0, 0, 0}};
+        if constexpr (kABA) AC[t] = Sym6{{0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}};
+      }
+      const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+      for (int k = 0; k < na; k++) {
+        const int t = tm.attach(k);
+        if constexpr (kRNEA) {
+          fbase[t] = frc[t];
+          frc[t] = zero;
+        }
+        if constexpr (kABA) {
+          pbase[t] = pA[t];
+          pA[t] = zero;
         }
       }
-      acc[i] = a;
+      for (int k = sm - 1; k >= 0; k--) {
+        const int j = tm.sched(k);
+        if (j > 0) pass2(j);
+      }
+      auto sum6 = [&](Mot& m) {
+        m.v.x = team_sum(m.v.x, L); m.v.y = team_sum(m.v.y, L); m.v.z = team_sum(m.v.z, L);
+        m.w.x = team_sum(m.w.x, L); m.w.y = team_sum(m.w.y, L); m.w.z = team_sum(m.w.z, L);
+      };
+      for (int k = 0; k < na; k++) {
+        const int t = tm.attach(k);
+        if constexpr (kRNEA) {
+          sum6(frc[t]);
+          frc[t] = add6(fbase[t], frc[t]);
+        }
+        if constexpr (kCRBA) {
+          RBI& c = CC[t];
+          c.m = team_sum(c.m, L);
+          c.h.x = team_sum(c.h.x, L); c.h.y = team_sum(c.h.y, L); c.h.z = team_sum(c.h.z, L);
+          for (int q = 0; q < 6; q++) c.I[q] = team_sum(c.I[q], L);
+        }
+        if constexpr (kABA) {
+          Sym6& s = AC[t];
+          for (int q = 0; q < 6; q++) {
+            s.A[q] = team_sum(s.A[q], L);
+            s.C[q] = team_sum(s.C[q], L);
+          }
+          for (int q = 0; q < 9; q++) s.B[q] = team_sum(s.B[q], L);
+          sum6(pA[t]);
+          pA[t] = add6(pbase[t], pA[t]);
+        }
+      }
+      for (int k = nt - 1; k >= 0; k--) pass2(tm.trunk(k));
+    }
+    if constexpr (kABA) {
+      for (int k = 0; k < nt; k++) pass3(tm.trunk(k));
+      for (int k = 0; k < sm; k++) {
+        const int j = tm.sched(k);
+        if (j > 0) pass3(j);
+      }
     }
   }
 }

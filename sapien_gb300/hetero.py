@@ -6,10 +6,11 @@
     graph = batch.capture(q, qd, qdd, tau, steps=10)                 # CUDA graph of 10 steps
     graph.replay()
 
-Environments are grouped per model into warps (tiles of 32) and the tiles are ordered by
-descending velocity dimension; a persistent grid pulls tiles from an atomic counter (see
-csrc/hetero.cu). The launch shape (persistent CTAs per SM, warps per CTA, tile order)
-is chosen by ``sapien_gb300.autotune.tune_batch``.
+Environments are grouped per model into warps (tiles of 32 / L environments for a model
+run with L lanes per environment) and the tiles are ordered by descending velocity
+dimension; a persistent grid pulls tiles from an atomic counter (see csrc/hetero.cu). The
+launch shape (persistent CTAs per SM, warps per CTA, tile order) and the lanes per
+environment of each model are chosen by ``sapien_gb300.autotune.tune_batch``.
 """
 from __future__ import annotations
 
@@ -47,6 +48,7 @@ class HeteroBatch:
         N.check(L.sgdyn_batch_info(h, ctypes.byref(n64), ctypes.byref(nq), ctypes.byref(nv), ctypes.byref(nl)))
         self.max_nq, self.max_nv, self.max_nlinks = nq.value, nv.value, nl.value
         self.launch = (4, 1, 0)
+        self.lanes = tuple([1] * len(self.models))
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -60,6 +62,18 @@ class HeteroBatch:
     def set_launch(self, ctas_per_sm, warps_per_cta, order):
         N.check(N.load().sgdyn_batch_set_launch(self._h, int(ctas_per_sm), int(warps_per_cta), int(order)))
         self.launch = (int(ctas_per_sm), int(warps_per_cta), int(order))
+
+    def set_lanes(self, lanes_per_model):
+        """Threads per environment for each model (1, 2, 4 or 8): with L > 1, L lanes share an
+        environment, the root joints on all of them and the subtrees off them split among
+        them, which shortens a wide tree's sequential sweep."""
+        lanes = [int(x) for x in lanes_per_model]
+        if len(lanes) != len(self.models):
+            raise RuntimeError(f"expected {len(self.models)} lane counts")
+        arr = (ctypes.c_int * len(lanes))(*lanes)
+        with torch.cuda.device(self.device):
+            N.check(N.load().sgdyn_batch_set_lanes(self._h, arr))
+        self.lanes = tuple(lanes)
 
     # -- padding helpers ------------------------------------------------------------
     def _pad(self, per_model, width, attr):

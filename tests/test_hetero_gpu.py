@@ -86,10 +86,53 @@ def test_autotuner_picks_a_shape_and_keeps_results(tmp_path, monkeypatch):
     monkeypatch.setenv("SGDYN_AUTOTUNE_CACHE", str(tmp_path))
     batch, oracles, inputs, (q, qd, qdd, tau) = setup(n=160, seed=4)
     ref = [v.clone() for v in valid_blocks(batch, batch.step(q, qd, qdd, tau))]
-    shape, table = autotune.tune_batch(batch, q, qd, qdd, tau, OPS_DYNAMICS, candidates=[(1, 1, 0), (4, 1, 0), (2, 2, 1)])
-    assert len(table) == 3 and tuple(shape) in {(1, 1, 0), (4, 1, 0), (2, 2, 1)}
-    shape2, _ = autotune.tune_batch(batch, q, qd, qdd, tau, OPS_DYNAMICS)  # served from the cache
+    cands = [(1, 1, 0), (4, 1, 0), (2, 2, 1)]
+    shape, table = autotune.tune_batch(batch, q, qd, qdd, tau, OPS_DYNAMICS, candidates=cands, lane_candidates=(1,))
+    assert len(table) == 3 and tuple(shape) in set(cands)
+    shape2, _ = autotune.tune_batch(batch, q, qd, qdd, tau, OPS_DYNAMICS, lane_candidates=(1,))  # from the cache
     assert tuple(shape2) == tuple(shape)
     out = batch.step(q, qd, qdd, tau)
     for a, b in zip(valid_blocks(batch, out), ref):
         assert torch.equal(a, b)
+    # with lanes per environment in the search: a valid choice, results equal to rounding
+    shape3, table3 = autotune.tune_batch(batch, q, qd, qdd, tau, OPS_DYNAMICS, candidates=cands)
+    assert all(L in (1, 2, 4, 8) for L in batch.lanes) and len(table3) == 3 + 3 * 3 * len(batch.models)
+    lanes = list(batch.lanes)
+    batch.set_lanes([1] * len(batch.models))
+    batch.set_lanes(lanes)
+    out = batch.step(q, qd, qdd, tau)
+    for a, b in zip(valid_blocks(batch, out), ref):
+        assert rel_per_env(a.cpu().numpy(), b.cpu().numpy()) <= 1e-11
+
+
+def test_lanes_per_environment_agree_with_one_lane():
+    """Teams of 2, 4 or 8 lanes per environment (trunk on every lane, subtrees split among
+    them, branch contributions summed with warp shuffles) give the one-lane results to
+    rounding, write every output entry exactly where one lane does, and match the oracle."""
+    import torch
+
+    from sapien_gb300 import _native as N
+
+    batch, oracles, inputs, (q, qd, qdd, tau) = setup(n=333, seed=5)
+
+    def run(lanes):
+        batch.set_lanes(lanes)
+        out = batch.alloc_outputs(N.OP_ALL)
+        for v in out.values():
+            v.fill_(float("nan"))
+        batch.step(q, qd, qdd, tau, N.OP_ALL, out)
+        torch.cuda.synchronize()
+        blocks = []
+        for k, m in enumerate(batch.models):
+            idx = torch.as_tensor(np.nonzero(batch.model_of_env == k)[0], device=q.device)
+            blocks += [out["qf"][idx, : m.nv], out["qacc"][idx, : m.nv], out["mass_matrix"][idx, : m.nv * m.nv],
+                       out["jacobian"][idx, : 6 * m.nv], out["link_poses"][idx, : 7 * m._nlinks]]
+        return [b.cpu().numpy() for b in blocks], out
+
+    ref, _ = run([1, 1, 1])
+    for lanes in ([1, 4, 4], [2, 2, 2], [8, 8, 8], [4, 8, 2]):
+        got, out = run(lanes)
+        for a, b in zip(got, ref):
+            assert not np.isnan(a).any(), lanes
+            assert rel_per_env(a, b) <= 1e-11, lanes
+    check_against_oracle(batch, oracles, inputs, out)
