@@ -4,6 +4,7 @@
 // names -> SGDYN_ERR_INVALID_ARGUMENT, std::runtime_error -> SGDYN_ERR_RUNTIME.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -551,6 +552,16 @@ static int derivatives(bool aba, const sgdyn_model* m, int64_t n, const double* 
     const int64_t nv = Mo.nv();
     DerivArgs a;
     a.n = n;
+    // Rows of the derivative matrices are independent given the forward sweep: split them
+    // over enough threads to give every FP64 scheduler about two warps (a warp's FP64
+    // issue, not the GPU's, bounds a small batch), each thread recomputing the forward sweep.
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want_warps = int64_t(sms > 0 ? sms : 1) * 4 * 2, warps = (n + 31) / 32;
+    const int64_t g = std::min<int64_t>(nv, std::max<int64_t>(1, (want_warps + warps - 1) / warps));
+    a.rows = int((nv + g - 1) / g);
+    a.groups = int((nv + a.rows - 1) / a.rows);
     a.q = make_arr(q, n, Mo.nq_ext(), layout);
     a.qd = make_arr(qd, n, nv, layout);
     a.x = make_arr(x, n, nv, layout);

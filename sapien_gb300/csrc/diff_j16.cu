@@ -11,12 +11,18 @@ namespace sgdyn {
 SG_LAUNCH(rnea_vjp, VjpArgs)
 SG_LAUNCH(aba_vjp, VjpArgs)
 SG_LAUNCH(fk_vjp, FkVjpArgs)
-SG_LAUNCH(rnea_derivatives, DerivArgs)
-SG_LAUNCH(aba_derivatives, DerivArgs)
 SG_LAUNCH(rollout_forward, RolloutArgs)
 SG_LAUNCH(rollout_reverse, RolloutArgs)
 #undef SG_LAUNCH
 
+cudaError_t launch_rnea_derivatives_j16(const DModel* dm, const DerivArgs& a, cudaStream_t s) {
+  rnea_derivatives_kernel<16><<<unsigned((a.n * a.groups + 31) / 32), 32, 0, s>>>(dm, a);
+  return cudaGetLastError();
+}
+cudaError_t launch_aba_derivatives_j16(const DModel* dm, const DerivArgs& a, cudaStream_t s) {
+  aba_derivatives_kernel<16><<<unsigned((a.n * a.groups + 31) / 32), 32, 0, s>>>(dm, a);
+  return cudaGetLastError();
+}
 cudaError_t launch_rollout_recompute_j16(const DModel* dm, const RolloutArgs& a, cudaStream_t s) {
   rollout_recompute_kernel<16><<<unsigned((a.n * a.s_cnt + 31) / 32), 32, 0, s>>>(dm, a);
   return cudaGetLastError();

@@ -114,8 +114,10 @@ __global__ void __launch_bounds__(32) fk_vjp_kernel(const DModel* __restrict__ m
 
 template <int MAXJ>
 __global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= a.n * a.groups) return;
+  const int64_t e = idx % a.n;
+  const int r0 = int(idx / a.n) * a.rows;
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
   const RuntimeTab T{model};
   const int nv = T.nv(), nq = T.nq_ext();
@@ -127,7 +129,8 @@ __global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __re
   AdjScratch<MAXJ> A;
   rnea_forward<MAXJ>(T, q, qd, qdd, W);
   rnea_subtree_forces<MAXJ>(T, W, A.F);
-  for (int r = 0; r < nv; r++) {
+  const int r1 = min(nv, r0 + a.rows);
+  for (int r = r0; r < r1; r++) {
     for (int c = 0; c < nv; c++) tb[c] = (c == r) ? 1.0 : 0.0;
     rnea_adjoint<MAXJ>(T, W, A, tb, o1, o2, a.d_x.p ? o3 : nullptr, 1.0);
     for (int c = 0; c < nv; c++) {
@@ -140,8 +143,10 @@ __global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __re
 
 template <int MAXJ>
 __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= a.n * a.groups) return;
+  const int64_t e = idx % a.n;
+  const int r0 = int(idx / a.n) * a.rows;
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
   const RuntimeTab T{model};
   const int nv = T.nv(), nq = T.nq_ext();
@@ -153,7 +158,8 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
   AdjScratch<MAXJ> A;
   aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
   rnea_subtree_forces<MAXJ>(T, W, A.F);
-  for (int r = 0; r < nv; r++) {
+  const int r1 = min(nv, r0 + a.rows);
+  for (int r = r0; r < r1; r++) {
     for (int c = 0; c < nv; c++) er[c] = (c == r) ? 1.0 : 0.0;
     minv_solve<MAXJ>(T, W, er, lam);
     rnea_adjoint<MAXJ>(T, W, A, lam, o1, o2, nullptr, -1.0);
