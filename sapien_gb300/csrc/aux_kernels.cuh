@@ -59,43 +59,6 @@ __global__ void __launch_bounds__(32) link_jacobian_kernel(const DModel* __restr
   }
 }
 
-// Dense 6x6 of a rigid-body inertia (linear, angular ordering).
-__device__ __forceinline__ void rbi_dense(const RBI& Y, double* I6) {
-  for (int k = 0; k < 36; k++) I6[k] = 0;
-  I6[0] = I6[7] = I6[14] = Y.m;
-  // top-right -[h]x, bottom-left [h]x
-  const double h[3] = {Y.h.x, Y.h.y, Y.h.z};
-  const double H[9] = {0, -h[2], h[1], h[2], 0, -h[0], -h[1], h[0], 0};
-  for (int r = 0; r < 3; r++)
-    for (int c = 0; c < 3; c++) {
-      I6[r * 6 + 3 + c] = -H[r * 3 + c];
-      I6[(3 + r) * 6 + c] = H[r * 3 + c];
-    }
-  const int sidx[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
-  for (int r = 0; r < 3; r++)
-    for (int c = 0; c < 3; c++) I6[(3 + r) * 6 + 3 + c] = Y.I[sidx[r * 3 + c]];
-}
-__device__ __forceinline__ Mot dense_mul(const double* A, Mot x) {
-  const double xv[6] = {x.v.x, x.v.y, x.v.z, x.w.x, x.w.y, x.w.z};
-  double y[6];
-  for (int r = 0; r < 6; r++) {
-    double s = 0;
-    for (int c = 0; c < 6; c++) s = fma(A[r * 6 + c], xv[c], s);
-    y[r] = s;
-  }
-  return Mot{mk(y[0], y[1], y[2]), mk(y[3], y[4], y[5])};
-}
-__device__ __forceinline__ Mot dense_mulT(const double* A, Mot x) {
-  const double xv[6] = {x.v.x, x.v.y, x.v.z, x.w.x, x.w.y, x.w.z};
-  double y[6];
-  for (int c = 0; c < 6; c++) {
-    double s = 0;
-    for (int r = 0; r < 6; r++) s = fma(A[r * 6 + c], xv[r], s);
-    y[c] = s;
-  }
-  return Mot{mk(y[0], y[1], y[2]), mk(y[3], y[4], y[5])};
-}
-
 // computeCoriolisMatrix (pinocchio_model.cpp:208-212): the Christoffel-consistent
 // factorisation C = sum_b J_b^T (I_b Jdot_b + B_b J_b) with
 // B(I, v) = 1/2 ((v x*) I - I (v x) + (I v) xbar*), evaluated with subtree composites:
@@ -103,6 +66,11 @@ __device__ __forceinline__ Mot dense_mulT(const double* A, Mot x) {
 //   C[k, l] = S_k . (Ic Sdot_l + Bc S_l)             l in joint i, k in ancestors-or-self,
 //   C[k, l] = (Ic S_k) . Sdot_l + (Bc^T S_k) . S_l   k in joint i, l in strict ancestors,
 // where Sdot = v_i x S (world frame) and all other entries vanish.
+// For an origin-form inertia (m, h, Ibar) and v = (nu, w), with I v = (f, n), B has a single
+// non-zero block column: B = [[0, -[f]x], [0, M]] with
+//   M = 1/2 ([w]x Ibar - Ibar [w]x - (h nu^T + nu h^T) + 2 (nu . h) 1 - [n]x),
+// so B x = (w_x x f, M w_x) and B^T y = (0, f x y_lin + M^T y_ang). Composites keep the sum
+// of f (3 numbers) and of M (9) instead of a dense 6x6.
 template <int MAXJ>
 __global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__ model, const CoriolisArgs a) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -114,21 +82,20 @@ __global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__
   V3 op[MAXJ];
   Mot vel[MAXJ], Sw[MAXV], Sd[MAXV];
   RBI Ic[MAXJ];
-  double Bc[MAXJ][36];
-  for (int r = 0; r < nv; r++)
-    for (int c = 0; c < nv; c++) stv(a.C, e, r * nv + c, 0.0);
+  V3 Bf[MAXJ];
+  M3 BM[MAXJ];
+  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
   for (int i = 1; i < nj; i++) {
     const DJoint& J = JT[i];
     const int p = J.parent, iv = J.ivx;
     joint_world_pose(J, a.q, e, oR, op, oR[i], op[i]);
-    Mot vJ{mk(0, 0, 0), mk(0, 0, 0)};
+    Mot vJ = zero;
     for (int k = 0; k < J.nv; k++) {
       Sw[iv + k] = world_S(J, oR[i], op[i], k);
       vJ = axpy6(ldv(a.qd, e, J.vcol + k), Sw[iv + k], vJ);
     }
     const Mot v = (p == 0) ? vJ : add6(vel[p], vJ);
     vel[i] = v;
-    const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
     for (int k = 0; k < J.nv; k++) Sd[iv + k] = add_crossm(zero, v, Sw[iv + k]);
     RBI Yl;
     Yl.m = J.m;
@@ -136,28 +103,38 @@ __global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__
     for (int k = 0; k < 6; k++) Yl.I[k] = J.I[k];
     const RBI Y = rbi_transport(Yl, oR[i], op[i]);
     Ic[i] = Y;
-    // B = 1/2 (crf(v) I - I crm(v) + Hbar(I v)), column by column
-    double I6[36];
-    rbi_dense(Y, I6);
-    const Mot h = rbi_mul(Y, v);
-    for (int c = 0; c < 6; c++) {
-      Mot ec{mk(c == 0, c == 1, c == 2), mk(c == 3, c == 4, c == 5)};
-      // I6 column c
-      Mot Icol{mk(I6[0 * 6 + c], I6[1 * 6 + c], I6[2 * 6 + c]), mk(I6[3 * 6 + c], I6[4 * 6 + c], I6[5 * 6 + c])};
-      Mot t1 = add_crossf(zero, v, Icol);               // (v x*) I e_c
-      Mot t2 = rbi_mul(Y, add_crossm(zero, v, ec));     // I (v x e_c)
-      Mot t3 = add_crossf(zero, ec, h);                 // e_c x* (I v)
-      const double col[6] = {t1.v.x - t2.v.x + t3.v.x, t1.v.y - t2.v.y + t3.v.y, t1.v.z - t2.v.z + t3.v.z,
-                             t1.w.x - t2.w.x + t3.w.x, t1.w.y - t2.w.y + t3.w.y, t1.w.z - t2.w.z + t3.w.z};
-      for (int r = 0; r < 6; r++) Bc[i][r * 6 + c] = 0.5 * col[r];
-    }
+    const Mot fn = rbi_mul(Y, v);  // (f, n) = I v
+    Bf[i] = fn.v;
+    // M = 1/2 (A + A^T - (h nu^T + nu h^T) + 2 (nu . h) 1 - [n]x), A = [w]x Ibar
+    const V3 w = v.w, nu = v.v, h = Y.h;
+    const double* S = Y.I;  // xx xy xz yy yz zz
+    const V3 c0 = cross(w, mk(S[0], S[1], S[2])), c1 = cross(w, mk(S[1], S[3], S[4])),
+             c2 = cross(w, mk(S[2], S[4], S[5]));  // columns of A
+    const double A[9] = {c0.x, c1.x, c2.x, c0.y, c1.y, c2.y, c0.z, c1.z, c2.z};
+    const double hv[3] = {h.x, h.y, h.z}, nv3[3] = {nu.x, nu.y, nu.z};
+    const double d2 = 2.0 * dot(nu, h);
+    const double N[9] = {0, -fn.w.z, fn.w.y, fn.w.z, 0, -fn.w.x, -fn.w.y, fn.w.x, 0};
+    M3 Mi;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        double t = A[r * 3 + c] + A[c * 3 + r] - fma(hv[r], nv3[c], nv3[r] * hv[c]) - N[r * 3 + c];
+        if (r == c) t += d2;
+        Mi.a[r * 3 + c] = 0.5 * t;
+      }
+    BM[i] = Mi;
   }
   for (int i = nj - 1; i >= 1; i--) {
     const DJoint& J = JT[i];
     const int p = J.parent, iv = J.ivx;
     const RBI Y = Ic[i];
+    const V3 f = Bf[i];
+    const M3 Mc = BM[i];
     for (int l = 0; l < J.nv; l++) {
-      const Mot F = add6(rbi_mul(Y, Sd[iv + l]), dense_mul(Bc[i], Sw[iv + l]));
+      // Bc S_l = (w_S x f, Mc w_S)
+      const Mot Sl = Sw[iv + l];
+      const Mot F = add6(rbi_mul(Y, Sd[iv + l]), Mot{cross(Sl.w, f), mul(Mc, Sl.w)});
       const int cl = J.vcol + l;
       for (int j = i; j > 0; j = JT[j].parent) {
         const DJoint& A = JT[j];
@@ -165,21 +142,35 @@ __global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__
       }
     }
     for (int k = 0; k < J.nv; k++) {
-      const Mot H = rbi_mul(Y, Sw[iv + k]);
-      const Mot K = dense_mulT(Bc[i], Sw[iv + k]);
+      const Mot Sk = Sw[iv + k];
+      const Mot H = rbi_mul(Y, Sk);
+      // Bc^T S_k = (0, f x S_k,lin + Mc^T S_k,ang)
+      const V3 Kw = cross(f, Sk.v) + mulT(Mc, Sk.w);
       const int rk = J.vcol + k;
       for (int j = p; j > 0; j = JT[j].parent) {
         const DJoint& A = JT[j];
-        for (int l = 0; l < A.nv; l++)
-          stv(a.C, e, rk * nv + A.vcol + l, dot6(H, Sd[A.ivx + l]) + dot6(K, Sw[A.ivx + l]));
+        for (int l = 0; l < A.nv; l++) {
+          const Mot Sl = Sw[A.ivx + l];
+          stv(a.C, e, rk * nv + A.vcol + l, dot6(H, Sd[A.ivx + l]) + dot(Kw, Sl.w));
+        }
       }
+    }
+    // entries with the joints after this joint's subtree (no ancestor relation) vanish
+    for (int j = J.subtree_end; j < nj; j++) {
+      const int jc = JT[j].vcol, nvj = JT[j].nv;
+      for (int k = 0; k < J.nv; k++)
+        for (int l = 0; l < nvj; l++) {
+          stv(a.C, e, (jc + l) * nv + J.vcol + k, 0.0);
+          stv(a.C, e, (J.vcol + k) * nv + jc + l, 0.0);
+        }
     }
     if (p > 0) {
       RBI& P = Ic[p];
       P.m += Y.m;
       P.h = P.h + Y.h;
       for (int k = 0; k < 6; k++) P.I[k] += Y.I[k];
-      for (int k = 0; k < 36; k++) Bc[p][k] += Bc[i][k];
+      Bf[p] = Bf[p] + f;
+      for (int k = 0; k < 9; k++) BM[p].a[k] += Mc.a[k];
     }
   }
 }
