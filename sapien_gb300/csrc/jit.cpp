@@ -106,6 +106,9 @@ void read_env_config() {
   if (const char* m = std::getenv("SGDYN_JIT_MIN_N")) g_min_n = std::atoll(m);
 }
 
+const char* const kNvrtcOptions[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
+constexpr int kNvrtcOptionCount = 3;
+
 uint64_t fnv1a(const std::string& s) {
   uint64_t h = 1469598103934665603ull;
   for (unsigned char c : s) {
@@ -194,8 +197,8 @@ bool compile_cubin(const std::string& src, std::vector<char>* cubin, std::string
     *why = "nvrtcCreateProgram failed";
     return false;
   }
-  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
-  nvrtcResult rc = A.compileProgram(prog, 3, opts);
+  const char* const* opts = kNvrtcOptions;
+  nvrtcResult rc = A.compileProgram(prog, kNvrtcOptionCount, opts);
   if (rc != NVRTC_SUCCESS) {
     size_t n = 0;
     A.getLogSize(prog, &n);
@@ -246,8 +249,17 @@ CUfunction get_function_slow(const Model& M, int kind, int ops, int dev, std::st
   const std::string src = generate_source(M, kind, ops);
   int major = 0, minor = 0;
   A.version(&major, &minor);
-  char hx[40];
-  std::snprintf(hx, sizeof hx, "%016llx-%d.%d", static_cast<unsigned long long>(fnv1a(src)), major, minor);
+  // The key covers the generated unit and the device headers it includes (so a rebuilt
+  // library never picks up a cubin compiled from older headers) and the compiler version.
+  static const uint64_t headers_hash = [] {
+    std::string all;
+    for (int k = 0; k < kNvrtcOptionCount; k++) all += std::string(kNvrtcOptions[k]) + '\n';
+    for (int k = 0; k < kJitHeaderCount; k++) all += std::string(kJitHeaderNames[k]) + '\n' + kJitHeaderSources[k];
+    return fnv1a(all);
+  }();
+  char hx[64];
+  std::snprintf(hx, sizeof hx, "%016llx-%016llx-%d.%d", static_cast<unsigned long long>(fnv1a(src)),
+                static_cast<unsigned long long>(headers_hash), major, minor);
   const std::string key = std::string(hx) + "@" + std::to_string(dev);
   auto it = g_functions.find(key);
   if (it != g_functions.end()) return it->second;
