@@ -29,6 +29,7 @@ namespace {
 
 // Runtime table with gravity replaced (zero when gravity terms are not wanted).
 struct GravityTab {
+  static constexpr bool kStatic = false;
   const DModel* m;
   double g[3];
   __device__ __forceinline__ int nj() const { return m->nj; }

@@ -26,6 +26,7 @@ namespace sgdyn {
 // table whose contents are compile-time constants (run-time-compiled per model, so every
 // joint loop unrolls into straight-line code with constant parents, axes and inertias).
 struct RuntimeTab {
+  static constexpr bool kStatic = false;
   const DModel* m;
   __device__ __forceinline__ int nj() const { return m->nj; }
   __device__ __forceinline__ int nv() const { return m->nv; }
@@ -37,6 +38,7 @@ struct RuntimeTab {
 };
 template <int NJ, int NV, int NL, const DJoint* JT, const DLink* LT, const DModel* M>
 struct StaticTab {
+  static constexpr bool kStatic = true;
   __device__ __forceinline__ static constexpr int nj() { return NJ; }
   __device__ __forceinline__ static constexpr int nv() { return NV; }
   __device__ __forceinline__ int nq_ext() const { return M->nq_ext; }
@@ -489,15 +491,10 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
     acc[i] = a;
   };
 
-  auto link_poses = [&]() {
-    const int nl = T.nlinks();
-#pragma unroll
-    for (int l = 0; l < nl; l++) {
-      const DLink& L = T.link(l);
-      const int j = L.joint;
-      if constexpr (kTeam) {
-        if (!writes(j)) continue;  // another lane holds this joint's pose
-      }
+  auto link_pose = [&](int l) {
+    const DLink& L = T.link(l);
+    const int j = L.joint;
+    {
       M3 R;
       V3 pp;
       M3 Rl;
@@ -522,6 +519,25 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
       stv(args.poses, e, l * 7 + 6, qt[3]);
     }
   };
+  auto link_poses = [&]() {
+    const int nl = T.nlinks();
+#pragma unroll
+    for (int l = 0; l < nl; l++) {
+      if constexpr (kTeam) {
+        if (!writes(T.link(l).joint)) continue;  // another lane holds this joint's pose
+      }
+      link_pose(l);
+    }
+  };
+  // With compile-time tables and other ops in the same sweep, each link's pose is emitted
+  // right after its joint, so the joint's world pose need not stay live to the end of
+  // pass 1 (FK alone is faster with the poses written in one run).
+  auto links_of = [&](int i) {
+    const int nl = T.nlinks();
+#pragma unroll
+    for (int l = 0; l < nl; l++)
+      if (T.link(l).joint == i) link_pose(l);
+  };
 
   auto load_tau = [&]() {
     if constexpr (kABA) {
@@ -532,9 +548,14 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
   };
 
   if constexpr (!kTeam) {
+    constexpr bool kInlineLinks = kFK && Tab::kStatic && (OPS & ~OP_FK) != 0;
+    if constexpr (kInlineLinks) links_of(0);
 #pragma unroll
-    for (int i = 1; i < nj; i++) pass1(i);
-    if constexpr (kFK) link_poses();
+    for (int i = 1; i < nj; i++) {
+      pass1(i);
+      if constexpr (kInlineLinks) links_of(i);
+    }
+    if constexpr (kFK && !kInlineLinks) link_poses();
     load_tau();
     if constexpr (kCRBA || kRNEA || kABA) {
 #pragma unroll
