@@ -160,6 +160,13 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
                const double* tau, double* link_poses, double* J, double* M, double* tau_out, double* qdd_out,
                int layout, void* stream);
 
+/* Lanes per environment for the single-model fused sweep and single-op entry points
+ * (addition): 0 = automatic (default), 1, 2, 4 or 8. With L > 1 a team of L lanes shares an
+ * environment: the joints near the root run on every lane and the subtrees off them on one
+ * lane each, which shortens a wide tree's sequential sweep; worth it when the batch leaves
+ * the GPU's FP64 schedulers idle (automatic: only then, and only if the tree splits). */
+int sgdyn_model_set_lanes(sgdyn_model* m, int lanes);
+
 /* Run-time specialisation (addition). The fused sweep behind sgdyn_step and the five
  * single-op entry points, and the forward rollout kernel, are compiled per model with NVRTC on
  * first use (tables baked in as constants; same arithmetic) when enabled and n >= min_n;

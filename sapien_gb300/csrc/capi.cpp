@@ -91,6 +91,35 @@ int check_ptrs(std::initializer_list<Req> reqs) {
   return SGDYN_OK;
 }
 
+// Lanes per environment for a single-model sweep: the model's setting, or (0 = automatic)
+// the count with the shortest estimated time when the batch leaves FP64 schedulers idle. A
+// small batch is bound by one warp's sequential sweep, so the estimate is the team plan's
+// critical path (trunk + heaviest lane) times the number of warp rounds the lanes need.
+int choose_lanes(Model& M, int64_t n) {
+  if (M.lanes > 0) return M.lanes;
+  static int schedulers = 0;
+  if (schedulers == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    schedulers = 4 * (sms > 0 ? sms : 1);
+  }
+  if ((n + 31) / 32 * 2 > schedulers) return 1;  // the batch alone fills the GPU
+  int best = 1;
+  double best_est = 0;
+  for (int L : {1, 2, 4, 8}) {
+    const int cp = M.team_critical_path(L);
+    const double rounds = std::max(1.0, double((n * L + 31) / 32) / schedulers);
+    const double est = cp * rounds;
+    if (L == 1) best_est = est;
+    else if (est < 0.8 * best_est) {
+      best = L;
+      best_est = est;
+    }
+  }
+  return best;
+}
+
 int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const double* qd, const double* qdd,
              const double* tau, double* poses, double* J, double* M, double* tau_out, double* qdd_out, int layout,
              void* stream) {
@@ -139,7 +168,18 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
     }
   for (int b = 1; b <= OP_ABA; b <<= 1)
     if (rest & b) launches.push_back(b);
+  const int lanes = choose_lanes(Mo, n);
+  const int* team = nullptr;
+  if (lanes > 1) {
+    team = Mo.device_team(lanes, &err);
+    if (!team) return fail(SGDYN_ERR_CUDA, "team table upload failed");
+  }
   for (int o : launches) {
+    if (team) {  // several lanes per environment
+      cudaError_t e = launch_step_team(dm, Mo.njoints(), team, lanes, o, a, s);
+      if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+      continue;
+    }
     std::string why;
     if (launch_step_jit(Mo, o, a, s, &why)) continue;  // model-specialised kernel
     cudaError_t e = launch_step(dm, Mo.njoints(), o, a, s);
@@ -288,6 +328,14 @@ int sgdyn_model_table(const sgdyn_model* m, const void** data, int64_t* bytes) {
   if (!m || !data || !bytes) return fail(SGDYN_ERR_NULL, "null argument");
   *data = m->impl->host_table().data();
   *bytes = int64_t(m->impl->host_table().size());
+  return SGDYN_OK;
+}
+
+int sgdyn_model_set_lanes(sgdyn_model* m, int lanes) {
+  if (int rc = check_model(m)) return rc;
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)
+    return fail(SGDYN_ERR_RUNTIME, "lanes must be 0 (automatic), 1, 2, 4 or 8");
+  m->impl->lanes = lanes;
   return SGDYN_OK;
 }
 

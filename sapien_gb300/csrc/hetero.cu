@@ -182,78 +182,6 @@ int upload_plan(sgdyn_batch* b) {
   return SGDYN_OK;
 }
 
-// Team table for L lanes per environment (layout in step_kernel.cuh). The trunk starts
-// empty with the root subtrees as branches; the heaviest branch's root is moved into the
-// trunk (its children become branches) while that lowers trunk cost + the heaviest lane's
-// cost, lanes being filled longest-branch-first. Joint cost: 1, a free flyer 4.
-std::vector<int> build_team_table(const Model& M, int L) {
-  const auto* hdr = reinterpret_cast<const DModel*>(M.host_table().data());
-  const DJoint* J = model_joints(hdr);
-  const int nj = hdr->nj;
-  std::vector<std::vector<int>> kids(nj);
-  for (int j = 1; j < nj; j++) kids[J[j].parent].push_back(j);
-  std::vector<int> cost(nj, 0), sub(nj, 0);
-  for (int j = 1; j < nj; j++) cost[j] = J[j].nv == 6 ? 4 : 1;
-  for (int j = nj - 1; j >= 1; j--) {
-    sub[j] += cost[j];
-    if (J[j].parent > 0) sub[J[j].parent] += sub[j];
-  }
-  std::vector<int> trunk, branches = kids[0];
-  int trunk_cost = 0;
-  int best = 1 << 30;
-  std::vector<int> best_trunk, best_owner;
-  for (;;) {
-    std::vector<int> order = branches;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sub[x] > sub[y]; });
-    std::vector<int> load(L, 0), role_of(nj, -1);
-    for (int r : order) {
-      const int lane = int(std::min_element(load.begin(), load.end()) - load.begin());
-      load[lane] += sub[r];
-      role_of[r] = lane;
-    }
-    const int cp = trunk_cost + *std::max_element(load.begin(), load.end());
-    if (cp < best) {
-      best = cp;
-      best_trunk = trunk;
-      best_owner.assign(nj, -1);
-      for (int j = 1; j < nj; j++) {  // a branch joint belongs to its branch root's lane
-        int r = j;
-        while (r > 0 && role_of[r] < 0 && std::find(trunk.begin(), trunk.end(), r) == trunk.end()) r = J[r].parent;
-        if (r > 0 && role_of[r] >= 0) best_owner[j] = role_of[r];
-      }
-    }
-    if (branches.empty()) break;
-    const int h = *std::max_element(branches.begin(), branches.end(), [&](int x, int y) { return sub[x] < sub[y]; });
-    if (kids[h].empty()) break;
-    branches.erase(std::find(branches.begin(), branches.end(), h));
-    trunk.push_back(h);
-    trunk_cost += cost[h];
-    for (int c : kids[h]) branches.push_back(c);
-  }
-  std::sort(best_trunk.begin(), best_trunk.end());
-  std::vector<std::vector<int>> lanes(L);
-  for (int j = 1; j < nj; j++)
-    if (best_owner[j] >= 0) lanes[best_owner[j]].push_back(j);
-  size_t smax = 0;
-  for (auto& l : lanes) smax = std::max(smax, l.size());
-  std::vector<int> attach;
-  for (int t : best_trunk)
-    for (int c : kids[t])
-      if (best_owner[c] >= 0) {
-        attach.push_back(t);
-        break;
-      }
-  std::vector<int> tab = {L, int(best_trunk.size()), int(smax), int(attach.size())};
-  tab.insert(tab.end(), best_trunk.begin(), best_trunk.end());
-  for (auto& l : lanes) {
-    tab.insert(tab.end(), l.begin(), l.end());
-    tab.insert(tab.end(), smax - l.size(), 0);
-  }
-  tab.insert(tab.end(), attach.begin(), attach.end());
-  tab.insert(tab.end(), best_owner.begin(), best_owner.end());
-  return tab;
-}
-
 int upload_teams(sgdyn_batch* b) {
   std::vector<int> all;
   std::vector<int64_t> offs;
@@ -263,7 +191,7 @@ int upload_teams(sgdyn_batch* b) {
       continue;
     }
     offs.push_back(int64_t(all.size()));
-    const auto t = build_team_table(*b->models[m]->impl, b->lanes[m]);
+    const auto t = b->models[m]->impl->team_table(b->lanes[m]);
     all.insert(all.end(), t.begin(), t.end());
   }
   cudaFree(b->teams);

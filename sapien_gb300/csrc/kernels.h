@@ -95,6 +95,9 @@ int stash_bucket(int nj);
 
 // Fused world-frame sweep: any subset of {FK poses, full WORLD Jacobian, CRBA, RNEA, ABA}.
 cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cudaStream_t s);
+// The same sweep with `lanes` lanes per environment (team table `team` on the device).
+cudaError_t launch_step_team(const DModel* dm, int nj, const int* team, int lanes, int ops, const StepArgs& a,
+                             cudaStream_t s);
 cudaError_t launch_link_jacobian(const DModel* dm, int nj, const LinkJacArgs& a, cudaStream_t s);
 cudaError_t launch_coriolis(const DModel* dm, int nj, const CoriolisArgs& a, cudaStream_t s);
 cudaError_t launch_ik(const DModel* dm, int nj, const IkArgs& a, cudaStream_t s);

@@ -96,6 +96,16 @@ class Model {
   // Host copy of the packed table (for tests and for the heterogeneous packer).
   const std::vector<unsigned char>& host_table() const { return table_; }
 
+  // Team table for L lanes per environment (layout in step_kernel.cuh: TeamLanes);
+  // *critical_path receives the joint-cost length of the trunk + heaviest lane.
+  std::vector<int> team_table(int L, int* critical_path = nullptr) const;
+  // Its device copy on the current device (uploaded on first use), or null.
+  const int* device_team(int L, int* err);
+  // The critical path of team_table(L), cached.
+  int team_critical_path(int L);
+  // Lanes per environment for the single-model entry points: 0 = automatic, 1, 2, 4, 8.
+  int lanes = 0;
+
   std::vector<HostJoint> joints;  // [0] = universe
   std::vector<HostBody> bodies;
   double gravity[3] = {0, 0, -9.81};
@@ -117,6 +127,8 @@ class Model {
   std::vector<int> link_bodies_;   // external link index -> bodies[]
   std::vector<unsigned char> table_;
   std::map<int, void*> dev_;       // device ordinal -> device copy of table_
+  std::map<std::pair<int, int>, void*> dev_team_;  // (device, L) -> device team table
+  std::map<int, int> team_cp_;                       // L -> critical path
   std::mutex mu_;
   uint64_t uid_ = next_uid();
   uint64_t version_ = 0;

@@ -650,4 +650,16 @@ __global__ void __launch_bounds__(32) step_kernel(const DModel* __restrict__ mod
   step_env<MAXJ, OPS>(model, args, e);
 }
 
+// L lanes per environment: one warp holds 32 / L environments. Every lane takes part in the
+// team sums; lanes past the end repeat the last environment and store nothing.
+template <int MAXJ, int OPS>
+__global__ void __launch_bounds__(32) step_team_kernel(const DModel* __restrict__ model, const int* __restrict__ team,
+                                                       const StepArgs args) {
+  const int L = team[0], lane = threadIdx.x & 31;
+  const int64_t e = int64_t(blockIdx.x) * (32 / L) + lane / L;
+  const bool valid = e < args.n;
+  const TeamLanes tm{team, lane % L, valid};
+  step_env_t<MAXJ, OPS>(RuntimeTab{model}, args, valid ? e : args.n - 1, tm);
+}
+
 }  // namespace sgdyn

@@ -147,6 +147,11 @@ class PinocchioModel:
     def nlinks(self):
         return self._nlinks if self._link_order_set else 0
 
+    def set_lanes(self, lanes=0):
+        """Lanes per environment for the batched sweeps (0 = automatic, 1, 2, 4 or 8): several
+        lanes share one environment of a wide tree, which pays off for small batches."""
+        N.check(N.load().sgdyn_model_set_lanes(self._h, int(lanes)))
+
     def table_bytes(self):
         """Host copy of the packed kernel tables (see csrc/device_model.h)."""
         L = N.load()

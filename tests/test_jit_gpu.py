@@ -35,6 +35,7 @@ def test_specialised_sweep_matches_generic_and_oracle(name):
     pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
     pm.set_joint_order(robot.joint_names)
     pm.set_link_order(robot.link_names)
+    pm.set_lanes(1)  # one lane per environment: the specialised kernel's domain
     q, qd, qdd, tau = (torch.from_numpy(a).cuda() for a in robot.sample(100, seed=23))
     old = jit_config(-1, -1)
     try:

@@ -220,6 +220,44 @@ def test_pinned_host_buffers_read_and_written_in_place(layout):
         assert T.equal(a, b)
 
 
+@pytest.mark.parametrize("name", ["humanoid", "quadruped", "arm9"])
+def test_lanes_per_environment_single_model(name):
+    """Teams of 2, 4 or 8 lanes per environment (and the automatic choice) reproduce the
+    one-lane sweep to rounding and write every output entry (buffers start as NaN)."""
+    robot = {"humanoid": syn.humanoid(), "quadruped": syn.quadruped(), "arm9": syn.arm_with_fingers()}[name]
+    pm, o = pair(robot)
+    T = torch()
+    n = 77
+    q, qd, qdd, tau = (T.from_numpy(a).cuda() for a in robot.sample(n, seed=31))
+
+    nv, nl = robot.nv, len(robot.link_names)
+    shapes = {"link_poses": (n, nl * 7), "jacobian": (n, 6 * nv), "mass_matrix": (n, nv * nv), "qf": (n, nv),
+              "qacc": (n, nv)}
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+
+    def run(lanes):
+        pm.set_lanes(lanes)
+        out = {k: T.full(sh, float("nan"), dtype=T.float64, device="cuda") for k, sh in shapes.items()}
+        pm._prepare(q.device)
+        rc = N.load().sgdyn_step(pm._h, n, N.OP_ALL, p(q), p(qd), p(qdd), p(tau), *[p(out[k]) for k in shapes],
+                                 N.ENV_MAJOR, None)
+        assert rc == 0, N.last_error()
+        T.cuda.synchronize()
+        return {k: v.cpu().numpy() for k, v in out.items()}
+
+    ref = run(1)
+    for lanes in (2, 4, 8, 0):
+        got = run(lanes)
+        for k in ref:
+            assert not np.isnan(got[k]).any(), (lanes, k)
+            assert rel_per_env(got[k], ref[k]) <= 1e-11, (lanes, k)
+    r = o.batch_step(*(x.cpu().numpy() for x in (q, qd, qdd, tau)), ops=4 | 8 | 16)
+    assert rel_per_env(got["qf"], r["tau"]) <= 1e-10
+    assert rel_per_env(got["qacc"], r["qdd"]) <= 1e-8
+    assert rel_per_env(got["mass_matrix"], r["M"].reshape(n, -1)) <= 1e-10
+    pm.set_lanes(0)
+
+
 def test_edge_cases_and_pointer_checks():
     robot = syn.serial_chain(7)
     pm, o = pair(robot)
