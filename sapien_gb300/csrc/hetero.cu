@@ -208,15 +208,7 @@ int upload_teams(sgdyn_batch* b) {
   return SGDYN_OK;
 }
 
-bool dev_ptr(const void* p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
+bool dev_ptr(const void* p) { return device_accessible(p); }
 
 Arr env_major(const void* p, int64_t cols) { return Arr{static_cast<double*>(const_cast<void*>(p)), cols, 1}; }
 
