@@ -168,14 +168,20 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
 int sgdyn_model_set_lanes(sgdyn_model* m, int lanes);
 
 /* Run-time specialisation (addition). The fused sweep behind sgdyn_step and the five
- * single-op entry points, and the forward rollout kernel, are compiled per model with NVRTC on
+ * single-op entry points, the forward rollout kernel and the RNEA / ABA vector-Jacobian
+ * product kernels, are compiled per model with NVRTC on
  * first use (tables baked in as constants; same arithmetic) when enabled and n >= min_n;
  * otherwise, or if the run-time compiler or the driver library is unavailable, the generic
  * kernel runs. enable / min_n < 0 leave a setting unchanged; the current values are
- * returned. Defaults: enabled unless SGDYN_JIT=0, min_n = 2048 (SGDYN_JIT_MIN_N). Compile
+ * returned. Defaults: enabled unless SGDYN_JIT=0, min_n = 2048 (SGDYN_JIT_MIN_N), trees of
+ * at most 16 joints incl. the universe (SGDYN_JIT_MAX_JOINTS; larger unrolled sweeps ran
+ * slower). Compile
  * ahead with sgdyn_jit_prepare (needed before capturing launches into a CUDA graph).
- * `ops`: an SGDYN_OP_* mask for the fused sweep, or -1 for the forward rollout kernel. */
+ * `ops`: an SGDYN_OP_* mask for the fused sweep, -1 for the forward rollout kernel, -2 / -3
+ * for the RNEA / ABA vector-Jacobian product kernels. */
 int sgdyn_jit_config(int enable, int64_t min_n, int* enabled, int64_t* min_n_out);
+/* Size limit of run-time specialisation (joints incl. the universe; < 0 leaves it). */
+int sgdyn_jit_max_joints(int max_joints, int* max_joints_out);
 int sgdyn_jit_prepare(const sgdyn_model* m, int ops);
 /* The generated translation unit for (model, ops); valid until the next call on this thread. */
 int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source);

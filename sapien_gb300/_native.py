@@ -68,6 +68,7 @@ EXPORTED = (
     "sgdyn_batch_set_lanes",
     "sgdyn_batch_step",
     "sgdyn_model_set_lanes",
+    "sgdyn_jit_max_joints",
     "sgdyn_jit_config",
     "sgdyn_jit_prepare",
     "sgdyn_jit_source",
@@ -138,6 +139,7 @@ def load():
     L.sgdyn_compute_passive_force_f32.argtypes = [vp, i64, vp, vp, i64, i32, i32, vp, i64, vp]
     L.sgdyn_jit_config.argtypes = [i32, i64, P(i32), P(i64)]
     L.sgdyn_model_set_lanes.argtypes = [vp, i32]
+    L.sgdyn_jit_max_joints.argtypes = [i32, P(i32)]
     L.sgdyn_jit_prepare.argtypes = [vp, i32]
     L.sgdyn_jit_source.argtypes = [vp, i32, P(ctypes.c_char_p)]
     L.sgdyn_rollout_backward_noalloc.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]

@@ -158,7 +158,7 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
   a.tau_out = make_arr(tau_out, n, nv, layout);
   a.qdd_out = make_arr(qdd_out, n, nv, layout);
   auto s = static_cast<cudaStream_t>(stream);
-  static const int fused[] = {OP_ALL, OP_RNEA | OP_ABA, OP_FK | OP_JAC};
+  static const int fused[] = {OP_ALL, OP_CRBA | OP_RNEA | OP_ABA, OP_RNEA | OP_ABA, OP_FK | OP_JAC};
   int rest = ops;
   std::vector<int> launches;
   for (int f : fused)
@@ -331,6 +331,11 @@ int sgdyn_model_table(const sgdyn_model* m, const void** data, int64_t* bytes) {
   return SGDYN_OK;
 }
 
+int sgdyn_jit_max_joints(int max_joints, int* max_joints_out) {
+  jit_max_joints(max_joints, max_joints_out);
+  return SGDYN_OK;
+}
+
 int sgdyn_model_set_lanes(sgdyn_model* m, int lanes) {
   if (int rc = check_model(m)) return rc;
   if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)
@@ -345,14 +350,17 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
   return SGDYN_OK;
 }
 
-// ops > 0: the fused sweep with that op set; -1: the forward rollout kernel
-static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || ops == -1; }
+// ops > 0: the fused sweep with that op set; -1: the forward rollout kernel; -2 / -3: the
+// RNEA / ABA vector-Jacobian product kernels
+static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -3 && ops <= -1); }
 
 int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
   if (!m) return fail(SGDYN_ERR_NULL, "null model");
   if (!jit_kind_ok(ops)) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
   std::string why;
-  const bool ok = ops > 0 ? prepare_step_jit(*m->impl, ops, &why) : prepare_rollout_jit(*m->impl, &why);
+  const bool ok = ops > 0     ? prepare_step_jit(*m->impl, ops, &why)
+                  : ops == -1 ? prepare_rollout_jit(*m->impl, &why)
+                              : prepare_vjp_jit(*m->impl, ops == -3, &why);
   if (!ok) return fail(SGDYN_ERR_UNSUPPORTED, "run-time compilation unavailable: " + why);
   return SGDYN_OK;
 }
@@ -361,7 +369,7 @@ int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
   if (!m || !source) return fail(SGDYN_ERR_NULL, "null argument");
   if (!jit_kind_ok(ops)) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
   thread_local std::string buf;
-  buf = ops > 0 ? step_jit_source(*m->impl, ops) : rollout_jit_source(*m->impl);
+  buf = ops > 0 ? step_jit_source(*m->impl, ops) : ops == -1 ? rollout_jit_source(*m->impl) : vjp_jit_source(*m->impl, ops == -3);
   *source = buf.c_str();
   return SGDYN_OK;
 }
@@ -530,6 +538,8 @@ int sgdyn_compute_inverse_dynamics_vjp(const sgdyn_model* m, int64_t n, const do
     a.o1 = make_arr(q_bar, n, nv, layout);
     a.o2 = make_arr(qd_bar, n, nv, layout);
     a.o3 = make_arr(qdd_bar, n, nv, layout);
+    std::string why;
+    if (launch_vjp_jit(Mo, false, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
     return launch_status(launch_rnea_vjp(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
   });
 }
@@ -558,6 +568,8 @@ int sgdyn_compute_forward_dynamics_vjp(const sgdyn_model* m, int64_t n, const do
     a.o1 = make_arr(q_bar, n, nv, layout);
     a.o2 = make_arr(qd_bar, n, nv, layout);
     a.o3 = make_arr(tau_bar, n, nv, layout);
+    std::string why;
+    if (launch_vjp_jit(Mo, true, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
     return launch_status(launch_aba_vjp(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
   });
 }

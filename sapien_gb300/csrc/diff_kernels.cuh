@@ -22,12 +22,9 @@ __device__ __forceinline__ void store_row(const Arr& a, int64_t e, int cols, con
   for (int c = 0; c < cols; c++) stv(a, e, c, in[c]);
 }
 
-template <int MAXJ>
-__global__ void __launch_bounds__(32) rnea_vjp_kernel(const DModel* __restrict__ model, const VjpArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void rnea_vjp_env(const Tab& T, const VjpArgs& a, const int64_t e) {
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const RuntimeTab T{model};
   const int nv = T.nv(), nq = T.nq_ext();
   double q[MAXQ], qd[MAXV], qdd[MAXV], tb[MAXV], o1[MAXV], o2[MAXV], o3[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
@@ -45,11 +42,15 @@ __global__ void __launch_bounds__(32) rnea_vjp_kernel(const DModel* __restrict__
 }
 
 template <int MAXJ>
-__global__ void __launch_bounds__(32) aba_vjp_kernel(const DModel* __restrict__ model, const VjpArgs a) {
+__global__ void __launch_bounds__(32) rnea_vjp_kernel(const DModel* __restrict__ model, const VjpArgs a) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
+  rnea_vjp_env<MAXJ>(RuntimeTab{model}, a, e);
+}
+
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void aba_vjp_env(const Tab& T, const VjpArgs& a, const int64_t e) {
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const RuntimeTab T{model};
   const int nv = T.nv(), nq = T.nq_ext();
   double q[MAXQ], qd[MAXV], tau[MAXV], qb[MAXV], qdd[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
@@ -65,6 +66,13 @@ __global__ void __launch_bounds__(32) aba_vjp_kernel(const DModel* __restrict__ 
   if (a.o1.p) store_row(a.o1, e, nv, o1);
   if (a.o2.p) store_row(a.o2, e, nv, o2);
   if (a.o3.p) store_row(a.o3, e, nv, lam);
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) aba_vjp_kernel(const DModel* __restrict__ model, const VjpArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  aba_vjp_env<MAXJ>(RuntimeTab{model}, a, e);
 }
 
 // Link pose adjoint: a link at p with rotation R receives the world force

@@ -93,6 +93,9 @@ Api& api() {
 std::mutex g_mu;
 int g_enable = -1;  // -1: read SGDYN_JIT on first use
 int64_t g_min_n = 2048;
+// Trees above this many joints (incl. the universe) keep the generic kernels: fully
+// unrolled sweeps of large trees overflow the instruction cache and spill, and ran slower.
+int g_max_joints = 16;
 std::map<std::string, CUfunction> g_functions;  // key: source hash + device
 std::map<std::string, std::string> g_failed;    // key -> reason
 // fast path: (model uid, table version, ops, device) -> kernel, so a launch does no string work
@@ -104,6 +107,7 @@ void read_env_config() {
   const char* e = std::getenv("SGDYN_JIT");
   g_enable = (e && std::strcmp(e, "0") == 0) ? 0 : 1;
   if (const char* m = std::getenv("SGDYN_JIT_MIN_N")) g_min_n = std::atoll(m);
+  if (const char* m = std::getenv("SGDYN_JIT_MAX_JOINTS")) g_max_joints = std::atoi(m);
 }
 
 const char* const kNvrtcOptions[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
@@ -133,8 +137,11 @@ std::string list(It b, It e) {
 
 // The rollout's backward kernels stay generic: specialised, they came out slower (the
 // fully unrolled reverse sweep spills heavily).
-enum JitKind { JIT_STEP = 0, JIT_ROLLOUT_FWD = 1 };
-const char* kernel_name(int kind) { return kind == JIT_STEP ? "sgjit_step" : "sgjit_rollout_forward"; }
+enum JitKind { JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_RNEA_VJP = 2, JIT_ABA_VJP = 3 };
+const char* kernel_name(int kind) {
+  static const char* const names[] = {"sgjit_step", "sgjit_rollout_forward", "sgjit_rnea_vjp", "sgjit_aba_vjp"};
+  return names[kind];
+}
 
 std::string generate_source(const Model& M, int kind, int ops) {
   const auto& t = M.host_table();
@@ -165,12 +172,14 @@ std::string generate_source(const Model& M, int kind, int ops) {
   o << "};\n}  // namespace sgjit\n";
   const std::string tab = "sgdyn::StaticTab<" + std::to_string(nj) + ", " + std::to_string(hdr->nv) + ", " +
                           std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM>()";
-  const char* args = kind == JIT_STEP ? "sgdyn::StepArgs" : "sgdyn::RolloutArgs";
+  const char* args = kind == JIT_STEP ? "sgdyn::StepArgs" : kind == JIT_ROLLOUT_FWD ? "sgdyn::RolloutArgs" : "sgdyn::VjpArgs";
   o << "extern \"C\" __global__ void __launch_bounds__(32) " << kernel_name(kind) << "(const " << args << " a) {\n"
     << "  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
     << "  if (e >= a.n) return;\n";
   if (kind == JIT_STEP) o << "  sgdyn::step_env_t<" << nj << ", " << ops << ">(" << tab << ", a, e);\n}\n";
-  else o << "  sgdyn::rollout_forward_env<" << nj << ">(" << tab << ", a, e);\n}\n";
+  else if (kind == JIT_ROLLOUT_FWD) o << "  sgdyn::rollout_forward_env<" << nj << ">(" << tab << ", a, e);\n}\n";
+  else if (kind == JIT_RNEA_VJP) o << "  sgdyn::rnea_vjp_env<" << nj << ">(" << tab << ", a, e);\n}\n";
+  else o << "  sgdyn::aba_vjp_env<" << nj << ">(" << tab << ", a, e);\n}\n";
   return o.str();
 }
 
@@ -321,6 +330,13 @@ void get_jit_config(int* enable, int64_t* min_n) {
   if (min_n) *min_n = g_min_n;
 }
 
+void jit_max_joints(int max_joints, int* out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  if (max_joints >= 0) g_max_joints = max_joints;
+  if (out) *out = g_max_joints;
+}
+
 bool prepare_step_jit(Model& M, int ops, std::string* why) {
   std::lock_guard<std::mutex> lk(g_mu);
   read_env_config();
@@ -348,6 +364,10 @@ bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std:
       *why = "batch below the run-time compilation threshold";
       return false;
     }
+    if (M.njoints() > g_max_joints) {
+      *why = "tree above the run-time compilation size limit";
+      return false;
+    }
     fn = get_function(M, kind, ops, why);
   }
   if (!fn) return false;
@@ -369,6 +389,18 @@ bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::
 
 bool launch_rollout_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why) {
   return launch_jit(M, JIT_ROLLOUT_FWD, 0, a, s, why);
+}
+
+bool launch_vjp_jit(Model& M, bool aba, const VjpArgs& a, cudaStream_t s, std::string* why) {
+  return launch_jit(M, aba ? JIT_ABA_VJP : JIT_RNEA_VJP, 0, a, s, why);
+}
+
+std::string vjp_jit_source(const Model& M, bool aba) { return generate_source(M, aba ? JIT_ABA_VJP : JIT_RNEA_VJP, 0); }
+
+bool prepare_vjp_jit(Model& M, bool aba, std::string* why) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  return get_function(M, aba ? JIT_ABA_VJP : JIT_RNEA_VJP, 0, why) != nullptr;
 }
 
 }  // namespace sgdyn

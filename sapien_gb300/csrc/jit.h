@@ -15,6 +15,10 @@ class Model;
 // the batch is large enough; returns false (with the reason) when the caller should use the
 // generic kernel. Compiles and caches on first use of (model tables, ops, device).
 bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why);
+// Same for the RNEA / ABA vector-Jacobian product kernels.
+bool launch_vjp_jit(Model& M, bool aba, const VjpArgs& a, cudaStream_t s, std::string* why);
+std::string vjp_jit_source(const Model& M, bool aba);
+bool prepare_vjp_jit(Model& M, bool aba, std::string* why);
 // Same for the forward rollout kernel.
 bool launch_rollout_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why);
 std::string rollout_jit_source(const Model& M);
@@ -25,5 +29,7 @@ void set_jit_config(int enable, int64_t min_n);
 // The generated translation unit (for inspection and tests).
 std::string step_jit_source(const Model& M, int ops);
 void get_jit_config(int* enable, int64_t* min_n);
+// Size limit (joints incl. the universe) for run-time specialisation; < 0 leaves it.
+void jit_max_joints(int max_joints, int* out);
 
 }  // namespace sgdyn

@@ -15,6 +15,7 @@ cudaError_t launch_step_j64(const DModel* dm, int ops, const StepArgs& a, cudaSt
     SG_CASE(OP_RNEA)
     SG_CASE(OP_ABA)
     SG_CASE(OP_RNEA | OP_ABA)
+    SG_CASE(OP_CRBA | OP_RNEA | OP_ABA)
     SG_CASE(OP_ALL)
 #undef SG_CASE
     default: return cudaErrorInvalidValue;
@@ -36,6 +37,7 @@ cudaError_t launch_step_team_j64(const DModel* dm, const int* team, int lanes, i
     SG_CASE(OP_RNEA)
     SG_CASE(OP_ABA)
     SG_CASE(OP_RNEA | OP_ABA)
+    SG_CASE(OP_CRBA | OP_RNEA | OP_ABA)
     SG_CASE(OP_ALL)
 #undef SG_CASE
     default: return cudaErrorInvalidValue;

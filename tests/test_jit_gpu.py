@@ -18,6 +18,15 @@ def jit_config(enable, min_n):
     return e.value, m.value
 
 
+@pytest.fixture(autouse=True)
+def any_tree_size():
+    """Specialise trees of every size here (the default limit keeps large trees generic)."""
+    old = ctypes.c_int()
+    N.check(N.load().sgdyn_jit_max_joints(64, ctypes.byref(old)))
+    yield
+    N.check(N.load().sgdyn_jit_max_joints(old.value, None))
+
+
 def rel_per_env(g, o):
     g = g.reshape(g.shape[0], -1)
     o = o.reshape(o.shape[0], -1)
@@ -97,3 +106,35 @@ def test_specialised_rollout_matches_generic(name):
     for a, b in zip(spec, gen):
         a2, b2 = a.reshape(-1, a.shape[-1]), b.reshape(-1, b.shape[-1])
         assert rel_per_env(a2, b2) <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["arm9", "humanoid"])
+def test_specialised_vjp_matches_generic(name):
+    """RNEA / ABA vector-Jacobian products: the model-specialised kernels reproduce the
+    generic ones (same operations, tables folded to constants)."""
+    import torch
+
+    from sapien_gb300 import autodiff as AD
+
+    robot = {"arm9": syn.arm_with_fingers(), "humanoid": syn.humanoid()}[name]
+    pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    q, qd, qdd, tau = (torch.from_numpy(a).cuda() for a in robot.sample(64, seed=7))
+
+    def run():
+        r = AD.inverse_dynamics_vjp(pm, q, qd, qdd, tau) + AD.forward_dynamics_vjp(pm, q, qd, tau, qdd)
+        return [x.cpu().numpy() for x in r if x is not None]
+
+    old = jit_config(-1, -1)
+    try:
+        jit_config(0, -1)
+        gen = run()
+        jit_config(1, 0)
+        for kind in (-2, -3):
+            assert N.load().sgdyn_jit_prepare(pm._h, kind) == 0, N.last_error()
+        spec = run()
+    finally:
+        jit_config(*old)
+    for a, b in zip(spec, gen):
+        assert rel_per_env(a, b) <= 1e-13
