@@ -233,14 +233,40 @@ def secondary_workloads(dev):
                                  "RNEA+ABA+CRBA; CUDA-graph replay of 10 steps",
                      "env_steps_per_s": 8192 / (hms * 1e-3), "ms_per_step": hms, "launch_shape": list(shape),
                      "lanes_per_env": list(hb.lanes)}
+    # a whole heterogeneous rollout (ABA + semi-implicit Euler, free flyers on SE(3)) as one graph
+    rq, rqd, rtau = hq.clone(), hqd.clone(), 0.1 * htau
+    rg = hb.capture_rollout(rq, rqd, rtau, 1.0 / 500, 100)
+    rms = _event_ms(torch, rg.replay, reps=3, warm=1) / 100
+    out["hetero_rollout"] = {"workload": "same 8192-robot mix, 100 semi-implicit-Euler steps (ABA + integrate) "
+                                         "captured as one CUDA graph, dt=1/500",
+                             "env_steps_per_s": 8192 / (rms * 1e-3), "ms_per_step": rms}
     nik = 65536
     qik, _, _, _ = arm.sample(nik, seed=3)
     tgt = pm.compute_forward_kinematics_batched(torch.from_numpy(qik).to(dev))[:, arm.ee_link].contiguous()
     ik_ms = _event_ms(torch, lambda: pm.compute_inverse_kinematics_batched(arm.ee_link, tgt, None, None, eps=0.0,
                                                                            max_iterations=100, dt=0.1, damp=1e-3),
                       reps=3, warm=1)
+    # parity of a sample against the oracle's CLIK (same targets, fixed 100 iterations)
+    from oracle.oracle import Oracle
+
+    q_ik = pm.compute_inverse_kinematics_batched(arm.ee_link, tgt, None, None, eps=0.0, max_iterations=100, dt=0.1,
+                                                 damp=1e-3)[0][:256].cpu().numpy()
+    t7 = tgt[:256].cpu().numpy()
+    t44 = np.zeros((256, 4, 4))
+    w, x, y, z = (t7[:, 3 + k] for k in range(4))
+    t44[:, 0, :3] = np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], 1)
+    t44[:, 1, :3] = np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], 1)
+    t44[:, 2, :3] = np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], 1)
+    t44[:, :3, 3] = t7[:, :3]
+    t44[:, 3, 3] = 1.0
+    o = Oracle(arm.urdf)
+    o.set_joint_order(arm.joint_names)
+    o.set_link_order(arm.link_names)
+    q_ref = o.batch_ik(arm.ee_link, t44, None, eps=0.0, max_iterations=100, dt=0.1, damp=1e-3, nthreads=8)[0]
+    ik_err = float((np.abs(q_ik - q_ref).max(axis=1) / np.maximum(np.abs(q_ref).max(axis=1), 1e-300)).max())
     out["ik"] = {"workload": "arm9 CLIK, 65536 FK targets, 100 iterations, damping 1e-3",
-                 "solves_per_s": nik / (ik_ms * 1e-3), "ms": ik_ms}
+                 "solves_per_s": nik / (ik_ms * 1e-3), "ms": ik_ms,
+                 "max_rel_err_vs_oracle": ik_err, "err_sample": "first 256 targets, joint positions"}
     hum = synthetic.humanoid()
     hm = model_of(hum)
     hq2, hqd2, hqdd2, htau2 = (torch.from_numpy(a).to(dev) for a in hum.sample(8192, seed=0))

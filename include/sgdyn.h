@@ -220,6 +220,11 @@ int sgdyn_batch_set_launch(sgdyn_batch* b, int ctas_per_sm, int warps_per_cta, i
 int sgdyn_batch_set_lanes(sgdyn_batch* b, const int* lanes_per_model);
 int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
                      double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream);
+/* Semi-implicit Euler on the batch's padded rows, in place: qd += dt qdd, then q advanced
+ * by dt qd with each environment's model (angles and slides add; a free flyer moves on
+ * SE(3) by its body twist, like Pinocchio's integrate). With sgdyn_batch_step (ABA) this
+ * makes one rollout step; both launches can be captured into one CUDA graph. */
+int sgdyn_batch_integrate(sgdyn_batch* b, double dt, double* q, double* qd, const double* qdd, void* stream);
 
 /* ---- differentiation (additions; the reference has no derivative API, see
  * pinocchio/cmake/pinocchio.cmake:4 which builds Pinocchio without autodiff) ----------

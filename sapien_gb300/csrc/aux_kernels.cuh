@@ -369,22 +369,9 @@ __device__ __forceinline__ void ik_env(const DModel* __restrict__ model, const I
           qs[i][1] = ns * k;
           break;
         }
-        case JK_FREEFLYER: {
-          const M3 R0 = quat_to_R(qs[i][3], qs[i][4], qs[i][5], qs[i][6]);
-          M3 dR;
-          V3 dp;
-          exp6(Mot{mk(vv[0], vv[1], vv[2]), mk(vv[3], vv[4], vv[5])}, dR, dp);
-          const M3 R1 = mul(R0, dR);
-          const V3 p1 = mul_add(R0, dp, mk(qs[i][0], qs[i][1], qs[i][2]));
-          double qw[4];
-          R_to_quat(R1, qw);  // w x y z
-          const double dq = qw[1] * qs[i][3] + qw[2] * qs[i][4] + qw[3] * qs[i][5] + qw[0] * qs[i][6];
-          const double sg = dq < 0 ? -1.0 : 1.0;
-          const double n = sqrt(qw[0] * qw[0] + qw[1] * qw[1] + qw[2] * qw[2] + qw[3] * qw[3]);
-          qs[i][0] = p1.x; qs[i][1] = p1.y; qs[i][2] = p1.z;
-          qs[i][3] = sg * qw[1] / n; qs[i][4] = sg * qw[2] / n; qs[i][5] = sg * qw[3] / n; qs[i][6] = sg * qw[0] / n;
+        case JK_FREEFLYER:
+          free_flyer_integrate(qs[i], vv);
           break;
-        }
         default: qs[i][0] += vv[0];
       }
     }

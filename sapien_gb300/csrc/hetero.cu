@@ -22,6 +22,7 @@
 
 #include "../../include/sgdyn.h"
 #include "model.h"
+#include "se3.cuh"
 #include "step_kernel.cuh"
 
 struct sgdyn_model {
@@ -68,6 +69,42 @@ __global__ void hetero_kernel(const HeteroArgs a) {
   }
 }
 
+// Semi-implicit Euler on padded env-major rows: qd += dt qdd, then q (+)= dt qd with each
+// environment's own model (angles and slides add; a free flyer moves on SE(3) by its body
+// twist).
+struct HeteroIntegrateArgs {
+  const unsigned char* tables;
+  const int64_t* table_offset;
+  const int* model_of_env;
+  int64_t n;
+  int max_nq, max_nv;
+  double dt;
+  double* q;
+  double* qd;
+  const double* qdd;
+};
+
+__global__ void __launch_bounds__(128) hetero_integrate_kernel(const HeteroIntegrateArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  const DModel* m = reinterpret_cast<const DModel*>(a.tables + a.table_offset[a.model_of_env[e]]);
+  const DJoint* JT = model_joints(m);
+  double* q = a.q + e * a.max_nq;
+  double* qd = a.qd + e * a.max_nv;
+  const double* qdd = a.qdd + e * a.max_nv;
+  for (int c = 0; c < m->nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
+  for (int i = 1; i < m->nj; i++) {
+    const DJoint& J = JT[i];
+    if (J.kind == JK_FREEFLYER) {
+      double v[6];
+      for (int k = 0; k < 6; k++) v[k] = a.dt * qd[J.vcol + k];
+      free_flyer_integrate(q + J.qcol, v);
+    } else {
+      q[J.qcol] = fma(a.dt, qd[J.vcol], q[J.qcol]);
+    }
+  }
+}
+
 template <int MAXJ>
 cudaError_t launch_hetero_bucket(int ops, const HeteroArgs& a, dim3 grid, dim3 block, cudaStream_t s) {
   switch (ops) {
@@ -100,6 +137,7 @@ struct sgdyn_batch {
   int64_t* offsets = nullptr;
   int* teams = nullptr;
   int64_t* team_offsets = nullptr;
+  int* model_of_env_dev = nullptr;
   int* perm = nullptr;
   int4* tiles = nullptr;
   int ntiles = 0;
@@ -117,8 +155,10 @@ void free_device(sgdyn_batch* b) {
   cudaFree(b->offsets);
   cudaFree(b->teams);
   cudaFree(b->team_offsets);
+  cudaFree(b->model_of_env_dev);
   b->teams = nullptr;
   b->team_offsets = nullptr;
+  b->model_of_env_dev = nullptr;
   cudaFree(b->perm);
   cudaFree(b->tiles);
   cudaFree(b->head);
@@ -264,6 +304,9 @@ int sgdyn_batch_create(const sgdyn_model* const* models, int nmodels, const int*
       cudaMalloc(&b->head, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemcpy(b->tables, packed.data(), packed.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->offsets, offs.data(), sizeof(int64_t) * offs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMalloc(&b->model_of_env_dev, sizeof(int) * std::max<int64_t>(n, 1)) != cudaSuccess ||
+      (n > 0 && cudaMemcpy(b->model_of_env_dev, b->model_of_env.data(), sizeof(int) * n, cudaMemcpyHostToDevice) !=
+                    cudaSuccess) ||
       upload_teams(b) != SGDYN_OK || upload_plan(b) != SGDYN_OK) {
     free_device(b);
     delete b;
@@ -310,6 +353,29 @@ int sgdyn_batch_set_lanes(sgdyn_batch* b, const int* lanes_per_model) {
   b->lanes.assign(lanes_per_model, lanes_per_model + b->models.size());
   if (upload_teams(b) != SGDYN_OK || upload_plan(b) != SGDYN_OK)
     return set_last_error(SGDYN_ERR_CUDA, "team / plan upload failed");
+  return SGDYN_OK;
+}
+
+int sgdyn_batch_integrate(sgdyn_batch* b, double dt, double* q, double* qd, const double* qdd, void* stream) {
+  if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
+  if (b->n == 0) return SGDYN_OK;
+  if (!dev_ptr(q) || !dev_ptr(qd) || !dev_ptr(qdd))
+    return set_last_error(SGDYN_ERR_NULL, "q / qd / qdd is null or not device memory");
+  if (!b->model_of_env_dev) return set_last_error(SGDYN_ERR_RUNTIME, "batch has no environment table");
+  HeteroIntegrateArgs a;
+  a.tables = b->tables;
+  a.table_offset = b->offsets;
+  a.model_of_env = b->model_of_env_dev;
+  a.n = b->n;
+  a.max_nq = b->max_nq;
+  a.max_nv = b->max_nv;
+  a.dt = dt;
+  a.q = q;
+  a.qd = qd;
+  a.qdd = qdd;
+  hetero_integrate_kernel<<<unsigned((b->n + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   return SGDYN_OK;
 }
 

@@ -151,6 +151,30 @@ __device__ __forceinline__ void exp6(Mot nu, M3& R, V3& p) {
   p = mul(V, nu.v);
 }
 
+// Free-flyer configuration q = (x y z qx qy qz qw) advanced by the body twist v (linear,
+// angular): (R, p) <- (R, p) exp6(v) (Pinocchio's integrate), the new quaternion taken on
+// the same hemisphere as the old one and renormalised. In place.
+__device__ __forceinline__ void free_flyer_integrate(double* q, const double* v) {
+  const M3 R0 = quat_to_R(q[3], q[4], q[5], q[6]);
+  M3 dR;
+  V3 dp;
+  exp6(Mot{mk(v[0], v[1], v[2]), mk(v[3], v[4], v[5])}, dR, dp);
+  const M3 R1 = mul(R0, dR);
+  const V3 p1 = mul_add(R0, dp, mk(q[0], q[1], q[2]));
+  double qw[4];
+  R_to_quat(R1, qw);  // w x y z
+  const double dq = qw[1] * q[3] + qw[2] * q[4] + qw[3] * q[5] + qw[0] * q[6];
+  const double sg = dq < 0 ? -1.0 : 1.0;
+  const double n = sqrt(qw[0] * qw[0] + qw[1] * qw[1] + qw[2] * qw[2] + qw[3] * qw[3]);
+  q[0] = p1.x;
+  q[1] = p1.y;
+  q[2] = p1.z;
+  q[3] = sg * qw[1] / n;
+  q[4] = sg * qw[2] / n;
+  q[5] = sg * qw[3] / n;
+  q[6] = sg * qw[0] / n;
+}
+
 // Jlog6 of (R, p) as a dense 6x6, row-major, (linear, angular) ordering.
 __device__ __forceinline__ void jlog6(const M3& R, V3 p, double* J) {
   Mot xi = log6(R, p);

@@ -130,6 +130,39 @@ class HeteroBatch:
                 ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
         return out
 
+    def integrate(self, q, qd, qdd, dt):
+        """Semi-implicit Euler in place on padded rows: qd += dt qdd, then q advanced by
+        dt qd with each environment's model (free flyers on SE(3) by their body twist)."""
+        with torch.cuda.device(self.device):
+            N.check(N.load().sgdyn_batch_integrate(self._h, float(dt), _p(q), _p(qd), _p(qdd),
+                                                   ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
+
+    def rollout_step(self, q, qd, tau, dt, out):
+        """One rollout step in place: qdd = ABA(q, qd, tau) into out["qacc"], then integrate."""
+        self.step(q, qd, None, tau, N.OP_FORWARD_DYNAMICS, out)
+        self.integrate(q, qd, out["qacc"], dt)
+
+    def capture_rollout(self, q, qd, tau, dt, steps):
+        """Record a whole rollout of `steps` semi-implicit-Euler steps (ABA + integrate per
+        step, q / qd updated in place, tau held) into one torch CUDA graph. Replaying it
+        advances q and qd by `steps` steps."""
+        out = self.alloc_outputs(N.OP_FORWARD_DYNAMICS)
+        q0, qd0 = q.clone(), qd.clone()
+        self.rollout_step(q, qd, tau, dt, out)  # warm-up outside the capture
+        torch.cuda.synchronize(self.device)
+        q.copy_(q0)
+        qd.copy_(qd0)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(steps):
+                    self.rollout_step(q, qd, tau, dt, out)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        g.outputs = out
+        return g
+
     def capture(self, q, qd, qdd, tau, steps=1, ops=OPS_DYNAMICS, out=None):
         """Record `steps` consecutive batch steps into a torch CUDA graph (returned with the
         output buffers it writes as graph.outputs)."""
