@@ -166,6 +166,10 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
  * lane each, which shortens a wide tree's sequential sweep; worth it when the batch leaves
  * the GPU's FP64 schedulers idle (automatic: only then, and only if the tree splits). */
 int sgdyn_model_set_lanes(sgdyn_model* m, int lanes);
+/* The team table the kernels use for `lanes` lanes per environment (ints: L, trunk count,
+ * longest lane, attach count, trunk joints, per-lane joints padded with 0, attach joints,
+ * owner per joint (-1 = trunk)); valid until the next call on this thread. */
+int sgdyn_model_team_table(const sgdyn_model* m, int lanes, const int** data, int* count);
 
 /* Run-time specialisation (addition). The fused sweep behind sgdyn_step and the five
  * single-op entry points, the forward rollout kernel and the RNEA / ABA vector-Jacobian

@@ -69,6 +69,7 @@ EXPORTED = (
     "sgdyn_batch_step",
     "sgdyn_batch_integrate",
     "sgdyn_model_set_lanes",
+    "sgdyn_model_team_table",
     "sgdyn_jit_max_joints",
     "sgdyn_jit_config",
     "sgdyn_jit_prepare",
@@ -141,6 +142,7 @@ def load():
     L.sgdyn_compute_passive_force_f32.argtypes = [vp, i64, vp, vp, i64, i32, i32, vp, i64, vp]
     L.sgdyn_jit_config.argtypes = [i32, i64, P(i32), P(i64)]
     L.sgdyn_model_set_lanes.argtypes = [vp, i32]
+    L.sgdyn_model_team_table.argtypes = [vp, i32, P(P(i32)), P(i32)]
     L.sgdyn_jit_max_joints.argtypes = [i32, P(i32)]
     L.sgdyn_jit_prepare.argtypes = [vp, i32]
     L.sgdyn_jit_source.argtypes = [vp, i32, P(ctypes.c_char_p)]

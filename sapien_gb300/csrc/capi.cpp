@@ -331,6 +331,17 @@ int sgdyn_model_table(const sgdyn_model* m, const void** data, int64_t* bytes) {
   return SGDYN_OK;
 }
 
+int sgdyn_model_team_table(const sgdyn_model* m, int lanes, const int** data, int* count) {
+  if (int rc = check_model(m)) return rc;
+  if (!data || !count) return fail(SGDYN_ERR_NULL, "null argument");
+  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8) return fail(SGDYN_ERR_RUNTIME, "lanes must be 1, 2, 4 or 8");
+  thread_local std::vector<int> buf;
+  buf = m->impl->team_table(lanes);
+  *data = buf.data();
+  *count = int(buf.size());
+  return SGDYN_OK;
+}
+
 int sgdyn_jit_max_joints(int max_joints, int* max_joints_out) {
   jit_max_joints(max_joints, max_joints_out);
   return SGDYN_OK;
