@@ -220,7 +220,8 @@ int sgdyn_batch_set_launch(sgdyn_batch* b, int ctas_per_sm, int warps_per_cta, i
 /* Threads per environment, per model (1, 2, 4 or 8; default 1). With L > 1 a team of L
  * lanes shares an environment: the joints near the root (trunk) run on every lane and the
  * subtrees hanging off them on one lane each, so a wide tree's sequential sweep gets
- * shorter at the price of more lanes. Chosen by sapien_gb300.autotune. */
+ * shorter at the price of more lanes. Chosen by sapien_gb300.autotune. Re-plans the batch
+ * (allocates): not while a stream of the batch's device is being captured. */
 int sgdyn_batch_set_lanes(sgdyn_batch* b, const int* lanes_per_model);
 int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
                      double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream);
