@@ -40,7 +40,7 @@ WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs p
 # summarised in profiles/step_kernel_arm9.md, for the model-specialised kernel (run-time
 # compiled) and the generic one.
 KERNEL_COUNTERS = {
-    "specialised": {"fp64_inst_per_env": 5024, "dram_bytes_per_env": 19.47e6 / 16384},
+    "specialised": {"fp64_inst_per_env": 5100, "dram_bytes_per_env": 34.79e6 / 16384},
     "generic": {"fp64_inst_per_env": 5047, "dram_bytes_per_env": 124.6e6 / 16384},
 }
 
