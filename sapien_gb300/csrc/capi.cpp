@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/sgdyn.h"
+#include "trace.h"
 #include "jit.h"
 #include "kernels.h"
 #include "model.h"
@@ -387,6 +388,7 @@ int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
 
 int sgdyn_compute_forward_kinematics(const sgdyn_model* m, int64_t n, const double* q, double* link_poses,
                                      int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_forward_kinematics");
   return guarded([&] {
     return run_step(m, n, OP_FK, q, nullptr, nullptr, nullptr, link_poses, nullptr, nullptr, nullptr, nullptr, layout,
                     stream);
@@ -395,6 +397,7 @@ int sgdyn_compute_forward_kinematics(const sgdyn_model* m, int64_t n, const doub
 
 int sgdyn_compute_full_jacobian(const sgdyn_model* m, int64_t n, const double* q, double* J, int layout,
                                 void* stream) {
+  SG_TRACE("sgdyn_compute_full_jacobian");
   return guarded([&] {
     return run_step(m, n, OP_JAC, q, nullptr, nullptr, nullptr, nullptr, J, nullptr, nullptr, nullptr, layout, stream);
   });
@@ -402,6 +405,7 @@ int sgdyn_compute_full_jacobian(const sgdyn_model* m, int64_t n, const double* q
 
 int sgdyn_compute_generalized_mass_matrix(const sgdyn_model* m, int64_t n, const double* q, double* M, int layout,
                                           void* stream) {
+  SG_TRACE("sgdyn_compute_generalized_mass_matrix");
   return guarded([&] {
     return run_step(m, n, OP_CRBA, q, nullptr, nullptr, nullptr, nullptr, nullptr, M, nullptr, nullptr, layout,
                     stream);
@@ -410,6 +414,7 @@ int sgdyn_compute_generalized_mass_matrix(const sgdyn_model* m, int64_t n, const
 
 int sgdyn_compute_inverse_dynamics(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                    const double* qdd, double* tau, int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_inverse_dynamics");
   return guarded([&] {
     return run_step(m, n, OP_RNEA, q, qd, qdd, nullptr, nullptr, nullptr, nullptr, tau, nullptr, layout, stream);
   });
@@ -417,6 +422,7 @@ int sgdyn_compute_inverse_dynamics(const sgdyn_model* m, int64_t n, const double
 
 int sgdyn_compute_forward_dynamics(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                    const double* tau, double* qdd, int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_forward_dynamics");
   return guarded([&] {
     return run_step(m, n, OP_ABA, q, qd, nullptr, tau, nullptr, nullptr, nullptr, nullptr, qdd, layout, stream);
   });
@@ -425,6 +431,7 @@ int sgdyn_compute_forward_dynamics(const sgdyn_model* m, int64_t n, const double
 int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const double* qd, const double* qdd,
                const double* tau, double* link_poses, double* J, double* M, double* tau_out, double* qdd_out,
                int layout, void* stream) {
+  SG_TRACE("sgdyn_step");
   return guarded([&] {
     return run_step(m, n, ops, q, qd, qdd, tau, link_poses, J, M, tau_out, qdd_out, layout, stream);
   });
@@ -432,6 +439,7 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
 
 int sgdyn_compute_link_jacobian(const sgdyn_model* m, int64_t n, int link, int local, const double* q, double* J,
                                 int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_link_jacobian");
   return guarded([&] {
     if (int rc = check_model(m)) return rc;
     Model& Mo = *m->impl;
@@ -457,11 +465,13 @@ int sgdyn_compute_link_jacobian(const sgdyn_model* m, int64_t n, int link, int l
 
 int sgdyn_compute_single_link_local_jacobian(const sgdyn_model* m, int64_t n, int link, const double* q, double* J,
                                              int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_single_link_local_jacobian");
   return sgdyn_compute_link_jacobian(m, n, link, 1, q, J, layout, stream);
 }
 
 int sgdyn_compute_coriolis_matrix(const sgdyn_model* m, int64_t n, const double* q, const double* qd, double* C,
                                   int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_coriolis_matrix");
   return guarded([&] {
     if (int rc = check_model(m)) return rc;
     Model& Mo = *m->impl;
@@ -487,6 +497,7 @@ int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, 
                                      const double* q0, const int* mask, double eps, int max_iterations, double dt,
                                      double damp, double* q_out, int* success, double* err_out, int layout,
                                      void* stream) {
+  SG_TRACE("sgdyn_compute_inverse_kinematics");
   return guarded([&] {
     if (int rc = check_model(m)) return rc;
     Model& Mo = *m->impl;
@@ -528,6 +539,7 @@ int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, 
 int sgdyn_compute_inverse_dynamics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                        const double* qdd, const double* tau_bar, double* q_bar, double* qd_bar,
                                        double* qdd_bar, int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_inverse_dynamics_vjp");
   return guarded([&] {
     if (int rc = check_diff_model(m)) return rc;
     if (int rc = common_checks(n, layout)) return rc;
@@ -558,6 +570,7 @@ int sgdyn_compute_inverse_dynamics_vjp(const sgdyn_model* m, int64_t n, const do
 int sgdyn_compute_forward_dynamics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                        const double* tau, const double* qdd_bar, double* q_bar, double* qd_bar,
                                        double* tau_bar, int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_forward_dynamics_vjp");
   return guarded([&] {
     if (int rc = check_diff_model(m)) return rc;
     if (int rc = common_checks(n, layout)) return rc;
@@ -587,6 +600,7 @@ int sgdyn_compute_forward_dynamics_vjp(const sgdyn_model* m, int64_t n, const do
 
 int sgdyn_compute_forward_kinematics_vjp(const sgdyn_model* m, int64_t n, const double* q, const double* pos_bar,
                                          const double* rot_bar, double* q_bar, int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_forward_kinematics_vjp");
   return guarded([&] {
     if (int rc = check_diff_model(m)) return rc;
     if (int rc = common_checks(n, layout)) return rc;
@@ -648,12 +662,14 @@ static int derivatives(bool aba, const sgdyn_model* m, int64_t n, const double* 
 int sgdyn_compute_rnea_derivatives(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                    const double* qdd, double* dtau_dq, double* dtau_dqd, double* dtau_dqdd,
                                    int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_rnea_derivatives");
   return derivatives(false, m, n, q, qd, qdd, dtau_dq, dtau_dqd, dtau_dqdd, layout, stream);
 }
 
 int sgdyn_compute_aba_derivatives(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                   const double* tau, double* dqdd_dq, double* dqdd_dqd, double* dqdd_dtau,
                                   int layout, void* stream) {
+  SG_TRACE("sgdyn_compute_aba_derivatives");
   return derivatives(true, m, n, q, qd, tau, dqdd_dq, dqdd_dqd, dqdd_dtau, layout, stream);
 }
 
@@ -668,6 +684,7 @@ static int rollout_checks(const sgdyn_model* m, int64_t n, int T, int K) {
 int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, const double* q0, const double* qd0,
                           const double* tau, int checkpoint_every, double* q_ckpt, double* qd_ckpt, double* qT,
                           double* qdT, void* stream) {
+  SG_TRACE("sgdyn_rollout_forward");
   return guarded([&] {
     if (int rc = rollout_checks(m, n, T, checkpoint_every)) return rc;
     if (n == 0) return SGDYN_OK;
@@ -706,6 +723,7 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
                            const double* q_ckpt, const double* qd_ckpt, const double* tau, const double* qT_bar,
                            const double* qdT_bar, double* q0_bar, double* qd0_bar, double* tau_bar, double* scratch,
                            int64_t scratch_bytes, void* stream) {
+  SG_TRACE("sgdyn_rollout_backward");
   return guarded([&] {
     if (int rc = rollout_checks(m, n, T, checkpoint_every)) return rc;
     if (n == 0) return SGDYN_OK;

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/sgdyn.h"
+#include "trace.h"
 #include "model.h"
 #include "se3.cuh"
 #include "step_kernel.cuh"
@@ -357,6 +358,7 @@ int sgdyn_batch_set_lanes(sgdyn_batch* b, const int* lanes_per_model) {
 }
 
 int sgdyn_batch_integrate(sgdyn_batch* b, double dt, double* q, double* qd, const double* qdd, void* stream) {
+  SG_TRACE("sgdyn_batch_integrate");
   if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
   if (b->n == 0) return SGDYN_OK;
   if (!dev_ptr(q) || !dev_ptr(qd) || !dev_ptr(qdd))
@@ -381,6 +383,7 @@ int sgdyn_batch_integrate(sgdyn_batch* b, double dt, double* q, double* qd, cons
 
 int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
                      double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream) {
+  SG_TRACE("sgdyn_batch_step");
   if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
   if (b->n == 0) return SGDYN_OK;
   if (!dev_ptr(q)) return set_last_error(SGDYN_ERR_NULL, "q is null or not device memory");

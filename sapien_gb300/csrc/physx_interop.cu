@@ -14,6 +14,7 @@
 #include <string>
 
 #include "../../include/sgdyn.h"
+#include "trace.h"
 #include "model.h"
 #include "step_kernel.cuh"
 
@@ -83,6 +84,7 @@ using namespace sgdyn;
 extern "C" int sgdyn_compute_passive_force_f32(const sgdyn_model* m, int64_t n, const float* qpos, const float* qvel,
                                                int64_t in_stride, int gravity, int coriolis_and_centrifugal,
                                                float* qf, int64_t out_stride, void* stream) {
+  SG_TRACE("sgdyn_compute_passive_force_f32");
   if (!m || !m->impl) return set_last_error(SGDYN_ERR_NULL, "null model");
   Model& Mo = *m->impl;
   if (Mo.has_free_flyer()) return set_last_error(SGDYN_ERR_UNSUPPORTED, "passive force needs a fixed-base model");

@@ -123,6 +123,34 @@ def test_dynamics_identities(name):
         assert np.abs(C @ qd[e] - (h - g)).max() < 1e-11 * max(1, np.abs(h - g).max())
 
 
+@pytest.mark.parametrize("name", ["chain7", "arm9", "quadruped18", "humanoid30"])
+def test_kinetic_energy_matches_body_sum(name):
+    """1/2 qd^T M qd = sum over bodies of 1/2 v_b^T I_b v_b, with v_b the body's spatial
+    velocity in its own frame from the single-link local Jacobian and I_b its spatial
+    inertia from the URDF (an independent path through the oracle's builder)."""
+    from oracle import urdf_model as um
+
+    robot = ROBOTS[name]()
+    o = _model(robot)
+    om = um.build_model(robot.urdf)
+    q, qd, _, _ = robot.sample(5, seed=12)
+    # the link whose frame is its joint's frame, one per moving joint
+    link_of = {}
+    for li, lname in enumerate(robot.link_names):
+        jid, (R, p) = om.body_frames[lname]
+        if jid > 0 and np.allclose(R, np.eye(3)) and np.allclose(p, 0) and jid not in link_of:
+            link_of[jid] = li
+    assert sorted(link_of) == list(range(1, om.njoints))
+    for e in range(len(q)):
+        M = o.compute_generalized_mass_matrix(q[e])
+        t_m = 0.5 * qd[e] @ M @ qd[e]
+        t_b = 0.0
+        for jid, li in link_of.items():
+            v = o.compute_single_link_local_jacobian(q[e], li) @ qd[e]
+            t_b += 0.5 * v @ om.inertia6[jid] @ v
+        assert abs(t_m - t_b) <= 1e-12 * max(1.0, abs(t_m))
+
+
 @pytest.mark.parametrize("name", ["arm9", "humanoid30", "mixed_chain"])
 def test_coriolis_is_christoffel(name):
     """Mdot = C + C^T (finite differences along qd) and C(q, x) y = C(q, y) x."""
