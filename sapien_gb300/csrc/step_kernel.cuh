@@ -51,12 +51,6 @@ struct StaticTab {
 __device__ __forceinline__ double ldv(const Arr& a, int64_t e, int c) { return a.p[e * a.es + int64_t(c) * a.cs]; }
 __device__ __forceinline__ void stv(const Arr& a, int64_t e, int c, double v) { a.p[e * a.es + int64_t(c) * a.cs] = v; }
 
-// Joint placement composed with the joint motion: (R_li, p_li) and the world pose.
-struct JointFrame {
-  M3 R;
-  V3 p;
-};
-
 // World pose of joint J from its parent's: (Ro, po) = oMi[parent] * placement * M_J(q).
 // A joint in a canonical frame (axis_kind AX_Z) rotates about / slides along z: with
 // B = R_parent R_placement, Ro = B Rz(q) mixes two columns of B and keeps the third. Other
