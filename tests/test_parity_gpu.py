@@ -26,6 +26,10 @@ ROBOTS = {
     "arm6": lambda: syn.serial_chain(6, seed=4),
     "mixed_chain": lambda: syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
                                                                 "continuous", "prismatic"]),
+    # joint-count bucket edges (16 / 32 / 64 joints incl. the universe)
+    "chain15": lambda: syn.serial_chain(15, seed=21),
+    "chain16": lambda: syn.serial_chain(16, seed=22),
+    "chain40": lambda: syn.serial_chain(40, seed=23),
 }
 
 
