@@ -67,6 +67,40 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+class _HostStage:
+    """Pinned host memory mapped into the device address space, for the single-instance
+    calls: the CPU writes the inputs in place, the kernel reads them and writes its results
+    straight into host memory, and one stream synchronisation ends the call (no copy
+    launches, no device allocations per call)."""
+
+    def __init__(self, nq, nv, nl):
+        torch = _torch()
+        sizes = {"q": nq, "qd": nv, "qdd": nv, "tau": nv, "q0": nq, "target": 7, "poses": 7 * max(nl, 1),
+                 "J": 6 * nv, "M": nv * nv, "out_v": nv, "out_q": nq, "err": 6}
+        self.off, total = {}, 0
+        for k, n in sizes.items():
+            self.off[k] = (total, n)
+            total += max(n, 1)
+        self.buf = torch.empty(total, dtype=torch.float64).pin_memory()
+        self.ibuf = torch.empty(nv + 1, dtype=torch.int32).pin_memory()
+        self.np, self.inp = self.buf.numpy(), self.ibuf.numpy()
+        self.key = (nq, nv, nl)
+
+    def put(self, k, a):
+        o, n = self.off[k]
+        self.np[o:o + n] = a
+
+    def get(self, k):
+        o, n = self.off[k]
+        return self.np[o:o + n].copy()
+
+    def p(self, k):
+        return ctypes.c_void_p(self.buf.data_ptr() + 8 * self.off[k][0])
+
+    def ip(self, i):
+        return ctypes.c_void_p(self.ibuf.data_ptr() + 4 * i)
+
+
 class PinocchioModel:
     """GPU-backed replacement of ``sapien.pysapien_pinocchio.PinocchioModel``."""
 
@@ -213,6 +247,24 @@ class PinocchioModel:
         torch = _torch()
         dev = self._dev()
         return [torch.from_numpy(a.reshape(1, -1)).to(dev) for a in arrays]
+
+    def _stage(self):
+        self._dev()  # a clear error without a CUDA device
+        key = (self.nq_ext, self.nv, self._nlinks)
+        st = getattr(self, "_host_stage", None)
+        if st is None or st.key != key:
+            st = self._host_stage = _HostStage(*key)
+        return st
+
+    def _run1(self, fn, *args):
+        """One single-instance C-ABI call on staged host buffers, then wait for it."""
+        torch = _torch()
+        dev = self._dev()
+        self._prepare(dev)
+        with torch.cuda.device(dev):
+            stream = torch.cuda.current_stream(dev)
+            N.check(fn(self._h, *args, ctypes.c_void_p(stream.cuda_stream)))
+            stream.synchronize()
 
     def _check_batch(self, t, cols, what):
         torch = _torch()
@@ -370,9 +422,12 @@ class PinocchioModel:
         """Compute and cache forward kinematics. After computation, use get_link_pose to
         retrieve the computed pose for a specific link."""
         self._require_order()
-        (q,) = self._single(self._vec(qpos, self.nq_ext, "qpos"))
+        q = self._vec(qpos, self.nq_ext, "qpos")
         if self._link_order_set and self._nlinks > 0:
-            self._fk_cache = self.compute_forward_kinematics_batched(q)[0].cpu().numpy()
+            st = self._stage()
+            st.put("q", q)
+            self._run1(N.load().sgdyn_compute_forward_kinematics, 1, st.p("q"), st.p("poses"), N.ENV_MAJOR)
+            self._fk_cache = st.get("poses").reshape(self._nlinks, 7)
         else:
             self._fk_cache = np.zeros((0, 7))
 
@@ -400,38 +455,64 @@ class PinocchioModel:
         self._check_link(link_index)
         if self._jac_q is None:
             raise RuntimeError("compute_full_jacobian must be called before get_link_jacobian")
-        (q,) = self._single(self._jac_q)
-        return self.compute_link_jacobian_batched(q, link_index, local)[0].cpu().numpy()
+        st = self._stage()
+        st.put("q", self._jac_q)
+        self._run1(N.load().sgdyn_compute_link_jacobian, 1, int(link_index), int(bool(local)), st.p("q"), st.p("J"),
+                   N.ENV_MAJOR)
+        return st.get("J").reshape(6, self.nv)
 
     def compute_single_link_local_jacobian(self, qpos, link_index):
         """Compute the link(body) Jacobian for a single link. It is faster than
         compute_full_jacobian followed by get_link_jacobian"""
         self._require_order()
         self._check_link(link_index)
-        (q,) = self._single(self._vec(qpos, self.nq_ext, "qpos"))
-        return self.compute_single_link_local_jacobian_batched(q, link_index)[0].cpu().numpy()
+        q = self._vec(qpos, self.nq_ext, "qpos")
+        st = self._stage()
+        st.put("q", q)
+        self._run1(N.load().sgdyn_compute_single_link_local_jacobian, 1, int(link_index), st.p("q"), st.p("J"),
+                   N.ENV_MAJOR)
+        return st.get("J").reshape(6, self.nv)
 
     def compute_generalized_mass_matrix(self, qpos):
         self._require_order()
-        (q,) = self._single(self._vec(qpos, self.nq_ext, "qpos"))
-        return self.compute_generalized_mass_matrix_batched(q)[0].cpu().numpy()
+        q = self._vec(qpos, self.nq_ext, "qpos")
+        st = self._stage()
+        st.put("q", q)
+        self._run1(N.load().sgdyn_compute_generalized_mass_matrix, 1, st.p("q"), st.p("M"), N.ENV_MAJOR)
+        return st.get("M").reshape(self.nv, self.nv)
 
     def compute_coriolis_matrix(self, qpos, qvel):
         self._require_order()
-        q, qd = self._single(self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"))
-        return self.compute_coriolis_matrix_batched(q, qd)[0].cpu().numpy()
+        q, qd = self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel")
+        st = self._stage()
+        st.put("q", q)
+        st.put("qd", qd)
+        self._run1(N.load().sgdyn_compute_coriolis_matrix, 1, st.p("q"), st.p("qd"), st.p("M"), N.ENV_MAJOR)
+        return st.get("M").reshape(self.nv, self.nv)
 
     def compute_inverse_dynamics(self, qpos, qvel, qacc):
         self._require_order()
-        q, qd, qdd = self._single(self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
-                                  self._vec(qacc, self.nv, "qacc"))
-        return self.compute_inverse_dynamics_batched(q, qd, qdd)[0].cpu().numpy()
+        q, qd, qdd = (self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
+                      self._vec(qacc, self.nv, "qacc"))
+        st = self._stage()
+        st.put("q", q)
+        st.put("qd", qd)
+        st.put("qdd", qdd)
+        self._run1(N.load().sgdyn_compute_inverse_dynamics, 1, st.p("q"), st.p("qd"), st.p("qdd"), st.p("out_v"),
+                   N.ENV_MAJOR)
+        return st.get("out_v")
 
     def compute_forward_dynamics(self, qpos, qvel, qf):
         self._require_order()
-        q, qd, tau = self._single(self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
-                                  self._vec(qf, self.nv, "qf"))
-        return self.compute_forward_dynamics_batched(q, qd, tau)[0].cpu().numpy()
+        q, qd, tau = (self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
+                      self._vec(qf, self.nv, "qf"))
+        st = self._stage()
+        st.put("q", q)
+        st.put("qd", qd)
+        st.put("tau", tau)
+        self._run1(N.load().sgdyn_compute_forward_dynamics, 1, st.p("q"), st.p("qd"), st.p("tau"), st.p("out_v"),
+                   N.ENV_MAJOR)
+        return st.get("out_v")
 
     def compute_inverse_kinematics(self, link_index, pose, initial_qpos=(), active_qmask=(), eps=1e-4,
                                    max_iterations=1000, dt=0.1, damp=1e-6):
@@ -452,14 +533,25 @@ class PinocchioModel:
         """
         self._require_order()
         self._check_link(link_index)
-        torch = _torch()
-        dev = self._dev()
         p = np.asarray(pose.p, dtype=np.float32).astype(np.float64)
         qq = np.asarray(pose.q, dtype=np.float32).astype(np.float64)
-        tgt = torch.from_numpy(np.concatenate([p, qq]).reshape(1, 7)).to(dev)
+        q0v = self._vec(initial_qpos, self.nq_ext, "qpos") if initial_qpos is not None and len(initial_qpos) else None
+        m = None
+        if active_qmask is not None and len(active_qmask):
+            m = np.asarray(active_qmask, dtype=np.int32).reshape(-1)
+            if m.size != self.nv:
+                raise RuntimeError(f"active_qmask must have {self.nv} entries")
+        st = self._stage()
+        st.put("target", np.concatenate([p, qq]))
         q0 = None
-        if initial_qpos is not None and len(initial_qpos):
-            (q0,) = self._single(self._vec(initial_qpos, self.nq_ext, "qpos"))
-        mask = active_qmask if active_qmask is not None and len(active_qmask) else None
-        q, ok, err = self.compute_inverse_kinematics_batched(link_index, tgt, q0, mask, eps, max_iterations, dt, damp)
-        return q[0].cpu().numpy(), bool(ok[0].item()), err[0].cpu().numpy()
+        if q0v is not None:
+            st.put("q0", q0v)
+            q0 = st.p("q0")
+        mask = None
+        if m is not None:
+            st.inp[: self.nv] = m
+            mask = st.ip(0)
+        self._run1(N.load().sgdyn_compute_inverse_kinematics, 1, int(link_index), st.p("target"), q0, mask, float(eps),
+                   int(max_iterations), float(dt), float(damp), st.p("out_q"), st.ip(self.nv), st.p("err"),
+                   N.ENV_MAJOR)
+        return st.get("out_q"), bool(st.inp[self.nv]), st.get("err")
