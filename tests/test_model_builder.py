@@ -203,3 +203,22 @@ def test_xml_reader_tolerates_comments_and_entities():
     pm = PinocchioModel(urdf, [0, 0, -9.81])
     assert pm.joint_names == ["j1"]
     assert pm.nq_ext == 1 and pm.nv == 1
+
+
+def test_lanes_and_run_time_compilation_settings_are_validated():
+    r = syn.arm_with_fingers()
+    pm = PinocchioModel(r.urdf, [0, 0, -9.81])
+    for bad in (3, 16, -1):
+        with pytest.raises(RuntimeError, match="lanes"):
+            pm.set_lanes(bad)
+    for ok in (0, 1, 2, 4, 8):
+        pm.set_lanes(ok)
+    L = N.load()
+    old = ctypes.c_int()
+    assert L.sgdyn_jit_max_joints(-1, ctypes.byref(old)) == N.OK and old.value > 0
+    assert L.sgdyn_jit_max_joints(32, None) == N.OK
+    cur = ctypes.c_int()
+    assert L.sgdyn_jit_max_joints(-1, ctypes.byref(cur)) == N.OK and cur.value == 32
+    assert L.sgdyn_jit_max_joints(old.value, None) == N.OK
+    src = ctypes.c_char_p()
+    assert L.sgdyn_jit_source(pm._h, -4, ctypes.byref(src)) != N.OK  # no such kernel kind
