@@ -72,37 +72,62 @@ __global__ void hetero_kernel(const HeteroArgs a) {
 
 // Semi-implicit Euler on padded env-major rows: qd += dt qdd, then q (+)= dt qd with each
 // environment's own model (angles and slides add; a free flyer moves on SE(3) by its body
-// twist).
+// twist). A block of kIntegrateThreads threads takes 32 consecutive environments, whose
+// padded rows form one contiguous block: its threads walk the flat (environment, joint)
+// pairs, each one-DoF joint updating its velocity and position in one go, and the first
+// warp then moves the free flyers, lane i those of environment i, so the exponential map
+// runs SIMD across environments. Every joint's columns are written by one thread only.
+constexpr int kIntegrateThreads = 128;
+
 struct HeteroIntegrateArgs {
   const unsigned char* tables;
   const int64_t* table_offset;
   const int* model_of_env;
   int64_t n;
-  int max_nq, max_nv;
+  int max_nq, max_nv, joints;  // joints: moving-joint slots per environment (max njoints - 1)
   double dt;
   double* q;
   double* qd;
   const double* qdd;
 };
 
-__global__ void __launch_bounds__(128) hetero_integrate_kernel(const HeteroIntegrateArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
-  const DModel* m = reinterpret_cast<const DModel*>(a.tables + a.table_offset[a.model_of_env[e]]);
+__global__ void __launch_bounds__(kIntegrateThreads) hetero_integrate_kernel(const HeteroIntegrateArgs a) {
+  __shared__ const DModel* models[32];
+  const int64_t e0 = int64_t(blockIdx.x) * 32;
+  const int envs = a.n - e0 < 32 ? int(a.n - e0) : 32;
+  if (threadIdx.x < envs)
+    models[threadIdx.x] = reinterpret_cast<const DModel*>(a.tables + a.table_offset[a.model_of_env[e0 + threadIdx.x]]);
+  __syncthreads();
+  double* __restrict__ Q = a.q + e0 * a.max_nq;
+  double* __restrict__ QD = a.qd + e0 * a.max_nv;
+  const double* __restrict__ QDD = a.qdd + e0 * a.max_nv;
+  const double dt = a.dt;
+#pragma unroll 4
+  for (int k = threadIdx.x; k < envs * a.joints; k += kIntegrateThreads) {
+    const int el = k / a.joints, i = 1 + (k - el * a.joints);
+    const DModel* m = models[el];
+    if (i >= m->nj) continue;
+    const DJoint& J = model_joints(m)[i];
+    if (J.kind == JK_FREEFLYER) continue;
+    const int64_t c = int64_t(el) * a.max_nv + J.vcol;
+    const double w = fma(dt, QDD[c], QD[c]);
+    QD[c] = w;
+    Q[int64_t(el) * a.max_nq + J.qcol] += dt * w;
+  }
+  if (threadIdx.x >= envs) return;
+  const DModel* m = models[threadIdx.x];
   const DJoint* JT = model_joints(m);
-  double* q = a.q + e * a.max_nq;
-  double* qd = a.qd + e * a.max_nv;
-  const double* qdd = a.qdd + e * a.max_nv;
-  for (int c = 0; c < m->nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
   for (int i = 1; i < m->nj; i++) {
-    const DJoint& J = JT[i];
-    if (J.kind == JK_FREEFLYER) {
-      double v[6];
-      for (int k = 0; k < 6; k++) v[k] = a.dt * qd[J.vcol + k];
-      free_flyer_integrate(q + J.qcol, v);
-    } else {
-      q[J.qcol] = fma(a.dt, qd[J.vcol], q[J.qcol]);
+    if (JT[i].kind != JK_FREEFLYER) continue;
+    const int64_t c = int64_t(threadIdx.x) * a.max_nv + JT[i].vcol;
+    double v[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const double w = fma(dt, QDD[c + k], QD[c + k]);
+      QD[c + k] = w;
+      v[k] = dt * w;
     }
+    free_flyer_integrate(Q + int64_t(threadIdx.x) * a.max_nq + JT[i].qcol, v);
   }
 }
 
@@ -371,11 +396,13 @@ int sgdyn_batch_integrate(sgdyn_batch* b, double dt, double* q, double* qd, cons
   a.n = b->n;
   a.max_nq = b->max_nq;
   a.max_nv = b->max_nv;
+  a.joints = b->max_nj - 1;
   a.dt = dt;
   a.q = q;
   a.qd = qd;
   a.qdd = qdd;
-  hetero_integrate_kernel<<<unsigned((b->n + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  if (a.joints <= 0 || b->n == 0) return SGDYN_OK;
+  hetero_integrate_kernel<<<unsigned((b->n + 31) / 32), kIntegrateThreads, 0, static_cast<cudaStream_t>(stream)>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   return SGDYN_OK;

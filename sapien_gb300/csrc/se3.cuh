@@ -14,71 +14,72 @@
 
 namespace sgdyn {
 
-__device__ __forceinline__ double se3_f_1mc(double t) {  // (1 - cos t) / t^2
+// sum_k c[k] x^k by Horner's rule; with a constant table and full unrolling this is K - 1
+// FMAs, no division.
+template <int K>
+__device__ __forceinline__ double se3_horner(const double (&c)[K], double x) {
+  double r = c[K - 1];
+#pragma unroll
+  for (int k = K - 2; k >= 0; k--) r = fma(r, x, c[k]);
+  return r;
+}
+
+// Series coefficients below are the exact rationals rounded to the nearest double.
+__device__ __forceinline__ double se3_f_1mc(double t) {  // (1 - cos t) / t^2 = sum (-1)^k t^2k / (2k+2)!
   if (t < 0.3) {
-    double t2 = t * t, r = 0, term = 0.5;
-    for (int k = 0; k < 10; k++) {
-      r += term;
-      term *= -t2 / double((2 * k + 3) * (2 * k + 4));
-    }
-    return r;
+    const double c[10] = {0.5, -0.041666666666666664, 0.001388888888888889, -2.48015873015873e-05,
+                          2.755731922398589e-07, -2.08767569878681e-09, 1.1470745597729725e-11,
+                          -4.779477332387385e-14, 1.5619206968586225e-16, -4.110317623312165e-19};
+    return se3_horner(c, t * t);
   }
   return (1 - cos(t)) / (t * t);
 }
-__device__ __forceinline__ double se3_f_sinc(double t) {  // sin t / t
+__device__ __forceinline__ double se3_f_sinc(double t) {  // sin t / t = sum (-1)^k t^2k / (2k+1)!
   if (t < 0.3) {
-    double t2 = t * t, r = 0, term = 1;
-    for (int k = 0; k < 10; k++) {
-      r += term;
-      term *= -t2 / double((2 * k + 2) * (2 * k + 3));
-    }
-    return r;
+    const double c[10] = {1.0, -0.16666666666666666, 0.008333333333333333, -0.0001984126984126984,
+                          2.7557319223985893e-06, -2.505210838544172e-08, 1.6059043836821613e-10,
+                          -7.647163731819816e-13, 2.8114572543455206e-15, -8.22063524662433e-18};
+    return se3_horner(c, t * t);
   }
   return sin(t) / t;
 }
-__device__ __forceinline__ double se3_f_tms(double t) {  // (t - sin t) / t^3
+__device__ __forceinline__ double se3_f_tms(double t) {  // (t - sin t) / t^3 = sum (-1)^k t^2k / (2k+3)!
   if (t < 0.3) {
-    double t2 = t * t, r = 0, term = 1.0 / 6;
-    for (int k = 0; k < 10; k++) {
-      r += term;
-      term *= -t2 / double((2 * k + 4) * (2 * k + 5));
-    }
-    return r;
+    const double c[10] = {0.16666666666666666, -0.008333333333333333, 0.0001984126984126984,
+                          -2.7557319223985893e-06, 2.505210838544172e-08, -1.6059043836821613e-10,
+                          7.647163731819816e-13, -2.8114572543455206e-15, 8.22063524662433e-18,
+                          -1.9572941063391263e-20};
+    return se3_horner(c, t * t);
   }
   return (t - sin(t)) / (t * t * t);
 }
-__device__ __forceinline__ double se3_f_c4(double t) {  // (t^2 + 2 cos t - 2) / (2 t^4)
+// (t^2 + 2 cos t - 2) / (2 t^4) = sum (-1)^k t^2k / (2k+4)!
+__device__ __forceinline__ double se3_f_c4(double t) {
   if (t < 0.6) {
-    double t2 = t * t, r = 0, term = 1.0 / 24;
-    for (int k = 0; k < 12; k++) {
-      r += term;
-      term *= -t2 / double((2 * k + 5) * (2 * k + 6));
-    }
-    return r;
+    const double c[12] = {0.041666666666666664, -0.001388888888888889, 2.48015873015873e-05,
+                          -2.755731922398589e-07, 2.08767569878681e-09, -1.1470745597729725e-11,
+                          4.779477332387385e-14, -1.5619206968586225e-16, 4.110317623312165e-19,
+                          -8.896791392450574e-22, 1.6117375710961184e-24, -2.4795962632247976e-27};
+    return se3_horner(c, t * t);
   }
   return (t * t + 2 * cos(t) - 2) / (2 * t * t * t * t);
 }
-__device__ __forceinline__ double se3_f_c5(double t) {  // (2t - 3 sin t + t cos t) / (2 t^5)
+// (2t - 3 sin t + t cos t) / (2 t^5) = sum_{n>=2} (-1)^n (n-1) t^(2n-4) / (2n+1)!
+__device__ __forceinline__ double se3_f_c5(double t) {
   if (t < 0.9) {
-    double t2 = t * t, r = 0, fact = 120, pw = 1;
-    for (int n = 2; n < 16; n++) {
-      r += ((n % 2) ? -1.0 : 1.0) * double(n - 1) * pw / fact;
-      pw *= t2;
-      fact *= double((2 * n + 2) * (2 * n + 3));
-    }
-    return r;
+    const double c[14] = {0.008333333333333333, -0.0003968253968253968, 8.267195767195768e-06,
+                          -1.0020843354176688e-07, 8.029521918410807e-10, -4.58829823909189e-12,
+                          1.9680200780418645e-14, -6.576508197299464e-17, 1.7615646957052136e-19,
+                          -3.868170170630684e-22, 7.091645312822921e-25, -1.1020427836554655e-27,
+                          1.4702951752382032e-30, -1.7025750581749252e-33};
+    return se3_horner(c, t * t);
   }
   return (2 * t - 3 * sin(t) + t * cos(t)) / (2 * t * t * t * t * t);
 }
 __device__ __forceinline__ double se3_f_g(double t) {  // (1 - (t/2) cot(t/2)) / t^2
   if (t < 0.3) {
     const double c[6] = {1.0 / 12, 1.0 / 720, 1.0 / 30240, 1.0 / 1209600, 1.0 / 47900160, 691.0 / 1307674368000.0};
-    double t2 = t * t, r = 0, pw = 1;
-    for (int k = 0; k < 6; k++) {
-      r += c[k] * pw;
-      pw *= t2;
-    }
-    return r;
+    return se3_horner(c, t * t);
   }
   double h = 0.5 * t;
   return (1 - h * cos(h) / sin(h)) / (t * t);
@@ -113,16 +114,6 @@ __device__ __forceinline__ V3 log3(const M3& R, double* theta) {
   return mk(k * q[1], k * q[2], k * q[3]);
 }
 
-__device__ __forceinline__ M3 exp3(V3 w) {
-  double t = sqrt(dot(w, w));
-  M3 K = skew3(w), K2 = mul(K, K);
-  double a = se3_f_sinc(t), b = se3_f_1mc(t);
-  M3 R = eye3();
-#pragma unroll
-  for (int k = 0; k < 9; k++) R.a[k] += a * K.a[k] + b * K2.a[k];
-  return R;
-}
-
 // log6 of (R, p): linear part, angular part.
 __device__ __forceinline__ Mot log6(const M3& R, V3 p) {
   double t;
@@ -138,16 +129,20 @@ __device__ __forceinline__ Mot log6(const M3& R, V3 p) {
   return out;
 }
 
-// exp6 of (v, w) -> (R, p).
+// exp6 of (v, w) -> (R, p): R = 1 + sinc(t) K + f_1mc(t) K^2, p = (1 + f_1mc(t) K + f_tms(t) K^2) v
+// with K = [w]x, t = |w|.
 __device__ __forceinline__ void exp6(Mot nu, M3& R, V3& p) {
   V3 w = nu.w;
   double t = sqrt(dot(w, w));
   M3 K = skew3(w), K2 = mul(K, K);
-  double b = se3_f_1mc(t), c = se3_f_tms(t);
+  double a = se3_f_sinc(t), b = se3_f_1mc(t), c = se3_f_tms(t);
   M3 V = eye3();
+  R = eye3();
 #pragma unroll
-  for (int k = 0; k < 9; k++) V.a[k] += b * K.a[k] + c * K2.a[k];
-  R = exp3(w);
+  for (int k = 0; k < 9; k++) {
+    V.a[k] += b * K.a[k] + c * K2.a[k];
+    R.a[k] += a * K.a[k] + b * K2.a[k];
+  }
   p = mul(V, nu.v);
 }
 
@@ -164,15 +159,14 @@ __device__ __forceinline__ void free_flyer_integrate(double* q, const double* v)
   double qw[4];
   R_to_quat(R1, qw);  // w x y z
   const double dq = qw[1] * q[3] + qw[2] * q[4] + qw[3] * q[5] + qw[0] * q[6];
-  const double sg = dq < 0 ? -1.0 : 1.0;
-  const double n = sqrt(qw[0] * qw[0] + qw[1] * qw[1] + qw[2] * qw[2] + qw[3] * qw[3]);
+  const double s = (dq < 0 ? -1.0 : 1.0) / sqrt(qw[0] * qw[0] + qw[1] * qw[1] + qw[2] * qw[2] + qw[3] * qw[3]);
   q[0] = p1.x;
   q[1] = p1.y;
   q[2] = p1.z;
-  q[3] = sg * qw[1] / n;
-  q[4] = sg * qw[2] / n;
-  q[5] = sg * qw[3] / n;
-  q[6] = sg * qw[0] / n;
+  q[3] = s * qw[1];
+  q[4] = s * qw[2];
+  q[5] = s * qw[3];
+  q[6] = s * qw[0];
 }
 
 // Jlog6 of (R, p) as a dense 6x6, row-major, (linear, angular) ordering.
