@@ -144,16 +144,16 @@ __device__ __forceinline__ Mot world_S(const DJoint& J, const M3& Ro, V3 po, int
   return S;
 }
 
-// Cholesky of a packed symmetric 6x6 (row-major lower triangle, 21 entries) in place.
+// Cholesky of a packed symmetric 6x6 (row-major lower triangle, 21 entries) in place; the
+// diagonal slots keep the reciprocals 1 / L_jj, so the solves multiply instead of divide.
 __device__ __forceinline__ void chol6(double* L) {
   // index of (r, c), c <= r
 #define LI(r, c) ((r) * ((r) + 1) / 2 + (c))
   for (int j = 0; j < 6; j++) {
     double d = L[LI(j, j)];
     for (int k = 0; k < j; k++) d = fma(-L[LI(j, k)], L[LI(j, k)], d);
-    d = sqrt(d);
-    L[LI(j, j)] = d;
-    double inv = 1.0 / d;
+    const double inv = 1.0 / sqrt(d);
+    L[LI(j, j)] = inv;
     for (int i = j + 1; i < 6; i++) {
       double s = L[LI(i, j)];
       for (int k = 0; k < j; k++) s = fma(-L[LI(i, k)], L[LI(j, k)], s);
@@ -165,12 +165,12 @@ __device__ __forceinline__ void chol6_solve(const double* L, double* b) {
   for (int i = 0; i < 6; i++) {
     double s = b[i];
     for (int k = 0; k < i; k++) s = fma(-L[LI(i, k)], b[k], s);
-    b[i] = s / L[LI(i, i)];
+    b[i] = s * L[LI(i, i)];
   }
   for (int i = 5; i >= 0; i--) {
     double s = b[i];
     for (int k = i + 1; k < 6; k++) s = fma(-L[LI(k, i)], b[k], s);
-    b[i] = s / L[LI(i, i)];
+    b[i] = s * L[LI(i, i)];
   }
 #undef LI
 }
