@@ -322,19 +322,16 @@ __device__ __forceinline__ void ik_env(const DModel* __restrict__ model, const I
         Jc[3][col] = w.x; Jc[4][col] = w.y; Jc[5][col] = w.z;
       }
     }
-    // Jlog6(iMd^-1)
-    double Jl[36];
-    const M3 Rinv = transpose(Re);
-    jlog6(Rinv, -mul(Rinv, pe), Jl);
-    // J2 = -Jl Jc diag(mask), in place column by column
+    // Jlog6(iMd^-1) = [[Jinv, -TR], [0, Jinv]], from log6(iMd^-1) = -err
+    M3 Jinv, TR;
+    jlog6_blocks(Mot{-err.v, -err.w}, Jinv, TR);
+    // J2 = -Jlog6 Jc diag(mask), in place column by column
     for (int c = 0; c < ncol; c++) {
-      double t[6];
-      for (int r = 0; r < 6; r++) {
-        double s = 0;
-        for (int k = 0; k < 6; k++) s = fma(Jl[r * 6 + k], Jc[k][c], s);
-        t[r] = -s * mk_[c];
-      }
-      for (int r = 0; r < 6; r++) Jc[r][c] = t[r];
+      const V3 jv = mk(Jc[0][c], Jc[1][c], Jc[2][c]), jw = mk(Jc[3][c], Jc[4][c], Jc[5][c]);
+      const V3 top = mul(Jinv, jv) - mul(TR, jw), bot = mul(Jinv, jw);
+      const double m = -mk_[c];
+      Jc[0][c] = m * top.x; Jc[1][c] = m * top.y; Jc[2][c] = m * top.z;
+      Jc[3][c] = m * bot.x; Jc[4][c] = m * bot.y; Jc[5][c] = m * bot.z;
     }
     // (J J^T + damp) x = err, Cholesky on the packed lower triangle
     double A[21];

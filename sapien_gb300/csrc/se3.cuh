@@ -6,7 +6,8 @@
 // alpha = 1 - theta^2 g(theta), g(t) = (1 - (t/2) cot(t/2)) / t^2.
 // Jlog6(M) is the derivative for a right perturbation, log6(M exp6(d)) ~ log6(M) + J d,
 // i.e. the inverse of the SE(3) right Jacobian J_r(xi) = J_l(-xi) in Barfoot's block
-// form [[J, Q], [0, J]] (T. Barfoot, "State Estimation for Robotics", 2017, sec. 7.1.5).
+// form [[J, Q], [0, J]] (T. Barfoot, "State Estimation for Robotics", 2017, sec. 7.1.5);
+// it depends on M only through xi = log6(M), and log6(M^-1) = -log6(M).
 // Coefficient functions switch to their Taylor series below fixed thresholds so no
 // branch loses precision to cancellation.
 #pragma once
@@ -169,34 +170,34 @@ __device__ __forceinline__ void free_flyer_integrate(double* q, const double* v)
   q[6] = s * qw[0];
 }
 
-// Jlog6 of (R, p) as a dense 6x6, row-major, (linear, angular) ordering.
-__device__ __forceinline__ void jlog6(const M3& R, V3 p, double* J) {
-  Mot xi = log6(R, p);
-  V3 rho = xi.v, phi = xi.w;
-  double t = sqrt(dot(phi, phi));
-  M3 K = skew3(phi), K2 = mul(K, K);
-  double g = se3_f_g(t);
-  M3 Jinv = eye3();
-#pragma unroll
-  for (int k = 0; k < 9; k++) Jinv.a[k] += 0.5 * K.a[k] + g * K2.a[k];
-  // Q_l(-rho, -phi)
-  M3 P = skew3(-phi), Rh = skew3(-rho);
-  M3 PR = mul(P, Rh), RP = mul(Rh, P), PRP = mul(PR, P);
-  M3 PPR = mul(P, PR), RPP = mul(RP, P), PRPP = mul(PRP, P), PPRP = mul(P, PRP);
-  double a = se3_f_tms(t), b = se3_f_c4(t), c = se3_f_c5(t);
+// Jlog6 of the transform whose log6 is xi = (rho, phi), as its blocks: Jlog6 =
+// [[Jinv, -TR], [0, Jinv]] in (linear, angular) ordering, with Jinv = 1 + 1/2 [phi]x +
+// g(t) [phi]x^2 and TR = Jinv Q Jinv, Q = Q_l(-rho, -phi). The skew products in Barfoot's
+// Q reduce to outer products (d = phi.rho, [a]x[b]x = b a^T - (a.b) 1, and
+// [phi]x [rho]x [phi]x = -d [phi]x):
+//   Q = -1/2 [rho]x + a (rho phi^T + phi rho^T - 2d 1 + d [phi]x)
+//       + b (phi (phi x rho)^T - (phi x rho) phi^T - d [phi]x) - 2 c d (phi phi^T - t^2 1)
+// with a = f_tms(t), b = f_c4(t), c = f_c5(t).
+__device__ __forceinline__ void jlog6_blocks(const Mot& xi, M3& Jinv, M3& TR) {
+  const V3 rho = xi.v, phi = xi.w;
+  const double t2 = dot(phi, phi), t = sqrt(t2), d = dot(phi, rho);
+  const double g = se3_f_g(t), a = se3_f_tms(t), b = se3_f_c4(t), c = se3_f_c5(t);
+  const double f[3] = {phi.x, phi.y, phi.z}, r[3] = {rho.x, rho.y, rho.z};
+  const V3 fxr = cross(phi, rho);
+  const double u[3] = {fxr.x, fxr.y, fxr.z};  // phi x rho
+  const M3 Kf = skew3(phi), Kr = skew3(rho);
   M3 Q;
 #pragma unroll
-  for (int k = 0; k < 9; k++)
-    Q.a[k] = 0.5 * Rh.a[k] + a * (PR.a[k] + RP.a[k] + PRP.a[k]) + b * (PPR.a[k] + RPP.a[k] - 3 * PRP.a[k]) +
-             c * (PRPP.a[k] + PPRP.a[k]);
-  M3 TR = mul(mul(Jinv, Q), Jinv);
-  for (int r = 0; r < 3; r++)
-    for (int cc = 0; cc < 3; cc++) {
-      J[r * 6 + cc] = Jinv.a[r * 3 + cc];
-      J[(r + 3) * 6 + cc + 3] = Jinv.a[r * 3 + cc];
-      J[r * 6 + cc + 3] = -TR.a[r * 3 + cc];
-      J[(r + 3) * 6 + cc] = 0;
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double id = i == k ? 1.0 : 0.0;
+      const double ppT = f[i] * f[k] - t2 * id;  // [phi]x^2
+      Jinv.a[i * 3 + k] = id + 0.5 * Kf.a[i * 3 + k] + g * ppT;
+      Q.a[i * 3 + k] = -0.5 * Kr.a[i * 3 + k] + a * (r[i] * f[k] + f[i] * r[k] - 2 * d * id + d * Kf.a[i * 3 + k]) +
+                       b * (f[i] * u[k] - u[i] * f[k] - d * Kf.a[i * 3 + k]) - 2 * c * d * ppT;
     }
+  TR = mul(mul(Jinv, Q), Jinv);
 }
 
 }  // namespace sgdyn
