@@ -252,39 +252,50 @@ __device__ __forceinline__ void ik_env(const DModel* __restrict__ model, const I
   V3 op[MAXJ];
   double Jc[6][MAXV];
   for (int it = 0;; it++) {
-    // FK along the chain, root first
+    // FK along the chain, root first: B, o = the joint's placement frame in the world, then
+    // the joint motion in that frame (a z rotation or slide in a canonical frame)
     for (int d = depth - 1; d >= 0; d--) {
       const int i = chain[d];
       const DJoint& J = JT[i];
+      const int p = J.parent;
       M3 Rpl;
       for (int k = 0; k < 9; k++) Rpl.a[k] = J.R[k];
       const V3 ppl = mk(J.p[0], J.p[1], J.p[2]);
-      const V3 ax = mk(J.axis[0], J.axis[1], J.axis[2]);  // +z in a canonical frame
-      M3 RJ = eye3();
-      V3 pJ = mk(0, 0, 0);
+      const M3 B = p == 0 ? Rpl : ((J.flags & JF_ROT_IDENTITY) ? oR[p] : mul(oR[p], Rpl));
+      const V3 o = p == 0 ? ppl : mul_add(oR[p], ppl, op[p]);
       switch (J.kind) {
-        case JK_PRISMATIC: pJ = qs[i][0] * ax; break;
         case JK_FREEFLYER:
-          pJ = mk(qs[i][0], qs[i][1], qs[i][2]);
-          RJ = quat_to_R(qs[i][3], qs[i][4], qs[i][5], qs[i][6]);
+          oR[i] = mul(B, quat_to_R(qs[i][3], qs[i][4], qs[i][5], qs[i][6]));
+          op[i] = mul_add(B, mk(qs[i][0], qs[i][1], qs[i][2]), o);
           break;
-        case JK_CONTINUOUS:
-          RJ = J.axis_kind == AX_Z ? rot_z(qs[i][1], qs[i][0]) : rodrigues(ax, qs[i][1], qs[i][0]);
+        case JK_PRISMATIC: {
+          const V3 ax = J.axis_kind == AX_Z ? mk(B.a[2], B.a[5], B.a[8])
+                                            : mul(B, mk(J.axis[0], J.axis[1], J.axis[2]));
+          oR[i] = B;
+          op[i] = axpy(qs[i][0], ax, o);
           break;
-        default: {
-          double s, c;
-          sincos(qs[i][0], &s, &c);
-          RJ = J.axis_kind == AX_Z ? rot_z(s, c) : rodrigues(ax, s, c);
         }
-      }
-      const M3 Rli = mul(Rpl, RJ);
-      const V3 pli = mul_add(Rpl, pJ, ppl);
-      if (J.parent == 0) {
-        oR[i] = Rli;
-        op[i] = pli;
-      } else {
-        oR[i] = mul(oR[J.parent], Rli);
-        op[i] = mul_add(oR[J.parent], pli, op[J.parent]);
+        default: {  // revolute (angle) and continuous (cos, sin)
+          double s, c;
+          if (J.kind == JK_CONTINUOUS) {
+            c = qs[i][0];
+            s = qs[i][1];
+          } else {
+            sincos(qs[i][0], &s, &c);
+          }
+          if (J.axis_kind == AX_Z) {
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+              const double b0 = B.a[r * 3], b1 = B.a[r * 3 + 1];
+              oR[i].a[r * 3 + 0] = fma(c, b0, s * b1);
+              oR[i].a[r * 3 + 1] = fma(c, b1, -s * b0);
+              oR[i].a[r * 3 + 2] = B.a[r * 3 + 2];
+            }
+          } else {
+            oR[i] = mul(B, rodrigues(mk(J.axis[0], J.axis[1], J.axis[2]), s, c));
+          }
+          op[i] = o;
+        }
       }
     }
     M3 Ro = eye3();
