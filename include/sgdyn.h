@@ -95,6 +95,13 @@ int sgdyn_model_set_link_order(sgdyn_model* m, const char* const* names, int n);
 
 /* Sizes: external q columns, velocity dimension, links in the link order, joints incl. universe. */
 int sgdyn_model_info(const sgdyn_model* m, int* nq_ext, int* nv, int* nlinks, int* njoints);
+/* PinocchioModel::getRandomConfiguration (pinocchio_model.cpp:142-144), for n rows at once
+ * (HOST memory, env-major [n, nq_ext], external joint order): each revolute or prismatic
+ * coordinate uniform in its URDF [lower, upper] (0, 0 without a <limit>), each continuous
+ * angle uniform in [-pi, pi). Deterministic for a seed on every platform (std::mt19937_64,
+ * 53-bit uniforms, joints in tree order within a row). Fails for a model with a free flyer,
+ * whose position has no limits. */
+int sgdyn_model_random_configuration(const sgdyn_model* m, int64_t n, uint64_t seed, double* qpos);
 /* Kind of the k-th joint in external order: 1 revolute, 2 prismatic, 3 continuous, 4 free flyer. */
 int sgdyn_model_joint_kind(const sgdyn_model* m, int k, int* kind);
 /* Name of the moving joint with tree index j (1..njoints-1) or of BODY frame b. */

@@ -37,6 +37,7 @@ EXPORTED = (
     "sgdyn_model_set_link_order",
     "sgdyn_model_info",
     "sgdyn_model_joint_kind",
+    "sgdyn_model_random_configuration",
     "sgdyn_model_joint_name",
     "sgdyn_model_body_count",
     "sgdyn_model_body_name",
@@ -107,6 +108,7 @@ def load():
     L.sgdyn_model_set_link_order.argtypes = [vp, P(ctypes.c_char_p), i32]
     L.sgdyn_model_info.argtypes = [vp, P(i32), P(i32), P(i32), P(i32)]
     L.sgdyn_model_joint_kind.argtypes = [vp, i32, P(i32)]
+    L.sgdyn_model_random_configuration.argtypes = [vp, i64, ctypes.c_uint64, vp]
     L.sgdyn_model_joint_name.argtypes = [vp, i32, P(ctypes.c_char_p)]
     L.sgdyn_model_body_count.argtypes = [vp, P(i32)]
     L.sgdyn_model_body_name.argtypes = [vp, i32, P(ctypes.c_char_p)]

@@ -282,6 +282,15 @@ int sgdyn_model_info(const sgdyn_model* m, int* nq_ext, int* nv, int* nlinks, in
   return SGDYN_OK;
 }
 
+int sgdyn_model_random_configuration(const sgdyn_model* m, int64_t n, uint64_t seed, double* qpos) {
+  if (!m || !m->impl || (n > 0 && !qpos)) return fail(SGDYN_ERR_NULL, "null argument");
+  if (n < 0) return fail(SGDYN_ERR_RUNTIME, "negative batch size");
+  return guarded([&] {
+    m->impl->random_configuration(n, seed, qpos);
+    return SGDYN_OK;
+  });
+}
+
 int sgdyn_model_joint_kind(const sgdyn_model* m, int k, int* kind) {
   if (!m || !kind) return fail(SGDYN_ERR_NULL, "null argument");
   const Model& M = *m->impl;

@@ -15,6 +15,8 @@
 // setJointOrder / setLinkOrder follow pinocchio/pinocchio_model.cpp:99-140.
 #include "model.h"
 
+#include <random>
+
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -254,6 +256,8 @@ Model* Model::build_tree(const std::map<std::string, BodyInertia>& links, const 
         J.parent = pb.joint;
         J.placement = P;
         J.inertia = Yc;
+        J.lower = d.lower;
+        J.upper = d.upper;
         if (d.type == "revolute") J.kind = JK_REVOLUTE;
         else if (d.type == "continuous") J.kind = JK_CONTINUOUS;
         else if (d.type == "prismatic") J.kind = JK_PRISMATIC;
@@ -322,6 +326,10 @@ Model* Model::from_urdf(const std::string& xml, const double g[3]) {
       d.axis[0] = 1; d.axis[1] = 0; d.axis[2] = 0;
       if (auto* ax = c->child("axis"))
         if (auto* a = ax->attr("xyz")) parse_doubles(*a, d.axis, 3);
+      if (auto* lim = c->child("limit")) {
+        if (auto* lo = lim->attr("lower")) parse_doubles(*lo, &d.lower, 1);
+        if (auto* up = lim->attr("upper")) parse_doubles(*up, &d.upper, 1);
+      }
       if (jdesc.count(*n)) throw std::runtime_error("URDF: duplicate joint " + *n);
       jdesc[*n] = d;
     }
@@ -407,6 +415,8 @@ Model* Model::from_articulation(const ArtLink* links, int nlinks, const ArtJoint
     js.parent = "link_" + std::to_string(a.parent);
     js.child = "link_dummy_" + ci;
     js.origin = pose7(a.pose_in_parent);
+    js.lower = a.lower;
+    js.upper = a.upper;
     J[name] = js;
     JointSpec dj;
     dj.type = "fixed";
@@ -761,6 +771,26 @@ Model::~Model() {
       cudaSetDevice(cur);
     }
   }
+}
+
+void Model::random_configuration(int64_t n, uint64_t seed, double* q) const {
+  for (int j = 1; j < njoints(); j++) {
+    const HostJoint& J = joints[j];
+    if (J.kind == JK_FREEFLYER)
+      throw std::runtime_error("random configuration: free-flyer joint " + J.name + " has no position limits");
+    if ((J.kind == JK_REVOLUTE || J.kind == JK_PRISMATIC) && !(J.lower <= J.upper))
+      throw std::runtime_error("random configuration: joint " + J.name + " has lower limit above upper limit");
+  }
+  std::mt19937_64 rng(seed);
+  const double pi = 3.14159265358979323846;
+  for (int64_t e = 0; e < n; e++)
+    for (int j = 1; j < njoints(); j++) {
+      const HostJoint& J = joints[j];
+      const double u = double(rng() >> 11) * (1.0 / 9007199254740992.0);  // [0, 1), 53 bits
+      double& x = q[e * nq_ext_ + qcol_[j]];
+      if (J.kind == JK_CONTINUOUS) x = -pi + 2 * pi * u;
+      else x = J.lower + (J.upper - J.lower) * u;
+    }
 }
 
 }  // namespace sgdyn

@@ -31,12 +31,14 @@ struct HostJoint {
   Placement placement;
   BodyInertia inertia;
   int idx_q = 0, idx_v = 0, nq = 0, nv = 0, depth = 0;
+  double lower = 0, upper = 0;  // position limits of a revolute or prismatic joint
 };
 
 struct JointSpec {  // a URDF joint before tree building
   std::string type, parent, child;
   Placement origin;
   double axis[3];
+  double lower = 0, upper = 0;  // <limit lower upper>, 0 when absent as in URDF
 };
 
 // An articulation as SAPIEN describes it (PhysxArticulationLinkComponent / Joint getters):
@@ -79,6 +81,12 @@ class Model {
 
   void set_joint_order(const std::vector<std::string>& names);
   void set_link_order(const std::vector<std::string>& names);
+
+  // getRandomConfiguration (pinocchio_model.cpp:142-144): n rows of external q, each
+  // revolute or prismatic coordinate uniform in its [lower, upper], each continuous angle
+  // uniform in [-pi, pi); std::mt19937_64 seeded with `seed`, 53-bit uniforms, so the
+  // samples are the same on every platform. Throws for a free flyer (no position limits).
+  void random_configuration(int64_t n, uint64_t seed, double* q) const;
 
   int njoints() const { return int(joints.size()); }
   int nq_ext() const { return nq_ext_; }

@@ -27,6 +27,7 @@ q block is (x y z qx qy qz qw) and their velocity block the 6-D body twist.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -211,6 +212,22 @@ class PinocchioModel:
         self._link_order_set = True
         self._fk_cache = None
         self._refresh()
+
+    def get_random_configuration(self, seed=None):
+        """getRandomConfiguration (pinocchio_model.cpp:142-144): one qpos in the joint order,
+        each revolute or prismatic coordinate uniform within its URDF limits, each continuous
+        angle uniform in [-pi, pi). `seed` (addition) makes the draw reproducible; without it
+        the seed comes from the OS. Raises for a model with a free flyer (no limits)."""
+        return self.get_random_configuration_batched(1, seed)[0]
+
+    def get_random_configuration_batched(self, n, seed=None):
+        """[n, nq] float64 host array of random configurations (see get_random_configuration);
+        the same seed gives the same rows on every platform."""
+        seed = int.from_bytes(os.urandom(8), "little") if seed is None else int(seed) & (2**64 - 1)
+        out = np.empty((int(n), self.nq_ext), dtype=np.float64)
+        N.check(N.load().sgdyn_model_random_configuration(self._h, int(n), seed,
+                                                          out.ctypes.data_as(ctypes.c_void_p)))
+        return out
 
     # ---- plumbing ----------------------------------------------------------
     def _require_order(self):

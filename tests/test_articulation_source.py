@@ -29,6 +29,10 @@ def test_native_source_matches_urdf_export(seed):
     # an unbounded revolute joint becomes continuous
     kinds = set(int(k) for k in a["joints"]["kind"][1:])
     assert kinds == {1, 2, 3}
+    # joint limits reach the model on both paths: equal seeded random configurations
+    qa = native.get_random_configuration_batched(64, seed=seed)
+    qb = ref.get_random_configuration_batched(64, seed=seed)
+    assert np.abs(qa - qb).max() <= 1e-12
 
 
 def _oracle_for(art):

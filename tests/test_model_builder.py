@@ -222,3 +222,33 @@ def test_lanes_and_run_time_compilation_settings_are_validated():
     assert L.sgdyn_jit_max_joints(old.value, None) == N.OK
     src = ctypes.c_char_p()
     assert L.sgdyn_jit_source(pm._h, -4, ctypes.byref(src)) != N.OK  # no such kernel kind
+
+
+@pytest.mark.parametrize("name", ["arm9", "arm9_sapien", "mixed_chain"])
+def test_random_configuration_within_limits_and_reproducible(name):
+    """getRandomConfiguration: each revolute / prismatic coordinate uniform within its URDF
+    limits, each continuous angle uniform in [-pi, pi), reproducible for a seed."""
+    r = ROBOTS[name]()
+    pm = PinocchioModel(r.urdf, [0, 0, -9.81])
+    pm.set_joint_order(r.joint_names)
+    n = 4000
+    q = pm.get_random_configuration_batched(n, seed=7)
+    assert q.shape == (n, r.nq_ext) and q.dtype == np.float64
+    assert np.array_equal(q, pm.get_random_configuration_batched(n, seed=7))
+    assert not np.array_equal(q, pm.get_random_configuration_batched(n, seed=8))
+    for c, (kind, (lo, hi)) in enumerate(zip(r.joint_kinds, r.joint_limits)):
+        if kind == syn.CONTINUOUS:
+            lo, hi = -np.pi, np.pi
+        assert lo <= q[:, c].min() and q[:, c].max() < hi, (c, kind)
+        assert abs(q[:, c].mean() - 0.5 * (lo + hi)) < 5 * (hi - lo) / np.sqrt(12 * n), (c, kind)
+    one = pm.get_random_configuration(seed=3)
+    assert one.shape == (r.nq_ext,)
+    assert np.array_equal(one, pm.get_random_configuration_batched(1, seed=3)[0])
+
+
+def test_random_configuration_refuses_free_flyer():
+    r = syn.quadruped()
+    pm = PinocchioModel(r.urdf, [0, 0, -9.81])
+    pm.set_joint_order(r.joint_names)
+    with pytest.raises(RuntimeError, match="free-flyer"):
+        pm.get_random_configuration()
