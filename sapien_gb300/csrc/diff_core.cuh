@@ -247,6 +247,72 @@ __device__ void rnea_subtree_forces(const Tab& T, const DynWork<MAXJ>& W, Mot* F
   }
 }
 
+// Time derivative of a world-frame rigid-body inertia moving with twist v,
+// Idot = v x* I - I (v x). It has the shape of a rigid-body inertia with zero mass: first
+// moment hdot = m v_lin + w x h and rotational part 2 (v_lin . h) 1 - (h v_lin^T + v_lin h^T)
+// + K + K^T with K = [w]x Ibar (I = [[m 1, -[h]x], [[h]x, Ibar]]).
+__device__ __forceinline__ RBI rbi_rate(const RBI& Y, const Mot& v) {
+  const V3 w = v.w, u = v.v, h = Y.h;
+  const double* I = Y.I;
+  RBI D;
+  D.m = 0;
+  D.h = add_cross(Y.m * u, w, h);
+  const double k00 = -w.z * I[1] + w.y * I[2], k01 = -w.z * I[3] + w.y * I[4], k02 = -w.z * I[4] + w.y * I[5];
+  const double k10 = w.z * I[0] - w.x * I[2], k11 = w.z * I[1] - w.x * I[4], k12 = w.z * I[2] - w.x * I[5];
+  const double k20 = -w.y * I[0] + w.x * I[1], k21 = -w.y * I[1] + w.x * I[3], k22 = -w.y * I[2] + w.x * I[4];
+  const double uh = 2 * dot(u, h);
+  D.I[0] = uh - 2 * h.x * u.x + 2 * k00;
+  D.I[1] = -(h.x * u.y + u.x * h.y) + k01 + k10;
+  D.I[2] = -(h.x * u.z + u.x * h.z) + k02 + k20;
+  D.I[3] = uh - 2 * h.y * u.y + 2 * k11;
+  D.I[4] = -(h.y * u.z + u.y * h.z) + k12 + k21;
+  D.I[5] = uh - 2 * h.z * u.z + 2 * k22;
+  return D;
+}
+
+// Subtree composites for the analytic RNEA derivatives, per joint i over subtree(i): F the
+// RNEA forces, H the momenta I v, Ib the inertias (CRBA's composite), Db their rates
+// (rbi_rate); per tree column c of joint i: P_c = Ib_i S_c and Q_c = Db_i S_c - S_c x* H_i.
+template <int MAXJ>
+struct DerivComposites {
+  static constexpr int MAXV = MAXJ + 5;
+  Mot F[MAXJ], H[MAXJ];
+  RBI Ib[MAXJ], Db[MAXJ];
+  Mot P[MAXV], Q[MAXV];
+};
+
+template <int MAXJ, class Tab>
+__device__ void deriv_composites(const Tab& T, const DynWork<MAXJ>& W, DerivComposites<MAXJ>& C) {
+  const int nj = T.nj();
+  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+#pragma unroll
+  for (int i = 1; i < nj; i++) {
+    C.F[i] = rbi_mul_add(W.Iw[i], W.acc[i], add_crossf(zero, W.vel[i], W.hY[i]));
+    C.H[i] = W.hY[i];
+    C.Ib[i] = W.Iw[i];
+    C.Db[i] = rbi_rate(W.Iw[i], W.vel[i]);
+  }
+#pragma unroll
+  for (int j = nj - 1; j >= 1; j--) {
+    const int p = T.joint(j).parent;
+    if (p > 0) {
+      C.F[p] = add6(C.F[p], C.F[j]);
+      C.H[p] = add6(C.H[p], C.H[j]);
+      C.Ib[p] = rbi_add(C.Ib[p], C.Ib[j]);
+      C.Db[p] = rbi_add(C.Db[p], C.Db[j]);
+    }
+  }
+#pragma unroll
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = T.joint(i);
+    for (int k = 0; k < J.nv; k++) {
+      const Mot S = W.Sw[J.ivx + k];
+      C.P[J.ivx + k] = rbi_mul(C.Ib[i], S);
+      C.Q[J.ivx + k] = add6(rbi_mul(C.Db[i], S), scale6(-1.0, add_crossf(zero, S, C.H[i])));
+    }
+  }
+}
+
 // Reverse-mode RNEA sweep over the forward quantities in W (acc must be the world
 // accelerations the torques were computed with) and the subtree forces in A.F (from
 // rnea_subtree_forces; read only). taubar and the outputs are external order; any output

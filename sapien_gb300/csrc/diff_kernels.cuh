@@ -120,33 +120,92 @@ __global__ void __launch_bounds__(32) fk_vjp_kernel(const DModel* __restrict__ m
   }
 }
 
+// Analytic RNEA derivatives, column by column (forward mode over the subtree composites).
+// Perturbing tree column c = (joint j, coordinate l), s = S_c, moves subtree(j) rigidly by
+// s; with lambda = parent(j), u = v_lambda x s, alpha = a_lambda x s (a_0 = -gravity,
+// v_0 = 0), beta = alpha - u x v_lambda and gamma = (v_lambda + v_j) x s, the columns are
+//   rows of a strict ancestor i of j (S_i fixed):
+//     dtau_i/dq_c   = S_i . (s x* F_j + Ib_j beta + Db_j u + u x* H_j)
+//     dtau_i/dqd_c  = S_i . (Db_j s + s x* H_j + Ib_j gamma)
+//     dtau_i/dqdd_c = S_i . Ib_j s
+//   rows of i in subtree(j) (S_i moves with the subtree; the s x* F term cancels):
+//     dtau_i/dq_c   = P_i . beta + Q_i . u
+//     dtau_i/dqd_c  = Q_i . s + P_i . gamma
+//     dtau_i/dqdd_c = P_i . s
+//   and 0 elsewhere (composites: deriv_composites). From tau_i = S_i . F_i with
+// v_k = v_lambda + (rigidly moved part), a_k likewise, and d(v x* I v)/dv, whose subtree
+// sum is the rate Db plus the momentum term. Subtrees are contiguous in the table's joint
+// order, so "i in subtree(j)" is j <= i < subtree_end(j). A thread writes the columns
+// c = g, g + G, ... (G = a.groups) of one environment, whole columns including zeros.
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void rnea_derivative_columns(const Tab& T, const DynWork<MAXJ>& W,
+                                                        const DerivComposites<MAXJ>& C, const DerivArgs& a,
+                                                        const int64_t e, const int g) {
+  const int nj = T.nj(), nv = T.nv();
+  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
+  for (int j = 1; j < nj; j++) {
+    const DJoint& J = T.joint(j);
+    const int p = J.parent;
+    const Mot vl = (p == 0) ? zero : W.vel[p];
+    const Mot al = (p == 0) ? a0 : W.acc[p];
+    for (int l = 0; l < J.nv; l++) {
+      const int t = J.ivx + l;
+      if (t % a.groups != g) continue;
+      const int c = J.vcol + l;
+      const Mot s = W.Sw[t];
+      const Mot u = add_crossm(zero, vl, s);
+      const Mot beta = add_crossm(add_crossm(zero, al, s), vl, u);  // alpha - u x v_lambda
+      const Mot gam = add_crossm(zero, add6(vl, W.vel[j]), s);
+      Mot Phi = rbi_mul_add(C.Ib[j], beta, add_crossf(zero, s, C.F[j]));
+      Phi = add_crossf(rbi_mul_add(C.Db[j], u, Phi), u, C.H[j]);
+      const Mot Psi = rbi_mul_add(C.Ib[j], gam, rbi_mul_add(C.Db[j], s, add_crossf(zero, s, C.H[j])));
+      const Mot Ms = C.P[t];
+      for (int i = 1; i < nj; i++) {
+        const DJoint& I = T.joint(i);
+        const bool anc = i < j && j < I.subtree_end;
+        const bool sub = i >= j && i < J.subtree_end;
+        for (int k = 0; k < I.nv; k++) {
+          const int r = I.vcol + k, ti = I.ivx + k;
+          double dq = 0, dqd = 0, dqdd = 0;
+          if (anc) {
+            const Mot Si = W.Sw[ti];
+            dq = dot6(Si, Phi);
+            dqd = dot6(Si, Psi);
+            dqdd = dot6(Si, Ms);
+          } else if (sub) {
+            const Mot P = C.P[ti], Q = C.Q[ti];
+            dq = dot6(P, beta) + dot6(Q, u);
+            dqd = dot6(Q, s) + dot6(P, gam);
+            dqdd = dot6(P, s);
+          }
+          stv(a.d_q, e, r * nv + c, dq);
+          stv(a.d_qd, e, r * nv + c, dqd);
+          if (a.d_x.p) stv(a.d_x, e, r * nv + c, dqdd);
+        }
+      }
+    }
+  }
+}
+
 template <int MAXJ>
 __global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
   const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= a.n * a.groups) return;
   const int64_t e = idx % a.n;
-  const int r0 = int(idx / a.n) * a.rows;
+  const int g = int(idx / a.n);
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
   const RuntimeTab T{model};
   const int nv = T.nv(), nq = T.nq_ext();
-  double q[MAXQ], qd[MAXV], qdd[MAXV], tb[MAXV], o1[MAXV], o2[MAXV], o3[MAXV];
+  double q[MAXQ], qd[MAXV], qdd[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
   load_row<MAXJ>(a.x, e, nv, qdd);
   DynWork<MAXJ> W;
-  AdjScratch<MAXJ> A;
+  DerivComposites<MAXJ> C;
   rnea_forward<MAXJ>(T, q, qd, qdd, W);
-  rnea_subtree_forces<MAXJ>(T, W, A.F);
-  const int r1 = min(nv, r0 + a.rows);
-  for (int r = r0; r < r1; r++) {
-    for (int c = 0; c < nv; c++) tb[c] = (c == r) ? 1.0 : 0.0;
-    rnea_adjoint<MAXJ>(T, W, A, tb, o1, o2, a.d_x.p ? o3 : nullptr, 1.0);
-    for (int c = 0; c < nv; c++) {
-      stv(a.d_q, e, r * nv + c, o1[c]);
-      stv(a.d_qd, e, r * nv + c, o2[c]);
-      if (a.d_x.p) stv(a.d_x, e, r * nv + c, o3[c]);
-    }
-  }
+  deriv_composites<MAXJ>(T, W, C);
+  rnea_derivative_columns<MAXJ>(T, W, C, a, e, g);
 }
 
 template <int MAXJ>
