@@ -137,48 +137,69 @@ __global__ void __launch_bounds__(32) fk_vjp_kernel(const DModel* __restrict__ m
 // sum is the rate Db plus the momentum term. Subtrees are contiguous in the table's joint
 // order, so "i in subtree(j)" is j <= i < subtree_end(j). A thread writes the columns
 // c = g, g + G, ... (G = a.groups) of one environment, whole columns including zeros.
+// The per-column vectors of the formulas above for tree column t = J.ivx + l of joint j.
+struct ColumnTerms {
+  Mot s, u, beta, gam, Phi, Psi;
+};
+
+template <int MAXJ, class Tab>
+__device__ __forceinline__ ColumnTerms column_terms(const Tab& T, const DynWork<MAXJ>& W,
+                                                    const DerivComposites<MAXJ>& C, int j, int t) {
+  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
+  const int p = T.joint(j).parent;
+  const Mot vl = (p == 0) ? zero : W.vel[p];
+  const Mot al = (p == 0) ? a0 : W.acc[p];
+  ColumnTerms ct;
+  ct.s = W.Sw[t];
+  ct.u = add_crossm(zero, vl, ct.s);
+  ct.beta = add_crossm(add_crossm(zero, al, ct.s), vl, ct.u);  // alpha - u x v_lambda
+  ct.gam = add_crossm(zero, add6(vl, W.vel[j]), ct.s);
+  ct.Phi = rbi_mul_add(C.Ib[j], ct.beta, add_crossf(zero, ct.s, C.F[j]));
+  ct.Phi = add_crossf(rbi_mul_add(C.Db[j], ct.u, ct.Phi), ct.u, C.H[j]);
+  ct.Psi = rbi_mul_add(C.Ib[j], ct.gam, rbi_mul_add(C.Db[j], ct.s, add_crossf(zero, ct.s, C.H[j])));
+  return ct;
+}
+
+// Entry (row column ti of joint i, column t of joint j) of dtau/dq, dtau/dqd, dtau/dqdd.
+template <int MAXJ>
+__device__ __forceinline__ void column_entry(const DynWork<MAXJ>& W, const DerivComposites<MAXJ>& C,
+                                             const ColumnTerms& ct, bool anc, bool sub, int t, int ti, double& dq,
+                                             double& dqd, double& dqdd) {
+  dq = dqd = dqdd = 0;
+  if (anc) {
+    const Mot Si = W.Sw[ti];
+    dq = dot6(Si, ct.Phi);
+    dqd = dot6(Si, ct.Psi);
+    dqdd = dot6(Si, C.P[t]);
+  } else if (sub) {
+    const Mot P = C.P[ti], Q = C.Q[ti];
+    dq = dot6(P, ct.beta) + dot6(Q, ct.u);
+    dqd = dot6(Q, ct.s) + dot6(P, ct.gam);
+    dqdd = dot6(P, ct.s);
+  }
+}
+
 template <int MAXJ, class Tab>
 __device__ __forceinline__ void rnea_derivative_columns(const Tab& T, const DynWork<MAXJ>& W,
                                                         const DerivComposites<MAXJ>& C, const DerivArgs& a,
                                                         const int64_t e, const int g) {
   const int nj = T.nj(), nv = T.nv();
-  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
-  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
   for (int j = 1; j < nj; j++) {
     const DJoint& J = T.joint(j);
-    const int p = J.parent;
-    const Mot vl = (p == 0) ? zero : W.vel[p];
-    const Mot al = (p == 0) ? a0 : W.acc[p];
     for (int l = 0; l < J.nv; l++) {
       const int t = J.ivx + l;
       if (t % a.groups != g) continue;
       const int c = J.vcol + l;
-      const Mot s = W.Sw[t];
-      const Mot u = add_crossm(zero, vl, s);
-      const Mot beta = add_crossm(add_crossm(zero, al, s), vl, u);  // alpha - u x v_lambda
-      const Mot gam = add_crossm(zero, add6(vl, W.vel[j]), s);
-      Mot Phi = rbi_mul_add(C.Ib[j], beta, add_crossf(zero, s, C.F[j]));
-      Phi = add_crossf(rbi_mul_add(C.Db[j], u, Phi), u, C.H[j]);
-      const Mot Psi = rbi_mul_add(C.Ib[j], gam, rbi_mul_add(C.Db[j], s, add_crossf(zero, s, C.H[j])));
-      const Mot Ms = C.P[t];
+      const ColumnTerms ct = column_terms<MAXJ>(T, W, C, j, t);
       for (int i = 1; i < nj; i++) {
         const DJoint& I = T.joint(i);
         const bool anc = i < j && j < I.subtree_end;
         const bool sub = i >= j && i < J.subtree_end;
         for (int k = 0; k < I.nv; k++) {
-          const int r = I.vcol + k, ti = I.ivx + k;
-          double dq = 0, dqd = 0, dqdd = 0;
-          if (anc) {
-            const Mot Si = W.Sw[ti];
-            dq = dot6(Si, Phi);
-            dqd = dot6(Si, Psi);
-            dqdd = dot6(Si, Ms);
-          } else if (sub) {
-            const Mot P = C.P[ti], Q = C.Q[ti];
-            dq = dot6(P, beta) + dot6(Q, u);
-            dqd = dot6(Q, s) + dot6(P, gam);
-            dqdd = dot6(P, s);
-          }
+          const int r = I.vcol + k;
+          double dq, dqd, dqdd;
+          column_entry<MAXJ>(W, C, ct, anc, sub, t, I.ivx + k, dq, dqd, dqdd);
           stv(a.d_q, e, r * nv + c, dq);
           stv(a.d_qd, e, r * nv + c, dqd);
           if (a.d_x.p) stv(a.d_x, e, r * nv + c, dqdd);
@@ -208,34 +229,135 @@ __global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __re
   rnea_derivative_columns<MAXJ>(T, W, C, a, e, g);
 }
 
+// Joint-space inertia in tree-column order factored as M = L^T D L with the tree's
+// sparsity (Featherstone, "Rigid Body Dynamics Algorithms", 2008, sec. 6.5): column a's
+// parent lam[a] is the previous column of its joint, else the last column of the parent
+// joint, else -1; L is unit lower triangular with nonzeros only at (a, ancestor of a), so
+// the factorisation costs sum depth^2 and a solve 2 sum depth. H holds M's lower triangle
+// (packed by rows: entry (a, b <= a) at ltdl_at(a, b)) on entry and L below the diagonal
+// on exit; Dinv = 1 / D.
+__device__ __forceinline__ int ltdl_at(int a, int b) { return a * (a + 1) / 2 + b; }
+
+__device__ __forceinline__ void ltdl_factor(double* H, const int* lam, double* Dinv, int n) {
+  for (int k = n - 1; k >= 0; k--) {
+    const double rk = 1.0 / H[ltdl_at(k, k)];
+    Dinv[k] = rk;
+    for (int i = lam[k]; i >= 0; i = lam[i]) {
+      const double f = H[ltdl_at(k, i)] * rk;
+      for (int j = i; j >= 0; j = lam[j]) H[ltdl_at(i, j)] -= f * H[ltdl_at(k, j)];
+      H[ltdl_at(k, i)] = f;
+    }
+  }
+}
+// B <- M^-1 B in place for R right-hand sides at once (B row-major [n][R]), M = L^T D L
+// from ltdl_factor: one walk over the ancestor chains serves all of them, so the chain
+// loads are paid once and each step has R independent updates.
+template <int R>
+__device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam, const double* Dinv, int n,
+                                                double* B) {
+  for (int k = n - 1; k >= 0; k--) {
+    double bk[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) bk[r] = B[k * R + r];
+    for (int i = lam[k]; i >= 0; i = lam[i]) {
+      const double h = H[ltdl_at(k, i)];
+#pragma unroll
+      for (int r = 0; r < R; r++) B[i * R + r] -= h * bk[r];
+    }
+  }
+  for (int k = 0; k < n; k++) {
+    double x[R];
+    const double d = Dinv[k];
+#pragma unroll
+    for (int r = 0; r < R; r++) x[r] = B[k * R + r] * d;
+    for (int i = lam[k]; i >= 0; i = lam[i]) {
+      const double h = H[ltdl_at(k, i)];
+#pragma unroll
+      for (int r = 0; r < R; r++) x[r] -= h * B[i * R + r];
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) B[k * R + r] = x[r];
+  }
+}
+
+// ABA derivatives from the RNEA ones at qdd = ABA(q, qd, tau): dqdd/dq = -M^-1 dtau/dq,
+// dqdd/dqd = -M^-1 dtau/dqd, dqdd/dtau = M^-1 (Carpentier & Mansard, RSS 2018). The tau
+// columns come from the analytic column formulas above, M from the same composites
+// (M_ab = P_a . S_b for b an ancestor-or-self column of a), and every M^-1 product is an
+// LTDL solve. A thread writes the columns c = g, g + G, ... of one environment.
 template <int MAXJ>
 __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
   const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= a.n * a.groups) return;
   const int64_t e = idx % a.n;
-  const int r0 = int(idx / a.n) * a.rows;
+  const int g = int(idx / a.n);
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
   const RuntimeTab T{model};
-  const int nv = T.nv(), nq = T.nq_ext();
-  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV], er[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
+  const int nj = T.nj(), nv = T.nv(), nq = T.nq_ext();
+  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
   load_row<MAXJ>(a.x, e, nv, tau);
   DynWork<MAXJ> W;
-  AdjScratch<MAXJ> A;
+  DerivComposites<MAXJ> C;
   aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
-  rnea_subtree_forces<MAXJ>(T, W, A.F);
-  const int r1 = min(nv, r0 + a.rows);
-  for (int r = r0; r < r1; r++) {
-    for (int c = 0; c < nv; c++) er[c] = (c == r) ? 1.0 : 0.0;
-    minv_solve<MAXJ>(T, W, er, lam);
-    rnea_adjoint<MAXJ>(T, W, A, lam, o1, o2, nullptr, -1.0);
-    for (int c = 0; c < nv; c++) {
-      stv(a.d_q, e, r * nv + c, o1[c]);
-      stv(a.d_qd, e, r * nv + c, o2[c]);
-      if (a.d_x.p) stv(a.d_x, e, r * nv + c, lam[c]);
+  deriv_composites<MAXJ>(T, W, C);
+  int lam[MAXV], ext[MAXV];
+  double H[MAXV * (MAXV + 1) / 2], Dinv[MAXV];
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = T.joint(i);
+    const int p = J.parent;
+    for (int k = 0; k < J.nv; k++) {
+      const int t = J.ivx + k;
+      lam[t] = k > 0 ? t - 1 : (p > 0 ? T.joint(p).ivx + T.joint(p).nv - 1 : -1);
+      ext[t] = J.vcol + k;
+      for (int b = t; b >= 0; b = lam[b]) H[ltdl_at(t, b)] = dot6(C.P[t], W.Sw[b]);
     }
   }
+  ltdl_factor(H, lam, Dinv, nv);
+  // this thread's columns c = g, g + G, ... in batches of CB; right-hand sides per batch:
+  // [dtau/dq columns | dtau/dqd columns | unit vectors] (CB each)
+  constexpr int CB = 8, RB = 3 * CB;
+  double B[MAXV * RB];
+  int cols[CB], ncols = 0;
+  auto flush = [&]() {
+    ltdl_solve_many<RB>(H, lam, Dinv, nv, B);
+    for (int m = 0; m < ncols; m++) {
+      const int c = ext[cols[m]];
+      for (int r = 0; r < nv; r++) {
+        stv(a.d_q, e, ext[r] * nv + c, -B[r * RB + m]);
+        stv(a.d_qd, e, ext[r] * nv + c, -B[r * RB + CB + m]);
+        if (a.d_x.p) stv(a.d_x, e, ext[r] * nv + c, B[r * RB + 2 * CB + m]);
+      }
+    }
+    ncols = 0;
+  };
+  for (int j = 1; j < nj; j++) {
+    const DJoint& J = T.joint(j);
+    for (int l = 0; l < J.nv; l++) {
+      const int t = J.ivx + l;
+      if (t % a.groups != g) continue;
+      if (ncols == 0)
+        for (int k = 0; k < nv * RB; k++) B[k] = 0.0;
+      const int m = ncols++;
+      cols[m] = t;
+      const ColumnTerms ct = column_terms<MAXJ>(T, W, C, j, t);
+      for (int i = 1; i < nj; i++) {
+        const DJoint& I = T.joint(i);
+        const bool anc = i < j && j < I.subtree_end;
+        const bool sub = i >= j && i < J.subtree_end;
+        if (!anc && !sub) continue;
+        for (int k = 0; k < I.nv; k++) {
+          const int ti = I.ivx + k;
+          double dqdd;
+          column_entry<MAXJ>(W, C, ct, anc, sub, t, ti, B[ti * RB + m], B[ti * RB + CB + m], dqdd);
+        }
+      }
+      B[t * RB + 2 * CB + m] = 1.0;
+      if (ncols == CB) flush();
+    }
+  }
+  if (ncols > 0) flush();
 }
 
 // ---- rollouts ---------------------------------------------------------------------

@@ -62,11 +62,11 @@ struct FkVjpArgs {
 // Dense derivative matrices, rows = outputs, columns = tangent inputs.
 //   RNEA: x = qdd -> d_q = dtau/dq, d_qd = dtau/dqd, d_x = dtau/dqdd (= M)
 //   ABA:  x = tau -> d_q = dqdd/dq, d_qd = dqdd/dqd, d_x = dqdd/dtau (= M^-1)
-// Rows are split into `groups` contiguous blocks of `rows` rows: thread (group g, env e)
-// recomputes e's forward sweep and produces rows [g rows, (g + 1) rows).
+// Columns are dealt out to `groups` threads per environment: thread (group g, env e)
+// recomputes e's forward sweep and writes the columns whose tree index is g mod groups.
 struct DerivArgs {
   int64_t n;
-  int groups, rows;
+  int groups;
   Arr q, qd, x, d_q, d_qd, d_x;
 };
 
