@@ -250,20 +250,23 @@ __device__ __forceinline__ void ltdl_factor(double* H, const int* lam, double* D
   }
 }
 // B <- M^-1 B in place for R right-hand sides at once (B row-major [n][R]), M = L^T D L
-// from ltdl_factor: one walk over the ancestor chains serves all of them, so the chain
-// loads are paid once and each step has R independent updates.
+// from ltdl_factor; end[i] = one past the last descendant column of column i (subtrees are
+// contiguous in tree-column order). L^T y = b runs in pull form over each column's
+// descendant range, L x = z over its ancestor chain; each step has R independent updates.
 template <int R>
-__device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam, const double* Dinv, int n,
-                                                double* B) {
-  for (int k = n - 1; k >= 0; k--) {
-    double bk[R];
+__device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam, const int* end, const double* Dinv,
+                                                int n, double* B) {
+  for (int i = n - 1; i >= 0; i--) {
+    double y[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) bk[r] = B[k * R + r];
-    for (int i = lam[k]; i >= 0; i = lam[i]) {
+    for (int r = 0; r < R; r++) y[r] = B[i * R + r];
+    for (int k = i + 1; k < end[i]; k++) {
       const double h = H[ltdl_at(k, i)];
 #pragma unroll
-      for (int r = 0; r < R; r++) B[i * R + r] -= h * bk[r];
+      for (int r = 0; r < R; r++) y[r] -= h * B[k * R + r];
     }
+#pragma unroll
+    for (int r = 0; r < R; r++) B[i * R + r] = y[r];
   }
   for (int k = 0; k < n; k++) {
     double x[R];
@@ -287,13 +290,28 @@ __device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam,
 // LTDL solve. A thread writes the columns c = g, g + G, ... of one environment.
 template <int MAXJ>
 __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const RuntimeTab T{model};
+  const int nj = T.nj(), nv = T.nv(), nq = T.nq_ext();
+  // the column tree, shared by the block (one model): parent column, external index,
+  // one past the last descendant column
+  __shared__ int lam[MAXV], ext[MAXV], cend[MAXV];
+  for (int i = 1 + int(threadIdx.x); i < nj; i += blockDim.x) {
+    const DJoint& J = T.joint(i);
+    const int p = J.parent;
+    const int last = J.subtree_end < nj ? T.joint(J.subtree_end).ivx : nv;
+    for (int k = 0; k < J.nv; k++) {
+      const int t = J.ivx + k;
+      lam[t] = k > 0 ? t - 1 : (p > 0 ? T.joint(p).ivx + T.joint(p).nv - 1 : -1);
+      ext[t] = J.vcol + k;
+      cend[t] = last;
+    }
+  }
+  __syncthreads();
   const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= a.n * a.groups) return;
   const int64_t e = idx % a.n;
   const int g = int(idx / a.n);
-  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const RuntimeTab T{model};
-  const int nj = T.nj(), nv = T.nv(), nq = T.nq_ext();
   double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
@@ -302,18 +320,9 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
   DerivComposites<MAXJ> C;
   aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
   deriv_composites<MAXJ>(T, W, C);
-  int lam[MAXV], ext[MAXV];
   double H[MAXV * (MAXV + 1) / 2], Dinv[MAXV];
-  for (int i = 1; i < nj; i++) {
-    const DJoint& J = T.joint(i);
-    const int p = J.parent;
-    for (int k = 0; k < J.nv; k++) {
-      const int t = J.ivx + k;
-      lam[t] = k > 0 ? t - 1 : (p > 0 ? T.joint(p).ivx + T.joint(p).nv - 1 : -1);
-      ext[t] = J.vcol + k;
-      for (int b = t; b >= 0; b = lam[b]) H[ltdl_at(t, b)] = dot6(C.P[t], W.Sw[b]);
-    }
-  }
+  for (int t = 0; t < nv; t++)
+    for (int b = t; b >= 0; b = lam[b]) H[ltdl_at(t, b)] = dot6(C.P[t], W.Sw[b]);
   ltdl_factor(H, lam, Dinv, nv);
   // this thread's columns c = g, g + G, ... in batches of CB; right-hand sides per batch:
   // [dtau/dq columns | dtau/dqd columns | unit vectors] (CB each)
@@ -321,7 +330,7 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
   double B[MAXV * RB];
   int cols[CB], ncols = 0;
   auto flush = [&]() {
-    ltdl_solve_many<RB>(H, lam, Dinv, nv, B);
+    ltdl_solve_many<RB>(H, lam, cend, Dinv, nv, B);
     for (int m = 0; m < ncols; m++) {
       const int c = ext[cols[m]];
       for (int r = 0; r < nv; r++) {
