@@ -658,6 +658,7 @@ static int derivatives(bool aba, const sgdyn_model* m, int64_t n, const double* 
     const int64_t want_warps = aba ? (schedulers * 5 + 3) / 4 : (schedulers * 4 + 4) / 5;
     const int64_t g = std::min<int64_t>(nv, std::max<int64_t>(1, (want_warps + warps - 1) / warps));
     a.groups = int(g);
+    a.cols_per_thread = int((nv + g - 1) / g);
     a.q = make_arr(q, n, Mo.nq_ext(), layout);
     a.qd = make_arr(qd, n, nv, layout);
     a.x = make_arr(x, n, nv, layout);

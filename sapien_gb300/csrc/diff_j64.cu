@@ -20,7 +20,9 @@ cudaError_t launch_rnea_derivatives_j64(const DModel* dm, const DerivArgs& a, cu
   return cudaGetLastError();
 }
 cudaError_t launch_aba_derivatives_j64(const DModel* dm, const DerivArgs& a, cudaStream_t s) {
-  aba_derivatives_kernel<64><<<unsigned((a.n * a.groups + 31) / 32), 32, 0, s>>>(dm, a);
+  const unsigned grid = unsigned((a.n * a.groups + 31) / 32);
+  if (a.cols_per_thread <= 6) aba_derivatives_kernel<64, 6><<<grid, 32, 0, s>>>(dm, a);
+  else aba_derivatives_kernel<64, 12><<<grid, 32, 0, s>>>(dm, a);
   return cudaGetLastError();
 }
 cudaError_t launch_rollout_recompute_j64(const DModel* dm, const RolloutArgs& a, cudaStream_t s) {

@@ -287,8 +287,10 @@ __device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam,
 // dqdd/dqd = -M^-1 dtau/dqd, dqdd/dtau = M^-1 (Carpentier & Mansard, RSS 2018). The tau
 // columns come from the analytic column formulas above, M from the same composites
 // (M_ab = P_a . S_b for b an ancestor-or-self column of a), and every M^-1 product is an
-// LTDL solve. A thread writes the columns c = g, g + G, ... of one environment.
-template <int MAXJ>
+// LTDL solve. A thread writes the columns c = g, g + G, ... of one environment, solving
+// them in batches of CB columns (3 CB right-hand sides); the launch picks CB >= the
+// columns per thread where it can, so no batch runs half empty.
+template <int MAXJ, int CB>
 __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
   constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
   const RuntimeTab T{model};
@@ -324,9 +326,8 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
   for (int t = 0; t < nv; t++)
     for (int b = t; b >= 0; b = lam[b]) H[ltdl_at(t, b)] = dot6(C.P[t], W.Sw[b]);
   ltdl_factor(H, lam, Dinv, nv);
-  // this thread's columns c = g, g + G, ... in batches of CB; right-hand sides per batch:
-  // [dtau/dq columns | dtau/dqd columns | unit vectors] (CB each)
-  constexpr int CB = 8, RB = 3 * CB;
+  // right-hand sides per batch: [dtau/dq columns | dtau/dqd columns | unit vectors]
+  constexpr int RB = 3 * CB;
   double B[MAXV * RB];
   int cols[CB], ncols = 0;
   auto flush = [&]() {

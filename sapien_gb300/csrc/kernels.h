@@ -66,7 +66,7 @@ struct FkVjpArgs {
 // recomputes e's forward sweep and writes the columns whose tree index is g mod groups.
 struct DerivArgs {
   int64_t n;
-  int groups;
+  int groups, cols_per_thread;  // cols_per_thread = ceil(nv / groups)
   Arr q, qd, x, d_q, d_qd, d_x;
 };
 
