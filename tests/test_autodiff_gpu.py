@@ -124,6 +124,45 @@ def test_dense_derivatives_match_finite_differences(name):
         assert rel(Minv[e], np.linalg.inv(Mref)) < 1e-8
 
 
+def test_dense_derivatives_do_not_depend_on_the_column_split():
+    """Columns are dealt to a number of threads per environment that depends on the batch
+    size; every column is computed the same way, so a small batch (one thread per column)
+    and the same environments inside a large batch (a few threads each) agree bit for bit."""
+    robot = syn.humanoid()
+    pm, _ = pair(robot)
+    q, qd, qdd, tau = robot.sample(4096, seed=17)
+    big_r = [x[:5].cpu() for x in ad.rnea_derivatives(pm, cu(q), cu(qd), cu(qdd))]
+    big_a = [x[:5].cpu() for x in ad.aba_derivatives(pm, cu(q), cu(qd), cu(tau))]
+    small_r = [x.cpu() for x in ad.rnea_derivatives(pm, cu(q[:5]), cu(qd[:5]), cu(qdd[:5]))]
+    small_a = [x.cpu() for x in ad.aba_derivatives(pm, cu(q[:5]), cu(qd[:5]), cu(tau[:5]))]
+    for x, y in zip(big_r + big_a, small_r + small_a):
+        assert T().equal(x, y)
+
+
+def test_dense_derivatives_of_a_40_joint_chain():
+    """The 64-joint kernels (largest per-thread frames): dtau/dqdd = M, dqdd/dtau = M^-1 and
+    rows equal to the reverse-mode VJP."""
+    robot = syn.serial_chain(40, seed=2)
+    pm, o = pair(robot)
+    q, qd, qdd, tau = robot.sample(6, seed=9)
+    dq, dqd, M = (x.cpu().numpy() for x in ad.rnea_derivatives(pm, cu(q), cu(qd), cu(qdd)))
+    aq, aqd, Minv = (x.cpu().numpy() for x in ad.aba_derivatives(pm, cu(q), cu(qd), cu(tau)))
+    w = np.random.default_rng(3).normal(size=(6, robot.nv))
+    qb, qdb, _ = (x.cpu().numpy() for x in ad.inverse_dynamics_vjp(pm, cu(q), cu(qd), cu(qdd), cu(w)))
+    assert rel(qb, np.einsum("er,erc->ec", w, dq)) < 1e-11
+    assert rel(qdb, np.einsum("er,erc->ec", w, dqd)) < 1e-11
+    for e in range(6):
+        Mref = o.compute_generalized_mass_matrix(q[e])
+        assert rel(M[e], Mref) < 1e-10
+        assert rel(Minv[e] @ Mref, np.eye(robot.nv)) < 1e-8
+    # dqdd/d(q, qd) = -M^-1 dtau/d(q, qd) at qdd = ABA(q, qd, tau)
+    qdd_a = np.stack([o.compute_forward_dynamics(q[e], qd[e], tau[e]) for e in range(6)])
+    dq_a, dqd_a, _ = (x.cpu().numpy() for x in ad.rnea_derivatives(pm, cu(q), cu(qd), cu(qdd_a)))
+    for e in range(6):
+        assert rel(aq[e], -Minv[e] @ dq_a[e]) < 1e-8
+        assert rel(aqd[e], -Minv[e] @ dqd_a[e]) < 1e-8
+
+
 def test_vjp_equals_dense_rows():
     robot = syn.arm_with_fingers()
     pm, _ = pair(robot)
