@@ -237,6 +237,12 @@ int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd,
  * SE(3) by its body twist, like Pinocchio's integrate). With sgdyn_batch_step (ABA) this
  * makes one rollout step; both launches can be captured into one CUDA graph. */
 int sgdyn_batch_integrate(sgdyn_batch* b, double dt, double* q, double* qd, const double* qdd, void* stream);
+/* One rollout step in one launch: qdd_out = ABA(q, qd, tau), then the semi-implicit Euler
+ * update of sgdyn_batch_integrate, each environment right after its own sweep, in place
+ * on q / qd. Results equal sgdyn_batch_step (SGDYN_OP_ABA) followed by
+ * sgdyn_batch_integrate, bit for bit. */
+int sgdyn_batch_step_integrate(sgdyn_batch* b, double dt, double* q, double* qd, const double* tau, double* qdd_out,
+                               void* stream);
 
 /* ---- differentiation (additions; the reference has no derivative API, see
  * pinocchio/cmake/pinocchio.cmake:4 which builds Pinocchio without autodiff) ----------

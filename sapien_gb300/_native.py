@@ -69,6 +69,7 @@ EXPORTED = (
     "sgdyn_batch_set_lanes",
     "sgdyn_batch_step",
     "sgdyn_batch_integrate",
+    "sgdyn_batch_step_integrate",
     "sgdyn_model_set_lanes",
     "sgdyn_model_team_table",
     "sgdyn_jit_max_joints",
@@ -140,6 +141,7 @@ def load():
     L.sgdyn_batch_set_lanes.argtypes = [vp, P(i32)]
     L.sgdyn_batch_step.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.sgdyn_batch_integrate.argtypes = [vp, dbl, vp, vp, vp, vp]
+    L.sgdyn_batch_step_integrate.argtypes = [vp, dbl, vp, vp, vp, vp, vp]
     L.sgdyn_model_from_articulation.argtypes = [vp, i32, vp, i32, P(dbl), i32, P(vp)]
     L.sgdyn_compute_passive_force_f32.argtypes = [vp, i64, vp, vp, i64, i32, i32, vp, i64, vp]
     L.sgdyn_jit_config.argtypes = [i32, i64, P(i32), P(i64)]

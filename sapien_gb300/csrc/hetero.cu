@@ -44,7 +44,35 @@ struct HeteroArgs {
   int ntiles;
   unsigned int* head;
   StepArgs io;
+  // semi-implicit Euler after the sweep (integrate != 0): q / qd rows updated in place
+  int integrate;
+  double dt;
+  double* q_state;
+  double* qd_state;
 };
+
+// qd += dt qdd, then q advanced by dt qd on one environment's padded rows (angles and
+// slides add; a free flyer moves on SE(3) by its body twist).
+__device__ __forceinline__ void integrate_env(const DModel* m, double* q, double* qd, const double* qdd, double dt) {
+  const DJoint* JT = model_joints(m);
+  for (int i = 1; i < m->nj; i++) {
+    const DJoint& J = JT[i];
+    if (J.kind == JK_FREEFLYER) {
+      double v[6];
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const double w = fma(dt, qdd[J.vcol + k], qd[J.vcol + k]);
+        qd[J.vcol + k] = w;
+        v[k] = dt * w;
+      }
+      free_flyer_integrate(q + J.qcol, v);
+    } else {
+      const double w = fma(dt, qdd[J.vcol], qd[J.vcol]);
+      qd[J.vcol] = w;
+      q[J.qcol] = fma(dt, w, q[J.qcol]);
+    }
+  }
+}
 
 template <int MAXJ, int OPS>
 __global__ void hetero_kernel(const HeteroArgs a) {
@@ -65,6 +93,17 @@ __global__ void hetero_kernel(const HeteroArgs a) {
       const bool valid = slot < tile.z;
       const TeamLanes tm{a.teams + a.team_offset[tile.x], lane % tile.w, valid};
       step_env_t<MAXJ, OPS>(RuntimeTab{m}, a.io, int64_t(a.perm[tile.y + (valid ? slot : 0)]), tm);
+    }
+    if (a.integrate) {
+      // the sweep's reads of q / qd and writes of qdd are done on every lane of the tile;
+      // one lane per environment then integrates it
+      __syncwarp();
+      const int w = tile.w <= 1 ? 1 : tile.w;
+      if (lane % w == 0 && lane / w < tile.z) {
+        const int64_t env = a.perm[tile.y + lane / w];
+        integrate_env(m, a.q_state + env * a.io.q.es, a.qd_state + env * a.io.qd.es,
+                      a.io.qdd_out.p + env * a.io.qdd_out.es, a.dt);
+      }
     }
     __syncwarp();
   }
@@ -112,7 +151,8 @@ __global__ void __launch_bounds__(kIntegrateThreads) hetero_integrate_kernel(con
     const int64_t c = int64_t(el) * a.max_nv + J.vcol;
     const double w = fma(dt, QDD[c], QD[c]);
     QD[c] = w;
-    Q[int64_t(el) * a.max_nq + J.qcol] += dt * w;
+    double& qc = Q[int64_t(el) * a.max_nq + J.qcol];
+    qc = fma(dt, w, qc);
   }
   if (threadIdx.x >= envs) return;
   const DModel* m = models[threadIdx.x];
@@ -408,9 +448,9 @@ int sgdyn_batch_integrate(sgdyn_batch* b, double dt, double* q, double* qd, cons
   return SGDYN_OK;
 }
 
-int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
-                     double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream) {
-  SG_TRACE("sgdyn_batch_step");
+static int batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
+                      double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream,
+                      bool integrate, double dt) {
   if (!b) return set_last_error(SGDYN_ERR_NULL, "null batch");
   if (b->n == 0) return SGDYN_OK;
   if (!dev_ptr(q)) return set_last_error(SGDYN_ERR_NULL, "q is null or not device memory");
@@ -440,6 +480,10 @@ int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd,
   a.io.M = env_major(M, nv * nv);
   a.io.tau_out = env_major(tau_out, nv);
   a.io.qdd_out = env_major(qdd_out, nv);
+  a.integrate = integrate ? 1 : 0;
+  a.dt = dt;
+  a.q_state = const_cast<double*>(q);
+  a.qd_state = const_cast<double*>(qd);
   auto s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemsetAsync(b->head, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("memset failed: ") + cudaGetErrorString(e));
@@ -448,6 +492,18 @@ int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd,
                         : launch_hetero_bucket<32>(ops, a, grid, block, s);
   if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   return SGDYN_OK;
+}
+
+int sgdyn_batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd, const double* qdd, const double* tau,
+                     double* link_poses, double* J, double* M, double* tau_out, double* qdd_out, void* stream) {
+  SG_TRACE("sgdyn_batch_step");
+  return batch_step(b, ops, q, qd, qdd, tau, link_poses, J, M, tau_out, qdd_out, stream, false, 0.0);
+}
+
+int sgdyn_batch_step_integrate(sgdyn_batch* b, double dt, double* q, double* qd, const double* tau, double* qdd_out,
+                               void* stream) {
+  SG_TRACE("sgdyn_batch_step_integrate");
+  return batch_step(b, OP_ABA, q, qd, nullptr, tau, nullptr, nullptr, nullptr, nullptr, qdd_out, stream, true, dt);
 }
 
 }  // extern "C"

@@ -138,9 +138,13 @@ class HeteroBatch:
                                                    ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
 
     def rollout_step(self, q, qd, tau, dt, out):
-        """One rollout step in place: qdd = ABA(q, qd, tau) into out["qacc"], then integrate."""
-        self.step(q, qd, None, tau, N.OP_FORWARD_DYNAMICS, out)
-        self.integrate(q, qd, out["qacc"], dt)
+        """One rollout step in place and in one launch: qdd = ABA(q, qd, tau) into
+        out["qacc"], then the semi-implicit Euler update of `integrate`, each environment
+        right after its own sweep (bitwise the same as `step` + `integrate`)."""
+        with torch.cuda.device(self.device):
+            N.check(N.load().sgdyn_batch_step_integrate(
+                self._h, float(dt), _p(q), _p(qd), _p(tau), _p(out["qacc"]),
+                ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
 
     def capture_rollout(self, q, qd, tau, dt, steps):
         """Record a whole rollout of `steps` semi-implicit-Euler steps (ABA + integrate per

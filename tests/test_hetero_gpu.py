@@ -166,3 +166,28 @@ def test_hetero_rollout_graph_matches_oracle():
         gqd = qd[idx, : m.nv].cpu().numpy()
         assert rel_per_env(gq, qk) <= 1e-9
         assert rel_per_env(gqd, qdk) <= 1e-8
+
+
+def test_fused_rollout_step_equals_step_then_integrate():
+    """sgdyn_batch_step_integrate (ABA and the Euler update in one launch) gives the same
+    q, qd and qacc bit for bit as the two-launch sequence, one lane and teams alike."""
+    import torch
+
+    from sapien_gb300 import _native as N
+
+    batch, oracles, inputs, (q, qd, qdd, tau) = setup(n=260, seed=9)
+    tau = 0.1 * tau
+    for lanes in ([1, 1, 1], [1, 2, 4]):
+        batch.set_lanes(lanes)
+        qa, qda, qb, qdb = q.clone(), qd.clone(), q.clone(), qd.clone()
+        oa, ob = batch.alloc_outputs(N.OP_FORWARD_DYNAMICS), batch.alloc_outputs(N.OP_FORWARD_DYNAMICS)
+        for _ in range(5):
+            batch.rollout_step(qa, qda, tau, 2e-3, oa)
+            batch.step(qb, qdb, None, tau, N.OP_FORWARD_DYNAMICS, ob)
+            batch.integrate(qb, qdb, ob["qacc"], 2e-3)
+        torch.cuda.synchronize()
+        for k, m in enumerate(batch.models):
+            idx = torch.as_tensor(np.nonzero(batch.model_of_env == k)[0], device=q.device)
+            assert torch.equal(qa[idx, : m.nq_ext], qb[idx, : m.nq_ext]), lanes
+            assert torch.equal(qda[idx, : m.nv], qdb[idx, : m.nv]), lanes
+            assert torch.equal(oa["qacc"][idx, : m.nv], ob["qacc"][idx, : m.nv]), lanes
