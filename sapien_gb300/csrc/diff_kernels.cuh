@@ -320,12 +320,40 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
   load_row<MAXJ>(a.x, e, nv, tau);
   DynWork<MAXJ> W;
   DerivComposites<MAXJ> C;
-  aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
+  // forward dynamics through the factorisation built anyway: the RNEA sweep at qdd = 0
+  // gives the bias accelerations and forces, qdd = M^-1 (tau - tau_bias), then the
+  // accelerations and subtree forces take the qdd terms (a_i += sum_{m <= i} S_m qdd_m,
+  // F_i += sum_{k in subtree(i)} I_k da_k)
+  for (int c = 0; c < nv; c++) qdd[c] = 0.0;
+  rnea_forward<MAXJ>(T, q, qd, qdd, W);
   deriv_composites<MAXJ>(T, W, C);
   double H[MAXV * (MAXV + 1) / 2], Dinv[MAXV];
   for (int t = 0; t < nv; t++)
     for (int b = t; b >= 0; b = lam[b]) H[ltdl_at(t, b)] = dot6(C.P[t], W.Sw[b]);
   ltdl_factor(H, lam, Dinv, nv);
+  {
+    double x[MAXV];
+    for (int i = 1; i < nj; i++) {
+      const DJoint& J = T.joint(i);
+      for (int k = 0; k < J.nv; k++) x[J.ivx + k] = tau[J.vcol + k] - dot6(W.Sw[J.ivx + k], C.F[i]);
+    }
+    ltdl_solve_many<1>(H, lam, cend, Dinv, nv, x);
+    const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+    Mot da[MAXJ];
+    for (int i = 1; i < nj; i++) {
+      const DJoint& J = T.joint(i);
+      Mot d = J.parent > 0 ? da[J.parent] : zero;
+      for (int k = 0; k < J.nv; k++) d = axpy6(x[J.ivx + k], W.Sw[J.ivx + k], d);
+      da[i] = d;
+      W.acc[i] = add6(W.acc[i], d);
+    }
+    for (int i = 1; i < nj; i++) da[i] = rbi_mul(W.Iw[i], da[i]);  // now I_i da_i, summed over subtrees below
+    for (int i = nj - 1; i >= 1; i--) {
+      const int p = T.joint(i).parent;
+      if (p > 0) da[p] = add6(da[p], da[i]);
+      C.F[i] = add6(C.F[i], da[i]);
+    }
+  }
   // right-hand sides per batch: [dtau/dq columns | dtau/dqd columns | unit vectors]
   constexpr int RB = 3 * CB;
   double B[MAXV * RB];

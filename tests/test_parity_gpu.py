@@ -162,6 +162,42 @@ def test_drop_in_single_instance_api():
         assert np.abs(M - o.compute_generalized_mass_matrix(q[e])).max() <= 1e-10 * np.abs(M).max()
 
 
+def test_chain7_single_instance_1000_samples():
+    """The CPU-runnable reference configuration: a seeded 7-DoF revolute chain (offsets
+    U[0.05, 0.4] m along random unit axes, random unit joint axes, masses U[0.5, 3] kg,
+    inertias R diag(U[1e-3, 5e-2]) R^T) and 1000 samples q ~ U[-pi, pi], qd, qdd ~ N(0, 1),
+    tau ~ N(0, 10), through the single-instance drop-in methods: FK + get_link_pose (float32
+    poses, as the reference returns them), full Jacobian + get_link_jacobian, mass matrix,
+    RNEA and ABA against the oracle."""
+    robot = syn.serial_chain(7)
+    pm, o = pair(robot)
+    n = 1000
+    q, qd, qdd, tau = robot.sample(n, seed=0)
+    nl = len(robot.link_names)
+    worst = dict.fromkeys(("poses", "J", "M", "tau", "qdd"), 0.0)
+
+    def upd(k, g, r):
+        worst[k] = max(worst[k], np.abs(g - r).max() / max(np.abs(r).max(), 1e-300))
+
+    for e in range(n):
+        pm.compute_forward_kinematics(q[e])
+        o.compute_forward_kinematics(q[e])
+        for li in range(nl):
+            pose = pm.get_link_pose(li)
+            T4 = o.get_link_pose_matrix(li)
+            upd("poses", pose.p.astype(np.float64), T4[:3, 3])
+        pm.compute_full_jacobian(q[e])
+        o.compute_full_jacobian(q[e])
+        for li in range(nl):
+            upd("J", pm.get_link_jacobian(li), o.get_link_jacobian(li))
+        upd("M", pm.compute_generalized_mass_matrix(q[e]), o.compute_generalized_mass_matrix(q[e]))
+        upd("tau", pm.compute_inverse_dynamics(q[e], qd[e], qdd[e]), o.compute_inverse_dynamics(q[e], qd[e], qdd[e]))
+        upd("qdd", pm.compute_forward_dynamics(q[e], qd[e], tau[e]), o.compute_forward_dynamics(q[e], qd[e], tau[e]))
+    assert worst["poses"] <= 2e-7, worst  # float32 positions
+    assert worst["J"] <= 1e-10 and worst["M"] <= 1e-10 and worst["tau"] <= 1e-10, worst
+    assert worst["qdd"] <= 1e-8, worst
+
+
 def test_col_major_layout_through_c_abi():
     robot = syn.arm_with_fingers()
     pm, o = pair(robot)
