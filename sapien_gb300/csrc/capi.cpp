@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -731,6 +733,73 @@ int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_
   return SGDYN_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// A second stream per device for the rollout backward's recompute launches (created once,
+// kept for the process); null if it cannot be created.
+cudaStream_t side_stream() {
+  static std::mutex mu;
+  static std::map<int, cudaStream_t> streams;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) s = nullptr;
+  streams[dev] = s;
+  return s;
+}
+
+// Rollout backward with the recompute of the next (earlier) group of segments running on a
+// second stream while the current group's reverse sweep runs on the caller's stream. The
+// reverse sweep at small batches keeps one warp per SM busy and leaves the other FP64
+// schedulers idle; the recompute fills them. Groups alternate between two halves of the
+// scratch; a recompute waits for the reverse that last used its half.
+cudaError_t rollout_backward_overlapped(const DModel* dm, int nj, RolloutArgs a, int64_t seg_doubles, int G,
+                                        cudaStream_t s1, cudaStream_t s2) {
+  const int nseg = (a.T + a.K - 1) / a.K;
+  std::vector<RolloutArgs> groups;
+  for (int hi = nseg; hi > 0; hi -= G) {
+    RolloutArgs g = a;
+    g.s_lo = hi - G > 0 ? hi - G : 0;
+    g.s_cnt = hi - g.s_lo;
+    g.scratch = a.scratch + int64_t(groups.size() % 2) * G * seg_doubles;
+    groups.push_back(g);
+  }
+  const int m = int(groups.size());
+  std::vector<cudaEvent_t> ev(2 * m + 1, nullptr);
+  cudaError_t e = cudaSuccess;
+  for (auto& x : ev)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+  cudaEvent_t start = ev[2 * m];
+  auto rec = [&](int k) { return ev[k]; };
+  auto rev = [&](int k) { return ev[m + k]; };
+  if (e == cudaSuccess) e = cudaEventRecord(start, s1);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, start, 0);
+  if (e == cudaSuccess) e = launch_rollout_recompute(dm, nj, groups[0], s2);
+  if (e == cudaSuccess) e = cudaEventRecord(rec(0), s2);
+  for (int k = 0; k < m && e == cudaSuccess; k++) {
+    e = cudaStreamWaitEvent(s1, rec(k), 0);
+    if (e == cudaSuccess) e = launch_rollout_reverse(dm, nj, groups[k], s1);
+    if (e == cudaSuccess) e = cudaEventRecord(rev(k), s1);
+    if (e == cudaSuccess && k + 1 < m) {
+      if (k >= 1) e = cudaStreamWaitEvent(s2, rev(k - 1), 0);
+      if (e == cudaSuccess) e = launch_rollout_recompute(dm, nj, groups[k + 1], s2);
+      if (e == cudaSuccess) e = cudaEventRecord(rec(k + 1), s2);
+    }
+  }
+  for (auto& x : ev)
+    if (x) cudaEventDestroy(x);  // released once the recorded work completes
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
 int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, int checkpoint_every,
                            const double* q_ckpt, const double* qd_ckpt, const double* tau, const double* qT_bar,
                            const double* qdT_bar, double* q0_bar, double* qd0_bar, double* tau_bar, double* scratch,
@@ -765,6 +834,16 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
     a.q0_bar = q0_bar; a.qd0_bar = qd0_bar; a.tau_bar = tau_bar; a.scratch = scratch;
     const cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nj = Mo.njoints();
+    // two scratch halves of G segments each and at least two groups: overlap recompute and
+    // reverse on two streams (not while the caller's stream is being captured)
+    const int nseg = T > 0 ? (T + checkpoint_every - 1) / checkpoint_every : 0;
+    const int64_t fit = need > 0 ? scratch_bytes / need : 0;
+    const int G = int(std::min<int64_t>(fit / 2, std::max(1, nseg / 5)));
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusActive;
+    if (nseg >= 2 && G >= 1 && (nseg + G - 1) / G >= 2 && cs == cudaStreamCaptureStatusNone)
+      if (cudaStream_t s2 = side_stream())
+        return launch_status(rollout_backward_overlapped(dm, nj, a, need / 8, G, st, s2));
     return launch_status(rollout_backward_grouped(
         a, need / 8, scratch_bytes / 8, [&](const RolloutArgs& g) { return launch_rollout_recompute(dm, nj, g, st); },
         [&](const RolloutArgs& g) { return launch_rollout_reverse(dm, nj, g, st); }));
