@@ -299,7 +299,11 @@ int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_
  * (caller-owned device memory of at least sgdyn_rollout_scratch_bytes bytes), and then
  * reversed step by step. A scratch of k times the minimum lets k segments recompute at
  * once (one thread per segment and environment), which fills the GPU at small n;
- * ceil(T / checkpoint_every) times the minimum recomputes all segments in one launch. */
+ * ceil(T / checkpoint_every) times the minimum recomputes all segments in one launch.
+ * With room for two groups of segments (and `stream` not being captured) the recompute of
+ * the next group runs on an internal second stream of the device while the current group
+ * is reversed on `stream`; every launch on it is ordered after the work already on
+ * `stream` and before what follows there, so the call stays stream-ordered. */
 int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, int checkpoint_every,
                            const double* q_ckpt, const double* qd_ckpt, const double* tau, const double* qT_bar,
                            const double* qdT_bar, double* q0_bar, double* qd0_bar, double* tau_bar, double* scratch,
