@@ -100,6 +100,61 @@ def test_two_link_closed_form():
         assert np.abs(o.compute_inverse_dynamics(q, qd, qdd) - (M @ qdd + C @ qd + gv)).max() < 1e-12
 
 
+def floating_body_urdf(m, c, rpy, I):
+    return f"""<robot name="fb">
+  <link name="world"/>
+  <link name="body"><inertial><origin xyz="{c[0]} {c[1]} {c[2]}" rpy="{rpy[0]} {rpy[1]} {rpy[2]}"/>
+    <mass value="{m}"/><inertia ixx="{I[0]}" ixy="{I[1]}" ixz="{I[2]}" iyy="{I[3]}" iyz="{I[4]}" izz="{I[5]}"/>
+  </inertial></link>
+  <joint name="ff" type="floating"><parent link="world"/><child link="body"/></joint>
+</robot>"""
+
+
+def test_floating_body_newton_euler():
+    """One free-floating rigid body: RNEA against the Newton-Euler equations written with
+    3-vectors in the body frame. q = (x y z qx qy qz qw) with R(q) body -> world; qd, qdd =
+    body twist (v, w) and its derivative; the classical acceleration of the centre of mass c
+    is a_v + w x v + a_w x c + w x (w x c); gravity enters as R^T g. tau = (F, c x F + Ic a_w
+    + w x Ic w) with F = m (that acceleration - R^T g). Also M = the body's 6x6 inertia about
+    its origin and ABA = RNEA^-1."""
+    rng = np.random.default_rng(4)
+    m, c, rpy = 2.3, np.array([0.11, -0.07, 0.19]), (0.3, -0.5, 1.1)
+    Ip = np.array([0.03, 0.004, -0.002, 0.05, 0.006, 0.04])  # principal frame at rpy, SPD
+    g = np.array([0.0, 0.0, -9.81])
+    o = Oracle(floating_body_urdf(m, c, rpy, Ip), tuple(g))
+    o.set_joint_order(["ff"])
+    o.set_link_order(["world", "body"])
+    # inertia about the centre of mass in the body frame: R_rpy I R_rpy^T
+    cr, sr, cp, sp, cy, sy = (math.cos(rpy[0]), math.sin(rpy[0]), math.cos(rpy[1]), math.sin(rpy[1]),
+                              math.cos(rpy[2]), math.sin(rpy[2]))
+    Rrpy = np.array([[cy * cp, cy * sp * sr - sy * cr, cy * sp * cr + sy * sr],
+                     [sy * cp, sy * sp * sr + cy * cr, sy * sp * cr - cy * sr],
+                     [-sp, cp * sr, cp * cr]])
+    Il = np.array([[Ip[0], Ip[1], Ip[2]], [Ip[1], Ip[3], Ip[4]], [Ip[2], Ip[4], Ip[5]]])
+    Ic = Rrpy @ Il @ Rrpy.T
+    cx = np.array([[0, -c[2], c[1]], [c[2], 0, -c[0]], [-c[1], c[0], 0]])
+    M6 = np.zeros((6, 6))
+    M6[:3, :3], M6[:3, 3:], M6[3:, :3], M6[3:, 3:] = m * np.eye(3), -m * cx, m * cx, Ic + m * cx.T @ cx
+    for _ in range(10):
+        quat = rng.normal(size=4)
+        quat /= np.linalg.norm(quat)
+        q = np.concatenate([rng.normal(size=3), quat])
+        qd, qdd = rng.normal(size=6), rng.normal(size=6)
+        x, y, z, w = quat
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        v, om, av, aw = qd[:3], qd[3:], qdd[:3], qdd[3:]
+        acc_c = av + np.cross(om, v) + np.cross(aw, c) + np.cross(om, np.cross(om, c))
+        F = m * (acc_c - R.T @ g)
+        N = np.cross(c, F) + Ic @ aw + np.cross(om, Ic @ om)
+        expect = np.concatenate([F, N])
+        tau = o.compute_inverse_dynamics(q, qd, qdd)
+        assert np.abs(tau - expect).max() <= 1e-12 * np.abs(expect).max()
+        assert np.abs(o.compute_generalized_mass_matrix(q) - M6).max() <= 1e-14
+        assert np.abs(o.compute_forward_dynamics(q, qd, tau) - qdd).max() <= 1e-11 * np.abs(qdd).max()
+
+
 @pytest.mark.parametrize("name", list(ROBOTS))
 def test_dynamics_identities(name):
     robot = ROBOTS[name]()

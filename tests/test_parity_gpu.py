@@ -338,3 +338,46 @@ def test_full_size_batch_properties_and_parity():
     t = lambda a: T.from_numpy(a).cuda()  # noqa: E731
     back = pm.compute_inverse_dynamics_batched(t(q), t(qd), T.from_numpy(g["qacc"]).cuda()).cpu().numpy()
     assert rel_per_env(back, tau) <= 1e-9
+
+
+def test_floating_body_newton_euler_on_gpu():
+    """The CUDA RNEA / CRBA / ABA of one free-floating rigid body against the Newton-Euler
+    closed form of tests/test_oracle.py (body-frame twist, gravity as R^T g), batched."""
+    import math
+
+    from test_oracle import floating_body_urdf
+
+    m, c, rpy = 2.3, np.array([0.11, -0.07, 0.19]), (0.3, -0.5, 1.1)
+    Ip = np.array([0.03, 0.004, -0.002, 0.05, 0.006, 0.04])
+    g = np.array([0.0, 0.0, -9.81])
+    pm = PinocchioModel(floating_body_urdf(m, c, rpy, Ip), list(g))
+    pm.set_joint_order(["ff"])
+    pm.set_link_order(["world", "body"])
+    cr, sr, cp, sp, cy, sy = (math.cos(rpy[0]), math.sin(rpy[0]), math.cos(rpy[1]), math.sin(rpy[1]),
+                              math.cos(rpy[2]), math.sin(rpy[2]))
+    Rrpy = np.array([[cy * cp, cy * sp * sr - sy * cr, cy * sp * cr + sy * sr],
+                     [sy * cp, sy * sp * sr + cy * cr, sy * sp * cr - cy * sr],
+                     [-sp, cp * sr, cp * cr]])
+    Il = np.array([[Ip[0], Ip[1], Ip[2]], [Ip[1], Ip[3], Ip[4]], [Ip[2], Ip[4], Ip[5]]])
+    Ic = Rrpy @ Il @ Rrpy.T
+    rng = np.random.default_rng(6)
+    n = 100
+    quat = rng.normal(size=(n, 4))
+    quat /= np.linalg.norm(quat, axis=1, keepdims=True)
+    q = np.concatenate([rng.normal(size=(n, 3)), quat], axis=1)
+    qd, qdd = rng.normal(size=(n, 6)), rng.normal(size=(n, 6))
+    T = torch()
+    tau = pm.compute_inverse_dynamics_batched(T.from_numpy(q).cuda(), T.from_numpy(qd).cuda(),
+                                              T.from_numpy(qdd).cuda()).cpu().numpy()
+    back = pm.compute_forward_dynamics_batched(T.from_numpy(q).cuda(), T.from_numpy(qd).cuda(),
+                                               T.from_numpy(tau).cuda()).cpu().numpy()
+    for e in range(n):
+        x, y, z, w = quat[e]
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        v, om, av, aw = qd[e, :3], qd[e, 3:], qdd[e, :3], qdd[e, 3:]
+        F = m * (av + np.cross(om, v) + np.cross(aw, c) + np.cross(om, np.cross(om, c)) - R.T @ g)
+        expect = np.concatenate([F, np.cross(c, F) + Ic @ aw + np.cross(om, Ic @ om)])
+        assert np.abs(tau[e] - expect).max() <= 1e-12 * np.abs(expect).max(), e
+        assert np.abs(back[e] - qdd[e]).max() <= 1e-10 * np.abs(qdd[e]).max(), e
