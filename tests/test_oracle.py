@@ -100,6 +100,43 @@ def test_two_link_closed_form():
         assert np.abs(o.compute_inverse_dynamics(q, qd, qdd) - (M @ qdd + C @ qd + gv)).max() < 1e-12
 
 
+def cart_pole_urdf(mc, mp, l, Iyy):
+    return f"""<robot name="cp">
+  <link name="rail"/>
+  <link name="cart"><inertial><mass value="{mc}"/>
+    <inertia ixx="0.02" ixy="0" ixz="0" iyy="0.03" iyz="0" izz="0.04"/></inertial></link>
+  <link name="pole"><inertial><origin xyz="0 0 {l}"/><mass value="{mp}"/>
+    <inertia ixx="0.01" ixy="0" ixz="0" iyy="{Iyy}" iyz="0" izz="0.01"/></inertial></link>
+  <joint name="slide" type="prismatic"><axis xyz="1 0 0"/><parent link="rail"/><child link="cart"/>
+    <limit lower="-5" upper="5" effort="0" velocity="0"/></joint>
+  <joint name="hinge" type="revolute"><axis xyz="0 1 0"/><parent link="cart"/><child link="pole"/>
+    <limit lower="-3.2" upper="3.2" effort="0" velocity="0"/></joint>
+</robot>"""
+
+
+def test_cart_pole_closed_form():
+    """Prismatic cart (x) carrying a pole hinged about y (angle th, centre of mass l up the
+    pole): from the Lagrangian T = (mc + mp) xd^2 / 2 + mp l cos(th) xd thd + (mp l^2 + Iyy)
+    thd^2 / 2, V = mp g l cos(th): M = [[mc + mp, mp l c], [mp l c, mp l^2 + Iyy]],
+    C = [[0, -mp l s thd], [0, 0]], gravity torques (0, -mp g l s)."""
+    mc, mp, l, Iyy, g = 1.9, 0.7, 0.45, 0.012, 9.81
+    o = Oracle(cart_pole_urdf(mc, mp, l, Iyy), (0, 0, -g))
+    o.set_joint_order(["slide", "hinge"])
+    o.set_link_order(["rail", "cart", "pole"])
+    rng = np.random.default_rng(2)
+    for _ in range(10):
+        q, qd, qdd = rng.uniform(-3, 3, 2), rng.normal(size=2), rng.normal(size=2)
+        c, s_ = math.cos(q[1]), math.sin(q[1])
+        M = np.array([[mc + mp, mp * l * c], [mp * l * c, mp * l * l + Iyy]])
+        C = np.array([[0.0, -mp * l * s_ * qd[1]], [0.0, 0.0]])
+        gv = np.array([0.0, -mp * g * l * s_])
+        assert np.abs(o.compute_generalized_mass_matrix(q) - M).max() < 1e-14
+        assert np.abs(o.compute_coriolis_matrix(q, qd) - C).max() < 1e-13
+        tau = o.compute_inverse_dynamics(q, qd, qdd)
+        assert np.abs(tau - (M @ qdd + C @ qd + gv)).max() < 1e-12
+        assert np.abs(o.compute_forward_dynamics(q, qd, tau) - qdd).max() < 1e-12
+
+
 def floating_body_urdf(m, c, rpy, I):
     return f"""<robot name="fb">
   <link name="world"/>

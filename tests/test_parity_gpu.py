@@ -381,3 +381,35 @@ def test_floating_body_newton_euler_on_gpu():
         expect = np.concatenate([F, np.cross(c, F) + Ic @ aw + np.cross(om, Ic @ om)])
         assert np.abs(tau[e] - expect).max() <= 1e-12 * np.abs(expect).max(), e
         assert np.abs(back[e] - qdd[e]).max() <= 1e-10 * np.abs(qdd[e]).max(), e
+
+
+def test_cart_pole_closed_form_on_gpu():
+    """The CUDA sweeps on a prismatic cart with a hinged pole against the Lagrangian closed
+    form of tests/test_oracle.py: M, the Coriolis matrix, RNEA and ABA, batched."""
+    import math
+
+    from test_oracle import cart_pole_urdf
+
+    mc, mp, l, Iyy, g = 1.9, 0.7, 0.45, 0.012, 9.81
+    pm = PinocchioModel(cart_pole_urdf(mc, mp, l, Iyy), [0, 0, -g])
+    pm.set_joint_order(["slide", "hinge"])
+    pm.set_link_order(["rail", "cart", "pole"])
+    rng = np.random.default_rng(3)
+    n = 64
+    q, qd, qdd = rng.uniform(-3, 3, (n, 2)), rng.normal(size=(n, 2)), rng.normal(size=(n, 2))
+    T = torch()
+    cq, cqd, cqdd = (T.from_numpy(x).cuda() for x in (q, qd, qdd))
+    Mg = pm.compute_generalized_mass_matrix_batched(cq).cpu().numpy().reshape(n, 2, 2)
+    Cg = pm.compute_coriolis_matrix_batched(cq, cqd).cpu().numpy().reshape(n, 2, 2)
+    tau = pm.compute_inverse_dynamics_batched(cq, cqd, cqdd)
+    back = pm.compute_forward_dynamics_batched(cq, cqd, tau).cpu().numpy()
+    tau = tau.cpu().numpy()
+    for e in range(n):
+        c, s = math.cos(q[e, 1]), math.sin(q[e, 1])
+        M = np.array([[mc + mp, mp * l * c], [mp * l * c, mp * l * l + Iyy]])
+        C = np.array([[0.0, -mp * l * s * qd[e, 1]], [0.0, 0.0]])
+        gv = np.array([0.0, -mp * g * l * s])
+        assert np.abs(Mg[e] - M).max() < 1e-14
+        assert np.abs(Cg[e] - C).max() < 1e-13
+        assert np.abs(tau[e] - (M @ qdd[e] + C @ qd[e] + gv)).max() < 1e-12
+        assert np.abs(back[e] - qdd[e]).max() < 1e-12
