@@ -32,12 +32,12 @@ ROBOTS = {
 }
 
 
-def pendulum_urdf(m, l, Iyy, axis="0 1 0"):
+def pendulum_urdf(m, l, Iyy, axis="0 1 0", kind="revolute"):
     return f"""<robot name="p">
   <link name="base"/>
   <link name="bob"><inertial><origin xyz="0 0 {-l}" rpy="0 0 0"/><mass value="{m}"/>
     <inertia ixx="0.01" ixy="0" ixz="0" iyy="{Iyy}" iyz="0" izz="0.01"/></inertial></link>
-  <joint name="j" type="revolute"><origin xyz="0 0 0" rpy="0 0 0"/><axis xyz="{axis}"/>
+  <joint name="j" type="{kind}"><origin xyz="0 0 0" rpy="0 0 0"/><axis xyz="{axis}"/>
     <parent link="base"/><child link="bob"/><limit lower="-3" upper="3" effort="0" velocity="0"/></joint>
 </robot>"""
 
@@ -54,9 +54,11 @@ def two_link_urdf(m1, m2, l1, lc1, lc2, I1, I2):
 </robot>"""
 
 
-def test_pendulum_closed_form():
+@pytest.mark.parametrize("kind", ["revolute", "continuous"])
+def test_pendulum_closed_form(kind):
+    """Continuous joints are stored as (cos, sin) inside but take the angle at the API."""
     m, l, Iyy, g = 1.7, 0.6, 0.03, 9.81
-    o = Oracle(pendulum_urdf(m, l, Iyy), (0, 0, -g))
+    o = Oracle(pendulum_urdf(m, l, Iyy, kind=kind), (0, 0, -g))
     o.set_joint_order(["j"])
     o.set_link_order(["base", "bob"])
     rng = np.random.default_rng(0)
