@@ -648,28 +648,23 @@ static int derivatives(bool aba, const sgdyn_model* m, int64_t n, const double* 
     const int64_t nv = Mo.nv();
     DerivArgs a;
     a.n = n;
-    // Columns of the derivative matrices are independent given the forward sweep: split
-    // them over enough threads to give the FP64 schedulers work (a warp's FP64 issue, not
-    // the GPU's, bounds a small batch), each thread recomputing the forward sweep and, for
-    // ABA, the factorisation of M. Measured on a 35-DoF humanoid at 8192 environments, the
-    // best splits were about 0.8 (RNEA) and 1.25 (ABA) warps per FP64 scheduler.
-    int sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t schedulers = int64_t(sms > 0 ? sms : 1) * 4, warps = (n + 31) / 32;
-    const int64_t want_warps = aba ? (schedulers * 5 + 3) / 4 : (schedulers * 4 + 4) / 5;
-    const int64_t g = std::min<int64_t>(nv, std::max<int64_t>(1, (want_warps + warps - 1) / warps));
-    a.groups = int(g);
-    a.cols_per_thread = int((nv + g - 1) / g);
     a.q = make_arr(q, n, Mo.nq_ext(), layout);
     a.qd = make_arr(qd, n, nv, layout);
     a.x = make_arr(x, n, nv, layout);
     a.d_q = make_arr(d_q, n, nv * nv, layout);
     a.d_qd = make_arr(d_qd, n, nv * nv, layout);
     a.d_x = make_arr(d_x, n, nv * nv, layout);
+    a.lay = deriv_layout(Mo.njoints(), int(nv), aba);
     auto s = static_cast<cudaStream_t>(stream);
-    return launch_status(aba ? launch_aba_derivatives(dm, Mo.njoints(), a, s)
-                             : launch_rnea_derivatives(dm, Mo.njoints(), a, s));
+    // stream-ordered scratch for the preparation kernel's per-environment results
+    void* scratch = nullptr;
+    cudaError_t me = cudaMallocAsync(&scratch, size_t(a.lay.total) * size_t(n) * sizeof(double), s);
+    if (me != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("scratch allocation failed: ") + cudaGetErrorString(me));
+    a.scratch = static_cast<double*>(scratch);
+    const int rc = launch_status(aba ? launch_aba_derivatives(dm, Mo.njoints(), a, s)
+                                     : launch_rnea_derivatives(dm, Mo.njoints(), a, s));
+    cudaFreeAsync(scratch, s);
+    return rc;
   });
 }
 

@@ -16,13 +16,17 @@ SG_LAUNCH(rollout_reverse, RolloutArgs)
 #undef SG_LAUNCH
 
 cudaError_t launch_rnea_derivatives_j16(const DModel* dm, const DerivArgs& a, cudaStream_t s) {
-  rnea_derivatives_kernel<16><<<unsigned((a.n * a.groups + 31) / 32), 32, 0, s>>>(dm, a);
+  deriv_prepare_kernel<16, false><<<unsigned((a.n + 31) / 32), 32, 0, s>>>(dm, a);
+  if (cudaError_t e = cudaGetLastError()) return e;
+  const int64_t nv = (a.lay.Q - a.lay.P) / 6;
+  rnea_deriv_columns_kernel<16><<<unsigned((a.n * nv + 127) / 128), 128, 0, s>>>(dm, a);
   return cudaGetLastError();
 }
 cudaError_t launch_aba_derivatives_j16(const DModel* dm, const DerivArgs& a, cudaStream_t s) {
-  const unsigned grid = unsigned((a.n * a.groups + 31) / 32);
-  if (a.cols_per_thread <= 6) aba_derivatives_kernel<16, 6><<<grid, 32, 0, s>>>(dm, a);
-  else aba_derivatives_kernel<16, 12><<<grid, 32, 0, s>>>(dm, a);
+  deriv_prepare_kernel<16, true><<<unsigned((a.n + 31) / 32), 32, 0, s>>>(dm, a);
+  if (cudaError_t e = cudaGetLastError()) return e;
+  const int64_t nv = (a.lay.Q - a.lay.P) / 6;
+  aba_deriv_columns_kernel<16><<<unsigned((a.n * nv + 127) / 128), 128, 0, s>>>(dm, a);
   return cudaGetLastError();
 }
 cudaError_t launch_rollout_recompute_j16(const DModel* dm, const RolloutArgs& a, cudaStream_t s) {

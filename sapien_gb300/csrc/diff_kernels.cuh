@@ -135,98 +135,25 @@ __global__ void __launch_bounds__(32) fk_vjp_kernel(const DModel* __restrict__ m
 //   and 0 elsewhere (composites: deriv_composites). From tau_i = S_i . F_i with
 // v_k = v_lambda + (rigidly moved part), a_k likewise, and d(v x* I v)/dv, whose subtree
 // sum is the rate Db plus the momentum term. Subtrees are contiguous in the table's joint
-// order, so "i in subtree(j)" is j <= i < subtree_end(j). A thread writes the columns
-// c = g, g + G, ... (G = a.groups) of one environment, whole columns including zeros.
-// The per-column vectors of the formulas above for tree column t = J.ivx + l of joint j.
+// order, so "i in subtree(j)" is j <= i < subtree_end(j).
+// The per-column vectors of the formulas above for tree column s = S_t of joint j, parent
+// velocity / acceleration vl, al (v_0 = 0, a_0 = -gravity) and v_j.
 struct ColumnTerms {
   Mot s, u, beta, gam, Phi, Psi;
 };
 
-template <int MAXJ, class Tab>
-__device__ __forceinline__ ColumnTerms column_terms(const Tab& T, const DynWork<MAXJ>& W,
-                                                    const DerivComposites<MAXJ>& C, int j, int t) {
+__device__ __forceinline__ ColumnTerms column_terms(Mot s, Mot vl, Mot al, Mot vj, Mot Fj, Mot Hj, const RBI& Ibj,
+                                                    const RBI& Dbj) {
   const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
-  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
-  const int p = T.joint(j).parent;
-  const Mot vl = (p == 0) ? zero : W.vel[p];
-  const Mot al = (p == 0) ? a0 : W.acc[p];
   ColumnTerms ct;
-  ct.s = W.Sw[t];
-  ct.u = add_crossm(zero, vl, ct.s);
-  ct.beta = add_crossm(add_crossm(zero, al, ct.s), vl, ct.u);  // alpha - u x v_lambda
-  ct.gam = add_crossm(zero, add6(vl, W.vel[j]), ct.s);
-  ct.Phi = rbi_mul_add(C.Ib[j], ct.beta, add_crossf(zero, ct.s, C.F[j]));
-  ct.Phi = add_crossf(rbi_mul_add(C.Db[j], ct.u, ct.Phi), ct.u, C.H[j]);
-  ct.Psi = rbi_mul_add(C.Ib[j], ct.gam, rbi_mul_add(C.Db[j], ct.s, add_crossf(zero, ct.s, C.H[j])));
+  ct.s = s;
+  ct.u = add_crossm(zero, vl, s);
+  ct.beta = add_crossm(add_crossm(zero, al, s), vl, ct.u);  // alpha - u x v_lambda
+  ct.gam = add_crossm(zero, add6(vl, vj), s);
+  ct.Phi = rbi_mul_add(Ibj, ct.beta, add_crossf(zero, s, Fj));
+  ct.Phi = add_crossf(rbi_mul_add(Dbj, ct.u, ct.Phi), ct.u, Hj);
+  ct.Psi = rbi_mul_add(Ibj, ct.gam, rbi_mul_add(Dbj, s, add_crossf(zero, s, Hj)));
   return ct;
-}
-
-// Entry (row column ti of joint i, column t of joint j) of dtau/dq, dtau/dqd, dtau/dqdd.
-template <int MAXJ>
-__device__ __forceinline__ void column_entry(const DynWork<MAXJ>& W, const DerivComposites<MAXJ>& C,
-                                             const ColumnTerms& ct, bool anc, bool sub, int t, int ti, double& dq,
-                                             double& dqd, double& dqdd) {
-  dq = dqd = dqdd = 0;
-  if (anc) {
-    const Mot Si = W.Sw[ti];
-    dq = dot6(Si, ct.Phi);
-    dqd = dot6(Si, ct.Psi);
-    dqdd = dot6(Si, C.P[t]);
-  } else if (sub) {
-    const Mot P = C.P[ti], Q = C.Q[ti];
-    dq = dot6(P, ct.beta) + dot6(Q, ct.u);
-    dqd = dot6(Q, ct.s) + dot6(P, ct.gam);
-    dqdd = dot6(P, ct.s);
-  }
-}
-
-template <int MAXJ, class Tab>
-__device__ __forceinline__ void rnea_derivative_columns(const Tab& T, const DynWork<MAXJ>& W,
-                                                        const DerivComposites<MAXJ>& C, const DerivArgs& a,
-                                                        const int64_t e, const int g) {
-  const int nj = T.nj(), nv = T.nv();
-  for (int j = 1; j < nj; j++) {
-    const DJoint& J = T.joint(j);
-    for (int l = 0; l < J.nv; l++) {
-      const int t = J.ivx + l;
-      if (t % a.groups != g) continue;
-      const int c = J.vcol + l;
-      const ColumnTerms ct = column_terms<MAXJ>(T, W, C, j, t);
-      for (int i = 1; i < nj; i++) {
-        const DJoint& I = T.joint(i);
-        const bool anc = i < j && j < I.subtree_end;
-        const bool sub = i >= j && i < J.subtree_end;
-        for (int k = 0; k < I.nv; k++) {
-          const int r = I.vcol + k;
-          double dq, dqd, dqdd;
-          column_entry<MAXJ>(W, C, ct, anc, sub, t, I.ivx + k, dq, dqd, dqdd);
-          stv(a.d_q, e, r * nv + c, dq);
-          stv(a.d_qd, e, r * nv + c, dqd);
-          if (a.d_x.p) stv(a.d_x, e, r * nv + c, dqdd);
-        }
-      }
-    }
-  }
-}
-
-template <int MAXJ>
-__global__ void __launch_bounds__(32) rnea_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
-  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= a.n * a.groups) return;
-  const int64_t e = idx % a.n;
-  const int g = int(idx / a.n);
-  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const RuntimeTab T{model};
-  const int nv = T.nv(), nq = T.nq_ext();
-  double q[MAXQ], qd[MAXV], qdd[MAXV];
-  load_row<MAXJ>(a.q, e, nq, q);
-  load_row<MAXJ>(a.qd, e, nv, qd);
-  load_row<MAXJ>(a.x, e, nv, qdd);
-  DynWork<MAXJ> W;
-  DerivComposites<MAXJ> C;
-  rnea_forward<MAXJ>(T, q, qd, qdd, W);
-  deriv_composites<MAXJ>(T, W, C);
-  rnea_derivative_columns<MAXJ>(T, W, C, a, e, g);
 }
 
 // Joint-space inertia in tree-column order factored as M = L^T D L with the tree's
@@ -250,18 +177,17 @@ __device__ __forceinline__ void ltdl_factor(double* H, const int* lam, double* D
   }
 }
 // B <- M^-1 B in place for R right-hand sides at once (B row-major [n][R]), M = L^T D L
-// from ltdl_factor; end[i] = one past the last descendant column of column i (subtrees are
-// contiguous in tree-column order). L^T y = b runs in pull form over each column's
-// descendant range, L x = z over its ancestor chain; each step has R independent updates.
-template <int R>
-__device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam, const int* end, const double* Dinv,
-                                                int n, double* B) {
+// with L(k, i) and Dinv(k) read through the accessors; end[i] = one past the last
+// descendant column of column i (subtrees are contiguous in tree-column order). L^T y = b
+// runs in pull form over each column's descendant range, L x = z over its ancestor chain.
+template <int R, class LF, class DF>
+__device__ __forceinline__ void ltdl_solve_many(LF Lk, DF Dk, const int* lam, const int* end, int n, double* B) {
   for (int i = n - 1; i >= 0; i--) {
     double y[R];
 #pragma unroll
     for (int r = 0; r < R; r++) y[r] = B[i * R + r];
     for (int k = i + 1; k < end[i]; k++) {
-      const double h = H[ltdl_at(k, i)];
+      const double h = Lk(k, i);
 #pragma unroll
       for (int r = 0; r < R; r++) y[r] -= h * B[k * R + r];
     }
@@ -270,11 +196,11 @@ __device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam,
   }
   for (int k = 0; k < n; k++) {
     double x[R];
-    const double d = Dinv[k];
+    const double d = Dk(k);
 #pragma unroll
     for (int r = 0; r < R; r++) x[r] = B[k * R + r] * d;
     for (int i = lam[k]; i >= 0; i = lam[i]) {
-      const double h = H[ltdl_at(k, i)];
+      const double h = Lk(k, i);
 #pragma unroll
       for (int r = 0; r < R; r++) x[r] -= h * B[i * R + r];
     }
@@ -283,21 +209,11 @@ __device__ __forceinline__ void ltdl_solve_many(const double* H, const int* lam,
   }
 }
 
-// ABA derivatives from the RNEA ones at qdd = ABA(q, qd, tau): dqdd/dq = -M^-1 dtau/dq,
-// dqdd/dqd = -M^-1 dtau/dqd, dqdd/dtau = M^-1 (Carpentier & Mansard, RSS 2018). The tau
-// columns come from the analytic column formulas above, M from the same composites
-// (M_ab = P_a . S_b for b an ancestor-or-self column of a), and every M^-1 product is an
-// LTDL solve. A thread writes the columns c = g, g + G, ... of one environment, solving
-// them in batches of CB columns (3 CB right-hand sides); the launch picks CB >= the
-// columns per thread where it can, so no batch runs half empty.
-template <int MAXJ, int CB>
-__global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __restrict__ model, const DerivArgs a) {
-  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
-  const RuntimeTab T{model};
-  const int nj = T.nj(), nv = T.nv(), nq = T.nq_ext();
-  // the column tree, shared by the block (one model): parent column, external index,
-  // one past the last descendant column
-  __shared__ int lam[MAXV], ext[MAXV], cend[MAXV];
+// The tree of velocity columns, built by every block in shared memory (one model per
+// launch): parent column, external index, one past the last descendant column.
+template <class Tab>
+__device__ __forceinline__ void column_tree(const Tab& T, int* lam, int* ext, int* cend) {
+  const int nj = T.nj(), nv = T.nv();
   for (int i = 1 + int(threadIdx.x); i < nj; i += blockDim.x) {
     const DJoint& J = T.joint(i);
     const int p = J.parent;
@@ -310,40 +226,81 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
     }
   }
   __syncthreads();
-  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= a.n * a.groups) return;
-  const int64_t e = idx % a.n;
-  const int g = int(idx / a.n);
-  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
+}
+
+// Scratch of the derivative kernels: field f of environment e at scratch[f n + e].
+struct DerivScratch {
+  double* p;
+  int64_t n, e;
+  __device__ __forceinline__ double& at(int f) const { return p[int64_t(f) * n + e]; }
+  __device__ __forceinline__ Mot mot(int f) const {
+    return Mot{mk(at(f), at(f + 1), at(f + 2)), mk(at(f + 3), at(f + 4), at(f + 5))};
+  }
+  __device__ __forceinline__ void put(int f, Mot m) const {
+    at(f) = m.v.x; at(f + 1) = m.v.y; at(f + 2) = m.v.z;
+    at(f + 3) = m.w.x; at(f + 4) = m.w.y; at(f + 5) = m.w.z;
+  }
+  __device__ __forceinline__ RBI rbi(int f) const {
+    RBI Y;
+    Y.m = at(f);
+    Y.h = mk(at(f + 1), at(f + 2), at(f + 3));
+#pragma unroll
+    for (int k = 0; k < 6; k++) Y.I[k] = at(f + 4 + k);
+    return Y;
+  }
+  __device__ __forceinline__ void put(int f, const RBI& Y) const {
+    at(f) = Y.m;
+    at(f + 1) = Y.h.x; at(f + 2) = Y.h.y; at(f + 3) = Y.h.z;
+#pragma unroll
+    for (int k = 0; k < 6; k++) at(f + 4 + k) = Y.I[k];
+  }
+};
+
+// Preparation, one thread per environment: the forward sweep and the subtree composites
+// into the scratch. ABA: the sweep at qdd = 0 gives the bias accelerations and forces; M
+// (M_ab = P_a . S_b for b an ancestor-or-self column of a) is factored, qdd = M^-1 (tau -
+// tau_bias), and the accelerations and subtree forces take the qdd terms (a_i += sum_{m <=
+// i} S_m qdd_m, F_i += sum_{k in subtree(i)} I_k da_k); the factor goes to the scratch too.
+template <int MAXJ, bool ABA>
+__global__ void __launch_bounds__(32) deriv_prepare_kernel(const DModel* __restrict__ model, const DerivArgs a) {
+  constexpr int MAXV = Ext<MAXJ>::MAXV, MAXQ = Ext<MAXJ>::MAXQ;
+  const RuntimeTab T{model};
+  const int nj = T.nj(), nv = T.nv(), nq = T.nq_ext();
+  __shared__ int lam[MAXV], ext[MAXV], cend[MAXV];
+  if (ABA) column_tree(T, lam, ext, cend);
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  double q[MAXQ], qd[MAXV], x[MAXV], qdd[MAXV];
   load_row<MAXJ>(a.q, e, nq, q);
   load_row<MAXJ>(a.qd, e, nv, qd);
-  load_row<MAXJ>(a.x, e, nv, tau);
+  load_row<MAXJ>(a.x, e, nv, x);
   DynWork<MAXJ> W;
   DerivComposites<MAXJ> C;
-  // forward dynamics through the factorisation built anyway: the RNEA sweep at qdd = 0
-  // gives the bias accelerations and forces, qdd = M^-1 (tau - tau_bias), then the
-  // accelerations and subtree forces take the qdd terms (a_i += sum_{m <= i} S_m qdd_m,
-  // F_i += sum_{k in subtree(i)} I_k da_k)
-  for (int c = 0; c < nv; c++) qdd[c] = 0.0;
-  rnea_forward<MAXJ>(T, q, qd, qdd, W);
-  deriv_composites<MAXJ>(T, W, C);
-  double H[MAXV * (MAXV + 1) / 2], Dinv[MAXV];
-  for (int t = 0; t < nv; t++)
-    for (int b = t; b >= 0; b = lam[b]) H[ltdl_at(t, b)] = dot6(C.P[t], W.Sw[b]);
-  ltdl_factor(H, lam, Dinv, nv);
-  {
-    double x[MAXV];
+  const DerivScratch D{a.scratch, a.n, e};
+  const DerivLayout& L = a.lay;
+  if (!ABA) {
+    rnea_forward<MAXJ>(T, q, qd, x, W);
+    deriv_composites<MAXJ>(T, W, C);
+  } else {
+    for (int c = 0; c < nv; c++) qdd[c] = 0.0;
+    rnea_forward<MAXJ>(T, q, qd, qdd, W);
+    deriv_composites<MAXJ>(T, W, C);
+    double H[MAXV * (MAXV + 1) / 2], Dinv[MAXV];
+    for (int t = 0; t < nv; t++)
+      for (int b = t; b >= 0; b = lam[b]) H[ltdl_at(t, b)] = dot6(C.P[t], W.Sw[b]);
+    ltdl_factor(H, lam, Dinv, nv);
     for (int i = 1; i < nj; i++) {
       const DJoint& J = T.joint(i);
-      for (int k = 0; k < J.nv; k++) x[J.ivx + k] = tau[J.vcol + k] - dot6(W.Sw[J.ivx + k], C.F[i]);
+      for (int k = 0; k < J.nv; k++) qdd[J.ivx + k] = x[J.vcol + k] - dot6(W.Sw[J.ivx + k], C.F[i]);
     }
-    ltdl_solve_many<1>(H, lam, cend, Dinv, nv, x);
+    ltdl_solve_many<1>([&](int k, int i) { return H[ltdl_at(k, i)]; }, [&](int k) { return Dinv[k]; }, lam, cend, nv,
+                       qdd);
     const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
     Mot da[MAXJ];
     for (int i = 1; i < nj; i++) {
       const DJoint& J = T.joint(i);
       Mot d = J.parent > 0 ? da[J.parent] : zero;
-      for (int k = 0; k < J.nv; k++) d = axpy6(x[J.ivx + k], W.Sw[J.ivx + k], d);
+      for (int k = 0; k < J.nv; k++) d = axpy6(qdd[J.ivx + k], W.Sw[J.ivx + k], d);
       da[i] = d;
       W.acc[i] = add6(W.acc[i], d);
     }
@@ -353,49 +310,114 @@ __global__ void __launch_bounds__(32) aba_derivatives_kernel(const DModel* __res
       if (p > 0) da[p] = add6(da[p], da[i]);
       C.F[i] = add6(C.F[i], da[i]);
     }
+    for (int k = 0; k < nv * (nv + 1) / 2; k++) D.at(L.L + k) = H[k];
+    for (int k = 0; k < nv; k++) D.at(L.Dinv + k) = Dinv[k];
   }
-  // right-hand sides per batch: [dtau/dq columns | dtau/dqd columns | unit vectors]
-  constexpr int RB = 3 * CB;
-  double B[MAXV * RB];
-  int cols[CB], ncols = 0;
-  auto flush = [&]() {
-    ltdl_solve_many<RB>(H, lam, cend, Dinv, nv, B);
-    for (int m = 0; m < ncols; m++) {
-      const int c = ext[cols[m]];
-      for (int r = 0; r < nv; r++) {
-        stv(a.d_q, e, ext[r] * nv + c, -B[r * RB + m]);
-        stv(a.d_qd, e, ext[r] * nv + c, -B[r * RB + CB + m]);
-        if (a.d_x.p) stv(a.d_x, e, ext[r] * nv + c, B[r * RB + 2 * CB + m]);
+  for (int t = 0; t < nv; t++) {
+    D.put(L.S + 6 * t, W.Sw[t]);
+    D.put(L.P + 6 * t, C.P[t]);
+    D.put(L.Q + 6 * t, C.Q[t]);
+  }
+  for (int i = 1; i < nj; i++) {
+    D.put(L.v + 6 * i, W.vel[i]);
+    D.put(L.a + 6 * i, W.acc[i]);
+    D.put(L.F + 6 * i, C.F[i]);
+    D.put(L.H + 6 * i, C.H[i]);
+    D.put(L.Ib + 10 * i, C.Ib[i]);
+    D.put(L.Db + 10 * i, C.Db[i]);
+  }
+}
+
+// One column, one environment: the column terms of tree column t (joint j) and the entries
+// of the ancestor rows (S_i . Phi, S_i . Psi, S_i . P_t) and subtree rows (P_i . beta +
+// Q_i . u, Q_i . s + P_i . gamma, P_i . s); others are 0. Calls f(tree row, dq, dqd, dqdd).
+template <class Tab, class F>
+__device__ __forceinline__ void derivative_column(const Tab& T, const DerivScratch& D, const DerivLayout& L,
+                                                  int t, F&& f) {
+  const int nj = T.nj();
+  int j = 1;
+  while (t >= T.joint(j).ivx + T.joint(j).nv) j++;
+  const DJoint& J = T.joint(j);
+  const int p = J.parent;
+  const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+  const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
+  const ColumnTerms ct = column_terms(D.mot(L.S + 6 * t), p ? D.mot(L.v + 6 * p) : zero, p ? D.mot(L.a + 6 * p) : a0,
+                                      D.mot(L.v + 6 * j), D.mot(L.F + 6 * j), D.mot(L.H + 6 * j),
+                                      D.rbi(L.Ib + 10 * j), D.rbi(L.Db + 10 * j));
+  const Mot Pt = D.mot(L.P + 6 * t);
+  for (int i = 1; i < nj; i++) {
+    const DJoint& I = T.joint(i);
+    const bool anc = i < j && j < I.subtree_end;
+    const bool sub = i >= j && i < J.subtree_end;
+    for (int k = 0; k < I.nv; k++) {
+      const int ti = I.ivx + k;
+      if (anc) {
+        const Mot Si = D.mot(L.S + 6 * ti);
+        f(ti, dot6(Si, ct.Phi), dot6(Si, ct.Psi), dot6(Si, Pt));
+      } else if (sub) {
+        const Mot P = D.mot(L.P + 6 * ti), Q = D.mot(L.Q + 6 * ti);
+        f(ti, dot6(P, ct.beta) + dot6(Q, ct.u), dot6(Q, ct.s) + dot6(P, ct.gam), dot6(P, ct.s));
+      } else {
+        f(ti, 0.0, 0.0, 0.0);
       }
     }
-    ncols = 0;
-  };
-  for (int j = 1; j < nj; j++) {
-    const DJoint& J = T.joint(j);
-    for (int l = 0; l < J.nv; l++) {
-      const int t = J.ivx + l;
-      if (t % a.groups != g) continue;
-      if (ncols == 0)
-        for (int k = 0; k < nv * RB; k++) B[k] = 0.0;
-      const int m = ncols++;
-      cols[m] = t;
-      const ColumnTerms ct = column_terms<MAXJ>(T, W, C, j, t);
-      for (int i = 1; i < nj; i++) {
-        const DJoint& I = T.joint(i);
-        const bool anc = i < j && j < I.subtree_end;
-        const bool sub = i >= j && i < J.subtree_end;
-        if (!anc && !sub) continue;
-        for (int k = 0; k < I.nv; k++) {
-          const int ti = I.ivx + k;
-          double dqdd;
-          column_entry<MAXJ>(W, C, ct, anc, sub, t, ti, B[ti * RB + m], B[ti * RB + CB + m], dqdd);
-        }
-      }
-      B[t * RB + 2 * CB + m] = 1.0;
-      if (ncols == CB) flush();
-    }
   }
-  if (ncols > 0) flush();
+}
+
+// RNEA derivatives: thread (tree column t, environment e) writes column ext(t) of the three
+// matrices of environment e.
+template <int MAXJ>
+__global__ void __launch_bounds__(128) rnea_deriv_columns_kernel(const DModel* __restrict__ model, const DerivArgs a) {
+  constexpr int MAXV = Ext<MAXJ>::MAXV;
+  const RuntimeTab T{model};
+  const int nv = T.nv();
+  __shared__ int lam[MAXV], ext[MAXV], cend[MAXV];
+  column_tree(T, lam, ext, cend);
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= a.n * nv) return;
+  const int64_t e = idx % a.n;
+  const int t = int(idx / a.n);
+  const int c = ext[t];
+  const DerivScratch D{a.scratch, a.n, e};
+  derivative_column(T, D, a.lay, t, [&](int ti, double dq, double dqd, double dqdd) {
+    const int r = ext[ti];
+    stv(a.d_q, e, r * nv + c, dq);
+    stv(a.d_qd, e, r * nv + c, dqd);
+    if (a.d_x.p) stv(a.d_x, e, r * nv + c, dqdd);
+  });
+}
+
+// ABA derivatives (Carpentier & Mansard, RSS 2018): dqdd/dq = -M^-1 dtau/dq, dqdd/dqd =
+// -M^-1 dtau/dqd, dqdd/dtau = M^-1, with the dtau columns at qdd = ABA(q, qd, tau) and every
+// M^-1 product one solve with the prepared factor: thread (tree column t, environment e)
+// solves its three right-hand sides in one walk and writes column ext(t).
+template <int MAXJ>
+__global__ void __launch_bounds__(128) aba_deriv_columns_kernel(const DModel* __restrict__ model, const DerivArgs a) {
+  constexpr int MAXV = Ext<MAXJ>::MAXV;
+  const RuntimeTab T{model};
+  const int nv = T.nv();
+  __shared__ int lam[MAXV], ext[MAXV], cend[MAXV];
+  column_tree(T, lam, ext, cend);
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= a.n * nv) return;
+  const int64_t e = idx % a.n;
+  const int t = int(idx / a.n);
+  const DerivScratch D{a.scratch, a.n, e};
+  const DerivLayout& L = a.lay;
+  double B[MAXV * 3];
+  derivative_column(T, D, L, t, [&](int ti, double dq, double dqd, double) {
+    B[3 * ti] = dq;
+    B[3 * ti + 1] = dqd;
+    B[3 * ti + 2] = ti == t ? 1.0 : 0.0;
+  });
+  ltdl_solve_many<3>([&](int k, int i) { return D.at(L.L + ltdl_at(k, i)); }, [&](int k) { return D.at(L.Dinv + k); },
+                     lam, cend, nv, B);
+  const int c = ext[t];
+  for (int r = 0; r < nv; r++) {
+    stv(a.d_q, e, ext[r] * nv + c, -B[3 * r]);
+    stv(a.d_qd, e, ext[r] * nv + c, -B[3 * r + 1]);
+    if (a.d_x.p) stv(a.d_x, e, ext[r] * nv + c, B[3 * r + 2]);
+  }
 }
 
 // ---- rollouts ---------------------------------------------------------------------

@@ -62,12 +62,18 @@ struct FkVjpArgs {
 // Dense derivative matrices, rows = outputs, columns = tangent inputs.
 //   RNEA: x = qdd -> d_q = dtau/dq, d_qd = dtau/dqd, d_x = dtau/dqdd (= M)
 //   ABA:  x = tau -> d_q = dqdd/dq, d_qd = dqdd/dqd, d_x = dqdd/dtau (= M^-1)
-// Columns are dealt out to `groups` threads per environment: thread (group g, env e)
-// recomputes e's forward sweep and writes the columns whose tree index is g mod groups.
+// Two launches: a preparation kernel (one thread per environment: forward sweep, subtree
+// composites and, for ABA, the L^T D L factor of M and qdd) writes its results to
+// `scratch` as structure of arrays ([field][env], `lay.total` doubles per environment);
+// the column kernel (one thread per environment and tree column) reads them.
+struct DerivLayout {
+  int S, v, a, F, H, Ib, Db, P, Q, L, Dinv, total;  // first field of each block
+};
 struct DerivArgs {
   int64_t n;
-  int groups, cols_per_thread;  // cols_per_thread = ceil(nv / groups)
   Arr q, qd, x, d_q, d_qd, d_x;
+  double* scratch;
+  DerivLayout lay;
 };
 
 // Semi-implicit Euler rollout qd += dt ABA(q, qd, tau_t); q += dt qd, with q / qd
@@ -109,6 +115,24 @@ cudaError_t launch_aba_derivatives(const DModel* dm, int nj, const DerivArgs& a,
 cudaError_t launch_rollout_forward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_recompute(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_reverse(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
+// Fields: S, P, Q: 6 per tree column; v, a, F, H: 6 per joint; Ib, Db: 10 per joint
+// (m, h, I xx xy xz yy yz zz); L: the packed factor (nv (nv + 1) / 2), Dinv: nv (ABA only).
+inline DerivLayout deriv_layout(int nj, int nv, bool aba) {
+  DerivLayout l;
+  l.S = 0;
+  l.v = l.S + 6 * nv;
+  l.a = l.v + 6 * nj;
+  l.F = l.a + 6 * nj;
+  l.H = l.F + 6 * nj;
+  l.Ib = l.H + 6 * nj;
+  l.Db = l.Ib + 10 * nj;
+  l.P = l.Db + 10 * nj;
+  l.Q = l.P + 6 * nv;
+  l.L = l.Q + 6 * nv;
+  l.Dinv = l.L + (aba ? nv * (nv + 1) / 2 : 0);
+  l.total = l.Dinv + (aba ? nv : 0);
+  return l;
+}
 // doubles of rollout-backward scratch per environment and segment (the minimum scratch is
 // one segment for all environments; k segments' worth lets k segments recompute at once)
 int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K);

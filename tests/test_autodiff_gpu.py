@@ -125,10 +125,9 @@ def test_dense_derivatives_match_finite_differences(name):
 
 
 def test_dense_derivatives_do_not_depend_on_the_column_split():
-    """Columns are dealt to a number of threads per environment that depends on the batch
-    size; every column is computed the same way, so a small batch (one thread per column)
-    and the same environments inside large batches (a few threads each; at 8192 the ABA
-    kernel solves 12 columns per batch, at 4096 six) agree bit for bit."""
+    """Every column is computed the same way whatever the batch size (one thread per
+    environment and column, reading the prepared per-environment data), so a small batch and
+    the same environments inside batches of 4096 and 8192 agree bit for bit."""
     robot = syn.humanoid()
     pm, _ = pair(robot)
     q, qd, qdd, tau = robot.sample(8192, seed=17)
