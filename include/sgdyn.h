@@ -270,7 +270,10 @@ int sgdyn_compute_forward_kinematics_vjp(const sgdyn_model* m, int64_t n, const 
 
 /* Dense derivatives of RNEA: dtau_dq, dtau_dqd, dtau_dqdd (= M; may be NULL), each
  * [n][nv*nv] row-major (row = torque, column = input). Analogue of Pinocchio's
- * computeRNEADerivatives, which the reference does not expose. */
+ * computeRNEADerivatives, which the reference does not expose. This and
+ * sgdyn_compute_aba_derivatives take stream-ordered scratch (cudaMallocAsync / cudaFreeAsync
+ * on `stream`, about 8 (18 nv + 44 njoints) bytes per environment, plus the factor of M
+ * for ABA) and enqueue two kernels. */
 int sgdyn_compute_rnea_derivatives(const sgdyn_model* m, int64_t n, const double* q, const double* qd,
                                    const double* qdd, double* dtau_dq, double* dtau_dqd, double* dtau_dqdd,
                                    int layout, void* stream);
