@@ -196,6 +196,7 @@ def secondary_workloads(dev):
     import torch
 
     from sapien_gb300 import PinocchioModel, autodiff as ad, autotune, synthetic
+    from sapien_gb300 import _native as N
     from sapien_gb300.hetero import OPS_DYNAMICS, HeteroBatch
 
     def model_of(r):
@@ -233,13 +234,16 @@ def secondary_workloads(dev):
                                  "RNEA+ABA+CRBA; CUDA-graph replay of 10 steps",
                      "env_steps_per_s": 8192 / (hms * 1e-3), "ms_per_step": hms, "launch_shape": list(shape),
                      "lanes_per_env": list(hb.lanes)}
-    # a whole heterogeneous rollout (ABA + semi-implicit Euler, free flyers on SE(3)) as one graph
+    # a whole heterogeneous rollout (ABA + semi-implicit Euler, free flyers on SE(3)) as one graph,
+    # with the launch shape and lanes tuned for ABA alone
     rq, rqd, rtau = hq.clone(), hqd.clone(), 0.1 * htau
+    rshape, _ = autotune.tune_batch(hb, hq, hqd, hqdd, rtau, N.OP_FORWARD_DYNAMICS)
     rg = hb.capture_rollout(rq, rqd, rtau, 1.0 / 500, 100)
     rms = _event_ms(torch, rg.replay, reps=3, warm=1) / 100
     out["hetero_rollout"] = {"workload": "same 8192-robot mix, 100 semi-implicit-Euler steps (ABA + integrate) "
                                          "captured as one CUDA graph, dt=1/500",
-                             "env_steps_per_s": 8192 / (rms * 1e-3), "ms_per_step": rms}
+                             "env_steps_per_s": 8192 / (rms * 1e-3), "ms_per_step": rms,
+                             "launch_shape": list(rshape), "lanes_per_env": list(hb.lanes)}
     nik = 65536
     qik, _, _, _ = arm.sample(nik, seed=3)
     tgt = pm.compute_forward_kinematics_batched(torch.from_numpy(qik).to(dev))[:, arm.ee_link].contiguous()
