@@ -100,6 +100,21 @@ def test_two_link_closed_form():
         assert np.abs(o.compute_inverse_dynamics(q, [0, 0], [0, 0]) - gv).max() < 1e-13
         qdd = rng.normal(size=2)
         assert np.abs(o.compute_inverse_dynamics(q, qd, qdd) - (M @ qdd + C @ qd + gv)).max() < 1e-12
+        # Jacobians of link l2 (frame at joint 2, at (l1 c1, l1 s1, 0), rotated by q1 + q2 about
+        # z): WORLD = spatial velocity at the world origin, columns (p_i x z, z); LOCAL = the
+        # link frame's own velocity in its axes
+        c1, s1, c12, s12 = math.cos(q[0]), math.sin(q[0]), math.cos(q.sum()), math.sin(q.sum())
+        Jw = np.zeros((6, 2))
+        Jw[5, :] = 1
+        Jw[0, 1], Jw[1, 1] = l1 * s1, -l1 * c1
+        R12 = np.array([[c12, -s12, 0], [s12, c12, 0], [0, 0, 1]])
+        Jl = np.zeros((6, 2))
+        Jl[:3, 0] = R12.T @ np.array([-l1 * s1, l1 * c1, 0])
+        Jl[5, :] = 1
+        o.compute_full_jacobian(q)
+        assert np.abs(o.get_link_jacobian(2) - Jw).max() < 1e-15
+        assert np.abs(o.get_link_jacobian(2, local=True) - Jl).max() < 1e-15
+        assert np.abs(o.compute_single_link_local_jacobian(q, 2) - Jl).max() < 1e-15
 
 
 def cart_pole_urdf(mc, mp, l, Iyy):
