@@ -36,9 +36,8 @@ WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs p
             "FK (all link poses) + WORLD Jacobian + CRBA + RNEA + ABA per env per step")
 
 # FP64 thread-instructions (DFMA + DMUL + DADD) per environment-step and DRAM bytes per
-# environment of one fused launch (structure-of-arrays buffers), from the ncu captures
-# summarised in profiles/step_kernel_arm9.md, for the model-specialised kernel (run-time
-# compiled) and the generic one.
+# environment of one fused launch (structure-of-arrays buffers), from an ncu capture of the
+# model-specialised kernel (run-time compiled) and of the generic one.
 KERNEL_COUNTERS = {
     "specialised": {"fp64_inst_per_env": 5100, "dram_bytes_per_env": 34.79e6 / 16384},
     "generic": {"fp64_inst_per_env": 5047, "dram_bytes_per_env": 124.6e6 / 16384},
@@ -153,10 +152,19 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def fp64_peak_dfma_per_s():
-    from sapien_gb300.build_native import PROBE_LIB
+PROBE_SRC = os.path.join(ROOT, "bench_fp64_peak.cu")
+PROBE_LIB = os.path.join(ROOT, "_bench_build", "libfp64_peak.so")
 
-    L = ctypes.CDLL(PROBE_LIB)
+
+def build_probe():
+    """Compile the FP64-peak microbenchmark (measurement only, not part of the library)."""
+    from sapien_gb300.build_native import build_standalone
+
+    return build_standalone(PROBE_SRC, PROBE_LIB)
+
+
+def fp64_peak_dfma_per_s():
+    L = ctypes.CDLL(build_probe())
     L.sgdyn_probe_fp64_dfma_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     v = ctypes.c_double()
     if L.sgdyn_probe_fp64_dfma_rate(5, ctypes.byref(v)) != 0:
@@ -479,7 +487,7 @@ def main():
     roofline_fp64 = None
     if dfma:
         roofline_fp64 = {"bound": "fp64", "peak": dfma / 1e9, "unit": "G FP64 inst/s (per lane)",
-                         "peak_source": "measured live: DFMA chain microbenchmark (csrc_probe/fp64_peak.cu)"}
+                         "peak_source": "measured live: DFMA chain microbenchmark (bench_fp64_peak.cu)"}
         ach = counters["fp64_inst_per_env"] * n / (ms * 1e-3) / 1e9
         roofline_fp64.update({"achieved": ach, "frac": ach / (dfma / 1e9),
                               "inst_per_env_step": counters["fp64_inst_per_env"]})

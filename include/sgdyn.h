@@ -318,8 +318,10 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
  * fixed SGDYN_NOALLOC_SCRATCH_BYTES device array that the library holds on every GPU that
  * loads it, until exit; calls needing more (sgdyn_rollout_scratch_bytes) fail with
  * SGDYN_ERR_RUNTIME. It calls no allocator: the model must already be on the device
- * (sgdyn_model_upload). The first call on a device looks the array up (make it before any
- * stream capture). All calls share the array: calls that overlap on the GPU race. */
+ * (sgdyn_model_upload). Every call looks the array's address up on the current device; the
+ * first lookup on a device may load the library's device code, so make one call on each
+ * device (n = 0 does only the lookup) before any stream capture. All calls share the
+ * array: calls that overlap on the GPU race. */
 #define SGDYN_NOALLOC_SCRATCH_BYTES (64LL << 20)
 int sgdyn_rollout_backward_noalloc(const sgdyn_model* m, int64_t n, int T, double dt, int checkpoint_every,
                                    const double* q_ckpt, const double* qd_ckpt, const double* tau,

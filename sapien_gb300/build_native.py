@@ -93,16 +93,20 @@ def build(verbose=False, jobs=None, force=False):
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
     _link(objs, LIB, verbose)
-    # FP64-peak microbenchmark used by bench.py (separate library, not part of the C ABI)
-    pobj, perr = _compile(PROBE_SRC, hmt, verbose)
-    if perr:
-        raise RuntimeError("nvcc failed:\n" + perr)
-    _link([pobj], PROBE_LIB, verbose)
     return LIB
 
 
-PROBE_SRC = os.path.join(HERE, "csrc_probe", "fp64_peak.cu")
-PROBE_LIB = os.path.join(LIBDIR, "libsgdyn_probe.so")
+def build_standalone(src, out, verbose=False):
+    """Compile one .cu file into its own shared library `out` (same flags as libsgdyn.so)."""
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    obj = out + ".o"
+    if not (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)):
+        cmd = [_nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed:\n{src}:\n{r.stdout}\n{r.stderr}")
+    _link([obj], out, verbose)
+    return out
 
 
 def _link(objs, out, verbose):

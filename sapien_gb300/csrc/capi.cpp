@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <stdexcept>
@@ -218,6 +219,9 @@ int launch_status(cudaError_t e) {
 namespace sgdyn {
 // Records a message for sgdyn_last_error() from entry points defined in other files.
 int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+// Runs an entry point's body with C++ exceptions turned into status codes, for entry
+// points defined in other files.
+int call_guarded(const std::function<int()>& body) { return guarded(body); }
 }  // namespace sgdyn
 
 using namespace sgdyn;
@@ -724,7 +728,9 @@ int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_
   if (!m || !bytes) return fail(SGDYN_ERR_NULL, "null argument");
   if (checkpoint_every <= 0 || n < 0) return fail(SGDYN_ERR_RUNTIME, "bad sizes");
   const Model& Mo = *m->impl;
-  *bytes = 8 * n * rollout_scratch_doubles_per_env(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every);
+  const int64_t b = rollout_scratch_bytes_for(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every, n);
+  if (b < 0) return fail(SGDYN_ERR_RUNTIME, "scratch size overflows int64");
+  *bytes = b;
   return SGDYN_OK;
 }
 
@@ -811,7 +817,8 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
     for (const void* o : {(const void*)qT_bar, (const void*)qdT_bar})
       if (o && !device_accessible(o)) return fail(SGDYN_ERR_NULL, "adjoint input is not device memory");
     Model& Mo = *m->impl;
-    int64_t need = 8 * n * rollout_scratch_doubles_per_env(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every);
+    const int64_t need = rollout_scratch_bytes_for(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every, n);
+    if (need < 0) return fail(SGDYN_ERR_RUNTIME, "scratch size overflows int64");
     if (T > 0 && scratch_bytes < need)
       return fail(SGDYN_ERR_RUNTIME, "scratch too small: need " + std::to_string(need) + " bytes");
     int err = 0;

@@ -136,6 +136,13 @@ inline DerivLayout deriv_layout(int nj, int nv, bool aba) {
 // doubles of rollout-backward scratch per environment and segment (the minimum scratch is
 // one segment for all environments; k segments' worth lets k segments recompute at once)
 int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K);
+// Bytes of rollout-backward scratch for n environments (one segment each), or -1 when the
+// product does not fit in an int64_t.
+inline int64_t rollout_scratch_bytes_for(int nj, int nq, int nv, int K, int64_t n) {
+  const int64_t per = 8 * rollout_scratch_doubles_per_env(nj, nq, nv, K);
+  if (n < 0 || (per > 0 && n > INT64_MAX / per)) return -1;
+  return per * n;
+}
 
 // Whole rollout backward: groups of as many segments as the scratch holds, latest first;
 // per group one recompute launch over (segment, env) and one reverse launch over envs.

@@ -52,6 +52,9 @@ def test_noalloc_backward_matches_allocating_entry_point():
 
     L = N.load()
     stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    # an empty call only looks the array up on this device (the warm-up before a capture)
+    rc = L.sgdyn_rollout_backward_noalloc(pm._h, 0, T, dt, K, None, None, None, None, None, None, None, None, stream)
+    assert rc == N.OK, N.last_error()
     for call in range(2):  # the shared array keeps the previous call's contents
         q0b = torch.full((n, robot.nq_ext), float("nan"), dtype=torch.float64, device=dev)
         qd0b = torch.full((n, robot.nv), float("nan"), dtype=torch.float64, device=dev)
@@ -81,6 +84,12 @@ def test_noalloc_rejects_oversized_calls_and_unuploaded_models():
                                           _p(dummy), _p(dummy), _p(dummy), None)
     assert rc == N.ERR_RUNTIME
     assert "bytes of scratch" in N.last_error()
+    # a batch size whose scratch size overflows int64 is refused, not wrapped around
+    rc = L.sgdyn_rollout_backward_noalloc(pm._h, 1 << 61, 10, 0.002, 20, _p(dummy), _p(dummy), _p(dummy), None, None,
+                                          _p(dummy), _p(dummy), _p(dummy), None)
+    assert rc == N.ERR_RUNTIME
+    assert "INT64_MAX" in N.last_error()
+    assert L.sgdyn_rollout_scratch_bytes(pm._h, 1 << 61, 20, ctypes.byref(nb)) == N.ERR_RUNTIME
     # a model never uploaded to this device is refused, not uploaded
     fresh = _model(robot)
     rc = L.sgdyn_rollout_backward_noalloc(fresh._h, 4, 10, 0.002, 20, _p(dummy), _p(dummy), _p(dummy), None, None,
