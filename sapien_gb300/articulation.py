@@ -113,10 +113,14 @@ def _rpy(pose):
     R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
                   [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
                   [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
-    pitch = math.asin(max(-1.0, min(1.0, -R[2, 0])))
-    if abs(R[2, 0]) < 1 - 1e-12:
-        return math.atan2(R[2, 1], R[2, 2]), pitch, math.atan2(R[1, 0], R[0, 0])
-    return math.atan2(-R[1, 2], R[1, 1]), pitch, 0.0
+    # R = Rz(yaw) Ry(pitch) Rx(roll); every angle from atan2, so a pitch near +-pi/2 (an
+    # axis frame turning x onto z) keeps full precision, as the reference's Eigen-based
+    # conversion does (include/sapien/math/conversion.h:53-57)
+    yaw = math.atan2(R[1, 0], R[0, 0])
+    pitch = math.atan2(-R[2, 0], math.hypot(R[0, 0], R[1, 0]))
+    s, c = math.sin(yaw), math.cos(yaw)
+    roll = math.atan2(s * R[0, 2] - c * R[1, 2], c * R[1, 1] - s * R[0, 1])
+    return roll, pitch, yaw
 
 
 def _inv(pose):

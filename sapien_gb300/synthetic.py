@@ -52,13 +52,10 @@ def _rand_rot(rng):
 
 def _rpy_of(R):
     """Fixed-axis roll, pitch, yaw of a rotation (R = Rz(y) Ry(p) Rx(r))."""
-    pitch = math.asin(max(-1.0, min(1.0, -R[2, 0])))
-    if abs(R[2, 0]) < 1 - 1e-12:
-        roll = math.atan2(R[2, 1], R[2, 2])
-        yaw = math.atan2(R[1, 0], R[0, 0])
-    else:
-        roll = math.atan2(-R[1, 2], R[1, 1])
-        yaw = 0.0
+    yaw = math.atan2(R[1, 0], R[0, 0])
+    pitch = math.atan2(-R[2, 0], math.hypot(R[0, 0], R[1, 0]))
+    s, c = math.sin(yaw), math.cos(yaw)
+    roll = math.atan2(s * R[0, 2] - c * R[1, 2], c * R[1, 1] - s * R[0, 1])
     return roll, pitch, yaw
 
 

@@ -12,6 +12,8 @@ from oracle import urdf_model as um
 from sapien_gb300 import PinocchioModel, synthetic as syn
 from sapien_gb300 import _native as N
 
+import reference_robots as rr
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 DJOINT = np.dtype([("R", "<f8", 9), ("p", "<f8", 3), ("axis", "<f8", 3), ("m", "<f8"), ("h", "<f8", 3),
@@ -135,18 +137,32 @@ def test_builder_matches_oracle_builder(name):
     compare_with_oracle_builder(r.urdf, r.joint_names, r.link_names)
 
 
-def test_builder_on_reference_assets_when_present():
-    """Panda (7R + 2P) and movo_simple (continuous joints, many fixed joints, nested
-    <transmission> joint tags) from the reference tree, when it is mounted."""
-    paths = ["/root/reference/assets/robot/panda/panda.urdf", "/root/reference/unittest/assets/movo_simple.urdf"]
-    found = [p for p in paths if os.path.exists(p)]
-    if not found:
-        pytest.skip("reference assets not mounted")
-    for path in found:
-        urdf = open(path).read()
-        om = um.build_model(urdf)
-        order = om.joint_names[1:][::-1]  # a non-trivial permutation
-        compare_with_oracle_builder(urdf, order, om.link_names_in_order)
+@pytest.mark.parametrize("name", rr.NAMES)
+def test_builder_on_reference_robots(name):
+    """The reference's panda (7R + 2P, a <mimic> finger) and movo_simple (continuous joints,
+    16 fixed joints merged into bodies) fixtures: the product's tables equal the oracle
+    builder's, in SAPIEN's loader order and in a reversed joint order."""
+    r = rr.load(name)
+    compare_with_oracle_builder(r.urdf, r.joint_names, r.link_names)
+    compare_with_oracle_builder(r.urdf, r.joint_names[::-1], r.link_names[::-1])
+    pm = PinocchioModel(r.urdf, [0, 0, -9.81])
+    pm.set_joint_order(r.joint_names)
+    pm.set_link_order(r.link_names)
+    assert pm.nv == r.nv and pm.nq_ext == r.nq_ext
+
+
+def test_reference_robot_orders_follow_sapien_loader():
+    """Depth-first pre-order, children in file order (urdf_loader.py:469-588)."""
+    movo = rr.load("movo_simple")
+    assert movo.nv == len(rr.MOVO_REFERENCE_Q) == 13
+    assert movo.link_names[:4] == ["base_link", "base_chassis_link", "linear_actuator_fixed_link",
+                                   "linear_actuator_link"]
+    assert movo.joint_names[0] == "linear_joint"
+    assert [k for k in movo.joint_kinds].count(syn.CONTINUOUS) == 7
+    panda = rr.load("panda")
+    assert panda.joint_names == [f"panda_joint{i}" for i in range(1, 8)] + ["panda_finger_joint1",
+                                                                           "panda_finger_joint2"]
+    assert len(panda.link_names) == 12
 
 
 def test_library_exports_every_declared_symbol():
