@@ -37,6 +37,19 @@ def max_across_ranks(value, dist=None, device=None):
     return float(t.item())
 
 
+def sum_across_ranks(value, dist=None, device=None):
+    """Sum of a float over all ranks (identity without a process group): the host-side
+    reduction of a loss that is a sum of per-environment terms, each rank holding the
+    partial sum over its own shard."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def aggregate_throughput(envs_per_rank, world, max_seconds):
     """Whole-job environment-steps per second: every rank's environments over the slowest
     rank's time."""
