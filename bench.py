@@ -229,6 +229,7 @@ def secondary_workloads(dev):
                       "fwd_bwd_env_steps_per_s": n * T / ((fwd_ck + bwd) * 1e-3),
                       "fwd_ms": fwd, "fwd_with_checkpoints_ms": fwd_ck, "bwd_ms": bwd,
                       "fwd_bwd_over_plain": (fwd_ck + bwd) / fwd}
+    out["rollout"].update(_rollout_parity(torch, ad, arm, pm, q0, qd0, tau, dt, K))
     robots, moe = synthetic.hetero_mix(8192, seed=0)
     models = [model_of(r) for r in robots]
     ins = [r.sample(int((moe == k).sum()), seed=k) for k, r in enumerate(robots)]
@@ -242,6 +243,7 @@ def secondary_workloads(dev):
                                  "RNEA+ABA+CRBA; CUDA-graph replay of 10 steps",
                      "env_steps_per_s": 8192 / (hms * 1e-3), "ms_per_step": hms, "launch_shape": list(shape),
                      "lanes_per_env": list(hb.lanes)}
+    out["hetero"].update(_hetero_parity(robots, moe, hb, g.outputs, ins))
     # a whole heterogeneous rollout (ABA + semi-implicit Euler, free flyers on SE(3)) as one graph,
     # with the launch shape and lanes tuned for ABA alone
     rq, rqd, rtau = hq.clone(), hqd.clone(), 0.1 * htau
@@ -252,6 +254,12 @@ def secondary_workloads(dev):
                                          "captured as one CUDA graph, dt=1/500",
                              "env_steps_per_s": 8192 / (rms * 1e-3), "ms_per_step": rms,
                              "launch_shape": list(rshape), "lanes_per_env": list(hb.lanes)}
+    # parity: one replay (100 steps) from the initial state against the oracle's rollout
+    rq.copy_(hq)
+    rqd.copy_(hqd)
+    rg.replay()
+    torch.cuda.synchronize()
+    out["hetero_rollout"].update(_hetero_rollout_parity(robots, moe, hb, hq, hqd, rtau, rq, rqd, 1.0 / 500, 100))
     nik = 65536
     qik, _, _, _ = arm.sample(nik, seed=3)
     tgt = pm.compute_forward_kinematics_batched(torch.from_numpy(qik).to(dev))[:, arm.ee_link].contiguous()
@@ -288,7 +296,174 @@ def secondary_workloads(dev):
                                       "dqdd/d(q,qd,tau)",
                           "rnea_derivatives_evals_per_s": 8192 / (rd * 1e-3),
                           "aba_derivatives_evals_per_s": 8192 / (adr * 1e-3)}
+    out["derivatives"].update(_derivative_parity(ad, hum, hm, hq2, hqd2, hqdd2, htau2))
+    out["reference_robots"] = _reference_robot_parity(torch, dev)
     return out
+
+
+def _oracle_of(robot):
+    from oracle.oracle import Oracle
+
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    return o
+
+
+def _rel(g, r):
+    """Largest per-environment normwise relative error (rows = environments)."""
+    g = np.asarray(g).reshape(len(g), -1)
+    r = np.asarray(r).reshape(len(r), -1)
+    return float((np.abs(g - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-300)).max())
+
+
+def _rollout_parity(torch, ad, arm, pm, q0, qd0, tau, dt, K, sample=64, grad_envs=4, h=1e-6):
+    """Final states of the first `sample` environments against the oracle's rollout, and
+    the loss gradient (loss = sum |p_ee(q_T) - target|^2) w.r.t. q0 and qd0 of the first
+    `grad_envs` environments against central differences of the oracle's rollout."""
+    o = _oracle_of(arm)
+    s = slice(0, sample)
+    qT, qdT, _, _ = ad.rollout_forward(pm, q0[s].contiguous(), qd0[s].contiguous(), tau[:, s].contiguous(), dt, K)
+    tau_h = tau[:, s].cpu().numpy()
+    targets = np.random.default_rng(2).uniform(-0.5, 0.5, size=(sample, 3))
+    rq, rqd, _ = o.rollout(q0[s].cpu().numpy(), qd0[s].cpu().numpy(), tau_h, dt, arm.ee_link, targets, nthreads=8)
+    g = slice(0, grad_envs)
+    q0t = q0[g].clone().requires_grad_()
+    qd0t = qd0[g].clone().requires_grad_()
+    qTg, _ = ad.rollout(pm, q0t, qd0t, tau[:, g].contiguous(), dt, checkpoint_every=K)
+    tg = torch.from_numpy(targets[g]).to(q0.device)
+    ((ad.link_positions(pm, qTg)[:, arm.ee_link] - tg) ** 2).sum().backward()
+    qn, qdn, taun = q0[g].cpu().numpy(), qd0[g].cpu().numpy(), tau_h[:, g]
+
+    def loss(a, b):
+        return o.rollout(a, b, taun, dt, arm.ee_link, targets[g])[2]
+
+    fq, fqd = np.zeros_like(qn), np.zeros_like(qdn)
+    for k in range(qn.shape[1]):
+        e = np.zeros(qn.shape[1])
+        e[k] = h
+        fq[:, k] = (loss(qn + e, qdn) - loss(qn - e, qdn)) / (2 * h)
+        fqd[:, k] = (loss(qn, qdn + e) - loss(qn, qdn - e)) / (2 * h)
+    return {"max_rel_err_vs_oracle": {"qT": _rel(qT.cpu().numpy(), rq), "qdT": _rel(qdT.cpu().numpy(), rqd)},
+            "grad_rel_err_vs_fd": {"q0": _rel(q0t.grad.cpu().numpy(), fq), "qd0": _rel(qd0t.grad.cpu().numpy(), fqd)},
+            "err_sample": f"final states of the first {sample} envs; loss gradients of the first {grad_envs} envs vs "
+                          f"oracle central differences (h={h:g})"}
+
+
+def _hetero_parity(robots, moe, hb, outs, ins, sample=256):
+    """RNEA / ABA / CRBA of the graph replay against the oracle, up to `sample`
+    environments of each robot type."""
+    errs = {"rnea": 0.0, "aba": 0.0, "crba": 0.0}
+    for k, r in enumerate(robots):
+        o = _oracle_of(r)
+        q, qd, qdd, tau = (x[:sample] for x in ins[k])
+        ref = o.batch_step(q, qd, qdd, tau, ops=4 | 8 | 16, nthreads=8)
+        m = len(q)
+        errs["rnea"] = max(errs["rnea"], _rel(hb.unpad_v(outs["qf"], k)[:m].cpu().numpy(), ref["tau"]))
+        errs["aba"] = max(errs["aba"], _rel(hb.unpad_v(outs["qacc"], k)[:m].cpu().numpy(), ref["qdd"]))
+        errs["crba"] = max(errs["crba"], _rel(hb.unpad_M(outs["mass_matrix"], k)[:m].cpu().numpy(), ref["M"]))
+    return {"max_rel_err_vs_oracle": errs, "err_sample": f"first {sample} envs of each robot type"}
+
+
+def _hetero_rollout_parity(robots, moe, hb, q0, qd0, tau, qT, qdT, dt, steps, sample=32):
+    """Final q / qd after the captured rollout against the oracle's semi-implicit-Euler
+    rollout (SE(3) integrate for free flyers), `sample` environments of each type."""
+    eq = eqd = 0.0
+    for k, r in enumerate(robots):
+        o = _oracle_of(r)
+        idx = np.nonzero(moe == k)[0][:sample]
+        nq, nv = r.nq_ext, r.nv
+        qk, qdk = q0[idx, :nq].cpu().numpy(), qd0[idx, :nv].cpu().numpy()
+        tk = np.repeat(tau[idx, :nv].cpu().numpy()[None], steps, axis=0)
+        rq, rqd, _ = o.rollout(qk, qdk, tk, dt, 0, np.zeros((len(idx), 3)), nthreads=8)
+        eq = max(eq, _rel(qT[idx, :nq].cpu().numpy(), rq))
+        eqd = max(eqd, _rel(qdT[idx, :nv].cpu().numpy(), rqd))
+    return {"max_rel_err_vs_oracle": {"q": eq, "qd": eqd}, "err_sample": f"first {sample} envs of each robot type"}
+
+
+def _derivative_parity(ad, robot, pm, q, qd, qdd, tau, envs=2, h=1e-6):
+    """Dense derivatives of the first `envs` environments against central differences of
+    the oracle's RNEA / ABA (configuration perturbed on the manifold by integrate)."""
+    o = _oracle_of(robot)
+    s = slice(0, envs)
+    dq, dqd, _ = (x.cpu().numpy() for x in ad.rnea_derivatives(pm, q[s], qd[s], qdd[s]))
+    aq, aqd, _ = (x.cpu().numpy() for x in ad.aba_derivatives(pm, q[s], qd[s], tau[s]))
+    qn, qdn, qddn, taun = (x[s].cpu().numpy() for x in (q, qd, qdd, tau))
+    nv = robot.nv
+    worst = {"dtau_dq": 0.0, "dtau_dqd": 0.0, "dqdd_dq": 0.0, "dqdd_dqd": 0.0}
+    for e in range(envs):
+        fd = {k: np.zeros((nv, nv)) for k in worst}
+        for k in range(nv):
+            d = np.zeros(nv)
+            d[k] = h
+            qp, qm = o.integrate(qn[e], d), o.integrate(qn[e], -d)
+            fd["dtau_dq"][:, k] = (o.compute_inverse_dynamics(qp, qdn[e], qddn[e])
+                                   - o.compute_inverse_dynamics(qm, qdn[e], qddn[e])) / (2 * h)
+            fd["dqdd_dq"][:, k] = (o.compute_forward_dynamics(qp, qdn[e], taun[e])
+                                   - o.compute_forward_dynamics(qm, qdn[e], taun[e])) / (2 * h)
+            fd["dtau_dqd"][:, k] = (o.compute_inverse_dynamics(qn[e], qdn[e] + d, qddn[e])
+                                    - o.compute_inverse_dynamics(qn[e], qdn[e] - d, qddn[e])) / (2 * h)
+            fd["dqdd_dqd"][:, k] = (o.compute_forward_dynamics(qn[e], qdn[e] + d, taun[e])
+                                    - o.compute_forward_dynamics(qn[e], qdn[e] - d, taun[e])) / (2 * h)
+        for key, got in (("dtau_dq", dq), ("dtau_dqd", dqd), ("dqdd_dq", aq), ("dqdd_dqd", aqd)):
+            worst[key] = max(worst[key], _rel(got[e][None], fd[key][None]))
+    return {"max_rel_err_vs_fd": worst, "err_sample": f"first {envs} envs, oracle central differences (h={h:g})"}
+
+
+def _reference_robot_parity(torch, dev, n=1024, sample=256):
+    """The reference's own robots (tests/golden: panda, movo_simple, sawyer, fetch, in SAPIEN's
+    loader order): per-op largest error of the batched kernels against the oracle, and the
+    reference test's movo_simple case (unittest/test_physx/test_articulation.py:75-97)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import reference_robots as rr
+
+    from sapien_gb300 import PinocchioModel
+
+    res = {}
+    for name in rr.NAMES:
+        r = rr.load(name)
+        pm = PinocchioModel(r.urdf, [0.0, 0.0, -9.81])
+        pm.set_joint_order(r.joint_names)
+        pm.set_link_order(r.link_names)
+        o = _oracle_of(r)
+        q, qd, qdd, tau = r.sample(n, seed=5)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        dyn = name in rr.DYNAMICS
+        ref = o.batch_step(q[:sample], qd[:sample], qdd[:sample], tau[:sample], ops=31 if dyn else 3, nthreads=8)
+        P = pm.compute_forward_kinematics_batched(t(q))[:sample].cpu().numpy()
+        errs = {"fk_positions": _rel(P[:, :, :3], ref["poses"][:, :, 9:]),
+                "jacobian": _rel(pm.compute_full_jacobian_batched(t(q))[:sample].cpu().numpy(), ref["J"])}
+        if dyn:
+            errs["crba"] = _rel(pm.compute_generalized_mass_matrix_batched(t(q))[:sample].cpu().numpy(), ref["M"])
+            errs["rnea"] = _rel(pm.compute_inverse_dynamics_batched(t(q), t(qd), t(qdd))[:sample].cpu().numpy(),
+                                ref["tau"])
+            errs["aba"] = _rel(pm.compute_forward_dynamics_batched(t(q), t(qd), t(tau))[:sample].cpu().numpy(),
+                               ref["qdd"])
+        res[name] = {"nv": r.nv, "links": len(r.link_names), "max_rel_err_vs_oracle": errs}
+        if name == "movo_simple":
+            q0, z, _ = rr.movo_reference_inputs()
+            g = pm.compute_inverse_dynamics(q0, z, z)
+            pm.compute_forward_kinematics(q0)
+            o.compute_forward_kinematics(q0)
+            pe = max(float(np.abs(pm.get_link_pose(i).p - o.get_link_pose_matrix(i)[:3, 3]).max())
+                     for i in range(len(r.link_names)))
+            res[name]["reference_test_case"] = {
+                "rnea_q_0_0_rel_err": _rel(g[None], o.compute_inverse_dynamics(q0, z, z)[None]),
+                "get_link_pose_max_abs_err_float32": pe}
+    res["err_sample"] = f"first {sample} of {n} seeded envs per robot"
+    return res
+
+
+def workload_config(n, nv, nl):
+    """The workload as both arms name it (identical dicts, so the two lines compare)."""
+    return {"workload": WORKLOAD, "n_envs_per_gpu": n, "nv": nv, "links": nl,
+            "layout": "structure of arrays ([cols][n], SGDYN_COL_MAJOR)",
+            "l2": "flushed between timed GPU steps (256 MiB write, outside the timed events)"}
+
+
+CPU_BASELINE_NOTE = ("the oracle: this project's FP64 C++ restatement of the reference path with dense 6x6 "
+                     "Plucker algebra (the reference's Pinocchio cannot be built here); slower per call than "
+                     "Pinocchio itself, so GPU/CPU ratios against it overstate the speed-up over SAPIEN's CPU path")
 
 
 def run_reference(args):
@@ -317,9 +492,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_envs": n, "parallelism": "threads over environments"},
+        "config": workload_config(n, robot.nv, len(robot.link_names)),
+        "execution": {"parallelism": "host threads over environments (one model per thread)", "threads": cores},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"full workload ({n} envs) per step, {args.steps} steps"},
+                         "sample": f"full workload ({n} envs) per step, {args.steps} steps", "what": CPU_BASELINE_NOTE},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -499,7 +675,7 @@ def main():
     o.set_joint_order(robot.joint_names)
     o.set_link_order(robot.link_names)
     cores = host_cores()
-    S = min(n, 4096)
+    S = n  # the whole workload, as the reference arm times it
     o.batch_step(q_h[:256], qd_h[:256], qdd_h[:256], tau_h[:256], nthreads=cores)
     cpu_dt, reps = time_median(lambda: o.batch_step(q_h[:S], qd_h[:S], qdd_h[:S], tau_h[:S], nthreads=cores))
     ref = o.batch_step(q_h[:S], qd_h[:S], qdd_h[:S], tau_h[:S], nthreads=cores)
@@ -523,11 +699,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_envs_per_gpu": n, "nv": nv, "links": nl,
-                   "layout": "structure of arrays ([cols][n], SGDYN_COL_MAJOR)",
-                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
-                   "parallelism": f"data-parallel replicas over environments x{world}",
-                   "kernel": kernel},
+        "config": workload_config(n, nv, nl),
+        "execution": {"parallelism": f"data-parallel replicas over environments x{world}", "kernel": kernel},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e,
                 "transfer": "sgdyn_step on mapped pinned host buffers (SoA): the kernel reads inputs from and "
@@ -540,8 +713,9 @@ def main():
         "roofline": roofline,
         "roofline_fp64": roofline_fp64,
         "cpu_baseline": {"value": S / cpu_dt, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"first {S} envs of the workload, median of {reps} repetitions (>= 2 s)",
-                         "single_thread_value": S1 / cpu1_dt, "nproc": os.cpu_count(), "cpu_model": cpu_model()},
+                         "sample": f"the whole workload ({S} envs) per step, median of {reps} repetitions (>= 2 s)",
+                         "single_thread_value": S1 / cpu1_dt, "nproc": os.cpu_count(), "cpu_model": cpu_model(),
+                         "what": CPU_BASELINE_NOTE},
         "per_op_kernel": per_op,
         "max_rel_err_vs_oracle": errs,
         "clocks": clk,

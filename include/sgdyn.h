@@ -206,6 +206,35 @@ int sgdyn_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, 
                                      const double* q0, const int* mask, double eps, int max_iterations, double dt,
                                      double damp, double* q_out, int* success, double* err, int layout, void* stream);
 
+/* ---- host path for single instances and small batches -------------------------------
+ * The same sweeps as the entry points above, compiled for the CPU and run on HOST memory
+ * (any host pointers; `layout` as above), environments split over `nthreads` host threads
+ * (<= 1: the calling thread). They serve the reference's one-configuration-at-a-time
+ * callers, for which a GPU launch plus synchronisation costs more than the sweep itself;
+ * batches belong on the device entry points. Results agree with the device kernels to
+ * rounding. Each replaces the reference method named beside it:
+ *   sgdyn_host_step                          computeForwardKinematics + getLinkPose (:146-161),
+ *                                            computeFullJacobian (:163-165),
+ *                                            computeGeneralizedMassMatrix (:201-206),
+ *                                            computeInverseDynamics (:214-219),
+ *                                            computeForwardDynamics (:221-226), as sgdyn_step
+ *   sgdyn_host_compute_link_jacobian         getLinkJacobian (:167-186) /
+ *                                            computeSingleLinkLocalJacobian (:188-199)
+ *   sgdyn_host_compute_coriolis_matrix       computeCoriolisMatrix (:208-212)
+ *   sgdyn_host_compute_inverse_kinematics    computeInverseKinematics (:228-300)
+ * (pinocchio/pinocchio_model.cpp line numbers). */
+int sgdyn_host_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const double* qd, const double* qdd,
+                    const double* tau, double* link_poses, double* J, double* M, double* tau_out, double* qdd_out,
+                    int layout, int nthreads);
+int sgdyn_host_compute_link_jacobian(const sgdyn_model* m, int64_t n, int link, int local, const double* q,
+                                     double* J, int layout, int nthreads);
+int sgdyn_host_compute_coriolis_matrix(const sgdyn_model* m, int64_t n, const double* q, const double* qd, double* C,
+                                       int layout, int nthreads);
+int sgdyn_host_compute_inverse_kinematics(const sgdyn_model* m, int64_t n, int link, const double* target,
+                                          const double* q0, const int* mask, double eps, int max_iterations,
+                                          double dt, double damp, double* q_out, int* success, double* err,
+                                          int layout, int nthreads);
+
 /* ---- heterogeneous batches (addition: the reference evaluates one robot per call) ------
  * Robots of different size and topology in one persistent launch. A batch is planned once
  * (tables packed, environments grouped per model into tiles of up to 32, tiles ordered by

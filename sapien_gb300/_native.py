@@ -78,6 +78,10 @@ EXPORTED = (
     "sgdyn_jit_source",
     "sgdyn_model_from_articulation",
     "sgdyn_compute_passive_force_f32",
+    "sgdyn_host_step",
+    "sgdyn_host_compute_link_jacobian",
+    "sgdyn_host_compute_coriolis_matrix",
+    "sgdyn_host_compute_inverse_kinematics",
 )
 
 _lib = None
@@ -125,6 +129,11 @@ def load():
     L.sgdyn_compute_forward_dynamics.argtypes = [vp, i64, vp, vp, vp, vp, i32, vp]
     L.sgdyn_step.argtypes = [vp, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp]
     L.sgdyn_compute_inverse_kinematics.argtypes = [vp, i64, i32, vp, vp, vp, dbl, i32, dbl, dbl, vp, vp, vp, i32, vp]
+    L.sgdyn_host_step.argtypes = [vp, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, i32]
+    L.sgdyn_host_compute_link_jacobian.argtypes = [vp, i64, i32, i32, vp, vp, i32, i32]
+    L.sgdyn_host_compute_coriolis_matrix.argtypes = [vp, i64, vp, vp, vp, i32, i32]
+    L.sgdyn_host_compute_inverse_kinematics.argtypes = [vp, i64, i32, vp, vp, vp, dbl, i32, dbl, dbl, vp, vp, vp, i32,
+                                                        i32]
     L.sgdyn_compute_inverse_dynamics_vjp.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, i32, vp]
     L.sgdyn_compute_forward_dynamics_vjp.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, i32, vp]
     L.sgdyn_compute_forward_kinematics_vjp.argtypes = [vp, i64, vp, vp, vp, vp, i32, vp]

@@ -1,4 +1,6 @@
 // Link Jacobians, Coriolis matrix and CLIK inverse kinematics, one environment per thread.
+// The per-environment bodies are host-device functions: the same code answers
+// single-instance calls on the host (host_path.cu).
 #pragma once
 #include "se3.cuh"
 #include "step_kernel.cuh"
@@ -10,9 +12,7 @@ namespace sgdyn {
 // action of the link pose. computeSingleLinkLocalJacobian (:188-199) is the same matrix
 // (link2joint^-1 action of the joint-frame Jacobian = link2world^-1 action of the world one).
 template <int MAXJ>
-__global__ void __launch_bounds__(32) link_jacobian_kernel(const DModel* __restrict__ model, const LinkJacArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+SG_HD void link_jacobian_env(const DModel* __restrict__ model, const LinkJacArgs& a, const int64_t e) {
   const DJoint* __restrict__ JT = model_joints(model);
   const DLink& L = model_links(model)[a.link];
   const int nv = model->nv;
@@ -59,6 +59,13 @@ __global__ void __launch_bounds__(32) link_jacobian_kernel(const DModel* __restr
   }
 }
 
+template <int MAXJ>
+__global__ void __launch_bounds__(32) link_jacobian_kernel(const DModel* __restrict__ model, const LinkJacArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  link_jacobian_env<MAXJ>(model, a, e);
+}
+
 // computeCoriolisMatrix (pinocchio_model.cpp:208-212): the Christoffel-consistent
 // factorisation C = sum_b J_b^T (I_b Jdot_b + B_b J_b) with
 // B(I, v) = 1/2 ((v x*) I - I (v x) + (I v) xbar*), evaluated with subtree composites:
@@ -72,9 +79,7 @@ __global__ void __launch_bounds__(32) link_jacobian_kernel(const DModel* __restr
 // so B x = (w_x x f, M w_x) and B^T y = (0, f x y_lin + M^T y_ang). Composites keep the sum
 // of f (3 numbers) and of M (9) instead of a dense 6x6.
 template <int MAXJ>
-__global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__ model, const CoriolisArgs a) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
+SG_HD void coriolis_env(const DModel* __restrict__ model, const CoriolisArgs& a, const int64_t e) {
   constexpr int MAXV = MAXJ + 5;
   const DJoint* __restrict__ JT = model_joints(model);
   const int nj = model->nj, nv = model->nv;
@@ -175,6 +180,13 @@ __global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__
   }
 }
 
+template <int MAXJ>
+__global__ void __launch_bounds__(32) coriolis_kernel(const DModel* __restrict__ model, const CoriolisArgs a) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  coriolis_env<MAXJ>(model, a, e);
+}
+
 #ifndef __CUDACC_RTC__
 // Grid for a grid-stride kernel of one-warp blocks: as few rounds as the resident capacity
 // (occupancy x SMs) allows, with the environments spread evenly over the rounds. Without
@@ -200,7 +212,7 @@ inline unsigned balanced_grid(int64_t n, int blocks_per_sm) {
 // Jacobian; J = -Jlog6(iMd^-1) J diag(mask); v = -J^T (J J^T + damp 1)^-1 err;
 // q = integrate(q, v dt). Returns posP2S(best q), success, best err.
 template <int MAXJ>
-__device__ __forceinline__ void ik_env(const DModel* __restrict__ model, const IkArgs& a, const int64_t e) {
+SG_HD void ik_env(const DModel* __restrict__ model, const IkArgs& a, const int64_t e) {
   constexpr int MAXV = MAXJ + 5;
   const DJoint* __restrict__ JT = model_joints(model);
   const DLink& L = model_links(model)[a.link];

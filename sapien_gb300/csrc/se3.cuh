@@ -18,7 +18,7 @@ namespace sgdyn {
 // sum_k c[k] x^k by Horner's rule; with a constant table and full unrolling this is K - 1
 // FMAs, no division.
 template <int K>
-__device__ __forceinline__ double se3_horner(const double (&c)[K], double x) {
+SG_HD double se3_horner(const double (&c)[K], double x) {
   double r = c[K - 1];
 #pragma unroll
   for (int k = K - 2; k >= 0; k--) r = fma(r, x, c[k]);
@@ -26,7 +26,7 @@ __device__ __forceinline__ double se3_horner(const double (&c)[K], double x) {
 }
 
 // Series coefficients below are the exact rationals rounded to the nearest double.
-__device__ __forceinline__ double se3_f_1mc(double t) {  // (1 - cos t) / t^2 = sum (-1)^k t^2k / (2k+2)!
+SG_HD double se3_f_1mc(double t) {  // (1 - cos t) / t^2 = sum (-1)^k t^2k / (2k+2)!
   if (t < 0.3) {
     const double c[10] = {0.5, -0.041666666666666664, 0.001388888888888889, -2.48015873015873e-05,
                           2.755731922398589e-07, -2.08767569878681e-09, 1.1470745597729725e-11,
@@ -35,7 +35,7 @@ __device__ __forceinline__ double se3_f_1mc(double t) {  // (1 - cos t) / t^2 = 
   }
   return (1 - cos(t)) / (t * t);
 }
-__device__ __forceinline__ double se3_f_sinc(double t) {  // sin t / t = sum (-1)^k t^2k / (2k+1)!
+SG_HD double se3_f_sinc(double t) {  // sin t / t = sum (-1)^k t^2k / (2k+1)!
   if (t < 0.3) {
     const double c[10] = {1.0, -0.16666666666666666, 0.008333333333333333, -0.0001984126984126984,
                           2.7557319223985893e-06, -2.505210838544172e-08, 1.6059043836821613e-10,
@@ -44,7 +44,7 @@ __device__ __forceinline__ double se3_f_sinc(double t) {  // sin t / t = sum (-1
   }
   return sin(t) / t;
 }
-__device__ __forceinline__ double se3_f_tms(double t) {  // (t - sin t) / t^3 = sum (-1)^k t^2k / (2k+3)!
+SG_HD double se3_f_tms(double t) {  // (t - sin t) / t^3 = sum (-1)^k t^2k / (2k+3)!
   if (t < 0.3) {
     const double c[10] = {0.16666666666666666, -0.008333333333333333, 0.0001984126984126984,
                           -2.7557319223985893e-06, 2.505210838544172e-08, -1.6059043836821613e-10,
@@ -55,7 +55,7 @@ __device__ __forceinline__ double se3_f_tms(double t) {  // (t - sin t) / t^3 = 
   return (t - sin(t)) / (t * t * t);
 }
 // (t^2 + 2 cos t - 2) / (2 t^4) = sum (-1)^k t^2k / (2k+4)!
-__device__ __forceinline__ double se3_f_c4(double t) {
+SG_HD double se3_f_c4(double t) {
   if (t < 0.6) {
     const double c[12] = {0.041666666666666664, -0.001388888888888889, 2.48015873015873e-05,
                           -2.755731922398589e-07, 2.08767569878681e-09, -1.1470745597729725e-11,
@@ -66,7 +66,7 @@ __device__ __forceinline__ double se3_f_c4(double t) {
   return (t * t + 2 * cos(t) - 2) / (2 * t * t * t * t);
 }
 // (2t - 3 sin t + t cos t) / (2 t^5) = sum_{n>=2} (-1)^n (n-1) t^(2n-4) / (2n+1)!
-__device__ __forceinline__ double se3_f_c5(double t) {
+SG_HD double se3_f_c5(double t) {
   if (t < 0.9) {
     const double c[14] = {0.008333333333333333, -0.0003968253968253968, 8.267195767195768e-06,
                           -1.0020843354176688e-07, 8.029521918410807e-10, -4.58829823909189e-12,
@@ -77,7 +77,7 @@ __device__ __forceinline__ double se3_f_c5(double t) {
   }
   return (2 * t - 3 * sin(t) + t * cos(t)) / (2 * t * t * t * t * t);
 }
-__device__ __forceinline__ double se3_f_g(double t) {  // (1 - (t/2) cot(t/2)) / t^2
+SG_HD double se3_f_g(double t) {  // (1 - (t/2) cot(t/2)) / t^2
   if (t < 0.3) {
     const double c[6] = {1.0 / 12, 1.0 / 720, 1.0 / 30240, 1.0 / 1209600, 1.0 / 47900160, 691.0 / 1307674368000.0};
     return se3_horner(c, t * t);
@@ -86,8 +86,8 @@ __device__ __forceinline__ double se3_f_g(double t) {  // (1 - (t/2) cot(t/2)) /
   return (1 - h * cos(h) / sin(h)) / (t * t);
 }
 
-__device__ __forceinline__ M3 skew3(V3 w) { return M3{{0, -w.z, w.y, w.z, 0, -w.x, -w.y, w.x, 0}}; }
-__device__ __forceinline__ M3 add3(const M3& A, const M3& B) {
+SG_HD M3 skew3(V3 w) { return M3{{0, -w.z, w.y, w.z, 0, -w.x, -w.y, w.x, 0}}; }
+SG_HD M3 add3(const M3& A, const M3& B) {
   M3 C;
 #pragma unroll
   for (int k = 0; k < 9; k++) C.a[k] = A.a[k] + B.a[k];
@@ -95,7 +95,7 @@ __device__ __forceinline__ M3 add3(const M3& A, const M3& B) {
 }
 
 // Rotation vector of R (theta in [0, pi]).
-__device__ __forceinline__ V3 log3(const M3& R, double* theta) {
+SG_HD V3 log3(const M3& R, double* theta) {
   double q[4];
   R_to_quat(R, q);
   if (q[0] < 0) {
@@ -116,7 +116,7 @@ __device__ __forceinline__ V3 log3(const M3& R, double* theta) {
 }
 
 // log6 of (R, p): linear part, angular part.
-__device__ __forceinline__ Mot log6(const M3& R, V3 p) {
+SG_HD Mot log6(const M3& R, V3 p) {
   double t;
   V3 w = log3(R, &t);
   double beta = se3_f_g(t);
@@ -132,7 +132,7 @@ __device__ __forceinline__ Mot log6(const M3& R, V3 p) {
 
 // exp6 of (v, w) -> (R, p): R = 1 + sinc(t) K + f_1mc(t) K^2, p = (1 + f_1mc(t) K + f_tms(t) K^2) v
 // with K = [w]x, t = |w|.
-__device__ __forceinline__ void exp6(Mot nu, M3& R, V3& p) {
+SG_HD void exp6(Mot nu, M3& R, V3& p) {
   V3 w = nu.w;
   double t = sqrt(dot(w, w));
   M3 K = skew3(w), K2 = mul(K, K);
@@ -150,7 +150,7 @@ __device__ __forceinline__ void exp6(Mot nu, M3& R, V3& p) {
 // Free-flyer configuration q = (x y z qx qy qz qw) advanced by the body twist v (linear,
 // angular): (R, p) <- (R, p) exp6(v) (Pinocchio's integrate), the new quaternion taken on
 // the same hemisphere as the old one and renormalised. In place.
-__device__ __forceinline__ void free_flyer_integrate(double* q, const double* v) {
+SG_HD void free_flyer_integrate(double* q, const double* v) {
   const M3 R0 = quat_to_R(q[3], q[4], q[5], q[6]);
   M3 dR;
   V3 dp;
@@ -178,7 +178,7 @@ __device__ __forceinline__ void free_flyer_integrate(double* q, const double* v)
 //   Q = -1/2 [rho]x + a (rho phi^T + phi rho^T - 2d 1 + d [phi]x)
 //       + b (phi (phi x rho)^T - (phi x rho) phi^T - d [phi]x) - 2 c d (phi phi^T - t^2 1)
 // with a = f_tms(t), b = f_c4(t), c = f_c5(t).
-__device__ __forceinline__ void jlog6_blocks(const Mot& xi, M3& Jinv, M3& TR) {
+SG_HD void jlog6_blocks(const Mot& xi, M3& Jinv, M3& TR) {
   const V3 rho = xi.v, phi = xi.w;
   const double t2 = dot(phi, phi), t = sqrt(t2), d = dot(phi, rho);
   const double g = se3_f_g(t), a = se3_f_tms(t), b = se3_f_c4(t), c = se3_f_c5(t);

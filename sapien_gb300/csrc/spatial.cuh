@@ -26,37 +26,37 @@ struct RBI {  // rigid-body inertia about the frame origin
   double I[6];  // xx xy xz yy yz zz
 };
 
-__device__ __forceinline__ V3 mk(double x, double y, double z) { return V3{x, y, z}; }
-__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ V3 operator*(double s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ V3 operator-(V3 a) { return V3{-a.x, -a.y, -a.z}; }
-__device__ __forceinline__ double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+SG_HD V3 mk(double x, double y, double z) { return V3{x, y, z}; }
+SG_HD V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+SG_HD V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+SG_HD V3 operator*(double s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
+SG_HD V3 operator-(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+SG_HD double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SG_HD V3 cross(V3 a, V3 b) {
   return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 // acc + a x b with the cross product folded into the accumulation.
-__device__ __forceinline__ V3 add_cross(V3 acc, V3 a, V3 b) {
+SG_HD V3 add_cross(V3 acc, V3 a, V3 b) {
   return V3{fma(a.y, b.z, fma(-a.z, b.y, acc.x)), fma(a.z, b.x, fma(-a.x, b.z, acc.y)),
             fma(a.x, b.y, fma(-a.y, b.x, acc.z))};
 }
-__device__ __forceinline__ V3 axpy(double s, V3 x, V3 y) { return V3{fma(s, x.x, y.x), fma(s, x.y, y.y), fma(s, x.z, y.z)}; }
+SG_HD V3 axpy(double s, V3 x, V3 y) { return V3{fma(s, x.x, y.x), fma(s, x.y, y.y), fma(s, x.z, y.z)}; }
 
-__device__ __forceinline__ V3 mul(const M3& R, V3 x) {
+SG_HD V3 mul(const M3& R, V3 x) {
   return V3{fma(R.a[2], x.z, fma(R.a[1], x.y, R.a[0] * x.x)), fma(R.a[5], x.z, fma(R.a[4], x.y, R.a[3] * x.x)),
             fma(R.a[8], x.z, fma(R.a[7], x.y, R.a[6] * x.x))};
 }
 // acc + R x
-__device__ __forceinline__ V3 mul_add(const M3& R, V3 x, V3 acc) {
+SG_HD V3 mul_add(const M3& R, V3 x, V3 acc) {
   return V3{fma(R.a[2], x.z, fma(R.a[1], x.y, fma(R.a[0], x.x, acc.x))),
             fma(R.a[5], x.z, fma(R.a[4], x.y, fma(R.a[3], x.x, acc.y))),
             fma(R.a[8], x.z, fma(R.a[7], x.y, fma(R.a[6], x.x, acc.z)))};
 }
-__device__ __forceinline__ V3 mulT(const M3& R, V3 x) {
+SG_HD V3 mulT(const M3& R, V3 x) {
   return V3{fma(R.a[6], x.z, fma(R.a[3], x.y, R.a[0] * x.x)), fma(R.a[7], x.z, fma(R.a[4], x.y, R.a[1] * x.x)),
             fma(R.a[8], x.z, fma(R.a[5], x.y, R.a[2] * x.x))};
 }
-__device__ __forceinline__ M3 mul(const M3& A, const M3& B) {
+SG_HD M3 mul(const M3& A, const M3& B) {
   M3 C;
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -65,26 +65,26 @@ __device__ __forceinline__ M3 mul(const M3& A, const M3& B) {
       C.a[i * 3 + j] = fma(A.a[i * 3 + 2], B.a[6 + j], fma(A.a[i * 3 + 1], B.a[3 + j], A.a[i * 3] * B.a[j]));
   return C;
 }
-__device__ __forceinline__ M3 transpose(const M3& A) {
+SG_HD M3 transpose(const M3& A) {
   return M3{{A.a[0], A.a[3], A.a[6], A.a[1], A.a[4], A.a[7], A.a[2], A.a[5], A.a[8]}};
 }
-__device__ __forceinline__ M3 eye3() { return M3{{1, 0, 0, 0, 1, 0, 0, 0, 1}}; }
+SG_HD M3 eye3() { return M3{{1, 0, 0, 0, 1, 0, 0, 0, 1}}; }
 
 // Symmetric 3x3 (xx xy xz yy yz zz) times vector.
-__device__ __forceinline__ V3 sym_mul(const double* S, V3 w) {
+SG_HD V3 sym_mul(const double* S, V3 w) {
   return V3{fma(S[2], w.z, fma(S[1], w.y, S[0] * w.x)), fma(S[4], w.z, fma(S[3], w.y, S[1] * w.x)),
             fma(S[5], w.z, fma(S[4], w.y, S[2] * w.x))};
 }
-__device__ __forceinline__ V3 sym_mul_add(const double* S, V3 w, V3 acc) {
+SG_HD V3 sym_mul_add(const double* S, V3 w, V3 acc) {
   return V3{fma(S[2], w.z, fma(S[1], w.y, fma(S[0], w.x, acc.x))),
             fma(S[4], w.z, fma(S[3], w.y, fma(S[1], w.x, acc.y))),
             fma(S[5], w.z, fma(S[4], w.y, fma(S[2], w.x, acc.z)))};
 }
 
 // Rotation about z with (s, c) = (sin, cos) of the angle.
-__device__ __forceinline__ M3 rot_z(double s, double c) { return M3{{c, -s, 0, s, c, 0, 0, 0, 1}}; }
+SG_HD M3 rot_z(double s, double c) { return M3{{c, -s, 0, s, c, 0, 0, 0, 1}}; }
 // Rotation about unit axis a by angle with (s, c) = (sin, cos): c 1 + s [a]x + (1-c) a a^T.
-__device__ __forceinline__ M3 rodrigues(V3 a, double s, double c) {
+SG_HD M3 rodrigues(V3 a, double s, double c) {
   double t = 1.0 - c;
   double txy = t * a.x * a.y, txz = t * a.x * a.z, tyz = t * a.y * a.z;
   M3 R;
@@ -100,7 +100,7 @@ __device__ __forceinline__ M3 rodrigues(V3 a, double s, double c) {
   return R;
 }
 // Unit quaternion (x, y, z, w) -> rotation matrix.
-__device__ __forceinline__ M3 quat_to_R(double x, double y, double z, double w) {
+SG_HD M3 quat_to_R(double x, double y, double z, double w) {
   double x2 = x + x, y2 = y + y, z2 = z + z;
   double xx = x * x2, yy = y * y2, zz = z * z2, xy = x * y2, xz = x * z2, yz = y * z2, wx = w * x2, wy = w * y2,
          wz = w * z2;
@@ -112,7 +112,7 @@ __device__ __forceinline__ M3 quat_to_R(double x, double y, double z, double w) 
 // rotations, and a divergent branch would run the square root and the division once per
 // case taken in the warp. The case only selects operands; the arithmetic per case is
 // unchanged.
-__device__ __forceinline__ void R_to_quat(const M3& R, double* q) {
+SG_HD void R_to_quat(const M3& R, double* q) {
   const double* a = R.a;
   const double t = a[0] + a[4] + a[8];
   int c = 0;  // 0: trace, 1 + i: diagonal entry i
@@ -142,35 +142,35 @@ __device__ __forceinline__ void R_to_quat(const M3& R, double* q) {
 }
 
 // Motion cross motion: a x b = (a.w x b.v + a.v x b.w, a.w x b.w); acc + a x b.
-__device__ __forceinline__ Mot add_crossm(Mot acc, Mot a, Mot b) {
+SG_HD Mot add_crossm(Mot acc, Mot a, Mot b) {
   Mot r;
   r.v = add_cross(add_cross(acc.v, a.w, b.v), a.v, b.w);
   r.w = add_cross(acc.w, a.w, b.w);
   return r;
 }
 // Motion cross force: v x* f = (v.w x f.f, v.w x f.n + v.v x f.f); acc + v x* f.
-__device__ __forceinline__ Mot add_crossf(Mot acc, Mot v, Mot f) {
+SG_HD Mot add_crossf(Mot acc, Mot v, Mot f) {
   Mot r;
   r.v = add_cross(acc.v, v.w, f.v);
   r.w = add_cross(add_cross(acc.w, v.w, f.w), v.v, f.v);
   return r;
 }
 // f = Y v with Y in origin form: (m v - h x w, I w + h x v).
-__device__ __forceinline__ Mot rbi_mul(const RBI& Y, Mot v) {
+SG_HD Mot rbi_mul(const RBI& Y, Mot v) {
   Mot f;
   f.v = add_cross(Y.m * v.v, v.w, Y.h);  // m v + w x h = m v - h x w
   f.w = add_cross(sym_mul(Y.I, v.w), Y.h, v.v);
   return f;
 }
 // acc + Y v
-__device__ __forceinline__ Mot rbi_mul_add(const RBI& Y, Mot v, Mot acc) {
+SG_HD Mot rbi_mul_add(const RBI& Y, Mot v, Mot acc) {
   Mot f;
   f.v = add_cross(axpy(Y.m, v.v, acc.v), v.w, Y.h);
   f.w = add_cross(sym_mul_add(Y.I, v.w, acc.w), Y.h, v.v);
   return f;
 }
 // Express an origin-form inertia given in a frame with pose (R, p) in the outer frame.
-__device__ __forceinline__ RBI rbi_transport(const RBI& Y, const M3& R, V3 p) {
+SG_HD RBI rbi_transport(const RBI& Y, const M3& R, V3 p) {
   // R I R^T: T = R I (I symmetric), then the upper triangle of T R^T
   const double* I = Y.I;
   double T[9];
@@ -206,7 +206,7 @@ __device__ __forceinline__ RBI rbi_transport(const RBI& Y, const M3& R, V3 p) {
 struct Sym6 {
   double A[6], B[9], C[6];
 };
-__device__ __forceinline__ Sym6 sym6_from_rbi(const RBI& Y) {
+SG_HD Sym6 sym6_from_rbi(const RBI& Y) {
   Sym6 S;
   S.A[0] = Y.m; S.A[1] = 0; S.A[2] = 0; S.A[3] = Y.m; S.A[4] = 0; S.A[5] = Y.m;
   // B = -[h]x
@@ -218,7 +218,7 @@ __device__ __forceinline__ Sym6 sym6_from_rbi(const RBI& Y) {
   return S;
 }
 // sym6_from_rbi(Y) + S, adding only where Y's matrix has non-zero entries
-__device__ __forceinline__ Sym6 sym6_rbi_add(const RBI& Y, const Sym6& S) {
+SG_HD Sym6 sym6_rbi_add(const RBI& Y, const Sym6& S) {
   Sym6 R = S;
   R.A[0] += Y.m; R.A[3] += Y.m; R.A[5] += Y.m;
   R.B[1] += Y.h.z; R.B[2] -= Y.h.y; R.B[3] -= Y.h.z;
@@ -227,7 +227,7 @@ __device__ __forceinline__ Sym6 sym6_rbi_add(const RBI& Y, const Sym6& S) {
   for (int k = 0; k < 6; k++) R.C[k] += Y.I[k];
   return R;
 }
-__device__ __forceinline__ void sym6_acc(Sym6& P, const Sym6& S) {
+SG_HD void sym6_acc(Sym6& P, const Sym6& S) {
 #pragma unroll
   for (int k = 0; k < 6; k++) {
     P.A[k] += S.A[k];
@@ -236,7 +236,7 @@ __device__ __forceinline__ void sym6_acc(Sym6& P, const Sym6& S) {
 #pragma unroll
   for (int k = 0; k < 9; k++) P.B[k] += S.B[k];
 }
-__device__ __forceinline__ RBI rbi_add(const RBI& a, const RBI& b) {
+SG_HD RBI rbi_add(const RBI& a, const RBI& b) {
   RBI r;
   r.m = a.m + b.m;
   r.h = a.h + b.h;
@@ -245,7 +245,7 @@ __device__ __forceinline__ RBI rbi_add(const RBI& a, const RBI& b) {
   return r;
 }
 // acc + S x  (x a 6-vector)
-__device__ __forceinline__ Mot sym6_mul_add(const Sym6& S, Mot x, Mot acc) {
+SG_HD Mot sym6_mul_add(const Sym6& S, Mot x, Mot acc) {
   Mot r;
   r.v = sym_mul_add(S.A, x.v, acc.v);
   M3 B;
@@ -255,15 +255,15 @@ __device__ __forceinline__ Mot sym6_mul_add(const Sym6& S, Mot x, Mot acc) {
   r.w = sym_mul_add(S.C, x.w, mulT(B, x.v) + acc.w);
   return r;
 }
-__device__ __forceinline__ Mot sym6_mul(const Sym6& S, Mot x) {
+SG_HD Mot sym6_mul(const Sym6& S, Mot x) {
   Mot z{{0, 0, 0}, {0, 0, 0}};
   return sym6_mul_add(S, x, z);
 }
-__device__ __forceinline__ double dot6(Mot a, Mot b) {
+SG_HD double dot6(Mot a, Mot b) {
   return fma(a.w.z, b.w.z, fma(a.w.y, b.w.y, fma(a.w.x, b.w.x, fma(a.v.z, b.v.z, fma(a.v.y, b.v.y, a.v.x * b.v.x)))));
 }
-__device__ __forceinline__ Mot scale6(double s, Mot a) { return Mot{s * a.v, s * a.w}; }
-__device__ __forceinline__ Mot axpy6(double s, Mot x, Mot y) { return Mot{axpy(s, x.v, y.v), axpy(s, x.w, y.w)}; }
-__device__ __forceinline__ Mot add6(Mot a, Mot b) { return Mot{a.v + b.v, a.w + b.w}; }
+SG_HD Mot scale6(double s, Mot a) { return Mot{s * a.v, s * a.w}; }
+SG_HD Mot axpy6(double s, Mot x, Mot y) { return Mot{axpy(s, x.v, y.v), axpy(s, x.w, y.w)}; }
+SG_HD Mot add6(Mot a, Mot b) { return Mot{a.v + b.v, a.w + b.w}; }
 
 }  // namespace sgdyn

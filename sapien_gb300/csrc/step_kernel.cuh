@@ -28,35 +28,35 @@ namespace sgdyn {
 struct RuntimeTab {
   static constexpr bool kStatic = false;
   const DModel* m;
-  __device__ __forceinline__ int nj() const { return m->nj; }
-  __device__ __forceinline__ int nv() const { return m->nv; }
-  __device__ __forceinline__ int nq_ext() const { return m->nq_ext; }
-  __device__ __forceinline__ int nlinks() const { return m->nlinks; }
-  __device__ __forceinline__ double gravity(int k) const { return m->gravity[k]; }
-  __device__ __forceinline__ const DJoint& joint(int i) const { return model_joints(m)[i]; }
-  __device__ __forceinline__ const DLink& link(int l) const { return model_links(m)[l]; }
+  SG_HD int nj() const { return m->nj; }
+  SG_HD int nv() const { return m->nv; }
+  SG_HD int nq_ext() const { return m->nq_ext; }
+  SG_HD int nlinks() const { return m->nlinks; }
+  SG_HD double gravity(int k) const { return m->gravity[k]; }
+  SG_HD const DJoint& joint(int i) const { return model_joints(m)[i]; }
+  SG_HD const DLink& link(int l) const { return model_links(m)[l]; }
 };
 template <int NJ, int NV, int NL, const DJoint* JT, const DLink* LT, const DModel* M>
 struct StaticTab {
   static constexpr bool kStatic = true;
-  __device__ __forceinline__ static constexpr int nj() { return NJ; }
-  __device__ __forceinline__ static constexpr int nv() { return NV; }
-  __device__ __forceinline__ int nq_ext() const { return M->nq_ext; }
-  __device__ __forceinline__ static constexpr int nlinks() { return NL; }
-  __device__ __forceinline__ double gravity(int k) const { return M->gravity[k]; }
-  __device__ __forceinline__ const DJoint& joint(int i) const { return JT[i]; }
-  __device__ __forceinline__ const DLink& link(int l) const { return LT[l]; }
+  SG_HD static constexpr int nj() { return NJ; }
+  SG_HD static constexpr int nv() { return NV; }
+  SG_HD int nq_ext() const { return M->nq_ext; }
+  SG_HD static constexpr int nlinks() { return NL; }
+  SG_HD double gravity(int k) const { return M->gravity[k]; }
+  SG_HD const DJoint& joint(int i) const { return JT[i]; }
+  SG_HD const DLink& link(int l) const { return LT[l]; }
 };
 
-__device__ __forceinline__ double ldv(const Arr& a, int64_t e, int c) { return a.p[e * a.es + int64_t(c) * a.cs]; }
-__device__ __forceinline__ void stv(const Arr& a, int64_t e, int c, double v) { a.p[e * a.es + int64_t(c) * a.cs] = v; }
+SG_HD double ldv(const Arr& a, int64_t e, int c) { return a.p[e * a.es + int64_t(c) * a.cs]; }
+SG_HD void stv(const Arr& a, int64_t e, int c, double v) { a.p[e * a.es + int64_t(c) * a.cs] = v; }
 
 // World pose of joint J from its parent's: (Ro, po) = oMi[parent] * placement * M_J(q).
 // A joint in a canonical frame (axis_kind AX_Z) rotates about / slides along z: with
 // B = R_parent R_placement, Ro = B Rz(q) mixes two columns of B and keeps the third. Other
 // 1-DoF joints keep their axis (Rodrigues), which is cheaper when both the placement and the
 // link frames on the joint are unrotated (the table builder decides per joint).
-__device__ __forceinline__ void joint_world_pose(const DJoint& J, const Arr& q, int64_t e, const M3* oR, const V3* op,
+SG_HD void joint_world_pose(const DJoint& J, const Arr& q, int64_t e, const M3* oR, const V3* op,
                                                  M3& Ro, V3& po) {
   const int p = J.parent;
   const bool rot_id = (J.flags & JF_ROT_IDENTITY) != 0;
@@ -120,7 +120,7 @@ __device__ __forceinline__ void joint_world_pose(const DJoint& J, const Arr& q, 
 
 // World-frame motion subspace column k of joint J (pose Ro, po): for a joint in a
 // canonical frame the z column of Ro, else Ro times the axis.
-__device__ __forceinline__ Mot world_S(const DJoint& J, const M3& Ro, V3 po, int k) {
+SG_HD Mot world_S(const DJoint& J, const M3& Ro, V3 po, int k) {
   Mot S;
   if (J.kind == JK_FREEFLYER) {
     V3 r = mk(Ro.a[k % 3], Ro.a[3 + k % 3], Ro.a[6 + k % 3]);  // column of Ro
@@ -146,7 +146,7 @@ __device__ __forceinline__ Mot world_S(const DJoint& J, const M3& Ro, V3 po, int
 
 // Cholesky of a packed symmetric 6x6 (row-major lower triangle, 21 entries) in place; the
 // diagonal slots keep the reciprocals 1 / L_jj, so the solves multiply instead of divide.
-__device__ __forceinline__ void chol6(double* L) {
+SG_HD void chol6(double* L) {
   // index of (r, c), c <= r
 #define LI(r, c) ((r) * ((r) + 1) / 2 + (c))
   for (int j = 0; j < 6; j++) {
@@ -161,7 +161,7 @@ __device__ __forceinline__ void chol6(double* L) {
     }
   }
 }
-__device__ __forceinline__ void chol6_solve(const double* L, double* b) {
+SG_HD void chol6_solve(const double* L, double* b) {
   for (int i = 0; i < 6; i++) {
     double s = b[i];
     for (int k = 0; k < i; k++) s = fma(-L[LI(i, k)], b[k], s);
@@ -199,25 +199,28 @@ struct TeamLanes {
   const int* t;
   int role;
   bool valid;  // false for the lanes of an empty tail slot: they compute but store nothing
-  __device__ __forceinline__ int L() const { return t[0]; }
-  __device__ __forceinline__ int ntrunk() const { return t[1]; }
-  __device__ __forceinline__ int smax() const { return t[2]; }
-  __device__ __forceinline__ int nattach() const { return t[3]; }
-  __device__ __forceinline__ int trunk(int k) const { return t[4 + k]; }
-  __device__ __forceinline__ int sched(int k) const { return t[4 + ntrunk() + role * smax() + k]; }
-  __device__ __forceinline__ int attach(int k) const { return t[4 + ntrunk() + L() * smax() + k]; }
-  __device__ __forceinline__ int owner(int j) const { return t[4 + ntrunk() + L() * smax() + nattach() + j]; }
+  SG_HD int L() const { return t[0]; }
+  SG_HD int ntrunk() const { return t[1]; }
+  SG_HD int smax() const { return t[2]; }
+  SG_HD int nattach() const { return t[3]; }
+  SG_HD int trunk(int k) const { return t[4 + k]; }
+  SG_HD int sched(int k) const { return t[4 + ntrunk() + role * smax() + k]; }
+  SG_HD int attach(int k) const { return t[4 + ntrunk() + L() * smax() + k]; }
+  SG_HD int owner(int j) const { return t[4 + ntrunk() + L() * smax() + nattach() + j]; }
 };
 
 // Sum over the L lanes of a team (L a power of two, teams aligned in the warp).
-__device__ __forceinline__ double team_sum(double v, int L) {
+// (Teams exist only on the device; the host instantiation of the sweep never forms one.)
+SG_HD double team_sum(double v, int L) {
+#ifdef __CUDA_ARCH__
   for (int m = 1; m < L; m <<= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+#endif
   return v;
 }
 
 // The whole fused sweep for environment e (rows of the StepArgs arrays).
 template <int MAXJ, int OPS, class Tab, class Team = NoTeam>
-__device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const Team& tm = Team{}) {
+SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const Team& tm = Team{}) {
   constexpr int MAXV = MAXJ + 5;
   constexpr bool kFK = OPS & OP_FK, kJAC = OPS & OP_JAC, kCRBA = OPS & OP_CRBA, kRNEA = OPS & OP_RNEA,
                  kABA = OPS & OP_ABA;
@@ -633,7 +636,7 @@ __device__ __forceinline__ void step_env_t(const Tab& T, const StepArgs& args, c
 }
 
 template <int MAXJ, int OPS>
-__device__ __forceinline__ void step_env(const DModel* __restrict__ model, const StepArgs& args, const int64_t e) {
+SG_HD void step_env(const DModel* __restrict__ model, const StepArgs& args, const int64_t e) {
   step_env_t<MAXJ, OPS>(RuntimeTab{model}, args, e);
 }
 

@@ -1,11 +1,12 @@
 """Drop-in ``PinocchioModel`` backed by GB300 kernels, plus batched tensor overloads.
 
 Mirrors the reference's pybind surface (pinocchio/pinocchio_model.cpp:306-367): method
-names, argument names, defaults, return types and exception types. Every compute call
-runs on the GPU through the C ABI of libsgdyn.so; single-instance calls are batches of
-one. The ``*_batched`` methods are the additions: they take float64 CUDA tensors of
-shape [N, ...] and return tensors on the same device, enqueued on the current torch
-stream of that device.
+names, argument names, defaults, return types and exception types. The ``*_batched``
+methods are the additions: they take float64 CUDA tensors of shape [N, ...], run the CUDA
+kernels of libsgdyn.so and return tensors on the same device, enqueued on the current
+torch stream of that device. The reference's one-configuration methods run the same sweep
+code compiled for the host (libsgdyn.so's sgdyn_host_* entry points) on the calling
+thread, or, with ``single_instance="cuda"``, on the GPU as batches of one.
 
 Behaviour kept from the reference:
 * the joint order must be set (``set_joint_order``) before any compute call, else
@@ -102,34 +103,77 @@ class _HostStage:
         return ctypes.c_void_p(self.ibuf.data_ptr() + 4 * i)
 
 
-class PinocchioModel:
-    """GPU-backed replacement of ``sapien.pysapien_pinocchio.PinocchioModel``."""
+SINGLE_INSTANCE_PATHS = ("host", "cuda")
 
-    def __init__(self, urdf, gravity=(0.0, 0.0, -9.81)):
+
+class PinocchioModel:
+    """Replacement of ``sapien.pysapien_pinocchio.PinocchioModel``.
+
+    The ``*_batched`` methods run the CUDA kernels on batches of float64 CUDA tensors. The
+    reference's one-configuration methods run, by default (``single_instance="host"``), the
+    same sweep code compiled for the CPU on the calling thread: one environment is a
+    sequential sweep, which a host core finishes in microseconds while a GPU call pays a
+    launch and a synchronisation around one thread's work. ``single_instance="cuda"`` sends
+    them to the GPU as batches of one instead."""
+
+    def __init__(self, urdf, gravity=(0.0, 0.0, -9.81), single_instance="host"):
         L = N.load()
         g = (ctypes.c_double * 3)(*[float(x) for x in gravity])
         h = ctypes.c_void_p()
         N.check(L.sgdyn_model_from_urdf(urdf.encode(), g, ctypes.byref(h)))
         self._h = h
-        self._joint_order_set = False
-        self._link_order_set = False
-        self._fk_cache = None
-        self._jac_q = None
-        self._device = None
-        self._refresh()
+        self._init_state(False, False, single_instance)
 
-    @classmethod
-    def _from_handle(cls, h, joint_order_set=False, link_order_set=False):
-        """Wrap a model handle created through another C-ABI constructor."""
-        self = cls.__new__(cls)
-        self._h = h
+    def _init_state(self, joint_order_set, link_order_set, single_instance):
         self._joint_order_set = joint_order_set
         self._link_order_set = link_order_set
         self._fk_cache = None
         self._jac_q = None
         self._device = None
+        self.single_instance = single_instance
         self._refresh()
+
+    @classmethod
+    def _from_handle(cls, h, joint_order_set=False, link_order_set=False, single_instance="host"):
+        """Wrap a model handle created through another C-ABI constructor."""
+        self = cls.__new__(cls)
+        self._h = h
+        self._init_state(joint_order_set, link_order_set, single_instance)
         return self
+
+    @property
+    def single_instance(self):
+        """Where the reference's one-configuration methods run: "host" or "cuda"."""
+        return self._single_instance
+
+    @single_instance.setter
+    def single_instance(self, where):
+        if where not in SINGLE_INSTANCE_PATHS:
+            raise ValueError(f"single_instance must be one of {SINGLE_INSTANCE_PATHS}")
+        self._single_instance = where
+
+    def _on_host(self):
+        return self._single_instance == "host"
+
+    def _host_step(self, ops, q, qd=None, qdd=None, tau=None):
+        """One environment through sgdyn_host_step; returns the requested outputs."""
+        nv, nl = self.nv, self._nlinks
+        out = {}
+        if ops & N.OP_FK:
+            out["poses"] = np.empty(7 * max(nl, 1))
+        if ops & N.OP_JACOBIAN:
+            out["J"] = np.empty(6 * nv)
+        if ops & N.OP_MASS_MATRIX:
+            out["M"] = np.empty(nv * nv)
+        if ops & N.OP_INVERSE_DYNAMICS:
+            out["tau"] = np.empty(nv)
+        if ops & N.OP_FORWARD_DYNAMICS:
+            out["qdd"] = np.empty(nv)
+        a = lambda x: x.ctypes.data_as(ctypes.c_void_p) if x is not None else None  # noqa: E731
+        N.check(N.load().sgdyn_host_step(self._h, 1, int(ops), a(q), a(qd), a(qdd), a(tau), a(out.get("poses")),
+                                         a(out.get("J")), a(out.get("M")), a(out.get("tau")), a(out.get("qdd")),
+                                         N.ENV_MAJOR, 1))
+        return out
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -440,7 +484,9 @@ class PinocchioModel:
         retrieve the computed pose for a specific link."""
         self._require_order()
         q = self._vec(qpos, self.nq_ext, "qpos")
-        if self._link_order_set and self._nlinks > 0:
+        if self._link_order_set and self._nlinks > 0 and self._on_host():
+            self._fk_cache = self._host_step(N.OP_FK, q)["poses"].reshape(self._nlinks, 7)
+        elif self._link_order_set and self._nlinks > 0:
             st = self._stage()
             st.put("q", q)
             self._run1(N.load().sgdyn_compute_forward_kinematics, 1, st.p("q"), st.p("poses"), N.ENV_MAJOR)
@@ -472,6 +518,8 @@ class PinocchioModel:
         self._check_link(link_index)
         if self._jac_q is None:
             raise RuntimeError("compute_full_jacobian must be called before get_link_jacobian")
+        if self._on_host():
+            return self._host_link_jacobian(self._jac_q, link_index, local)
         st = self._stage()
         st.put("q", self._jac_q)
         self._run1(N.load().sgdyn_compute_link_jacobian, 1, int(link_index), int(bool(local)), st.p("q"), st.p("J"),
@@ -484,15 +532,26 @@ class PinocchioModel:
         self._require_order()
         self._check_link(link_index)
         q = self._vec(qpos, self.nq_ext, "qpos")
+        if self._on_host():
+            return self._host_link_jacobian(q, link_index, True)
         st = self._stage()
         st.put("q", q)
         self._run1(N.load().sgdyn_compute_single_link_local_jacobian, 1, int(link_index), st.p("q"), st.p("J"),
                    N.ENV_MAJOR)
         return st.get("J").reshape(6, self.nv)
 
+    def _host_link_jacobian(self, q, link_index, local):
+        J = np.empty(6 * self.nv)
+        N.check(N.load().sgdyn_host_compute_link_jacobian(self._h, 1, int(link_index), int(bool(local)),
+                                                          q.ctypes.data_as(ctypes.c_void_p),
+                                                          J.ctypes.data_as(ctypes.c_void_p), N.ENV_MAJOR, 1))
+        return J.reshape(6, self.nv)
+
     def compute_generalized_mass_matrix(self, qpos):
         self._require_order()
         q = self._vec(qpos, self.nq_ext, "qpos")
+        if self._on_host():
+            return self._host_step(N.OP_MASS_MATRIX, q)["M"].reshape(self.nv, self.nv)
         st = self._stage()
         st.put("q", q)
         self._run1(N.load().sgdyn_compute_generalized_mass_matrix, 1, st.p("q"), st.p("M"), N.ENV_MAJOR)
@@ -501,6 +560,12 @@ class PinocchioModel:
     def compute_coriolis_matrix(self, qpos, qvel):
         self._require_order()
         q, qd = self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel")
+        if self._on_host():
+            C = np.empty(self.nv * self.nv)
+            N.check(N.load().sgdyn_host_compute_coriolis_matrix(
+                self._h, 1, q.ctypes.data_as(ctypes.c_void_p), qd.ctypes.data_as(ctypes.c_void_p),
+                C.ctypes.data_as(ctypes.c_void_p), N.ENV_MAJOR, 1))
+            return C.reshape(self.nv, self.nv)
         st = self._stage()
         st.put("q", q)
         st.put("qd", qd)
@@ -511,6 +576,8 @@ class PinocchioModel:
         self._require_order()
         q, qd, qdd = (self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
                       self._vec(qacc, self.nv, "qacc"))
+        if self._on_host():
+            return self._host_step(N.OP_INVERSE_DYNAMICS, q, qd, qdd)["tau"]
         st = self._stage()
         st.put("q", q)
         st.put("qd", qd)
@@ -523,6 +590,8 @@ class PinocchioModel:
         self._require_order()
         q, qd, tau = (self._vec(qpos, self.nq_ext, "qpos"), self._vec(qvel, self.nv, "qvel"),
                       self._vec(qf, self.nv, "qf"))
+        if self._on_host():
+            return self._host_step(N.OP_FORWARD_DYNAMICS, q, qd, tau=tau)["qdd"]
         st = self._stage()
         st.put("q", q)
         st.put("qd", qd)
@@ -558,6 +627,14 @@ class PinocchioModel:
             m = np.asarray(active_qmask, dtype=np.int32).reshape(-1)
             if m.size != self.nv:
                 raise RuntimeError(f"active_qmask must have {self.nv} entries")
+        if self._on_host():
+            tgt = np.concatenate([p, qq])
+            qo, ok, err = np.empty(self.nq_ext), np.zeros(1, dtype=np.int32), np.empty(6)
+            a = lambda x: x.ctypes.data_as(ctypes.c_void_p) if x is not None else None  # noqa: E731
+            N.check(N.load().sgdyn_host_compute_inverse_kinematics(
+                self._h, 1, int(link_index), a(tgt), a(q0v), a(m), float(eps), int(max_iterations), float(dt),
+                float(damp), a(qo), a(ok), a(err), N.ENV_MAJOR, 1))
+            return qo, bool(ok[0]), err
         st = self._stage()
         st.put("target", np.concatenate([p, qq]))
         q0 = None

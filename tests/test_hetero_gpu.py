@@ -191,3 +191,18 @@ def test_fused_rollout_step_equals_step_then_integrate():
             assert torch.equal(qa[idx, : m.nq_ext], qb[idx, : m.nq_ext]), lanes
             assert torch.equal(qda[idx, : m.nv], qdb[idx, : m.nv]), lanes
             assert torch.equal(oa["qacc"][idx, : m.nv], ob["qacc"][idx, : m.nv]), lanes
+
+
+@pytest.mark.parametrize("lanes", [(1, 1, 1), (1, 2, 4), (2, 2, 4)])
+def test_hetero_full_size_mix_matches_oracle(lanes):
+    """The heterogeneous workload at its full size: 8192 robots (50 / 30 / 20 % 6-DoF arms,
+    18-DoF quadrupeds, 35-DoF humanoids), RNEA + ABA + CRBA from a CUDA-graph replay with
+    the lane counts the autotuner picks for this mix, every environment against the oracle."""
+    import torch
+
+    batch, oracles, inputs, (q, qd, qdd, tau) = setup(n=8192, seed=0)
+    batch.set_lanes(list(lanes))
+    g = batch.capture(q, qd, qdd, tau, steps=2)
+    g.replay()
+    torch.cuda.synchronize()
+    check_against_oracle(batch, oracles, inputs, g.outputs)

@@ -141,9 +141,11 @@ def test_single_op_entry_points_match_fused(name):
         assert rel_per_env(a, b) < (1e-11 if k == "qacc" else 1e-13), k
 
 
-def test_drop_in_single_instance_api():
+@pytest.mark.parametrize("where", ["cuda", "host"])
+def test_drop_in_single_instance_api(where):
     robot = syn.arm_with_fingers(sapien_style=True)
     pm, o = pair(robot)
+    pm.single_instance = where
     q, qd, qdd, tau = robot.sample(3, seed=17)
     for e in range(3):
         pm.compute_forward_kinematics(q[e])
@@ -162,7 +164,8 @@ def test_drop_in_single_instance_api():
         assert np.abs(M - o.compute_generalized_mass_matrix(q[e])).max() <= 1e-10 * np.abs(M).max()
 
 
-def test_chain7_single_instance_1000_samples():
+@pytest.mark.parametrize("where", ["cuda", "host"])
+def test_chain7_single_instance_1000_samples(where):
     """The CPU-runnable reference configuration: a seeded 7-DoF revolute chain (offsets
     U[0.05, 0.4] m along random unit axes, random unit joint axes, masses U[0.5, 3] kg,
     inertias R diag(U[1e-3, 5e-2]) R^T) and 1000 samples q ~ U[-pi, pi], qd, qdd ~ N(0, 1),
@@ -171,6 +174,7 @@ def test_chain7_single_instance_1000_samples():
     RNEA and ABA against the oracle."""
     robot = syn.serial_chain(7)
     pm, o = pair(robot)
+    pm.single_instance = where
     n = 1000
     q, qd, qdd, tau = robot.sample(n, seed=0)
     nl = len(robot.link_names)
@@ -413,3 +417,24 @@ def test_cart_pole_closed_form_on_gpu():
         assert np.abs(Cg[e] - C).max() < 1e-13
         assert np.abs(tau[e] - (M @ qdd[e] + C @ qd[e] + gv)).max() < 1e-12
         assert np.abs(back[e] - qdd[e]).max() < 1e-12
+
+
+@pytest.mark.parametrize("name", ["arm9", "humanoid", "quadruped18", "chain40"])
+def test_host_path_matches_device_kernels(name):
+    """The host instantiation of the sweep (sgdyn_host_step, several threads) and the CUDA
+    kernels agree to rounding on the same batch."""
+    import ctypes
+
+    robot = ROBOTS[name]()
+    pm, _ = pair(robot)
+    q, qd, qdd, tau = robot.sample(64, seed=3)
+    g = run_step(pm, q, qd, qdd, tau)
+    n, nv, nl = 64, robot.nv, len(robot.link_names)
+    out = {"link_poses": np.empty((n, nl, 7)), "jacobian": np.empty((n, 6, nv)), "mass_matrix": np.empty((n, nv, nv)),
+           "qf": np.empty((n, nv)), "qacc": np.empty((n, nv))}
+    a = lambda x: x.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    N.check(N.load().sgdyn_host_step(pm._h, n, N.OP_ALL, a(q), a(qd), a(qdd), a(tau), a(out["link_poses"]),
+                                     a(out["jacobian"]), a(out["mass_matrix"]), a(out["qf"]), a(out["qacc"]),
+                                     N.ENV_MAJOR, 4))
+    for k in out:
+        assert rel_per_env(out[k], g[k]) <= (1e-10 if k == "qacc" else 1e-12), k
