@@ -37,11 +37,49 @@ WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs p
 
 # FP64 thread-instructions (DFMA + DMUL + DADD) per environment-step and DRAM bytes per
 # environment of one fused launch (structure-of-arrays buffers), from an ncu capture of the
-# model-specialised kernel (run-time compiled) and of the generic one.
+# model-specialised kernel (run-time compiled) and of the generic one. They hold for the
+# kernel source whose digest is KERNEL_SOURCE_SHA256 (kernel_source_digest()); a CPU test
+# fails when the source changes, so the figures are re-captured with every kernel change.
 KERNEL_COUNTERS = {
     "specialised": {"fp64_inst_per_env": 5100, "dram_bytes_per_env": 34.79e6 / 16384},
     "generic": {"fp64_inst_per_env": 5047, "dram_bytes_per_env": 124.6e6 / 16384},
 }
+KERNEL_SOURCE_SHA256 = "2b0a355c58ee61d895a6bdda7cf14cfbcc8b73803bd4cfbf6609683a2adc77dd"
+KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
+
+
+def kernel_source_digest(model):
+    """SHA-256 of what the fused sweep of `model` is compiled from: the run-time-generated
+    translation unit for all five ops and the device headers it includes."""
+    import hashlib
+
+    from sapien_gb300 import _native as N
+
+    src = ctypes.c_char_p()
+    N.check(N.load().sgdyn_jit_source(model._h, N.OP_ALL, ctypes.byref(src)))
+    h = hashlib.sha256(src.value)
+    for name in KERNEL_HEADERS:
+        with open(os.path.join(ROOT, "sapien_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
+def algorithmic_flops(robot):
+    """FP64 operations per environment of each op, counted by the oracle's counting scalar
+    (local-frame recursions with operations on structural zeros and ones skipped) at one
+    seeded input: {op: flops} for fk, jacobian, crba, rnea, aba, the fused five-op step
+    (the joint-placement pass they share counted once) and rnea+aba; plus the
+    transcendental calls per step."""
+    o = _oracle_of(robot)
+    q, qd, qdd, tau = robot.sample(1, seed=0)
+    c = o.count_ops(q[0], qd[0], qdd[0], tau[0])
+    fl = {k: v["add"] + v["mul"] + v["div"] + v["sqrt"] for k, v in c.items()}
+    ops = ("fk", "jacobian", "crba", "rnea", "aba")
+    out = {k: fl[k] for k in ops}
+    out["step"] = sum(fl[k] for k in ops) - (len(ops) - 1) * fl["placements"]
+    out["rnea+aba"] = fl["rnea"] + fl["aba"] - fl["placements"]
+    out["transcendental_calls_per_step"] = c["placements"]["trig"]
+    return out
 
 
 def parse_args():
@@ -660,13 +698,26 @@ def main():
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": alg}
     dfma = fp64_peak_dfma_per_s()
+    alg = algorithmic_flops(robot)
     roofline_fp64 = None
     if dfma:
-        roofline_fp64 = {"bound": "fp64", "peak": dfma / 1e9, "unit": "G FP64 inst/s (per lane)",
-                         "peak_source": "measured live: DFMA chain microbenchmark (bench_fp64_peak.cu)"}
-        ach = counters["fp64_inst_per_env"] * n / (ms * 1e-3) / 1e9
-        roofline_fp64.update({"achieved": ach, "frac": ach / (dfma / 1e9),
-                              "inst_per_env_step": counters["fp64_inst_per_env"]})
+        peak_gflops = 2 * dfma / 1e9  # one DFMA = 2 flops
+        ach = alg["step"] * n / (ms * 1e-3) / 1e9
+        issued = counters["fp64_inst_per_env"] * n / (ms * 1e-3) / 1e9
+        roofline_fp64 = {
+            "bound": "fp64", "unit": "GFLOP/s", "peak": peak_gflops,
+            "peak_source": "measured live: DFMA chain microbenchmark (bench_fp64_peak.cu), 2 flops per DFMA",
+            "algorithmic_flops_per_env": alg["step"], "achieved": ach, "frac": ach / peak_gflops,
+            "algorithmic_source": "oracle counting scalar: local-frame recursions, operations on structural "
+                                  "zeros and ones skipped; the kernels' world-frame sweep needs fewer",
+            "issued_inst_per_env": counters["fp64_inst_per_env"],
+            "issued_inst_per_s": issued * 1e9, "issued_frac": issued / (dfma / 1e9),
+            "issued_source": "ncu sass FP64 instruction counts of this kernel source "
+                             f"(sha256 {KERNEL_SOURCE_SHA256[:12] or 'unset'}); frac against the DFMA issue peak",
+            "source_matches_counters": kernel_source_digest(pm) == KERNEL_SOURCE_SHA256,
+            "algorithmic_flops_per_op": alg}
+    for name, r in per_op.items():
+        r["algorithmic_gflops"] = alg[name] * n / (r["us"] * 1e-6) / 1e9
 
     # ---- CPU baseline on a bounded sample + parity of that sample --------------------
     from oracle.oracle import Oracle

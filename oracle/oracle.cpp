@@ -38,6 +38,81 @@
 #include <thread>
 #include <vector>
 
+// ---- counting scalar ---------------------------------------------------------------
+// Cnt carries a double and counts the floating-point operations the templated algorithms
+// below perform on it, per thread. Operations whose result needs no arithmetic are not
+// counted: a product with an exact 0, 1 or -1 operand, a sum or difference with an exact 0
+// operand, a division by +-1, a negation. The dense 6x6 Plucker matrices of this oracle
+// hold such structural zeros and ones (the zero block of a motion transform, unit motion
+// subspaces, identity placements), so the counts are those of the same recursions with
+// the structure exploited, i.e. the algorithm's own work rather than this restatement's
+// dense storage. sqrt, divisions and transcendental calls are counted apart.
+namespace orc_count {
+struct Counts {
+  long long add = 0, mul = 0, div = 0, sqrt = 0, trig = 0;
+};
+inline thread_local Counts g_counts;
+struct Cnt {
+  double v = 0;
+  Cnt() = default;
+  Cnt(double x) : v(x) {}
+  explicit operator double() const { return v; }
+  Cnt& operator+=(Cnt b);
+  Cnt& operator-=(Cnt b);
+  Cnt& operator*=(Cnt b);
+  Cnt& operator/=(Cnt b);
+};
+inline bool unit(double x) { return x == 1.0 || x == -1.0; }
+inline Cnt operator+(Cnt a, Cnt b) {
+  if (a.v != 0 && b.v != 0) g_counts.add++;
+  return Cnt(a.v + b.v);
+}
+inline Cnt operator-(Cnt a, Cnt b) {
+  if (a.v != 0 && b.v != 0) g_counts.add++;
+  return Cnt(a.v - b.v);
+}
+inline Cnt operator*(Cnt a, Cnt b) {
+  if (a.v != 0 && b.v != 0 && !unit(a.v) && !unit(b.v)) g_counts.mul++;
+  return Cnt(a.v * b.v);
+}
+inline Cnt operator/(Cnt a, Cnt b) {
+  if (a.v != 0 && !unit(b.v)) g_counts.div++;
+  return Cnt(a.v / b.v);
+}
+inline Cnt operator-(Cnt a) { return Cnt(-a.v); }
+inline Cnt& Cnt::operator+=(Cnt b) { return *this = *this + b; }
+inline Cnt& Cnt::operator-=(Cnt b) { return *this = *this - b; }
+inline Cnt& Cnt::operator*=(Cnt b) { return *this = *this * b; }
+inline Cnt& Cnt::operator/=(Cnt b) { return *this = *this / b; }
+inline bool operator<(Cnt a, Cnt b) { return a.v < b.v; }
+inline bool operator>(Cnt a, Cnt b) { return a.v > b.v; }
+inline bool operator<=(Cnt a, Cnt b) { return a.v <= b.v; }
+inline bool operator>=(Cnt a, Cnt b) { return a.v >= b.v; }
+inline bool operator==(Cnt a, Cnt b) { return a.v == b.v; }
+inline bool operator!=(Cnt a, Cnt b) { return a.v != b.v; }
+}  // namespace orc_count
+
+// math functions on the counting scalar, found by the std:: calls in the templates
+namespace std {
+inline orc_count::Cnt sqrt(orc_count::Cnt x) {
+  orc_count::g_counts.sqrt++;
+  return orc_count::Cnt(std::sqrt(x.v));
+}
+inline orc_count::Cnt sin(orc_count::Cnt x) {
+  orc_count::g_counts.trig++;
+  return orc_count::Cnt(std::sin(x.v));
+}
+inline orc_count::Cnt cos(orc_count::Cnt x) {
+  orc_count::g_counts.trig++;
+  return orc_count::Cnt(std::cos(x.v));
+}
+inline orc_count::Cnt atan2(orc_count::Cnt y, orc_count::Cnt x) {
+  orc_count::g_counts.trig++;
+  return orc_count::Cnt(std::atan2(y.v, x.v));
+}
+inline orc_count::Cnt fabs(orc_count::Cnt x) { return orc_count::Cnt(std::fabs(x.v)); }
+}  // namespace std
+
 namespace {
 
 constexpr int kMaxJ = 96;   // joints incl. universe
@@ -1187,6 +1262,44 @@ void orc_jlog6(const double* M12, double* out36) {
   for (int k = 0; k < 3; k++) M.p[k] = M12[9 + k];
   auto J = jlog6(M);
   for (int k = 0; k < 36; k++) out36[k] = J[k];
+}
+
+// ---- operation counts ----------------------------------------------------------------
+// Runs each of forward kinematics (link poses), the full WORLD Jacobian, CRBA, RNEA and ABA
+// once on the counting scalar and writes, per op, {add, mul, div, sqrt, trig} to
+// counts[op * 5 + k] (op 0..4 in that order); op 5 is the shared joint-placement pass
+// (posS2P + forward kinematics of the joints) that every one of them starts with.
+int orc_count_ops(void* hh, const double* q, const double* qd, const double* qdd, const double* tau,
+                  long long* counts) {
+  using orc_count::Cnt;
+  using orc_count::g_counts;
+  auto& m = static_cast<Handle*>(hh)->m;
+  const int nv = m.nv, nl = int(m.link_joint.size());
+  std::vector<double> poses(size_t(nl) * 12), J(6 * size_t(nv)), M(size_t(nv) * nv), t(nv), a(nv);
+  auto record = [&](int op) {
+    const long long v[5] = {g_counts.add, g_counts.mul, g_counts.div, g_counts.sqrt, g_counts.trig};
+    for (int k = 0; k < 5; k++) counts[op * 5 + k] = v[k];
+    g_counts = orc_count::Counts{};
+  };
+  g_counts = orc_count::Counts{};
+  fk_poses<Cnt>(m, q, poses.data());
+  record(0);
+  jac_full_ext<Cnt>(m, q, J.data());
+  record(1);
+  crba_ext<Cnt>(m, q, M.data());
+  record(2);
+  rnea_ext<Cnt>(m, q, qd, qdd, t.data());
+  record(3);
+  if (aba_ext<Cnt>(m, q, qd, tau, a.data()) != 0) return -3;
+  record(4);
+  {
+    Cnt qi[kMaxV];
+    pos_s2p(m, q, qi);
+    static thread_local Work<Cnt> w;
+    kinematics(m, qi, w);
+  }
+  record(5);
+  return 0;
 }
 
 // ---- batched drivers (per-environment single-instance calls, threads over envs) ----

@@ -56,6 +56,7 @@ def lib():
         L.orc_log6.argtypes = [P(d), P(d)]
         L.orc_exp6.argtypes = [P(d), P(d)]
         L.orc_jlog6.argtypes = [P(d), P(d)]
+        L.orc_count_ops.argtypes = [ctypes.c_void_p, P(d), P(d), P(d), P(d), P(ctypes.c_longlong)]
         L.orc_batch_step.argtypes = [ctypes.c_void_p, ctypes.c_long, i, P(d), P(d), P(d), P(d), P(d), P(d), P(d),
                                      P(d), P(d), i]
         L.orc_batch_ik.argtypes = [ctypes.c_void_p, ctypes.c_long, i, P(d), P(d), d, i, d, d, P(d), P(i), P(d), i]
@@ -281,6 +282,20 @@ class Oracle:
             if v is not None:
                 out[k] = v
         return out
+
+    OPS_COUNTED = ("fk", "jacobian", "crba", "rnea", "aba", "placements")
+
+    def count_ops(self, q, qd, qdd, tau):
+        """Floating-point operations of one evaluation of each op at this input (see
+        orc_count_ops): {op: {"add", "mul", "div", "sqrt", "trig"}} for fk (link poses),
+        jacobian, crba, rnea, aba and placements (the joint-placement pass all of them share)."""
+        c = np.zeros(6 * 5, dtype=np.int64)
+        rc = lib().orc_count_ops(self._h, _dp(_f64(q)), _dp(_f64(qd)), _dp(_f64(qdd)), _dp(_f64(tau)),
+                                 c.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
+        if rc != 0:
+            raise RuntimeError("orc_count_ops failed")
+        keys = ("add", "mul", "div", "sqrt", "trig")
+        return {op: dict(zip(keys, (int(x) for x in c[5 * i:5 * i + 5]))) for i, op in enumerate(self.OPS_COUNTED)}
 
     def batch_ik(self, link, targets, q0=None, eps=1e-4, max_iterations=1000, dt=0.1, damp=1e-6, nthreads=1):
         """targets: [n, 4, 4]. Returns (q [n, nq_ext], success [n], err [n, 6])."""
