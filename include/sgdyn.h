@@ -312,8 +312,9 @@ int sgdyn_compute_aba_derivatives(const sgdyn_model* m, int64_t n, const double*
                                   const double* tau, double* dqdd_dq, double* dqdd_dqd, double* dqdd_dtau,
                                   int layout, void* stream);
 
-/* Semi-implicit Euler rollout of T steps, qd += dt ABA(q, qd, tau_t); q += dt qd, for
- * models without free flyers. Contiguous env-major arrays: q0, qT [n][nq], qd0, qdT
+/* Semi-implicit Euler rollout of T steps, qd += dt ABA(q, qd, tau_t); q <- q (+) dt qd
+ * (angles and slides add; a free-flyer root moves on SE(3) by the body twist dt qd, as
+ * Pinocchio's integrate). Contiguous env-major arrays: q0, qT [n][nq], qd0, qdT
  * [n][nv], tau [T][n][nv]. With q_ckpt [C][n][nq] and qd_ckpt [C][n][nv],
  * C = ceil(T / checkpoint_every), the state at steps 0, K, 2K, ... is recorded for the
  * backward pass (both NULL for a plain forward rollout). */
@@ -326,7 +327,10 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
 int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_every, int64_t* bytes);
 
 /* Reverse pass of sgdyn_rollout_forward: given the adjoints of the final state (either may
- * be NULL = zero) returns q0_bar, qd0_bar and tau_bar [T][n][nv]. Checkpoint segments are
+ * be NULL = zero) returns q0_bar, qd0_bar and tau_bar [T][n][nv]. A free flyer's block of
+ * qT_bar / q0_bar ([n][nq]) holds its tangent adjoint (with respect to a right
+ * perturbation q exp6(eps), eps a body twist) in its first six slots; the seventh is
+ * ignored on input and zero on output. Checkpoint segments are
  * recomputed from their q / qd checkpoints, their spatial intermediates kept in `scratch`
  * (caller-owned device memory of at least sgdyn_rollout_scratch_bytes bytes), and then
  * reversed step by step. A scratch of k times the minimum lets k segments recompute at

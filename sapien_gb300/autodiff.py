@@ -5,15 +5,20 @@
   wrappers whose backward passes call the hand-written adjoint kernels (RNEA adjoint,
   ABA adjoint = M^-1 solve + RNEA adjoint, link-pose adjoint).
 * ``rollout(model, q0, qd0, tau, dt, checkpoint_every)``: a semi-implicit Euler rollout
-  (qd += dt ABA(q, qd, tau_t); q += dt qd) run by one fused kernel that records only q / qd
+  (qd += dt ABA(q, qd, tau_t); q <- q (+) dt qd, a free-flyer root on SE(3)) run by one fused kernel that records only q / qd
   every ``checkpoint_every`` steps; its backward recomputes one segment at a time.
 * ``rnea_derivatives`` / ``aba_derivatives``: dense tangent-space derivative matrices.
 
 The reference has no derivative API (Pinocchio is built without autodiff,
-pinocchio/cmake/pinocchio.cmake:4); these are additions. Gradients with respect to q are
-tangent-space gradients; for models with a free-flyer joint q has 7 coordinates per free
-flyer but its tangent has 6, so the autograd wrappers reject such models (use the dense
-derivative functions, which return tangent-space matrices).
+pinocchio/cmake/pinocchio.cmake:4); these are additions. The kernels return gradients with
+respect to q in the tangent space. For a free-flyer joint (q block x y z qx qy qz qw,
+tangent block = body twist, q exp6(eps)) the autograd wrappers turn them into coordinate
+gradients through the chart eps = (R^T dp, 2 vec(quat^-1 * dquat)): the position gradient
+is R g_lin and the quaternion gradient has no component along the quaternion itself, so it
+gives the exact directional derivative along every perturbation that keeps the quaternion
+unit. Gradients arriving for a free flyer's coordinates are mapped back the other way
+(``coordinate_to_tangent_grad``). The raw ``*_vjp`` functions and the dense derivatives
+stay in the tangent space.
 """
 from __future__ import annotations
 
@@ -40,10 +45,79 @@ def _f64(t, cols, what):
     return t.contiguous()
 
 
-def _require_no_free_flyer(model):
-    if model.nq_ext != model.nv:
-        raise NotImplementedError("autograd through q needs q and its tangent to coincide (no free-flyer joint); "
-                                  "use rnea_derivatives / aba_derivatives for floating-base models")
+# ---- free-flyer coordinates and tangents -------------------------------------------
+def _joint_blocks(model):
+    """(kind, q column, v column) of every joint in external order."""
+    out, qc, vc = [], 0, 0
+    for kind in model._kinds:
+        out.append((kind, qc, vc))
+        ff = kind == 4  # free flyer
+        qc += 7 if ff else 1
+        vc += 6 if ff else 1
+    return out
+
+
+def _ff_frame(q, qc):
+    x, y, z, w = (q[:, qc + 3 + k] for k in range(4))
+    R = _quat_to_R(torch.stack([w, x, y, z], dim=-1))
+    return R, torch.stack([x, y, z], dim=-1), w
+
+
+def tangent_to_coordinate_grad(model, q, g):
+    """[N, nv] tangent-space gradient at q -> [N, nq_ext] coordinate gradient."""
+    if model.nq_ext == model.nv:
+        return g
+    out = torch.zeros(q.shape[0], model.nq_ext, dtype=g.dtype, device=g.device)
+    for kind, qc, vc in _joint_blocks(model):
+        if kind != 4:
+            out[:, qc] = g[:, vc]
+            continue
+        R, v, w = _ff_frame(q, qc)
+        glin, gw = g[:, vc:vc + 3], g[:, vc + 3:vc + 6]
+        out[:, qc:qc + 3] = (R @ glin.unsqueeze(-1)).squeeze(-1)
+        out[:, qc + 3:qc + 6] = 2 * (w.unsqueeze(-1) * gw + torch.cross(v, gw, dim=-1))
+        out[:, qc + 6] = -2 * (v * gw).sum(-1)
+    return out
+
+
+def coordinate_to_tangent_grad(model, q, gc):
+    """[N, nq_ext] gradient with respect to q's coordinates -> [N, nv] tangent gradient (the
+    transpose of the chart's derivative d q exp6(eps) / d eps at eps = 0)."""
+    if model.nq_ext == model.nv:
+        return gc
+    out = torch.zeros(q.shape[0], model.nv, dtype=gc.dtype, device=gc.device)
+    for kind, qc, vc in _joint_blocks(model):
+        if kind != 4:
+            out[:, vc] = gc[:, qc]
+            continue
+        R, v, w = _ff_frame(q, qc)
+        gp, gv, gw = gc[:, qc:qc + 3], gc[:, qc + 3:qc + 6], gc[:, qc + 6]
+        out[:, vc:vc + 3] = (R.transpose(-1, -2) @ gp.unsqueeze(-1)).squeeze(-1)
+        out[:, vc + 3:vc + 6] = 0.5 * (w.unsqueeze(-1) * gv + torch.cross(gv, v, dim=-1) - v * gw.unsqueeze(-1))
+    return out
+
+
+def _tangent_in_q_layout(model, g):
+    """[N, nv] tangent vector -> [N, nq_ext] array laid out as the rollout kernels take a
+    configuration adjoint (a free flyer's six tangent entries in the first six slots of its
+    seven)."""
+    if model.nq_ext == model.nv:
+        return g.contiguous()
+    out = torch.zeros(g.shape[0], model.nq_ext, dtype=g.dtype, device=g.device)
+    for kind, qc, vc in _joint_blocks(model):
+        k = 6 if kind == 4 else 1
+        out[:, qc:qc + k] = g[:, vc:vc + k]
+    return out
+
+
+def _tangent_from_q_layout(model, a):
+    if model.nq_ext == model.nv:
+        return a
+    out = torch.empty(a.shape[0], model.nv, dtype=a.dtype, device=a.device)
+    for kind, qc, vc in _joint_blocks(model):
+        k = 6 if kind == 4 else 1
+        out[:, vc:vc + k] = a[:, qc:qc + k]
+    return out
 
 
 # ---- raw adjoint calls -----------------------------------------------------------
@@ -124,7 +198,7 @@ class _InverseDynamics(torch.autograd.Function):
     def backward(ctx, tau_bar):
         q, qd, qdd = ctx.saved_tensors
         qb, qdb, qddb = inverse_dynamics_vjp(ctx.model, q, qd, qdd, tau_bar.contiguous())
-        return None, qb, qdb, qddb
+        return None, tangent_to_coordinate_grad(ctx.model, q, qb), qdb, qddb
 
 
 class _ForwardDynamics(torch.autograd.Function):
@@ -138,7 +212,7 @@ class _ForwardDynamics(torch.autograd.Function):
     def backward(ctx, qdd_bar):
         q, qd, tau = ctx.saved_tensors
         qb, qdb, tb = forward_dynamics_vjp(ctx.model, q, qd, tau, qdd_bar.contiguous())
-        return None, qb, qdb, tb
+        return None, tangent_to_coordinate_grad(ctx.model, q, qb), qdb, tb
 
 
 def _quat_to_R(qwxyz):
@@ -164,24 +238,21 @@ class _LinkPoses(torch.autograd.Function):
             pos_bar = torch.zeros(q.shape[0], ctx.model.nlinks, 3, dtype=q.dtype, device=q.device)
         qb = forward_kinematics_vjp(ctx.model, q, pos_bar.contiguous(),
                                     rot_bar.contiguous() if rot_bar is not None else None)
-        return None, qb
+        return None, tangent_to_coordinate_grad(ctx.model, q, qb)
 
 
 def inverse_dynamics(model, q, qd, qdd):
-    """Differentiable batched RNEA: [N, nv] tensors -> tau [N, nv]."""
-    _require_no_free_flyer(model)
+    """Differentiable batched RNEA: q [N, nq_ext], qd, qdd [N, nv] -> tau [N, nv]."""
     return _InverseDynamics.apply(model, q, qd, qdd)
 
 
 def forward_dynamics(model, q, qd, tau):
-    """Differentiable batched ABA: [N, nv] tensors -> qdd [N, nv]."""
-    _require_no_free_flyer(model)
+    """Differentiable batched ABA: q [N, nq_ext], qd, tau [N, nv] -> qdd [N, nv]."""
     return _ForwardDynamics.apply(model, q, qd, tau)
 
 
 def link_poses_rt(model, q):
     """Differentiable link poses: (positions [N, L, 3], rotations [N, L, 3, 3])."""
-    _require_no_free_flyer(model)
     return _LinkPoses.apply(model, q)
 
 
@@ -246,17 +317,22 @@ class _Rollout(torch.autograd.Function):
     def forward(ctx, model, q0, qd0, tau, dt, checkpoint_every):
         qT, qdT, qc, qdc = rollout_forward(model, q0, qd0, tau, dt, checkpoint_every)
         ctx.model, ctx.dt, ctx.K = model, dt, checkpoint_every
-        ctx.save_for_backward(qc, qdc, tau)
+        ctx.save_for_backward(qc, qdc, tau, q0, qT)
         return qT, qdT
 
     @staticmethod
     def backward(ctx, qT_bar, qdT_bar):
-        qc, qdc, tau = ctx.saved_tensors
-        q0b, qd0b, taub = rollout_backward(ctx.model, qc, qdc, tau, ctx.dt, ctx.K, qT_bar, qdT_bar)
+        qc, qdc, tau, q0, qT = ctx.saved_tensors
+        m = ctx.model
+        if qT_bar is not None and m.nq_ext != m.nv:  # coordinates -> kernel layout of the tangent
+            qT_bar = _tangent_in_q_layout(m, coordinate_to_tangent_grad(m, qT, qT_bar))
+        q0b, qd0b, taub = rollout_backward(m, qc, qdc, tau, ctx.dt, ctx.K, qT_bar, qdT_bar)
+        if m.nq_ext != m.nv:
+            q0b = tangent_to_coordinate_grad(m, q0, _tangent_from_q_layout(m, q0b))
         return None, q0b, qd0b, taub, None, None
 
 
 def rollout(model, q0, qd0, tau, dt, checkpoint_every=20):
-    """Differentiable rollout: returns (qT, qdT). Gradients flow to q0, qd0 and tau."""
-    _require_no_free_flyer(model)
+    """Differentiable rollout: returns (qT, qdT). Gradients flow to q0, qd0 and tau; for a
+    free-flyer root they are coordinate gradients (module docstring)."""
     return _Rollout.apply(model, q0, qd0, tau, float(dt), int(checkpoint_every))

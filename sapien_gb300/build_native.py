@@ -54,7 +54,8 @@ def _compile(src, hmt, verbose):
     return obj, None
 
 
-JIT_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh", "diff_core.cuh", "diff_kernels.cuh")
+JIT_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "se3.cuh", "step_kernel.cuh", "diff_core.cuh",
+               "diff_kernels.cuh")
 
 
 def _write_jit_headers():

@@ -688,7 +688,6 @@ int sgdyn_compute_aba_derivatives(const sgdyn_model* m, int64_t n, const double*
 
 static int rollout_checks(const sgdyn_model* m, int64_t n, int T, int K) {
   if (int rc = check_diff_model(m)) return rc;
-  if (m->impl->has_free_flyer()) return fail(SGDYN_ERR_UNSUPPORTED, "rollouts do not support free-flyer joints");
   if (n < 0 || T < 0) return fail(SGDYN_ERR_RUNTIME, "negative size");
   if (K <= 0) return fail(SGDYN_ERR_RUNTIME, "checkpoint_every must be positive");
   return SGDYN_OK;

@@ -5,6 +5,7 @@
 // time and keeps that segment's intermediates in caller-provided scratch.
 #pragma once
 #include "diff_core.cuh"
+#include "se3.cuh"
 
 namespace sgdyn {
 
@@ -422,13 +423,21 @@ __global__ void __launch_bounds__(128) aba_deriv_columns_kernel(const DModel* __
 
 // ---- rollouts ---------------------------------------------------------------------
 
-// q <- q + dt qd for angle / slide coordinates (models without free flyers).
+// q <- q (+) dt qd: angle / slide coordinates advance by dt qd, a free flyer (the root
+// joint) moves on SE(3) by the body twist dt qd (Pinocchio's integrate).
 template <class Tab>
 __device__ __forceinline__ void euler_positions(const Tab& T, double* q, const double* qd, double dt) {
 #pragma unroll
   for (int i = 1; i < T.nj(); i++) {
     const DJoint& J = T.joint(i);
-    q[J.qcol] = fma(dt, qd[J.vcol], q[J.qcol]);
+    if (J.kind == JK_FREEFLYER) {
+      double d[6];
+#pragma unroll
+      for (int k = 0; k < 6; k++) d[k] = dt * qd[J.vcol + k];
+      free_flyer_integrate(q + J.qcol, d);
+    } else {
+      q[J.qcol] = fma(dt, qd[J.vcol], q[J.qcol]);
+    }
   }
 }
 
@@ -465,14 +474,15 @@ __global__ void __launch_bounds__(32) rollout_forward_kernel(const DModel* __res
 
 // Per step of a segment the scratch holds, structure-of-arrays over environments:
 // S (6 per velocity), U (6 per velocity), then per joint D^-1 (1), v (6), a (6), I v (6),
-// world inertia (10), subtree force (6); plus the free-flyer factor (21).
+// world inertia (10), subtree force (6); plus the free-flyer factor (21) and the step's
+// free-flyer displacement dt qd' (6, the body twist its integrate applied).
 __host__ __device__ inline int64_t stash_doubles_per_step(int nj, int nq, int nv) {
   (void)nq;
-  return 12 * int64_t(nv) + int64_t(nj) * 35 + 21;
+  return 12 * int64_t(nv) + int64_t(nj) * 35 + 21 + 6;
 }
 
 template <int MAXJ, class Tab>
-__device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, Mot* F, double* base, int64_t n,
+__device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, Mot* F, double* ffd, double* base, int64_t n,
                                          int64_t e, bool store) {
   const int nj = T.nj(), nv = T.nv();
   int64_t f = 0;
@@ -500,6 +510,16 @@ __device__ __forceinline__ void stash_io(const Tab& T, DynWork<MAXJ>& W, Mot* F,
     io6(F[i]);
   }
   for (int k = 0; k < 21; k++) io(W.Lff[k]);
+  for (int k = 0; k < 6; k++) io(ffd[k]);
+}
+
+// The free-flyer joint of a model (0 if none; only the root may be one).
+template <class Tab>
+__device__ __forceinline__ int free_flyer_joint(const Tab& T) {
+#pragma unroll
+  for (int i = 1; i < T.nj(); i++)
+    if (T.joint(i).kind == JK_FREEFLYER) return i;
+  return 0;
 }
 
 // Backward, part 1. Segments are independent given their checkpoints, so one thread per
@@ -517,14 +537,18 @@ __device__ __forceinline__ void rollout_recompute_env(const Tab& T, const Rollou
   for (int c = 0; c < nq; c++) q[c] = a.q_ckpt[(int64_t(s) * n + e) * nq + c];
   for (int c = 0; c < nv; c++) qd[c] = a.qd_ckpt[(int64_t(s) * n + e) * nv + c];
   DynWork<MAXJ> W;
+  const int ff = free_flyer_joint(T);
   const int t0 = s * a.K, t1 = min(a.T, t0 + a.K);
   for (int t = t0; t < t1; t++) {
     double* base = a.scratch + (int64_t(g) * a.K + (t - t0)) * per_step * n;
     for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
     aba_forward<MAXJ>(T, q, qd, tau, qdd, W);
     rnea_subtree_forces<MAXJ>(T, W, W.pA);  // ABA's bias forces are no longer needed
-    stash_io<MAXJ>(T, W, W.pA, base, n, e, true);
     for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
+    double ffd[6] = {0, 0, 0, 0, 0, 0};
+    if (ff > 0)
+      for (int k = 0; k < 6; k++) ffd[k] = a.dt * qd[T.joint(ff).vcol + k];
+    stash_io<MAXJ>(T, W, W.pA, ffd, base, n, e, true);
     euler_positions(T, q, qd, a.dt);
   }
 }
@@ -543,34 +567,51 @@ __device__ __forceinline__ void rollout_reverse_env(const Tab& T, const RolloutA
   const bool last = a.s_lo + a.s_cnt == nseg;
   const double* qin = last ? a.qT_bar : a.q0_bar;
   const double* qdin = last ? a.qdT_bar : a.qd0_bar;
+  // A free flyer's block of qb holds its tangent (body-twist) adjoint in the first six of
+  // its seven slots, as the caller passes and receives it.
   double qb[MAXQ], qdb[MAXV], qddb[MAXV], lam[MAXV], o1[MAXV], o2[MAXV];
   for (int c = 0; c < nq; c++) qb[c] = qin ? qin[e * nq + c] : 0.0;
   for (int c = 0; c < nv; c++) qdb[c] = qdin ? qdin[e * nv + c] : 0.0;
   DynWork<MAXJ> W;
   AdjScratch<MAXJ> A;
+  const int ff = free_flyer_joint(T);
   for (int s = a.s_lo + a.s_cnt - 1; s >= a.s_lo; s--) {
     const int t0 = s * a.K, t1 = min(a.T, t0 + a.K);
-    // q' = q + dt qd' and qd' = qd + dt qdd, reversed
+    // q' = q (+) dt qd' and qd' = qd + dt qdd, reversed
     for (int t = t1 - 1; t >= t0; t--) {
       double* base = a.scratch + (int64_t(s - a.s_lo) * a.K + (t - t0)) * per_step * n;
+      double ffd[6];
+      stash_io<MAXJ>(T, W, A.F, ffd, base, n, e, false);
 #pragma unroll
       for (int i = 1; i < nj; i++) {
         const DJoint& J = T.joint(i);
+        if (J.kind == JK_FREEFLYER) continue;
         qdb[J.vcol] = fma(a.dt, qb[J.qcol], qdb[J.vcol]);
       }
+      if (ff > 0) {
+        const int qc = T.joint(ff).qcol, vc = T.joint(ff).vcol;
+        const Mot g{mk(qb[qc], qb[qc + 1], qb[qc + 2]), mk(qb[qc + 3], qb[qc + 4], qb[qc + 5])};
+        Mot vb{mk(qdb[vc], qdb[vc + 1], qdb[vc + 2]), mk(qdb[vc + 3], qdb[vc + 4], qdb[vc + 5])};
+        const Mot gq = free_flyer_integrate_adjoint(Mot{mk(ffd[0], ffd[1], ffd[2]), mk(ffd[3], ffd[4], ffd[5])}, g,
+                                                    a.dt, vb);
+        qb[qc] = gq.v.x; qb[qc + 1] = gq.v.y; qb[qc + 2] = gq.v.z;
+        qb[qc + 3] = gq.w.x; qb[qc + 4] = gq.w.y; qb[qc + 5] = gq.w.z;
+        qdb[vc] = vb.v.x; qdb[vc + 1] = vb.v.y; qdb[vc + 2] = vb.v.z;
+        qdb[vc + 3] = vb.w.x; qdb[vc + 4] = vb.w.y; qdb[vc + 5] = vb.w.z;
+      }
       for (int c = 0; c < nv; c++) qddb[c] = a.dt * qdb[c];
-      stash_io<MAXJ>(T, W, A.F, base, n, e, false);
       minv_solve<MAXJ>(T, W, qddb, lam);
       for (int c = 0; c < nv; c++) a.tau_bar[(int64_t(t) * n + e) * nv + c] = lam[c];
       rnea_adjoint<MAXJ>(T, W, A, lam, o1, o2, nullptr, -1.0);
 #pragma unroll
       for (int i = 1; i < nj; i++) {
         const DJoint& J = T.joint(i);
-        qb[J.qcol] += o1[J.vcol];
+        for (int k = 0; k < J.nv; k++) qb[J.qcol + k] += o1[J.vcol + k];
       }
       for (int c = 0; c < nv; c++) qdb[c] += o2[c];
     }
   }
+  if (ff > 0) qb[T.joint(ff).qcol + 6] = 0.0;
   for (int c = 0; c < nq; c++) a.q0_bar[e * nq + c] = qb[c];
   for (int c = 0; c < nv; c++) a.qd0_bar[e * nv + c] = qdb[c];
 }

@@ -75,8 +75,9 @@ extern "C" int sgdyn_rollout_backward_noalloc(const sgdyn_model* m, int64_t n, i
     if (!m || !m->impl) return set_last_error(SGDYN_ERR_NULL, "null model");
     Model& Mo = *m->impl;
     if (stash_bucket(Mo.njoints()) == 0) return set_last_error(SGDYN_ERR_UNSUPPORTED, "model has too many joints");
-    if (Mo.has_free_flyer())
-      return set_last_error(SGDYN_ERR_UNSUPPORTED, "rollouts do not support free-flyer joints");
+    for (auto& J : Mo.joints)
+      if (J.kind == JK_FREEFLYER && J.parent != 0)
+        return set_last_error(SGDYN_ERR_UNSUPPORTED, "rollouts need the free-flyer joint at the root");
     if (n < 0 || T < 0) return set_last_error(SGDYN_ERR_RUNTIME, "negative size");
     if (checkpoint_every <= 0) return set_last_error(SGDYN_ERR_RUNTIME, "checkpoint_every must be positive");
     const int64_t need = rollout_scratch_bytes_for(Mo.njoints(), Mo.nq_ext(), Mo.nv(), checkpoint_every, n);

@@ -200,4 +200,40 @@ SG_HD void jlog6_blocks(const Mot& xi, M3& Jinv, M3& TR) {
   TR = mul(mul(Jinv, Q), Jinv);
 }
 
+// Adjoint of the free-flyer integrate q' = q exp6(delta) (right perturbations, body
+// twists): given the adjoint g of q', returns the adjoint of q, Ad(exp6(-delta))^T g, and
+// adds dt J_r(delta)^T g to the adjoint of the velocity that made delta = dt v. Here
+// J_r(delta) = [[J, Q], [0, J]] is the right Jacobian of SE(3), q exp6(delta + eta) ~
+// q exp6(delta) exp6(J_r eta), with J = 1 - f_1mc(t) [phi]x + f_tms(t) [phi]x^2 and Q the
+// block of jlog6_blocks (whose Jinv, -TR are the blocks of J_r^-1), delta = (rho, phi).
+// Ad(R, p)^T (a, b) = (R^T a, R^T (b - p x a)).
+SG_HD Mot free_flyer_integrate_adjoint(const Mot& delta, const Mot& g, double dt, Mot& vbar) {
+  const V3 rho = delta.v, phi = delta.w;
+  const double t2 = dot(phi, phi), t = sqrt(t2), d = dot(phi, rho);
+  const double b1 = se3_f_1mc(t), c1 = se3_f_tms(t);
+  const double a = se3_f_tms(t), b = se3_f_c4(t), c = se3_f_c5(t);
+  const double f[3] = {phi.x, phi.y, phi.z}, r[3] = {rho.x, rho.y, rho.z};
+  const V3 fxr = cross(phi, rho);
+  const double u[3] = {fxr.x, fxr.y, fxr.z};
+  const M3 Kf = skew3(phi), Kr = skew3(rho);
+  M3 J, Q;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double id = i == k ? 1.0 : 0.0;
+      const double ppT = f[i] * f[k] - t2 * id;
+      J.a[i * 3 + k] = id - b1 * Kf.a[i * 3 + k] + c1 * ppT;
+      Q.a[i * 3 + k] = -0.5 * Kr.a[i * 3 + k] + a * (r[i] * f[k] + f[i] * r[k] - 2 * d * id + d * Kf.a[i * 3 + k]) +
+                       b * (f[i] * u[k] - u[i] * f[k] - d * Kf.a[i * 3 + k]) - 2 * c * d * ppT;
+    }
+  // J_r^T g = (J^T g_lin, Q^T g_lin + J^T g_ang)
+  vbar.v = vbar.v + dt * mulT(J, g.v);
+  vbar.w = vbar.w + dt * (mulT(Q, g.v) + mulT(J, g.w));
+  M3 Re;
+  V3 pe;
+  exp6(Mot{-delta.v, -delta.w}, Re, pe);
+  return Mot{mulT(Re, g.v), mulT(Re, g.w - cross(pe, g.v))};
+}
+
 }  // namespace sgdyn

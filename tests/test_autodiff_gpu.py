@@ -293,3 +293,92 @@ def test_rollout_backward_segment_groups_agree(T, K):
             assert torch.equal(a, b)
     if T == 0:
         assert torch.equal(outs[0][0], qTb) and torch.equal(outs[0][1], qdTb)
+
+
+FLOATING = {"quadruped18": lambda: syn.quadruped(), "humanoid": lambda: syn.humanoid()}
+
+
+def _ff_rollout_setup(robot, n, T, seed):
+    pm, o = pair(robot)
+    q0, qd0, _, _ = robot.sample(n, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    tau = rng.normal(scale=5.0, size=(T, n, robot.nv))
+    targets = rng.uniform(-0.5, 0.5, size=(n, 3))
+    return pm, o, q0, qd0, tau, targets
+
+
+@pytest.mark.parametrize("name", list(FLOATING))
+def test_floating_base_rollout_forward_matches_oracle(name):
+    """Free-flyer root: the base moves on SE(3) by the body twist dt qd each step (the
+    oracle's integrate), as in the heterogeneous rollout."""
+    robot = FLOATING[name]()
+    pm, o, q0, qd0, tau, targets = _ff_rollout_setup(robot, 24, 120, 31)
+    qT, qdT, _, _ = ad.rollout_forward(pm, cu(q0), cu(qd0), cu(tau), 1.0 / 500)
+    rq, rqd, _ = o.rollout(q0, qd0, tau, 1.0 / 500, robot.ee_link, targets)
+    assert rel(qT.cpu().numpy(), rq) < 1e-9
+    assert rel(qdT.cpu().numpy(), rqd) < 1e-9
+
+
+def test_floating_base_rollout_gradient_matches_finite_differences():
+    """The quadruped (free-flyer root + 4 legs of 3 joints), 16 environments, T = 200 at
+    dt = 1/500, tau ~ N(0, 5) per step, checkpoints every 20 steps, loss = sum of squared
+    distances of the end-effector link at q_T to seeded targets. The q0 gradient, mapped to
+    the tangent space, against central differences of the oracle's rollout with q0
+    perturbed on the manifold (integrate(q0, +-h e_k)); qd0 directly; tau along random
+    directions."""
+    torch = T()
+    robot = syn.quadruped()
+    n, steps, dt, ee = 16, 200, 1.0 / 500, robot.ee_link
+    pm, o, q0, qd0, tau, targets = _ff_rollout_setup(robot, n, steps, 123)
+    q0t, qd0t, taut = cu(q0).requires_grad_(), cu(qd0).requires_grad_(), cu(tau).requires_grad_()
+    qT, _ = ad.rollout(pm, q0t, qd0t, taut, dt, checkpoint_every=20)
+    loss = ((ad.link_positions(pm, qT)[:, ee] - cu(targets)) ** 2).sum()
+    loss.backward()
+    g_tan = ad.coordinate_to_tangent_grad(pm, cu(q0), q0t.grad).cpu().numpy()
+    g_qd0, g_tau = qd0t.grad.cpu().numpy(), taut.grad.cpu().numpy()
+    # the coordinate gradient is the tangent one pulled back through the chart
+    back = ad.tangent_to_coordinate_grad(pm, cu(q0), cu(g_tan)).cpu().numpy()
+    assert rel(back, q0t.grad.cpu().numpy()) < 1e-12
+
+    def L(q0_, qd0_, tau_):
+        return o.rollout(q0_, qd0_, tau_, dt, ee, targets)[2]
+
+    nv = robot.nv
+    fq, fqd = np.zeros((n, nv)), np.zeros((n, nv))
+    for k in range(nv):
+        d = np.zeros(nv)
+        d[k] = H
+        qp = np.stack([o.integrate(q0[e], d) for e in range(n)])
+        qm = np.stack([o.integrate(q0[e], -d) for e in range(n)])
+        fq[:, k] = (L(qp, qd0, tau) - L(qm, qd0, tau)) / (2 * H)
+        fqd[:, k] = (L(q0, qd0 + d, tau) - L(q0, qd0 - d, tau)) / (2 * H)
+    for env in range(n):
+        assert rel(g_tan[env], fq[env]) < 1e-6, env
+        assert rel(g_qd0[env], fqd[env]) < 1e-6, env
+    rng = np.random.default_rng(9)
+    for _ in range(3):
+        D = rng.normal(size=tau.shape)
+        fd = (L(q0, qd0, tau + H * D) - L(q0, qd0, tau - H * D)) / (2 * H)
+        dd = np.einsum("tek,tek->e", g_tau, D)
+        assert np.abs(dd - fd).max() <= 1e-6 * np.abs(fd).max()
+
+
+def test_floating_base_rollout_backward_matches_single_step_vjps():
+    """One step of the rollout backward equals the chain of the per-step pieces: the ABA
+    adjoint (sgdyn_compute_forward_dynamics_vjp) and the SE(3) integrate adjoint, checked
+    through checkpoint-interval invariance on the 35-DoF humanoid."""
+    torch = T()
+    robot = syn.humanoid()
+    pm, _, q0, qd0, tau, _ = _ff_rollout_setup(robot, 40, 30, 7)
+    dt = 1.0 / 500
+    g = torch.Generator(device="cpu").manual_seed(3)
+    qTb = torch.randn(40, pm.nq_ext, generator=g, dtype=torch.float64).cuda()
+    qdTb = torch.randn(40, pm.nv, generator=g, dtype=torch.float64).cuda()
+    outs = []
+    for K in (1, 7, 30):
+        _, _, qc, qdc = ad.rollout_forward(pm, cu(q0), cu(qd0), cu(tau), dt, K)
+        outs.append(ad.rollout_backward(pm, qc, qdc, cu(tau), dt, K, qTb, qdTb))
+    for o_ in outs[1:]:
+        for a, b in zip(o_, outs[0]):
+            assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-12
+    assert torch.all(outs[0][0][:, 6] == 0)  # the free flyer's seventh slot
