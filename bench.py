@@ -44,20 +44,25 @@ KERNEL_COUNTERS = {
     "specialised": {"fp64_inst_per_env": 5100, "dram_bytes_per_env": 34.79e6 / 16384},
     "generic": {"fp64_inst_per_env": 5047, "dram_bytes_per_env": 124.6e6 / 16384},
 }
-KERNEL_SOURCE_SHA256 = "2b0a355c58ee61d895a6bdda7cf14cfbcc8b73803bd4cfbf6609683a2adc77dd"
+KERNEL_SOURCE_SHA256 = "6a84dc5ec223ecc416fc706737e9a022fdb6a2ace4df9c19a1362e373b3f888d"
 KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
+STEP_OPS = 31 | 256  # the five ops as two kinds of warps (OP_ALL | OP_SPLIT), as sgdyn_step runs N = 16384
 
 
-def kernel_source_digest(model):
-    """SHA-256 of what the fused sweep of `model` is compiled from: the run-time-generated
-    translation unit for all five ops and the device headers it includes."""
+def kernel_source_digest(model, ops=None):
+    """SHA-256 of what the step kernel of `model` is compiled from: the run-time-generated
+    translation unit (its floating-point constants masked: the last bits of the model tables
+    differ between host libms, the instruction stream does not) and the device headers it
+    includes. `ops` defaults to the five-op step as bench.py runs it."""
     import hashlib
+    import re
 
     from sapien_gb300 import _native as N
 
     src = ctypes.c_char_p()
-    N.check(N.load().sgdyn_jit_source(model._h, N.OP_ALL, ctypes.byref(src)))
-    h = hashlib.sha256(src.value)
+    N.check(N.load().sgdyn_jit_source(model._h, STEP_OPS if ops is None else ops, ctypes.byref(src)))
+    text = re.sub(rb"[-+]?(?:(?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)", b"#", src.value)
+    h = hashlib.sha256(text)
     for name in KERNEL_HEADERS:
         with open(os.path.join(ROOT, "sapien_gb300", "csrc", name), "rb") as f:
             h.update(f.read())

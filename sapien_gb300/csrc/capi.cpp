@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <functional>
 #include <map>
 #include <mutex>
@@ -95,12 +96,12 @@ int check_ptrs(std::initializer_list<Req> reqs) {
   return SGDYN_OK;
 }
 
-// Lanes per environment for a single-model sweep: the model's setting, or (0 = automatic)
-// the count with the shortest estimated time when the batch leaves FP64 schedulers idle. A
-// small batch is bound by one warp's sequential sweep, so the estimate is the team plan's
-// critical path (trunk + heaviest lane) times the number of warp rounds the lanes need.
-int choose_lanes(Model& M, int64_t n) {
-  if (M.lanes > 0) return M.lanes;
+// Whether the five-op step runs as two kinds of warps (OP_SPLIT): 0 never, 1 always, 2
+// automatic (the default: when one warp per 32 environments gives fewer than two warps per
+// FP64 scheduler, so the extra FK + Jacobian warps land on idle or lightly loaded ones).
+std::atomic<int> g_split_mode{2};
+
+int device_schedulers() {
   static int schedulers = 0;
   if (schedulers == 0) {
     int dev = 0, sms = 0;
@@ -108,6 +109,22 @@ int choose_lanes(Model& M, int64_t n) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     schedulers = 4 * (sms > 0 ? sms : 1);
   }
+  return schedulers;
+}
+
+bool use_split(int64_t n) {
+  const int mode = g_split_mode.load();
+  if (mode != 2) return mode == 1;
+  return (n + 31) / 32 < 2 * int64_t(device_schedulers());
+}
+
+// Lanes per environment for a single-model sweep: the model's setting, or (0 = automatic)
+// the count with the shortest estimated time when the batch leaves FP64 schedulers idle. A
+// small batch is bound by one warp's sequential sweep, so the estimate is the team plan's
+// critical path (trunk + heaviest lane) times the number of warp rounds the lanes need.
+int choose_lanes(Model& M, int64_t n) {
+  if (M.lanes > 0) return M.lanes;
+  const int schedulers = device_schedulers();
   if ((n + 31) / 32 * 2 > schedulers) return 1;  // the batch alone fills the GPU
   int best = 1;
   double best_est = 0;
@@ -177,6 +194,12 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
   if (lanes > 1) {
     team = Mo.device_team(lanes, &err);
     if (!team) return fail(SGDYN_ERR_CUDA, "team table upload failed");
+  } else if (ops == OP_ALL && use_split(n)) {
+    std::string why;
+    if (launch_step_jit(Mo, OP_ALL | OP_SPLIT, a, s, &why)) return SGDYN_OK;
+    cudaError_t e = launch_step_split(dm, Mo.njoints(), a, s);
+    if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+    return SGDYN_OK;
   }
   for (int o : launches) {
     if (team) {  // several lanes per environment
@@ -379,7 +402,16 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
 
 // ops > 0: the fused sweep with that op set; -1: the forward rollout kernel; -2 / -3: the
 // RNEA / ABA vector-Jacobian product kernels
-static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -3 && ops <= -1); }
+static bool jit_kind_ok(int ops) {
+  return (ops > 0 && ops <= OP_ALL) || ops == (OP_ALL | OP_SPLIT) || (ops >= -3 && ops <= -1);
+}
+
+int sgdyn_step_split(int mode, int* mode_out) {
+  if (mode != -1 && (mode < 0 || mode > 2)) return fail(SGDYN_ERR_RUNTIME, "split mode must be -1, 0, 1 or 2");
+  if (mode >= 0) g_split_mode.store(mode);
+  if (mode_out) *mode_out = g_split_mode.load();
+  return SGDYN_OK;
+}
 
 int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
   if (!m) return fail(SGDYN_ERR_NULL, "null model");

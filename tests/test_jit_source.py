@@ -1,5 +1,6 @@
 """The run-time-specialised kernels' generated source compiles with NVRTC for sm_103a (CPU
-test: NVRTC needs no GPU). ``ops`` > 0 selects the fused sweep with that op set, -1 the forward
+test: NVRTC needs no GPU). ``ops`` > 0 selects the fused sweep with that op set (31 | 256: the
+five-op step as two kinds of warps), -1 the forward
 rollout kernel, -2 / -3 the RNEA / ABA vector-Jacobian product kernels. GPU parity of the specialised kernels is in
 test_jit_gpu.py."""
 import ctypes
@@ -28,10 +29,10 @@ def _headers():
     return [h.encode() for h in JIT_HEADERS], [open(os.path.join(CSRC, h)).read().encode() for h in JIT_HEADERS]
 
 
-@pytest.mark.parametrize("name,ops", [("arm9", 31), ("humanoid", 28), ("mixed", 8), ("arm9", -1), ("mixed", -1),
-                                      ("arm9", -2), ("humanoid", -3)])
+@pytest.mark.parametrize("name,ops", [("arm9", 31), ("arm9", 31 | 256), ("humanoid", 28), ("mixed", 8), ("arm9", -1),
+                                      ("mixed", -1), ("quadruped", -1), ("arm9", -2), ("humanoid", -3)])
 def test_generated_source_compiles(name, ops):
-    robot = {"arm9": syn.arm_with_fingers(), "humanoid": syn.humanoid(),
+    robot = {"arm9": syn.arm_with_fingers(), "humanoid": syn.humanoid(), "quadruped": syn.quadruped(),
              "mixed": syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
                                                           "continuous", "prismatic"])}[name]
     pm = PinocchioModel(robot.urdf, [0, 0, -9.81])

@@ -438,3 +438,38 @@ def test_host_path_matches_device_kernels(name):
                                      N.ENV_MAJOR, 4))
     for k in out:
         assert rel_per_env(out[k], g[k]) <= (1e-10 if k == "qacc" else 1e-12), k
+
+
+@pytest.mark.parametrize("name", ["arm9", "humanoid", "chain40"])
+def test_step_as_two_kinds_of_warps_matches_single_kind(name):
+    """sgdyn_step for all five ops as one kind of warp (split mode 0) and as CRBA + RNEA +
+    ABA warps beside FK + Jacobian warps (mode 1), generic and run-time-compiled kernels:
+    equal to rounding, and both equal to the oracle."""
+    import ctypes
+
+    robot = ROBOTS[name]()
+    pm, o = pair(robot)
+    L = N.load()
+    old = ctypes.c_int()
+    assert L.sgdyn_step_split(-1, ctypes.byref(old)) == N.OK and old.value == 2
+    q, qd, qdd, tau = robot.sample(200, seed=12)
+    r = o.batch_step(q, qd, qdd, tau, nthreads=8)
+    want = {"link_poses": oracle_pose7(r["poses"]), "jacobian": r["J"], "mass_matrix": r["M"], "qf": r["tau"],
+            "qacc": r["qdd"]}
+    outs = {}
+    old_jit, old_min = ctypes.c_int(), ctypes.c_int64()
+    L.sgdyn_jit_config(-1, -1, ctypes.byref(old_jit), ctypes.byref(old_min))
+    try:
+        for jit in (0, 1):
+            L.sgdyn_jit_config(jit, 0, None, None)
+            for mode in (0, 1):
+                assert L.sgdyn_step_split(mode, None) == N.OK
+                outs[(jit, mode)] = run_step(pm, q, qd, qdd, tau)
+    finally:
+        L.sgdyn_step_split(2, None)
+        L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
+    for key, g in outs.items():
+        for k, w in want.items():
+            tol = 1e-8 if k == "qacc" else 1e-10
+            assert rel_per_env(g[k], w) <= tol, (key, k)
+            assert rel_per_env(g[k], outs[(0, 0)][k]) <= (1e-11 if k == "qacc" else 1e-13), (key, k)
