@@ -36,33 +36,35 @@ WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs p
             "FK (all link poses) + WORLD Jacobian + CRBA + RNEA + ABA per env per step")
 
 # FP64 thread-instructions (DFMA + DMUL + DADD) per environment-step and DRAM bytes per
-# environment of one fused launch (structure-of-arrays buffers), from an ncu capture of the
-# model-specialised kernel (run-time compiled) and of the generic one. They hold for the
+# environment of one step (structure-of-arrays buffers; both launches when the step is split),
+# from an ncu capture of the model-specialised kernels (run-time compiled) and of the generic
+# ones. They hold for the
 # kernel source whose digest is KERNEL_SOURCE_SHA256 (kernel_source_digest()); a CPU test
 # fails when the source changes, so the figures are re-captured with every kernel change.
 KERNEL_COUNTERS = {
     "specialised": {"fp64_inst_per_env": 5100, "dram_bytes_per_env": 34.79e6 / 16384},
     "generic": {"fp64_inst_per_env": 5047, "dram_bytes_per_env": 124.6e6 / 16384},
 }
-KERNEL_SOURCE_SHA256 = "6a84dc5ec223ecc416fc706737e9a022fdb6a2ace4df9c19a1362e373b3f888d"
+KERNEL_SOURCE_SHA256 = "725fd200f86301984b421a4fb9edf120c31d40dbbbc9710fadfa166c63b95e14"
 KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
-STEP_OPS = 31 | 256  # the five ops as two kinds of warps (OP_ALL | OP_SPLIT), as sgdyn_step runs N = 16384
+STEP_OPS = (3, 28)  # sgdyn_step at N = 16384: FK + Jacobian beside CRBA + RNEA + ABA, two launches
 
 
 def kernel_source_digest(model, ops=None):
-    """SHA-256 of what the step kernel of `model` is compiled from: the run-time-generated
-    translation unit (its floating-point constants masked: the last bits of the model tables
-    differ between host libms, the instruction stream does not) and the device headers it
-    includes. `ops` defaults to the five-op step as bench.py runs it."""
+    """SHA-256 of what the step kernels of `model` are compiled from: the run-time-generated
+    translation units (their floating-point constants masked: the last bits of the model
+    tables differ between host libms, the instruction stream does not) and the device headers
+    they include. `ops` defaults to the two launches of the five-op step as bench.py runs it."""
     import hashlib
     import re
 
     from sapien_gb300 import _native as N
 
-    src = ctypes.c_char_p()
-    N.check(N.load().sgdyn_jit_source(model._h, STEP_OPS if ops is None else ops, ctypes.byref(src)))
-    text = re.sub(rb"[-+]?(?:(?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)", b"#", src.value)
-    h = hashlib.sha256(text)
+    h = hashlib.sha256()
+    for o in (STEP_OPS if ops is None else (ops,)):
+        src = ctypes.c_char_p()
+        N.check(N.load().sgdyn_jit_source(model._h, o, ctypes.byref(src)))
+        h.update(re.sub(rb"[-+]?(?:(?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)", b"#", src.value))
     for name in KERNEL_HEADERS:
         with open(os.path.join(ROOT, "sapien_gb300", "csrc", name), "rb") as f:
             h.update(f.read())
@@ -595,6 +597,14 @@ def main():
             raise RuntimeError(N.last_error())
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    # sgdyn_step runs the five ops as two concurrent launches (FK + Jacobian beside CRBA +
+    # RNEA + ABA) while one warp per 32 environments gives fewer than two warps per FP64
+    # scheduler (split mode 2, the default)
+    mode = ctypes.c_int()
+    N.check(L.sgdyn_step_split(-1, ctypes.byref(mode)))
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    split = mode.value == 1 or (mode.value == 2 and (n + 31) // 32 < 2 * 4 * sms)
+    launches_per_step = 2 if split else 1
 
     # ---- kernel-only timing, inputs resident in HBM ---------------------------------
     for _ in range(args.warmup):
@@ -756,7 +766,10 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(n, nv, nl),
-        "execution": {"parallelism": f"data-parallel replicas over environments x{world}", "kernel": kernel},
+        "execution": {"parallelism": f"data-parallel replicas over environments x{world}", "kernel": kernel,
+                      "launches_per_step": launches_per_step,
+                      "step": "FK+Jacobian and CRBA+RNEA+ABA as two concurrent launches" if split
+                      else "one fused launch"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e,
                 "transfer": "sgdyn_step on mapped pinned host buffers (SoA): the kernel reads inputs from and "
@@ -765,7 +778,7 @@ def main():
                 "staged_copies": {"value": aggregate_throughput(n, world, ms_e2e_staged * 1e-3),
                                   "ms_per_step": ms_e2e_staged,
                                   "transfer": "cudaMemcpyAsync host->device, kernel, device->host on one stream"}},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * launches_per_step,
         "roofline": roofline,
         "roofline_fp64": roofline_fp64,
         "cpu_baseline": {"value": S / cpu_dt, "unit": UNIT, "cores": cores, "kind": "port",

@@ -167,12 +167,14 @@ int sgdyn_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const 
                const double* tau, double* link_poses, double* J, double* M, double* tau_out, double* qdd_out,
                int layout, void* stream);
 
-/* How sgdyn_step (and the single-op entry points) run a request for all five ops:
- * 0 as one kind of warp (each thread computes all five ops for one environment), 1 as one
- * launch with two kinds of warps over the same environments (CRBA + RNEA + ABA warps, and
- * FK + Jacobian warps that repeat the joint placements but fill FP64 schedulers the others
- * leave idle), 2 automatic (the default: two kinds while the batch gives fewer than two warps
- * per FP64 scheduler), -1 only reads the mode. Results agree to rounding. (Addition.) */
+/* How sgdyn_step runs a request for all five ops: 0 as one launch (each thread computes
+ * all five ops for one environment), 1 as two concurrent launches over the same
+ * environments (CRBA + RNEA + ABA on `stream`, FK + Jacobian on an internal second stream of
+ * the device, ordered after the work already on `stream` and before what follows there; the
+ * FK + Jacobian warps repeat the joint placements but fill FP64 schedulers the others leave
+ * idle), 2 automatic (the default: two launches while the batch gives fewer than two warps
+ * per FP64 scheduler and `stream` is not being captured), -1 only reads the mode. Results
+ * agree to rounding. (Addition.) */
 int sgdyn_step_split(int mode, int* mode_out);
 
 /* Lanes per environment for the single-model fused sweep and single-op entry points

@@ -96,9 +96,28 @@ int check_ptrs(std::initializer_list<Req> reqs) {
   return SGDYN_OK;
 }
 
-// Whether the five-op step runs as two kinds of warps (OP_SPLIT): 0 never, 1 always, 2
+// A second stream per device (created once, kept for the process) for work that runs beside
+// the caller's stream: the rollout backward's recompute launches and the FK + Jacobian half
+// of a split five-op step; null if it cannot be created.
+cudaStream_t side_stream() {
+  static std::mutex mu;
+  static std::map<int, cudaStream_t> streams;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) s = nullptr;
+  streams[dev] = s;
+  return s;
+}
+
+// Whether the five-op step runs as two concurrent launches (CRBA + RNEA + ABA on the caller's
+// stream, FK + Jacobian on the side stream, joined by events): 0 never, 1 always, 2
 // automatic (the default: when one warp per 32 environments gives fewer than two warps per
-// FP64 scheduler, so the extra FK + Jacobian warps land on idle or lightly loaded ones).
+// FP64 scheduler, so the FK + Jacobian warps land on idle or lightly loaded schedulers).
+// Never while the caller's stream is being captured.
 std::atomic<int> g_split_mode{2};
 
 int device_schedulers() {
@@ -195,11 +214,29 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
     team = Mo.device_team(lanes, &err);
     if (!team) return fail(SGDYN_ERR_CUDA, "team table upload failed");
   } else if (ops == OP_ALL && use_split(n)) {
-    std::string why;
-    if (launch_step_jit(Mo, OP_ALL | OP_SPLIT, a, s, &why)) return SGDYN_OK;
-    cudaError_t e = launch_step_split(dm, Mo.njoints(), a, s);
-    if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
-    return SGDYN_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusActive;
+    cudaStream_t s2 = cs == cudaStreamCaptureStatusNone ? side_stream() : nullptr;
+    if (s2) {
+      auto one = [&](int o, cudaStream_t st) -> cudaError_t {
+        std::string why;
+        if (launch_step_jit(Mo, o, a, st, &why)) return cudaSuccess;
+        return launch_step(dm, Mo.njoints(), o, a, st);
+      };
+      cudaEvent_t fork = nullptr, join = nullptr;
+      cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(fork, s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
+      if (e == cudaSuccess) e = one(OP_SPLIT_B, s);
+      if (e == cudaSuccess) e = one(OP_SPLIT_A, s2);
+      if (e == cudaSuccess) e = cudaEventRecord(join, s2);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+      if (fork) cudaEventDestroy(fork);  // released once the recorded work completes
+      if (join) cudaEventDestroy(join);
+      if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+      return SGDYN_OK;
+    }
   }
   for (int o : launches) {
     if (team) {  // several lanes per environment
@@ -402,9 +439,7 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
 
 // ops > 0: the fused sweep with that op set; -1: the forward rollout kernel; -2 / -3: the
 // RNEA / ABA vector-Jacobian product kernels
-static bool jit_kind_ok(int ops) {
-  return (ops > 0 && ops <= OP_ALL) || ops == (OP_ALL | OP_SPLIT) || (ops >= -3 && ops <= -1);
-}
+static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -3 && ops <= -1); }
 
 int sgdyn_step_split(int mode, int* mode_out) {
   if (mode != -1 && (mode < 0 || mode > 2)) return fail(SGDYN_ERR_RUNTIME, "split mode must be -1, 0, 1 or 2");
@@ -768,22 +803,6 @@ int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_
 }  // extern "C"
 
 namespace {
-
-// A second stream per device for the rollout backward's recompute launches (created once,
-// kept for the process); null if it cannot be created.
-cudaStream_t side_stream() {
-  static std::mutex mu;
-  static std::map<int, cudaStream_t> streams;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = streams.find(dev);
-  if (it != streams.end()) return it->second;
-  cudaStream_t s = nullptr;
-  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) s = nullptr;
-  streams[dev] = s;
-  return s;
-}
 
 // Rollout backward with the recompute of the next (earlier) group of segments running on a
 // second stream while the current group's reverse sweep runs on the caller's stream. The

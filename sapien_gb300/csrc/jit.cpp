@@ -174,14 +174,6 @@ std::string generate_source(const Model& M, int kind, int ops) {
                           std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM>()";
   const char* args = kind == JIT_STEP ? "sgdyn::StepArgs" : kind == JIT_ROLLOUT_FWD ? "sgdyn::RolloutArgs" : "sgdyn::VjpArgs";
   o << "extern \"C\" __global__ void __launch_bounds__(32) " << kernel_name(kind) << "(const " << args << " a) {\n";
-  if (kind == JIT_STEP && (ops & OP_SPLIT)) {  // two kinds of warps, as step_split_kernel
-    o << "  const long long nb = (a.n + 31) / 32, b = blockIdx.x;\n"
-      << "  const long long e = (b < nb ? b : b - nb) * 32 + threadIdx.x;\n"
-      << "  if (e >= a.n) return;\n"
-      << "  if (b < nb) sgdyn::step_env_t<" << nj << ", " << int(OP_SPLIT_B) << ">(" << tab << ", a, e);\n"
-      << "  else sgdyn::step_env_t<" << nj << ", " << int(OP_SPLIT_A) << ">(" << tab << ", a, e);\n}\n";
-    return o.str();
-  }
   o << "  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
     << "  if (e >= a.n) return;\n";
   if (kind == JIT_STEP) o << "  sgdyn::step_env_t<" << nj << ", " << ops << ">(" << tab << ", a, e);\n}\n";
@@ -381,7 +373,7 @@ bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std:
   if (!fn) return false;
   Args args = a;
   void* params[] = {&args};
-  const unsigned blocks = unsigned((kind == JIT_STEP && (ops & OP_SPLIT) ? 2 : 1) * ((a.n + 31) / 32));
+  const unsigned blocks = unsigned((a.n + 31) / 32);
   if (api().launchKernel(fn, blocks, 1, 1, 32, 1, 1, 0, reinterpret_cast<CUstream>(s), params, nullptr) !=
       CUDA_SUCCESS) {
     *why = "cuLaunchKernel failed";

@@ -18,11 +18,9 @@ struct Arr {
 };
 
 enum Ops : int { OP_FK = 1, OP_JAC = 2, OP_CRBA = 4, OP_RNEA = 8, OP_ABA = 16, OP_ALL = 31 };
-// The five-op step in one launch with two kinds of warps: blocks [0, nb) run CRBA + RNEA +
-// ABA, blocks [nb, 2 nb) run FK + Jacobian for the same environments (nb = ceil(n / 32)).
-// The short FK + Jacobian warps fill FP64 schedulers the long ones leave idle. OP_SPLIT
-// marks the op set of that launch (OP_ALL | OP_SPLIT) for the run-time compiler.
-enum SplitOps : int { OP_SPLIT = 256, OP_SPLIT_A = OP_FK | OP_JAC, OP_SPLIT_B = OP_CRBA | OP_RNEA | OP_ABA };
+// The five-op step split in two concurrent launches over the same environments: CRBA + RNEA +
+// ABA, and FK + Jacobian, whose short warps fill FP64 schedulers the long ones leave idle.
+enum SplitOps : int { OP_SPLIT_A = OP_FK | OP_JAC, OP_SPLIT_B = OP_CRBA | OP_RNEA | OP_ABA };
 
 struct StepArgs {
   int64_t n;
@@ -106,8 +104,6 @@ int stash_bucket(int nj);
 
 // Fused world-frame sweep: any subset of {FK poses, full WORLD Jacobian, CRBA, RNEA, ABA}.
 cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cudaStream_t s);
-// The five-op step as two kinds of warps (OP_SPLIT), one launch of 2 ceil(n / 32) blocks.
-cudaError_t launch_step_split(const DModel* dm, int nj, const StepArgs& a, cudaStream_t s);
 // The same sweep with `lanes` lanes per environment (team table `team` on the device).
 cudaError_t launch_step_team(const DModel* dm, int nj, const int* team, int lanes, int ops, const StepArgs& a,
                              cudaStream_t s);

@@ -6,9 +6,6 @@ namespace sgdyn {
 cudaError_t launch_step_j16(const DModel*, int, const StepArgs&, cudaStream_t);
 cudaError_t launch_step_j32(const DModel*, int, const StepArgs&, cudaStream_t);
 cudaError_t launch_step_j64(const DModel*, int, const StepArgs&, cudaStream_t);
-cudaError_t launch_step_split_j16(const DModel*, const StepArgs&, cudaStream_t);
-cudaError_t launch_step_split_j32(const DModel*, const StepArgs&, cudaStream_t);
-cudaError_t launch_step_split_j64(const DModel*, const StepArgs&, cudaStream_t);
 cudaError_t launch_step_team_j16(const DModel*, const int*, int, int, const StepArgs&, cudaStream_t);
 cudaError_t launch_step_team_j32(const DModel*, const int*, int, int, const StepArgs&, cudaStream_t);
 cudaError_t launch_step_team_j64(const DModel*, const int*, int, int, const StepArgs&, cudaStream_t);
@@ -25,16 +22,6 @@ cudaError_t launch_step_team(const DModel* dm, int nj, const int* team, int lane
 }
 
 int stash_bucket(int nj) { return nj <= 16 ? 16 : nj <= 32 ? 32 : nj <= 64 ? 64 : 0; }
-
-cudaError_t launch_step_split(const DModel* dm, int nj, const StepArgs& a, cudaStream_t s) {
-  if (a.n <= 0) return cudaSuccess;
-  switch (stash_bucket(nj)) {
-    case 16: return launch_step_split_j16(dm, a, s);
-    case 32: return launch_step_split_j32(dm, a, s);
-    case 64: return launch_step_split_j64(dm, a, s);
-    default: return cudaErrorInvalidValue;
-  }
-}
 
 cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cudaStream_t s) {
   if (a.n <= 0) return cudaSuccess;

@@ -23,12 +23,6 @@ cudaError_t launch_step_j16(const DModel* dm, int ops, const StepArgs& a, cudaSt
   return cudaGetLastError();
 }
 
-cudaError_t launch_step_split_j16(const DModel* dm, const StepArgs& a, cudaStream_t s) {
-  const unsigned blocks = unsigned(2 * ((a.n + 31) / 32));
-  step_split_kernel<16><<<blocks, 32, 0, s>>>(dm, a);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_step_team_j16(const DModel* dm, const int* team, int lanes, int ops, const StepArgs& a,
                                   cudaStream_t s) {
   const int per = 32 / lanes;

@@ -647,19 +647,6 @@ __global__ void __launch_bounds__(32) step_kernel(const DModel* __restrict__ mod
   step_env<MAXJ, OPS>(model, args, e);
 }
 
-// The five-op step as two kinds of warps in one launch (OP_SPLIT): the first ceil(n / 32)
-// blocks run CRBA + RNEA + ABA, the next as many FK + Jacobian, for the same environments.
-// Both repeat the joint placements; in exchange a batch that leaves FP64 schedulers idle
-// gets twice the warps, and the short FK + Jacobian warps fill the idle schedulers.
-template <int MAXJ>
-__global__ void __launch_bounds__(32) step_split_kernel(const DModel* __restrict__ model, const StepArgs args) {
-  const int64_t nb = (args.n + 31) / 32, b = blockIdx.x;
-  const int64_t e = (b < nb ? b : b - nb) * 32 + threadIdx.x;
-  if (e >= args.n) return;
-  if (b < nb) step_env<MAXJ, OP_SPLIT_B>(model, args, e);
-  else step_env<MAXJ, OP_SPLIT_A>(model, args, e);
-}
-
 // L lanes per environment: one warp holds 32 / L environments. Every lane takes part in the
 // team sums; lanes past the end repeat the last environment and store nothing.
 template <int MAXJ, int OPS>
