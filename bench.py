@@ -45,7 +45,7 @@ KERNEL_COUNTERS = {
     "specialised": {"fp64_inst_per_env": 5100, "dram_bytes_per_env": 34.79e6 / 16384},
     "generic": {"fp64_inst_per_env": 5047, "dram_bytes_per_env": 124.6e6 / 16384},
 }
-KERNEL_SOURCE_SHA256 = "725fd200f86301984b421a4fb9edf120c31d40dbbbc9710fadfa166c63b95e14"
+KERNEL_SOURCE_SHA256 = "f7813092802a51d2971fcaa6d8d9fe70494316f7223dcd1483c7ac5cec3e43f2"
 KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
 STEP_OPS = (3, 28)  # sgdyn_step at N = 16384: FK + Jacobian beside CRBA + RNEA + ABA, two launches
 

@@ -332,6 +332,14 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
                           const double* tau, int checkpoint_every, double* q_ckpt, double* qd_ckpt, double* qT,
                           double* qdT, void* stream);
 
+/* Lanes per environment of sgdyn_rollout_forward (addition): 0 automatic (the default:
+ * three lanes while one warp per ten environments leaves no FP64 scheduler with two warps),
+ * 1, or 3 (one lane per Cartesian axis of every spatial quantity, warp shuffles between
+ * them, so each lane issues about half the FP64 instructions of one lane per environment;
+ * one-DoF joints only, a model with a free flyer keeps one lane); -1 only reads the
+ * setting. Results agree to rounding. */
+int sgdyn_rollout_lanes(int lanes, int* lanes_out);
+
 /* Bytes of device scratch sgdyn_rollout_backward needs for n environments: the
  * intermediates of one checkpoint segment. */
 int sgdyn_rollout_scratch_bytes(const sgdyn_model* m, int64_t n, int checkpoint_every, int64_t* bytes);

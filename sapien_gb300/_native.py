@@ -79,6 +79,7 @@ EXPORTED = (
     "sgdyn_model_from_articulation",
     "sgdyn_compute_passive_force_f32",
     "sgdyn_step_split",
+    "sgdyn_rollout_lanes",
     "sgdyn_host_step",
     "sgdyn_host_compute_link_jacobian",
     "sgdyn_host_compute_coriolis_matrix",
@@ -131,6 +132,7 @@ def load():
     L.sgdyn_step.argtypes = [vp, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp]
     L.sgdyn_compute_inverse_kinematics.argtypes = [vp, i64, i32, vp, vp, vp, dbl, i32, dbl, dbl, vp, vp, vp, i32, vp]
     L.sgdyn_step_split.argtypes = [i32, P(i32)]
+    L.sgdyn_rollout_lanes.argtypes = [i32, P(i32)]
     L.sgdyn_host_step.argtypes = [vp, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, i32]
     L.sgdyn_host_compute_link_jacobian.argtypes = [vp, i64, i32, i32, vp, vp, i32, i32]
     L.sgdyn_host_compute_coriolis_matrix.argtypes = [vp, i64, vp, vp, vp, i32, i32]

@@ -55,7 +55,7 @@ def _compile(src, hmt, verbose):
 
 
 JIT_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "se3.cuh", "step_kernel.cuh", "diff_core.cuh",
-               "diff_kernels.cuh")
+               "diff_kernels.cuh", "team3.cuh")
 
 
 def _write_jit_headers():

@@ -131,6 +131,19 @@ int device_schedulers() {
   return schedulers;
 }
 
+// Lanes per environment of the forward rollout: 1, or 3 (team3.cuh: one lane per axis,
+// one-DoF joints only). The setting: 0 automatic (the default: three lanes while one warp
+// per ten environments leaves no FP64 scheduler with two warps), 1 or 3.
+std::atomic<int> g_rollout_lanes{0};
+
+int rollout_lanes(const Model& M, int64_t n) {
+  for (auto& J : M.joints)
+    if (J.kind == JK_FREEFLYER) return 1;
+  const int mode = g_rollout_lanes.load();
+  if (mode != 0) return mode;
+  return (n + 9) / 10 <= int64_t(device_schedulers()) ? 3 : 1;
+}
+
 bool use_split(int64_t n) {
   const int mode = g_split_mode.load();
   if (mode != 2) return mode == 1;
@@ -438,8 +451,17 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
 }
 
 // ops > 0: the fused sweep with that op set; -1: the forward rollout kernel; -2 / -3: the
-// RNEA / ABA vector-Jacobian product kernels
-static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -3 && ops <= -1); }
+// RNEA / ABA vector-Jacobian product kernels; -4: the forward rollout with three lanes per
+// environment
+static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -4 && ops <= -1); }
+
+int sgdyn_rollout_lanes(int lanes, int* lanes_out) {
+  if (lanes != -1 && lanes != 0 && lanes != 1 && lanes != 3)
+    return fail(SGDYN_ERR_RUNTIME, "rollout lanes must be -1, 0 (automatic), 1 or 3");
+  if (lanes >= 0) g_rollout_lanes.store(lanes);
+  if (lanes_out) *lanes_out = g_rollout_lanes.load();
+  return SGDYN_OK;
+}
 
 int sgdyn_step_split(int mode, int* mode_out) {
   if (mode != -1 && (mode < 0 || mode > 2)) return fail(SGDYN_ERR_RUNTIME, "split mode must be -1, 0, 1 or 2");
@@ -454,6 +476,7 @@ int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
   std::string why;
   const bool ok = ops > 0     ? prepare_step_jit(*m->impl, ops, &why)
                   : ops == -1 ? prepare_rollout_jit(*m->impl, &why)
+                  : ops == -4 ? prepare_rollout3_jit(*m->impl, &why)
                               : prepare_vjp_jit(*m->impl, ops == -3, &why);
   if (!ok) return fail(SGDYN_ERR_UNSUPPORTED, "run-time compilation unavailable: " + why);
   return SGDYN_OK;
@@ -463,7 +486,10 @@ int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
   if (!m || !source) return fail(SGDYN_ERR_NULL, "null argument");
   if (!jit_kind_ok(ops)) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
   thread_local std::string buf;
-  buf = ops > 0 ? step_jit_source(*m->impl, ops) : ops == -1 ? rollout_jit_source(*m->impl) : vjp_jit_source(*m->impl, ops == -3);
+  buf = ops > 0     ? step_jit_source(*m->impl, ops)
+        : ops == -1 ? rollout_jit_source(*m->impl)
+        : ops == -4 ? rollout3_jit_source(*m->impl)
+                    : vjp_jit_source(*m->impl, ops == -3);
   *source = buf.c_str();
   return SGDYN_OK;
 }
@@ -785,8 +811,13 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
     a.q0 = q0; a.qd0 = qd0; a.tau = tau;
     a.qT = qT; a.qdT = qdT; a.q_ckpt = q_ckpt; a.qd_ckpt = qd_ckpt;
     std::string why;
-    if (launch_rollout_jit(Mo, a, static_cast<cudaStream_t>(stream), &why)) return SGDYN_OK;
-    return launch_status(launch_rollout_forward(dm, Mo.njoints(), a, static_cast<cudaStream_t>(stream)));
+    const auto st = static_cast<cudaStream_t>(stream);
+    if (rollout_lanes(Mo, n) == 3) {
+      if (launch_rollout3_jit(Mo, a, st, &why)) return SGDYN_OK;
+      return launch_status(launch_rollout_forward3(dm, Mo.njoints(), a, st));
+    }
+    if (launch_rollout_jit(Mo, a, st, &why)) return SGDYN_OK;
+    return launch_status(launch_rollout_forward(dm, Mo.njoints(), a, st));
   });
 }
 

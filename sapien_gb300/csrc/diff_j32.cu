@@ -1,5 +1,6 @@
 // Instantiations of the differentiation kernels for trees of up to 32 joints.
 #include "diff_kernels.cuh"
+#include "team3.cuh"
 
 namespace sgdyn {
 
@@ -27,6 +28,10 @@ cudaError_t launch_aba_derivatives_j32(const DModel* dm, const DerivArgs& a, cud
   if (cudaError_t e = cudaGetLastError()) return e;
   const int64_t nv = (a.lay.Q - a.lay.P) / 6;
   aba_deriv_columns_kernel<32><<<unsigned((a.n * nv + 127) / 128), 128, 0, s>>>(dm, a);
+  return cudaGetLastError();
+}
+cudaError_t launch_rollout_forward3_j32(const DModel* dm, const RolloutArgs& a, cudaStream_t s) {
+  rollout_forward3_kernel<32><<<unsigned((a.n + 9) / 10), 32, 0, s>>>(dm, a);
   return cudaGetLastError();
 }
 cudaError_t launch_rollout_recompute_j32(const DModel* dm, const RolloutArgs& a, cudaStream_t s) {

@@ -116,6 +116,8 @@ cudaError_t launch_fk_vjp(const DModel* dm, int nj, const FkVjpArgs& a, cudaStre
 cudaError_t launch_rnea_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
 cudaError_t launch_aba_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_forward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
+// The forward rollout with three lanes per environment (team3.cuh; one-DoF joints only).
+cudaError_t launch_rollout_forward3(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_recompute(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_reverse(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 // Fields: S, P, Q: 6 per tree column; v, a, F, H: 6 per joint; Ib, Db: 10 per joint

@@ -101,6 +101,7 @@ SG_DISPATCH(fk_vjp, FkVjpArgs)
 SG_DISPATCH(rnea_derivatives, DerivArgs)
 SG_DISPATCH(aba_derivatives, DerivArgs)
 SG_DISPATCH(rollout_forward, RolloutArgs)
+SG_DISPATCH(rollout_forward3, RolloutArgs)
 SG_DISPATCH(rollout_recompute, RolloutArgs)
 SG_DISPATCH(rollout_reverse, RolloutArgs)
 #undef SG_DISPATCH

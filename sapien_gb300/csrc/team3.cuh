@@ -1,0 +1,278 @@
+// Three lanes per environment, one per Cartesian axis ("xyz teams"), for sweeps whose batch
+// leaves FP64 schedulers idle.
+//
+// A warp issues at most one FP64 instruction per ~64 cycles whatever its active lanes, so a
+// batch of one environment per thread with fewer warps than FP64 schedulers (the 4096-env
+// rollout: 128 warps for 608 schedulers) is bound by each warp's own instruction count.
+// Here lane k of a team holds component k of every spatial vector (linear and angular part)
+// and row k of every 3x3 block (world rotations, rigid-body and articulated inertias), so
+// matrix-vector products, cross products and rank-one updates cost each lane a third of the
+// FP64 instructions; a team gathers the other components with warp shuffles, which use no
+// FP64 issue slots. Dot products end in a fixed-order sum over the team, and every scalar
+// (joint coordinates, D, D^-1, u, q'') is computed identically on the three lanes, so the
+// lanes never disagree. Ten teams share a warp; lanes 30 and 31 shadow lanes 27 and 28 and
+// store nothing.
+//
+// The recursions are those of aba_forward (world-frame ABA): pass 1 poses, motion subspaces,
+// world inertias, velocities and bias forces; pass 2 articulated inertias
+// IA_p += IA - U D^-1 U^T, pA_p += pA + Ia c + U D^-1 u; pass 3 accelerations
+// (pinocchio_model.cpp:221-226). Joints with one degree of freedom only; a model with a
+// free flyer keeps the one-lane kernels.
+#pragma once
+#include "kernels.h"
+#include "spatial.cuh"
+#include "step_kernel.cuh"
+
+namespace sgdyn {
+
+struct Team3 {
+  int k, k1, k2;  // this lane's axis and the next two (cyclic)
+  int base;       // first lane of the team
+  bool valid;     // false on the two shadow lanes of a warp and on teams past the batch
+
+  __device__ __forceinline__ double at(double x, int j) const { return __shfl_sync(0xffffffffu, x, base + j); }
+  __device__ __forceinline__ V3 all(double x) const { return mk(at(x, 0), at(x, 1), at(x, 2)); }
+  // sum over the team in a fixed order: the same bits on all three lanes
+  __device__ __forceinline__ double sum(double x) const { return (at(x, 0) + at(x, 1)) + at(x, 2); }
+  // component k of a x b, both distributed
+  __device__ __forceinline__ double cross(double a, double b) const {
+    return fma(at(a, k1), at(b, k2), -at(a, k2) * at(b, k1));
+  }
+  // component k of a full 3-vector held by every lane
+  __device__ __forceinline__ double pick(V3 v) const { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+};
+
+__device__ __forceinline__ Team3 team3_of_lane(int lane) {
+  Team3 t;
+  const int l = lane < 30 ? lane : lane - 3;
+  t.base = l / 3 * 3;
+  t.k = l - t.base;
+  t.k1 = t.k == 2 ? 0 : t.k + 1;
+  t.k2 = t.k == 0 ? 2 : t.k - 1;
+  t.valid = lane < 30;
+  return t;
+}
+
+// Row k of a row-major 3x3 table matrix.
+__device__ __forceinline__ V3 row_of(const double* R, int k) { return mk(R[3 * k], R[3 * k + 1], R[3 * k + 2]); }
+// Row k of a symmetric 3x3 stored as xx xy xz yy yz zz.
+__device__ __forceinline__ V3 sym_row(const double* S, int k) {
+  return k == 0 ? mk(S[0], S[1], S[2]) : (k == 1 ? mk(S[1], S[3], S[4]) : mk(S[2], S[4], S[5]));
+}
+// Row vector r times the matrix with rows m0, m1, m2.
+__device__ __forceinline__ V3 row_mul(V3 r, V3 m0, V3 m1, V3 m2) {
+  return mk(fma(r.z, m2.x, fma(r.y, m1.x, r.x * m0.x)), fma(r.z, m2.y, fma(r.y, m1.y, r.x * m0.y)),
+            fma(r.z, m2.z, fma(r.y, m1.z, r.x * m0.z)));
+}
+
+// Per-lane state of one environment's ABA (component k / row k of every quantity).
+template <int MAXJ>
+struct Aba3Work {
+  V3 oR[MAXJ];                // row k of the joint's world rotation
+  double op[MAXJ];            // component k of its world position
+  double Sl[MAXJ], Sa[MAXJ];  // motion subspace (one column per joint)
+  double vl[MAXJ], va[MAXJ], cl[MAXJ], ca[MAXJ], pl[MAXJ], pa[MAXJ], al[MAXJ], aa[MAXJ];
+  V3 A[MAXJ], B[MAXJ], BT[MAXJ], C[MAXJ];  // articulated inertia [[A, B], [B^T, C]], row k
+  double Ul[MAXJ], Ua[MAXJ], u[MAXJ], Dinv[MAXJ];
+};
+
+// World-frame ABA of one environment on a team: qdd (external order) from q, qd, tau, all
+// three replicated on the lanes.
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void aba3(const Tab& T, const Team3& tm, const double* q, const double* qd,
+                                     const double* tau, double* qdd, Aba3Work<MAXJ>& W) {
+  const int nj = T.nj(), k = tm.k;
+  const V3 ek = mk(k == 0 ? 1.0 : 0.0, k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0);
+  // ---- pass 1: root to leaves ----
+#pragma unroll
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = T.joint(i);
+    const int p = J.parent;
+    const bool rot_id = (J.flags & JF_ROT_IDENTITY) != 0;
+    const V3 ppl = mk(J.p[0], J.p[1], J.p[2]);
+    const V3 Rp = p == 0 ? ek : W.oR[p];  // row k of the parent's world rotation
+    const double x = q[J.qcol];
+    V3 Ro;      // row k of this joint's world rotation
+    double po;  // component k of its world position
+    double u;   // component k of its world axis
+    if (J.axis_kind == AX_Z) {
+      const V3 B = rot_id ? Rp : row_mul(Rp, row_of(J.R, 0), row_of(J.R, 1), row_of(J.R, 2));
+      const double o = p == 0 ? tm.pick(ppl) : fma(Rp.z, ppl.z, fma(Rp.y, ppl.y, fma(Rp.x, ppl.x, W.op[p])));
+      if (J.kind == JK_PRISMATIC) {
+        Ro = B;
+        po = fma(x, B.z, o);
+      } else {
+        double s, c;
+        sincos(x, &s, &c);
+        Ro = mk(fma(c, B.x, s * B.y), fma(c, B.y, -s * B.x), B.z);
+        po = o;
+      }
+      u = Ro.z;
+    } else {
+      const V3 ax = mk(J.axis[0], J.axis[1], J.axis[2]);
+      V3 pli = ppl;
+      M3 Rli;
+      if (J.kind == JK_PRISMATIC) {
+#pragma unroll
+        for (int t = 0; t < 9; t++) Rli.a[t] = J.R[t];
+        pli = rot_id ? axpy(x, ax, ppl) : mul_add(Rli, x * ax, ppl);
+      } else {
+        double s, c;
+        sincos(x, &s, &c);
+        const M3 RJ = rodrigues(ax, s, c);
+        if (rot_id) {
+          Rli = RJ;
+        } else {
+          M3 Rpl;
+#pragma unroll
+          for (int t = 0; t < 9; t++) Rpl.a[t] = J.R[t];
+          Rli = mul(Rpl, RJ);
+        }
+      }
+      Ro = row_mul(Rp, row_of(Rli.a, 0), row_of(Rli.a, 1), row_of(Rli.a, 2));
+      po = p == 0 ? tm.pick(pli) : fma(Rp.z, pli.z, fma(Rp.y, pli.y, fma(Rp.x, pli.x, W.op[p])));
+      u = fma(Ro.z, ax.z, fma(Ro.y, ax.y, Ro.x * ax.x));
+    }
+    W.oR[i] = Ro;
+    W.op[i] = po;
+    double Sl, Sa;
+    if (J.kind == JK_PRISMATIC) {
+      Sl = u;
+      Sa = 0.0;
+    } else {
+      Sl = tm.cross(po, u);
+      Sa = u;
+    }
+    W.Sl[i] = Sl;
+    W.Sa[i] = Sa;
+    // world inertia (m, s = R h + m p, I') with I'_kj = (R I R^T)_kj + d delta_kj - p_k s_j - hr_k p_j,
+    // d = m |p|^2 + 2 hr.p, hr = R h (rbi_transport restated per row)
+    const double m = J.m;
+    const double hr = fma(Ro.z, J.h[2], fma(Ro.y, J.h[1], Ro.x * J.h[0]));
+    const double sk = fma(m, po, hr);
+    const double d = fma(m, tm.sum(po * po), 2.0 * tm.sum(hr * po));
+    const V3 Tk = row_mul(Ro, sym_row(J.I, 0), sym_row(J.I, 1), sym_row(J.I, 2));  // row k of R I
+    const V3 R0 = mk(tm.at(Ro.x, 0), tm.at(Ro.y, 0), tm.at(Ro.z, 0));
+    const V3 R1 = mk(tm.at(Ro.x, 1), tm.at(Ro.y, 1), tm.at(Ro.z, 1));
+    const V3 R2 = mk(tm.at(Ro.x, 2), tm.at(Ro.y, 2), tm.at(Ro.z, 2));
+    const V3 sv = tm.all(sk), pv = tm.all(po);
+    V3 Ik;
+    Ik.x = fma(-hr, pv.x, fma(-po, sv.x, dot(Tk, R0) + (k == 0 ? d : 0.0)));
+    Ik.y = fma(-hr, pv.y, fma(-po, sv.y, dot(Tk, R1) + (k == 1 ? d : 0.0)));
+    Ik.z = fma(-hr, pv.z, fma(-po, sv.z, dot(Tk, R2) + (k == 2 ? d : 0.0)));
+    // velocity, momentum (f, n) = Y v, bias force v x* Y v, velocity-product acceleration
+    const double qdi = qd[J.vcol];
+    const double vJl = qdi * Sl, vJa = qdi * Sa;
+    const double vl = p == 0 ? vJl : W.vl[p] + vJl;
+    const double va = p == 0 ? vJa : W.va[p] + vJa;
+    W.vl[i] = vl;
+    W.va[i] = va;
+    const double fl = fma(m, vl, -tm.cross(sk, va));   // m v - s x w
+    const double fa = dot(Ik, tm.all(va)) + tm.cross(sk, vl);  // I' w + s x v
+    W.pl[i] = tm.cross(va, fl);                         // w x f
+    W.pa[i] = tm.cross(va, fa) + tm.cross(vl, fl);      // w x n + v x f
+    W.cl[i] = tm.cross(va, vJl) + tm.cross(vl, vJa);    // w x vJ_lin + v x vJ_ang
+    W.ca[i] = tm.cross(va, vJa);
+    // the articulated inertia starts as the rigid-body inertia [[m 1, -[s]x], [[s]x, I']]
+    W.A[i] = m * ek;
+    const V3 Bk = k == 0 ? mk(0.0, sv.z, -sv.y) : (k == 1 ? mk(-sv.z, 0.0, sv.x) : mk(sv.y, -sv.x, 0.0));
+    W.B[i] = Bk;
+    W.BT[i] = -Bk;
+    W.C[i] = Ik;
+  }
+  // ---- pass 2: leaves to root ----
+#pragma unroll
+  for (int i = nj - 1; i >= 1; i--) {
+    const DJoint& J = T.joint(i);
+    const int p = J.parent;
+    const V3 Slv = tm.all(W.Sl[i]), Sav = tm.all(W.Sa[i]);
+    const V3 A = W.A[i], B = W.B[i], BT = W.BT[i], C = W.C[i];
+    const double Ul = dot(A, Slv) + dot(B, Sav);
+    const double Ua = dot(BT, Slv) + dot(C, Sav);
+    const double D = tm.sum(fma(W.Sl[i], Ul, W.Sa[i] * Ua));
+    const double u = tau[J.vcol] - tm.sum(fma(W.Sl[i], W.pl[i], W.Sa[i] * W.pa[i]));
+    const double di = 1.0 / D;
+    W.Ul[i] = Ul;
+    W.Ua[i] = Ua;
+    W.u[i] = u;
+    W.Dinv[i] = di;
+    if (p > 0) {
+      const double Udl = di * Ul, Uda = di * Ua;
+      const V3 Ulv = tm.all(Ul), Uav = tm.all(Ua);
+      const V3 Ia = mk(fma(-Udl, Ulv.x, A.x), fma(-Udl, Ulv.y, A.y), fma(-Udl, Ulv.z, A.z));
+      const V3 Ib = mk(fma(-Udl, Uav.x, B.x), fma(-Udl, Uav.y, B.y), fma(-Udl, Uav.z, B.z));
+      const V3 Ibt = mk(fma(-Uda, Ulv.x, BT.x), fma(-Uda, Ulv.y, BT.y), fma(-Uda, Ulv.z, BT.z));
+      const V3 Ic = mk(fma(-Uda, Uav.x, C.x), fma(-Uda, Uav.y, C.y), fma(-Uda, Uav.z, C.z));
+      const V3 clv = tm.all(W.cl[i]), cav = tm.all(W.ca[i]);
+      const double pal = fma(u, Udl, dot(Ia, clv) + dot(Ib, cav) + W.pl[i]);
+      const double paa = fma(u, Uda, dot(Ibt, clv) + dot(Ic, cav) + W.pa[i]);
+      W.A[p] = W.A[p] + Ia;
+      W.B[p] = W.B[p] + Ib;
+      W.BT[p] = W.BT[p] + Ibt;
+      W.C[p] = W.C[p] + Ic;
+      W.pl[p] += pal;
+      W.pa[p] += paa;
+    }
+  }
+  // ---- pass 3: root to leaves ----
+  const double gk = -T.gravity(k);
+#pragma unroll
+  for (int i = 1; i < nj; i++) {
+    const DJoint& J = T.joint(i);
+    const int p = J.parent;
+    double al = (p == 0 ? gk : W.al[p]) + W.cl[i];
+    double aa = (p == 0 ? 0.0 : W.aa[p]) + W.ca[i];
+    const double x = W.Dinv[i] * (W.u[i] - tm.sum(fma(W.Ul[i], al, W.Ua[i] * aa)));
+    al = fma(x, W.Sl[i], al);
+    aa = fma(x, W.Sa[i], aa);
+    W.al[i] = al;
+    W.aa[i] = aa;
+    qdd[J.vcol] = x;
+  }
+}
+
+// Forward rollout (as rollout_forward_env) with a team of three lanes per environment: q,
+// qd, tau and the checkpoints are replicated on the lanes; lane 0 stores.
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void rollout_forward3_env(const Tab& T, const Team3& tm, const RolloutArgs& a,
+                                                     const int64_t e) {
+  constexpr int MAXV = MAXJ + 5, MAXQ = MAXJ + 6;
+  const int nv = T.nv(), nq = T.nq_ext();
+  const int64_t n = a.n;
+  const bool st = tm.valid && tm.k == 0;
+  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
+  for (int c = 0; c < nq; c++) q[c] = a.q0[e * nq + c];
+  for (int c = 0; c < nv; c++) qd[c] = a.qd0[e * nv + c];
+  Aba3Work<MAXJ> W;
+  for (int t = 0; t < a.T; t++) {
+    if (a.q_ckpt && t % a.K == 0 && st) {
+      const int64_t s = t / a.K;
+      for (int c = 0; c < nq; c++) a.q_ckpt[(s * n + e) * nq + c] = q[c];
+      for (int c = 0; c < nv; c++) a.qd_ckpt[(s * n + e) * nv + c] = qd[c];
+    }
+    for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
+    aba3<MAXJ>(T, tm, q, qd, tau, qdd, W);
+    for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
+#pragma unroll
+    for (int i = 1; i < T.nj(); i++) {
+      const DJoint& J = T.joint(i);
+      q[J.qcol] = fma(a.dt, qd[J.vcol], q[J.qcol]);
+    }
+  }
+  if (st) {
+    for (int c = 0; c < nq; c++) a.qT[e * nq + c] = q[c];
+    for (int c = 0; c < nv; c++) a.qdT[e * nv + c] = qd[c];
+  }
+}
+
+// Ten environments per warp; teams past the end of the batch repeat the last environment
+// and store nothing.
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rollout_forward3_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+  Team3 tm = team3_of_lane(threadIdx.x);
+  const int64_t e0 = int64_t(blockIdx.x) * 10 + tm.base / 3;
+  tm.valid = tm.valid && e0 < a.n;
+  rollout_forward3_env<MAXJ>(RuntimeTab{model}, tm, a, e0 < a.n ? e0 : a.n - 1);
+}
+
+}  // namespace sgdyn

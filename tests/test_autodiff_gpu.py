@@ -382,3 +382,46 @@ def test_floating_base_rollout_backward_matches_single_step_vjps():
         for a, b in zip(o_, outs[0]):
             assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-12
     assert torch.all(outs[0][0][:, 6] == 0)  # the free flyer's seventh slot
+
+
+ROLLOUT3 = {
+    "arm9": lambda: syn.arm_with_fingers(),
+    "arm9_sapien": lambda: syn.arm_with_fingers(sapien_style=True),
+    "mixed_chain": lambda: syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
+                                                                "continuous", "prismatic"]),
+    "chain40": lambda: syn.serial_chain(40, seed=23),
+}
+
+
+@pytest.mark.parametrize("name", list(ROLLOUT3))
+def test_three_lane_rollout_forward_matches_one_lane_and_oracle(name):
+    """The forward rollout with one lane per Cartesian axis (sgdyn_rollout_lanes(3)), generic
+    and run-time-compiled, against one lane per environment and the oracle; 23 environments
+    so that the last warp has teams past the end of the batch."""
+    import ctypes
+
+    from sapien_gb300 import _native as N
+
+    robot = ROLLOUT3[name]()
+    pm, o = pair(robot)
+    n, steps, K, dt = 23, 60, 20, 1.0 / 500
+    q0, qd0, _, _ = robot.sample(n, seed=4)
+    tau = np.random.default_rng(5).normal(scale=5.0, size=(steps, n, robot.nv))
+    L = N.load()
+    old_jit, old_min = ctypes.c_int(), ctypes.c_int64()
+    L.sgdyn_jit_config(-1, -1, ctypes.byref(old_jit), ctypes.byref(old_min))
+    outs = {}
+    try:
+        for jit in (0, 1):
+            L.sgdyn_jit_config(jit, 0, None, None)
+            for lanes in (1, 3):
+                assert L.sgdyn_rollout_lanes(lanes, None) == N.OK
+                outs[(jit, lanes)] = [x.cpu().numpy() for x in ad.rollout_forward(pm, cu(q0), cu(qd0), cu(tau), dt, K)]
+    finally:
+        L.sgdyn_rollout_lanes(0, None)
+        L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
+    rq, rqd, _ = o.rollout(q0, qd0, tau, dt, robot.ee_link, np.zeros((n, 3)))
+    for key, (qT, qdT, qc, qdc) in outs.items():
+        assert rel(qT, rq) < 1e-9 and rel(qdT, rqd) < 1e-9, key
+        ref = outs[(0, 1)]
+        assert rel(qc, ref[2]) < 1e-11 and rel(qdc, ref[3]) < 1e-11, key  # checkpoints
