@@ -98,6 +98,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_ENVS)
+    ap.add_argument("--only-rollout", action="store_true",
+                    help="run only the differentiable-rollout workload (for profiling its kernels)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the secondary workloads (rollout, heterogeneous batch, IK, derivatives)")
     return ap.parse_args()
@@ -242,7 +244,7 @@ def _event_ms(torch, fn, reps=5, warm=2):
     return a.elapsed_time(b) / reps
 
 
-def secondary_workloads(dev):
+def secondary_workloads(dev, only_rollout=False):
     """The other workloads of the benchmark spec, timed with CUDA events on rank 0:
     differentiable rollout (9-DoF arm, 4096 envs, 200 steps, dt 1/500, q/qd checkpoints
     every 20 steps), heterogeneous batch (8192 mixed robots, RNEA + ABA + CRBA, CUDA-graph
@@ -277,6 +279,8 @@ def secondary_workloads(dev):
                       "fwd_ms": fwd, "fwd_with_checkpoints_ms": fwd_ck, "bwd_ms": bwd,
                       "fwd_bwd_over_plain": (fwd_ck + bwd) / fwd}
     out["rollout"].update(_rollout_parity(torch, ad, arm, pm, q0, qd0, tau, dt, K))
+    if only_rollout:
+        return out
     robots, moe = synthetic.hetero_mix(8192, seed=0)
     models = [model_of(r) for r in robots]
     ins = [r.sample(int((moe == k).sum()), seed=k) for k, r in enumerate(robots)]
@@ -554,6 +558,12 @@ def main():
         run_reference(args)
         return
     import torch
+
+    if args.only_rollout:
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        torch.cuda.set_device(dev)
+        print(json.dumps({"secondary": secondary_workloads(dev, only_rollout=True)}), flush=True)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
