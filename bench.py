@@ -47,7 +47,7 @@ KERNEL_COUNTERS = {
     # where most of the 29 MB of results is still held in L2 when the launches end
     "specialised": {"fp64_inst_per_env": 2810368 * 32 / 16384, "dram_bytes_per_env": 9.82e6 / 16384},
 }
-KERNEL_SOURCE_SHA256 = "f7813092802a51d2971fcaa6d8d9fe70494316f7223dcd1483c7ac5cec3e43f2"
+KERNEL_SOURCE_SHA256 = "37d502ffa51e7b7ba200e881472ba3649ea3a1379e109cb4f186f6b82d5910fe"
 KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
 STEP_OPS = (3, 28)  # sgdyn_step at N = 16384: FK + Jacobian beside CRBA + RNEA + ABA, two launches
 

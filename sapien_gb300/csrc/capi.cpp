@@ -131,7 +131,9 @@ int device_schedulers() {
   return schedulers;
 }
 
-// Lanes per environment of the forward rollout: 1, or 3 (team3.cuh: one lane per axis,
+// Lanes per environment of the forward rollout and of the backward's reverse sweep (the
+// recompute keeps one lane: all its segments run at once and fill the GPU): 1, or 3
+// (team3.cuh: one lane per axis,
 // one-DoF joints only). The setting: 0 automatic (the default: three lanes while one warp
 // per ten environments leaves no FP64 scheduler with two warps), 1 or 3.
 std::atomic<int> g_rollout_lanes{0};
@@ -143,6 +145,13 @@ int rollout_lanes(const Model& M, int64_t n) {
   if (mode != 0) return mode;
   return (n + 9) / 10 <= int64_t(device_schedulers()) ? 3 : 1;
 }
+
+}  // namespace
+
+// Lanes per environment of the rollout kernels for this model and batch (1 or 3).
+int rollout_lanes_for(const Model& M, int64_t n) { return rollout_lanes(M, n); }
+
+namespace {
 
 bool use_split(int64_t n) {
   const int mode = g_split_mode.load();
@@ -840,8 +849,8 @@ namespace {
 // reverse sweep at small batches keeps one warp per SM busy and leaves the other FP64
 // schedulers idle; the recompute fills them. Groups alternate between two halves of the
 // scratch; a recompute waits for the reverse that last used its half.
-cudaError_t rollout_backward_overlapped(const DModel* dm, int nj, RolloutArgs a, int64_t seg_doubles, int G,
-                                        cudaStream_t s1, cudaStream_t s2) {
+cudaError_t rollout_backward_overlapped(const DModel* dm, int nj, int lanes, RolloutArgs a, int64_t seg_doubles,
+                                        int G, cudaStream_t s1, cudaStream_t s2) {
   const int nseg = (a.T + a.K - 1) / a.K;
   std::vector<RolloutArgs> groups;
   for (int hi = nseg; hi > 0; hi -= G) {
@@ -865,7 +874,8 @@ cudaError_t rollout_backward_overlapped(const DModel* dm, int nj, RolloutArgs a,
   if (e == cudaSuccess) e = cudaEventRecord(rec(0), s2);
   for (int k = 0; k < m && e == cudaSuccess; k++) {
     e = cudaStreamWaitEvent(s1, rec(k), 0);
-    if (e == cudaSuccess) e = launch_rollout_reverse(dm, nj, groups[k], s1);
+    if (e == cudaSuccess)
+      e = lanes == 3 ? launch_rollout_reverse3(dm, nj, groups[k], s1) : launch_rollout_reverse(dm, nj, groups[k], s1);
     if (e == cudaSuccess) e = cudaEventRecord(rev(k), s1);
     if (e == cudaSuccess && k + 1 < m) {
       if (k >= 1) e = cudaStreamWaitEvent(s2, rev(k - 1), 0);
@@ -917,6 +927,7 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
     a.q0_bar = q0_bar; a.qd0_bar = qd0_bar; a.tau_bar = tau_bar; a.scratch = scratch;
     const cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nj = Mo.njoints();
+    const int lanes = rollout_lanes(Mo, n);
     // two scratch halves of G segments each and at least two groups: overlap recompute and
     // reverse on two streams (not while the caller's stream is being captured)
     const int nseg = T > 0 ? (T + checkpoint_every - 1) / checkpoint_every : 0;
@@ -926,10 +937,12 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
     if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusActive;
     if (nseg >= 2 && G >= 1 && (nseg + G - 1) / G >= 2 && cs == cudaStreamCaptureStatusNone)
       if (cudaStream_t s2 = side_stream())
-        return launch_status(rollout_backward_overlapped(dm, nj, a, need / 8, G, st, s2));
+        return launch_status(rollout_backward_overlapped(dm, nj, lanes, a, need / 8, G, st, s2));
     return launch_status(rollout_backward_grouped(
         a, need / 8, scratch_bytes / 8, [&](const RolloutArgs& g) { return launch_rollout_recompute(dm, nj, g, st); },
-        [&](const RolloutArgs& g) { return launch_rollout_reverse(dm, nj, g, st); }));
+        [&](const RolloutArgs& g) {
+          return lanes == 3 ? launch_rollout_reverse3(dm, nj, g, st) : launch_rollout_reverse(dm, nj, g, st);
+        }));
   });
 }
 

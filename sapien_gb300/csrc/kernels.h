@@ -120,6 +120,8 @@ cudaError_t launch_rollout_forward(const DModel* dm, int nj, const RolloutArgs& 
 cudaError_t launch_rollout_forward3(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_recompute(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_reverse(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
+// The reverse rollout with three lanes per environment (team3.cuh; one-DoF joints only).
+cudaError_t launch_rollout_reverse3(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 // Fields: S, P, Q: 6 per tree column; v, a, F, H: 6 per joint; Ib, Db: 10 per joint
 // (m, h, I xx xy xz yy yz zz); L: the packed factor (nv (nv + 1) / 2), Dinv: nv (ABA only).
 inline DerivLayout deriv_layout(int nj, int nv, bool aba) {

@@ -43,6 +43,7 @@ namespace sgdyn {
 
 int set_last_error(int code, const std::string& msg);
 int call_guarded(const std::function<int()>& body);
+int rollout_lanes_for(const Model& M, int64_t n);
 
 namespace {
 
@@ -119,10 +120,13 @@ extern "C" int sgdyn_rollout_backward_noalloc(const sgdyn_model* m, int64_t n, i
     a.scratch = scratch;
     const cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nj = Mo.njoints();
+    const int lanes = rollout_lanes_for(Mo, n);
     cudaError_t e = rollout_backward_grouped(
         a, need / 8, kNoAllocScratchBytes / 8,
         [&](const RolloutArgs& g) { return launch_rollout_recompute(dm, nj, g, st); },
-        [&](const RolloutArgs& g) { return launch_rollout_reverse(dm, nj, g, st); });
+        [&](const RolloutArgs& g) {
+          return lanes == 3 ? launch_rollout_reverse3(dm, nj, g, st) : launch_rollout_reverse(dm, nj, g, st);
+        });
     if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
     return SGDYN_OK;
   });

@@ -22,6 +22,7 @@
 #include "kernels.h"
 #include "spatial.cuh"
 #include "step_kernel.cuh"
+#include "diff_kernels.cuh"
 
 namespace sgdyn {
 
@@ -263,6 +264,183 @@ __device__ __forceinline__ void rollout_forward3_env(const Tab& T, const Team3& 
     for (int c = 0; c < nq; c++) a.qT[e * nq + c] = q[c];
     for (int c = 0; c < nv; c++) a.qdT[e * nv + c] = qd[c];
   }
+}
+
+// ---- reverse rollout with three lanes per environment ----------------------------------
+// The same reverse step as rollout_reverse_env (M^-1 solve through ABA's factorisation, then
+// the world-frame RNEA adjoint of diff_core.cuh, then the semi-implicit Euler adjoint), each
+// lane reading its components of the stored intermediates (the stash is one field per
+// component, environments contiguous) and computing its components of the adjoint
+// quantities w, P = Y w, Q = v x* P, R = w x* Y v, T = Y (v x w).
+template <int MAXJ>
+struct Rev3Work {
+  double Sl[MAXJ], Sa[MAXJ], Ul[MAXJ], Ua[MAXJ], Dinv[MAXJ];
+  double vl[MAXJ], va[MAXJ], al[MAXJ], aa[MAXJ], hl[MAXJ], ha[MAXJ], Fl[MAXJ], Fa[MAXJ];
+  double m[MAXJ], h[MAXJ];  // mass and component k of the first moment of the world inertia
+  V3 I[MAXJ];               // row k of its rotational inertia
+  // scratch of the solve and of the adjoint sweep
+  double us[MAXJ], xl[MAXJ], xa[MAXJ];
+  double wl[MAXJ], wa[MAXJ], Pl[MAXJ], Pa[MAXJ], Ql[MAXJ], Qa[MAXJ], Rl[MAXJ], Ra[MAXJ], Tl[MAXJ], Ta[MAXJ];
+};
+
+// Component k of x x* f = (x_ang x f_lin, x_ang x f_ang + x_lin x f_lin).
+__device__ __forceinline__ void crossf3(const Team3& tm, double xl, double xa, double fl, double fa, double& ol,
+                                        double& oa) {
+  ol = tm.cross(xa, fl);
+  oa = tm.cross(xa, fa) + tm.cross(xl, fl);
+}
+// Component k of Y x for the world inertia (m, h, I): (m x_lin - h x x_ang, I x_ang + h x x_lin).
+__device__ __forceinline__ void rbi3(const Team3& tm, double m, double h, V3 Irow, double xl, double xa, double& ol,
+                                     double& oa) {
+  ol = fma(m, xl, -tm.cross(h, xa));
+  oa = dot(Irow, tm.all(xa)) + tm.cross(h, xl);
+}
+
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& tm, const RolloutArgs& a,
+                                                     const int64_t e) {
+  constexpr int MAXV = MAXJ + 5, MAXQ = MAXJ + 6;
+  const int nv = T.nv(), nq = T.nq_ext(), nj = T.nj(), k = tm.k;
+  const int64_t n = a.n;
+  const int64_t per_step = stash_doubles_per_step(nj, nq, nv);
+  const int nseg = (a.T + a.K - 1) / a.K;
+  const bool last = a.s_lo + a.s_cnt == nseg;
+  const bool st = tm.valid && k == 0;
+  const double* qin = last ? a.qT_bar : a.q0_bar;
+  const double* qdin = last ? a.qdT_bar : a.qd0_bar;
+  double qb[MAXQ], qdb[MAXV], lam[MAXV];
+  for (int c = 0; c < nq; c++) qb[c] = qin ? qin[e * nq + c] : 0.0;
+  for (int c = 0; c < nv; c++) qdb[c] = qdin ? qdin[e * nv + c] : 0.0;
+  Rev3Work<MAXJ> W;
+  const double gk = -T.gravity(k);
+  for (int s = a.s_lo + a.s_cnt - 1; s >= a.s_lo; s--) {
+    const int t0 = s * a.K, t1 = min(a.T, t0 + a.K);
+    for (int t = t1 - 1; t >= t0; t--) {
+      const double* base = a.scratch + (int64_t(s - a.s_lo) * a.K + (t - t0)) * per_step * n;
+      auto ld = [&](int64_t f) { return base[f * n + e]; };
+      // q' = q + dt qd' and qd' = qd + dt qdd, reversed: qdd_bar = dt qd'_bar
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+        qdb[J.vcol] = fma(a.dt, qb[J.qcol], qdb[J.vcol]);
+      }
+      // this lane's components of the stored intermediates (stash_io's layout)
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const int iv = T.joint(i).ivx;
+        const int64_t jb = 12 * int64_t(nv) + int64_t(i - 1) * 35;
+        W.Sl[i] = ld(6 * iv + k);
+        W.Sa[i] = ld(6 * iv + 3 + k);
+        W.Ul[i] = ld(6 * nv + 6 * iv + k);
+        W.Ua[i] = ld(6 * nv + 6 * iv + 3 + k);
+        W.Dinv[i] = ld(jb);
+        W.vl[i] = ld(jb + 1 + k);
+        W.va[i] = ld(jb + 4 + k);
+        W.al[i] = ld(jb + 7 + k);
+        W.aa[i] = ld(jb + 10 + k);
+        W.hl[i] = ld(jb + 13 + k);
+        W.ha[i] = ld(jb + 16 + k);
+        W.m[i] = ld(jb + 19);
+        W.h[i] = ld(jb + 20 + k);
+        const int r0 = k == 0 ? 0 : (k == 1 ? 1 : 2), r1 = k == 0 ? 1 : (k == 1 ? 3 : 4),
+                  r2 = k == 0 ? 2 : (k == 1 ? 4 : 5);
+        W.I[i] = mk(ld(jb + 23 + r0), ld(jb + 23 + r1), ld(jb + 23 + r2));
+        W.Fl[i] = ld(jb + 29 + k);
+        W.Fa[i] = ld(jb + 32 + k);
+      }
+      // lam = M^-1 (dt qd'_bar): the ABA recursion with zero velocity and gravity
+#pragma unroll
+      for (int i = 1; i < nj; i++) W.xl[i] = W.xa[i] = 0.0;
+#pragma unroll
+      for (int i = nj - 1; i >= 1; i--) {
+        const DJoint& J = T.joint(i);
+        const int p = J.parent;
+        const double u = a.dt * qdb[J.vcol] - tm.sum(fma(W.Sl[i], W.xl[i], W.Sa[i] * W.xa[i]));
+        W.us[i] = u;
+        if (p > 0) {
+          const double ud = u * W.Dinv[i];
+          W.xl[p] += fma(ud, W.Ul[i], W.xl[i]);
+          W.xa[p] += fma(ud, W.Ua[i], W.xa[i]);
+        }
+      }
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+        const int p = J.parent;
+        const double pl = p == 0 ? 0.0 : W.xl[p], pa = p == 0 ? 0.0 : W.xa[p];
+        const double z = W.Dinv[i] * (W.us[i] - tm.sum(fma(W.Ul[i], pl, W.Ua[i] * pa)));
+        W.xl[i] = fma(z, W.Sl[i], pl);  // accelerations of the solve (the bias forces are spent)
+        W.xa[i] = fma(z, W.Sa[i], pa);
+        lam[J.vcol] = z;
+      }
+      if (st)
+        for (int c = 0; c < nv; c++) a.tau_bar[(int64_t(t) * n + e) * nv + c] = lam[c];
+      // RNEA adjoint at lam, scaled by -1 (ABA's adjoint): root to leaves ...
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+        const int p = J.parent;
+        const double x = lam[J.vcol];
+        const double wl = p == 0 ? x * W.Sl[i] : fma(x, W.Sl[i], W.wl[p]);
+        const double wa = p == 0 ? x * W.Sa[i] : fma(x, W.Sa[i], W.wa[p]);
+        W.wl[i] = wl;
+        W.wa[i] = wa;
+        double Pl, Pa, Ql, Qa, Rl, Ra, cl, ca, Tl, Ta;
+        rbi3(tm, W.m[i], W.h[i], W.I[i], wl, wa, Pl, Pa);
+        crossf3(tm, W.vl[i], W.va[i], Pl, Pa, Ql, Qa);
+        crossf3(tm, wl, wa, W.hl[i], W.ha[i], Rl, Ra);
+        cl = tm.cross(W.va[i], wl) + tm.cross(W.vl[i], wa);  // v x w (motion)
+        ca = tm.cross(W.va[i], wa);
+        rbi3(tm, W.m[i], W.h[i], W.I[i], cl, ca, Tl, Ta);
+        W.Pl[i] = Pl; W.Pa[i] = Pa; W.Ql[i] = Ql; W.Qa[i] = Qa;
+        W.Rl[i] = Rl; W.Ra[i] = Ra; W.Tl[i] = Tl; W.Ta[i] = Ta;
+      }
+      // ... and leaves to root (subtree sums of P, Q, R, T)
+#pragma unroll
+      for (int j = nj - 1; j >= 1; j--) {
+        const DJoint& J = T.joint(j);
+        const int p = J.parent;
+        const double Pl = W.Pl[j], Pa = W.Pa[j], Ql = W.Ql[j], Qa = W.Qa[j];
+        const double Rl = W.Rl[j], Ra = W.Ra[j], Tl = W.Tl[j], Ta = W.Ta[j];
+        const double vll = p == 0 ? 0.0 : W.vl[p], vla = p == 0 ? 0.0 : W.va[p];
+        const double all = p == 0 ? gk : W.al[p], ala = p == 0 ? 0.0 : W.aa[p];
+        const double Wll = p == 0 ? 0.0 : W.wl[p], Wla = p == 0 ? 0.0 : W.wa[p];
+        // Z = -Q + v_parent x* P + R + T;  G = v_parent x* Z - a_parent x* P - w_parent x* F
+        double xl, xa;
+        crossf3(tm, vll, vla, Pl, Pa, xl, xa);
+        const double Zl = xl + (Rl + Tl) - Ql, Za = xa + (Ra + Ta) - Qa;
+        double Gl, Ga, yl, ya, zl, za;
+        crossf3(tm, vll, vla, Zl, Za, Gl, Ga);
+        crossf3(tm, all, ala, Pl, Pa, yl, ya);
+        crossf3(tm, Wll, Wla, W.Fl[j], W.Fa[j], zl, za);
+        Gl = Gl - yl - zl;
+        Ga = Ga - ya - za;
+        const double o1 = -tm.sum(fma(W.Sl[j], Gl, W.Sa[j] * Ga));
+        // Gd = Q - (v_parent + v) x* P - R - T
+        crossf3(tm, vll + W.vl[j], vla + W.va[j], Pl, Pa, yl, ya);
+        const double Gdl = Ql - yl - (Rl + Tl), Gda = Qa - ya - (Ra + Ta);
+        const double o2 = -tm.sum(fma(W.Sl[j], Gdl, W.Sa[j] * Gda));
+        qb[J.qcol] += o1;
+        qdb[J.vcol] += o2;
+        if (p > 0) {
+          W.Pl[p] += Pl; W.Pa[p] += Pa; W.Ql[p] += Ql; W.Qa[p] += Qa;
+          W.Rl[p] += Rl; W.Ra[p] += Ra; W.Tl[p] += Tl; W.Ta[p] += Ta;
+        }
+      }
+    }
+  }
+  if (st) {
+    for (int c = 0; c < nq; c++) a.q0_bar[e * nq + c] = qb[c];
+    for (int c = 0; c < nv; c++) a.qd0_bar[e * nv + c] = qdb[c];
+  }
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) rollout_reverse3_kernel(const DModel* __restrict__ model, const RolloutArgs a) {
+  Team3 tm = team3_of_lane(threadIdx.x);
+  const int64_t e0 = int64_t(blockIdx.x) * 10 + tm.base / 3;
+  tm.valid = tm.valid && e0 < a.n;
+  rollout_reverse3_env<MAXJ>(RuntimeTab{model}, tm, a, e0 < a.n ? e0 : a.n - 1);
 }
 
 // Ten environments per warp; teams past the end of the batch repeat the last environment

@@ -425,3 +425,44 @@ def test_three_lane_rollout_forward_matches_one_lane_and_oracle(name):
         assert rel(qT, rq) < 1e-9 and rel(qdT, rqd) < 1e-9, key
         ref = outs[(0, 1)]
         assert rel(qc, ref[2]) < 1e-11 and rel(qdc, ref[3]) < 1e-11, key  # checkpoints
+
+
+@pytest.mark.parametrize("name", ["arm9", "mixed_chain", "chain40"])
+def test_three_lane_rollout_backward_matches_one_lane(name):
+    """The reverse sweep with one lane per Cartesian axis against one lane per environment,
+    on the allocating and the allocation-free entry points: same adjoints to rounding."""
+    import ctypes
+
+    import torch
+
+    from sapien_gb300 import _native as N
+
+    robot = ROLLOUT3[name]()
+    pm, _ = pair(robot)
+    n, steps, K, dt = 23, 40, 7, 1.0 / 500
+    q0, qd0, _, _ = robot.sample(n, seed=14)
+    tau = cu(np.random.default_rng(15).normal(scale=5.0, size=(steps, n, robot.nv)))
+    g = torch.Generator(device="cpu").manual_seed(2)
+    qTb = torch.randn(n, pm.nq_ext, generator=g, dtype=torch.float64).cuda()
+    qdTb = torch.randn(n, pm.nv, generator=g, dtype=torch.float64).cuda()
+    L = N.load()
+    outs = {}
+    try:
+        for lanes in (1, 3):
+            assert L.sgdyn_rollout_lanes(lanes, None) == N.OK
+            _, _, qc, qdc = ad.rollout_forward(pm, cu(q0), cu(qd0), tau, dt, K)
+            outs[lanes] = [x.cpu().numpy() for x in ad.rollout_backward(pm, qc, qdc, tau, dt, K, qTb, qdTb)]
+            if lanes == 3:
+                q0b = torch.empty(n, pm.nq_ext, dtype=torch.float64, device="cuda")
+                qd0b = torch.empty(n, pm.nv, dtype=torch.float64, device="cuda")
+                taub = torch.empty_like(tau)
+                p = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+                s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+                assert L.sgdyn_rollout_backward_noalloc(pm._h, n, steps, dt, K, p(qc), p(qdc), p(tau), p(qTb),
+                                                        p(qdTb), p(q0b), p(qd0b), p(taub), s) == N.OK, N.last_error()
+                outs["noalloc"] = [x.cpu().numpy() for x in (q0b, qd0b, taub)]
+    finally:
+        L.sgdyn_rollout_lanes(0, None)
+    for key in (3, "noalloc"):
+        for a, b in zip(outs[key], outs[1]):
+            assert rel(a, b) < 1e-10, key
