@@ -461,8 +461,8 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
 
 // ops > 0: the fused sweep with that op set; -1: the forward rollout kernel; -2 / -3: the
 // RNEA / ABA vector-Jacobian product kernels; -4: the forward rollout with three lanes per
-// environment
-static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -4 && ops <= -1); }
+// environment; -5: the backward's reverse sweep with three lanes per environment
+static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -5 && ops <= -1); }
 
 int sgdyn_rollout_lanes(int lanes, int* lanes_out) {
   if (lanes != -1 && lanes != 0 && lanes != 1 && lanes != 3)
@@ -485,7 +485,7 @@ int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
   std::string why;
   const bool ok = ops > 0     ? prepare_step_jit(*m->impl, ops, &why)
                   : ops == -1 ? prepare_rollout_jit(*m->impl, &why)
-                  : ops == -4 ? prepare_rollout3_jit(*m->impl, &why)
+                  : ops <= -4 ? prepare_rollout3_jit(*m->impl, ops == -5, &why)
                               : prepare_vjp_jit(*m->impl, ops == -3, &why);
   if (!ok) return fail(SGDYN_ERR_UNSUPPORTED, "run-time compilation unavailable: " + why);
   return SGDYN_OK;
@@ -497,7 +497,7 @@ int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
   thread_local std::string buf;
   buf = ops > 0     ? step_jit_source(*m->impl, ops)
         : ops == -1 ? rollout_jit_source(*m->impl)
-        : ops == -4 ? rollout3_jit_source(*m->impl)
+        : ops <= -4 ? rollout3_jit_source(*m->impl, ops == -5)
                     : vjp_jit_source(*m->impl, ops == -3);
   *source = buf.c_str();
   return SGDYN_OK;
@@ -849,8 +849,16 @@ namespace {
 // reverse sweep at small batches keeps one warp per SM busy and leaves the other FP64
 // schedulers idle; the recompute fills them. Groups alternate between two halves of the
 // scratch; a recompute waits for the reverse that last used its half.
-cudaError_t rollout_backward_overlapped(const DModel* dm, int nj, int lanes, RolloutArgs a, int64_t seg_doubles,
-                                        int G, cudaStream_t s1, cudaStream_t s2) {
+// The backward's reverse sweep with three lanes per environment: the model-specialised
+// kernel if run-time compilation serves it, else the generic one.
+cudaError_t reverse3(Model& M, const DModel* dm, int nj, const RolloutArgs& g, cudaStream_t s) {
+  std::string why;
+  if (launch_rollout_reverse3_jit(M, g, s, &why)) return cudaSuccess;
+  return launch_rollout_reverse3(dm, nj, g, s);
+}
+
+cudaError_t rollout_backward_overlapped(Model& M, const DModel* dm, int nj, int lanes, RolloutArgs a,
+                                        int64_t seg_doubles, int G, cudaStream_t s1, cudaStream_t s2) {
   const int nseg = (a.T + a.K - 1) / a.K;
   std::vector<RolloutArgs> groups;
   for (int hi = nseg; hi > 0; hi -= G) {
@@ -875,7 +883,7 @@ cudaError_t rollout_backward_overlapped(const DModel* dm, int nj, int lanes, Rol
   for (int k = 0; k < m && e == cudaSuccess; k++) {
     e = cudaStreamWaitEvent(s1, rec(k), 0);
     if (e == cudaSuccess)
-      e = lanes == 3 ? launch_rollout_reverse3(dm, nj, groups[k], s1) : launch_rollout_reverse(dm, nj, groups[k], s1);
+      e = lanes == 3 ? reverse3(M, dm, nj, groups[k], s1) : launch_rollout_reverse(dm, nj, groups[k], s1);
     if (e == cudaSuccess) e = cudaEventRecord(rev(k), s1);
     if (e == cudaSuccess && k + 1 < m) {
       if (k >= 1) e = cudaStreamWaitEvent(s2, rev(k - 1), 0);
@@ -932,16 +940,18 @@ int sgdyn_rollout_backward(const sgdyn_model* m, int64_t n, int T, double dt, in
     // reverse on two streams (not while the caller's stream is being captured)
     const int nseg = T > 0 ? (T + checkpoint_every - 1) / checkpoint_every : 0;
     const int64_t fit = need > 0 ? scratch_bytes / need : 0;
-    const int G = int(std::min<int64_t>(fit / 2, std::max(1, nseg / 5)));
+    // about as long a recompute of the next group as a reverse sweep of the current one:
+    // fifths of the segments for the one-lane reverse, halves for the three-lane one
+    const int G = int(std::min<int64_t>(fit / 2, std::max(1, lanes == 3 ? (nseg + 1) / 2 : nseg / 5)));
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusActive;
     if (nseg >= 2 && G >= 1 && (nseg + G - 1) / G >= 2 && cs == cudaStreamCaptureStatusNone)
       if (cudaStream_t s2 = side_stream())
-        return launch_status(rollout_backward_overlapped(dm, nj, lanes, a, need / 8, G, st, s2));
+        return launch_status(rollout_backward_overlapped(Mo, dm, nj, lanes, a, need / 8, G, st, s2));
     return launch_status(rollout_backward_grouped(
         a, need / 8, scratch_bytes / 8, [&](const RolloutArgs& g) { return launch_rollout_recompute(dm, nj, g, st); },
         [&](const RolloutArgs& g) {
-          return lanes == 3 ? launch_rollout_reverse3(dm, nj, g, st) : launch_rollout_reverse(dm, nj, g, st);
+          return lanes == 3 ? reverse3(Mo, dm, nj, g, st) : launch_rollout_reverse(dm, nj, g, st);
         }));
   });
 }

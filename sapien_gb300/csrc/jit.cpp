@@ -137,14 +137,17 @@ std::string list(It b, It e) {
 
 // The rollout's backward kernels stay generic: specialised, they came out slower (the
 // fully unrolled reverse sweep spills heavily).
-enum JitKind { JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_RNEA_VJP = 2, JIT_ABA_VJP = 3, JIT_ROLLOUT_FWD3 = 4 };
+enum JitKind {
+  JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_RNEA_VJP = 2, JIT_ABA_VJP = 3, JIT_ROLLOUT_FWD3 = 4, JIT_ROLLOUT_REV3 = 5
+};
 const char* kernel_name(int kind) {
-  static const char* const names[] = {"sgjit_step", "sgjit_rollout_forward", "sgjit_rnea_vjp", "sgjit_aba_vjp",
-                                      "sgjit_rollout_forward3"};
+  static const char* const names[] = {"sgjit_step",    "sgjit_rollout_forward",  "sgjit_rnea_vjp",
+                                      "sgjit_aba_vjp", "sgjit_rollout_forward3", "sgjit_rollout_reverse3"};
   return names[kind];
 }
+bool team3_kind(int kind) { return kind == JIT_ROLLOUT_FWD3 || kind == JIT_ROLLOUT_REV3; }
 // Environments per 32-thread block of each kernel kind.
-int envs_per_block(int kind) { return kind == JIT_ROLLOUT_FWD3 ? 10 : 32; }
+int envs_per_block(int kind) { return team3_kind(kind) ? 10 : 32; }
 
 std::string generate_source(const Model& M, int kind, int ops) {
   const auto& t = M.host_table();
@@ -153,9 +156,9 @@ std::string generate_source(const Model& M, int kind, int ops) {
   const DLink* L = model_links(hdr);
   const int nj = hdr->nj, nl = hdr->nlinks;
   std::ostringstream o;
-  o << (kind == JIT_STEP           ? "#include \"step_kernel.cuh\"\n"
-        : kind == JIT_ROLLOUT_FWD3 ? "#include \"team3.cuh\"\n"
-                                   : "#include \"diff_kernels.cuh\"\n");
+  o << (kind == JIT_STEP        ? "#include \"step_kernel.cuh\"\n"
+        : team3_kind(kind) ? "#include \"team3.cuh\"\n"
+                           : "#include \"diff_kernels.cuh\"\n");
   o << "namespace sgjit {\n";
   o << "__device__ constexpr sgdyn::DModel kM = {" << hdr->nj << ", " << hdr->nv << ", " << hdr->nq_ext << ", "
     << hdr->nlinks << ", " << hdr->max_depth << ", " << hdr->n_free_flyer << ", {0, 0}, {"
@@ -178,14 +181,15 @@ std::string generate_source(const Model& M, int kind, int ops) {
   const std::string tab = "sgdyn::StaticTab<" + std::to_string(nj) + ", " + std::to_string(hdr->nv) + ", " +
                           std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM>()";
   const char* args = kind == JIT_STEP                                      ? "sgdyn::StepArgs"
-                     : (kind == JIT_ROLLOUT_FWD || kind == JIT_ROLLOUT_FWD3) ? "sgdyn::RolloutArgs"
+                     : (kind == JIT_ROLLOUT_FWD || team3_kind(kind)) ? "sgdyn::RolloutArgs"
                                                                              : "sgdyn::VjpArgs";
   o << "extern \"C\" __global__ void __launch_bounds__(32) " << kernel_name(kind) << "(const " << args << " a) {\n";
-  if (kind == JIT_ROLLOUT_FWD3) {  // ten environments per warp, three lanes each (team3.cuh)
+  if (team3_kind(kind)) {  // ten environments per warp, three lanes each (team3.cuh)
     o << "  sgdyn::Team3 t = sgdyn::team3_of_lane(threadIdx.x);\n"
       << "  const long long e0 = (long long)blockIdx.x * 10 + t.base / 3;\n"
       << "  t.valid = t.valid && e0 < a.n;\n"
-      << "  sgdyn::rollout_forward3_env<" << nj << ">(" << tab << ", t, a, e0 < a.n ? e0 : a.n - 1);\n}\n";
+      << "  sgdyn::" << (kind == JIT_ROLLOUT_FWD3 ? "rollout_forward3_env" : "rollout_reverse3_env") << "<" << nj
+      << ">(" << tab << ", t, a, e0 < a.n ? e0 : a.n - 1);\n}\n";
     return o.str();
   }
   o << "  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n"
@@ -410,12 +414,18 @@ bool launch_rollout3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::st
   return launch_jit(M, JIT_ROLLOUT_FWD3, 0, a, s, why);
 }
 
-std::string rollout3_jit_source(const Model& M) { return generate_source(M, JIT_ROLLOUT_FWD3, 0); }
+bool launch_rollout_reverse3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why) {
+  return launch_jit(M, JIT_ROLLOUT_REV3, 0, a, s, why);
+}
 
-bool prepare_rollout3_jit(Model& M, std::string* why) {
+std::string rollout3_jit_source(const Model& M, bool reverse) {
+  return generate_source(M, reverse ? JIT_ROLLOUT_REV3 : JIT_ROLLOUT_FWD3, 0);
+}
+
+bool prepare_rollout3_jit(Model& M, bool reverse, std::string* why) {
   std::lock_guard<std::mutex> lk(g_mu);
   read_env_config();
-  return get_function(M, JIT_ROLLOUT_FWD3, 0, why) != nullptr;
+  return get_function(M, reverse ? JIT_ROLLOUT_REV3 : JIT_ROLLOUT_FWD3, 0, why) != nullptr;
 }
 
 bool launch_vjp_jit(Model& M, bool aba, const VjpArgs& a, cudaStream_t s, std::string* why) {

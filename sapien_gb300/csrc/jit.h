@@ -23,10 +23,12 @@ bool prepare_vjp_jit(Model& M, bool aba, std::string* why);
 bool launch_rollout_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why);
 std::string rollout_jit_source(const Model& M);
 bool prepare_rollout_jit(Model& M, std::string* why);
-// The forward rollout with three lanes per environment (team3.cuh).
+// The forward rollout and the backward's reverse sweep with three lanes per environment
+// (team3.cuh).
 bool launch_rollout3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why);
-std::string rollout3_jit_source(const Model& M);
-bool prepare_rollout3_jit(Model& M, std::string* why);
+bool launch_rollout_reverse3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why);
+std::string rollout3_jit_source(const Model& M, bool reverse);
+bool prepare_rollout3_jit(Model& M, bool reverse, std::string* why);
 // Compiles (or loads from the cache) now; false with the reason if not possible.
 bool prepare_step_jit(Model& M, int ops, std::string* why);
 void set_jit_config(int enable, int64_t min_n);

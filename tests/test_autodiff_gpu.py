@@ -447,11 +447,17 @@ def test_three_lane_rollout_backward_matches_one_lane(name):
     qdTb = torch.randn(n, pm.nv, generator=g, dtype=torch.float64).cuda()
     L = N.load()
     outs = {}
+    old_jit, old_min = ctypes.c_int(), ctypes.c_int64()
+    L.sgdyn_jit_config(-1, -1, ctypes.byref(old_jit), ctypes.byref(old_min))
     try:
         for lanes in (1, 3):
             assert L.sgdyn_rollout_lanes(lanes, None) == N.OK
             _, _, qc, qdc = ad.rollout_forward(pm, cu(q0), cu(qd0), tau, dt, K)
             outs[lanes] = [x.cpu().numpy() for x in ad.rollout_backward(pm, qc, qdc, tau, dt, K, qTb, qdTb)]
+            if lanes == 3:  # the run-time-compiled reverse sweep
+                L.sgdyn_jit_config(1, 0, None, None)
+                outs["jit"] = [x.cpu().numpy() for x in ad.rollout_backward(pm, qc, qdc, tau, dt, K, qTb, qdTb)]
+                L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
             if lanes == 3:
                 q0b = torch.empty(n, pm.nq_ext, dtype=torch.float64, device="cuda")
                 qd0b = torch.empty(n, pm.nv, dtype=torch.float64, device="cuda")
@@ -463,6 +469,7 @@ def test_three_lane_rollout_backward_matches_one_lane(name):
                 outs["noalloc"] = [x.cpu().numpy() for x in (q0b, qd0b, taub)]
     finally:
         L.sgdyn_rollout_lanes(0, None)
-    for key in (3, "noalloc"):
+        L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
+    for key in (3, "jit", "noalloc"):
         for a, b in zip(outs[key], outs[1]):
             assert rel(a, b) < 1e-10, key
