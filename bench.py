@@ -761,6 +761,18 @@ def main():
     S1 = min(n, 512)
     cpu1_dt, _ = time_median(lambda: o.batch_step(q_h[:S1], qd_h[:S1], qdd_h[:S1], tau_h[:S1], nthreads=1),
                              min_seconds=1.0)
+    # the product's own sweep compiled for the host (sgdyn_host_step, world-frame algebra),
+    # on the same cores: what a structured FP64 CPU implementation reaches, for context
+    hout = [np.empty((n, c)) for c in (nl * 7, 6 * nv, nv * nv, nv, nv)]
+    hin = [np.ascontiguousarray(a) for a in (q_h, qd_h, qdd_h, tau_h)]
+    hp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+
+    def host_step():
+        N.check(L.sgdyn_host_step(pm._h, n, N.OP_ALL, *[hp(a) for a in hin], *[hp(a) for a in hout], N.ENV_MAJOR,
+                                  cores))
+
+    host_step()
+    host_dt, host_reps = time_median(host_step)
     step(q, qd, qdd, tau)
     torch.cuda.synchronize()
 
@@ -797,7 +809,11 @@ def main():
         "cpu_baseline": {"value": S / cpu_dt, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"the whole workload ({S} envs) per step, median of {reps} repetitions (>= 2 s)",
                          "single_thread_value": S1 / cpu1_dt, "nproc": os.cpu_count(), "cpu_model": cpu_model(),
-                         "what": CPU_BASELINE_NOTE},
+                         "what": CPU_BASELINE_NOTE,
+                         "host_sweep_value": n / host_dt,
+                         "host_sweep": f"this library's sweep compiled for the host (sgdyn_host_step), {cores} threads, "
+                                       f"the whole workload, median of {host_reps} repetitions (>= 2 s); for context, "
+                                       "not the baseline"},
         "per_op_kernel": per_op,
         "max_rel_err_vs_oracle": errs,
         "clocks": clk,
