@@ -332,8 +332,10 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
                           const double* tau, int checkpoint_every, double* q_ckpt, double* qd_ckpt, double* qT,
                           double* qdT, void* stream);
 
-/* Lanes per environment of the rollout kernels, sgdyn_rollout_forward and the reverse sweep
- * of sgdyn_rollout_backward / _noalloc (addition): 0 automatic (the default:
+/* Lanes per environment of the ABA-based sweeps: sgdyn_rollout_forward, the reverse sweep
+ * of sgdyn_rollout_backward / _noalloc, and forward dynamics requested alone
+ * (sgdyn_compute_forward_dynamics, sgdyn_step with only SGDYN_OP_FORWARD_DYNAMICS)
+ * (addition): 0 automatic (the default:
  * three lanes while one warp per ten environments leaves no FP64 scheduler with two warps),
  * 1, or 3 (one lane per Cartesian axis of every spatial quantity, warp shuffles between
  * them, so each lane issues about half the FP64 instructions of one lane per environment;

@@ -131,8 +131,9 @@ int device_schedulers() {
   return schedulers;
 }
 
-// Lanes per environment of the forward rollout and of the backward's reverse sweep (the
-// recompute keeps one lane: all its segments run at once and fill the GPU): 1, or 3
+// Lanes per environment of the forward rollout, of the backward's reverse sweep (the
+// recompute keeps one lane: all its segments run at once and fill the GPU) and of forward
+// dynamics requested alone: 1, or 3
 // (team3.cuh: one lane per axis,
 // one-DoF joints only). The setting: 0 automatic (the default: three lanes while one warp
 // per ten environments leaves no FP64 scheduler with two warps), 1 or 3.
@@ -235,6 +236,12 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
   if (lanes > 1) {
     team = Mo.device_team(lanes, &err);
     if (!team) return fail(SGDYN_ERR_CUDA, "team table upload failed");
+  } else if (ops == OP_ABA && rollout_lanes(Mo, n) == 3) {  // forward dynamics alone on three lanes
+    std::string why;
+    if (launch_aba3_jit(Mo, a, s, &why)) return SGDYN_OK;
+    cudaError_t e = launch_aba3(dm, Mo.njoints(), a, s);
+    if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+    return SGDYN_OK;
   } else if (ops == OP_ALL && use_split(n)) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusActive;
@@ -461,8 +468,9 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
 
 // ops > 0: the fused sweep with that op set; -1: the forward rollout kernel; -2 / -3: the
 // RNEA / ABA vector-Jacobian product kernels; -4: the forward rollout with three lanes per
-// environment; -5: the backward's reverse sweep with three lanes per environment
-static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -5 && ops <= -1); }
+// environment; -5: the backward's reverse sweep with three lanes per environment; -6:
+// forward dynamics alone with three lanes per environment
+static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -6 && ops <= -1); }
 
 int sgdyn_rollout_lanes(int lanes, int* lanes_out) {
   if (lanes != -1 && lanes != 0 && lanes != 1 && lanes != 3)
@@ -485,6 +493,7 @@ int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
   std::string why;
   const bool ok = ops > 0     ? prepare_step_jit(*m->impl, ops, &why)
                   : ops == -1 ? prepare_rollout_jit(*m->impl, &why)
+                  : ops == -6 ? prepare_aba3_jit(*m->impl, &why)
                   : ops <= -4 ? prepare_rollout3_jit(*m->impl, ops == -5, &why)
                               : prepare_vjp_jit(*m->impl, ops == -3, &why);
   if (!ok) return fail(SGDYN_ERR_UNSUPPORTED, "run-time compilation unavailable: " + why);
@@ -497,6 +506,7 @@ int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
   thread_local std::string buf;
   buf = ops > 0     ? step_jit_source(*m->impl, ops)
         : ops == -1 ? rollout_jit_source(*m->impl)
+        : ops == -6 ? aba3_jit_source(*m->impl)
         : ops <= -4 ? rollout3_jit_source(*m->impl, ops == -5)
                     : vjp_jit_source(*m->impl, ops == -3);
   *source = buf.c_str();

@@ -38,6 +38,10 @@ cudaError_t launch_rollout_reverse3_j16(const DModel* dm, const RolloutArgs& a, 
   rollout_reverse3_kernel<16><<<unsigned((a.n + 9) / 10), 32, 0, s>>>(dm, a);
   return cudaGetLastError();
 }
+cudaError_t launch_aba3_j16(const DModel* dm, const StepArgs& a, cudaStream_t s) {
+  aba3_kernel<16><<<unsigned((a.n + 9) / 10), 32, 0, s>>>(dm, a);
+  return cudaGetLastError();
+}
 cudaError_t launch_rollout_recompute_j16(const DModel* dm, const RolloutArgs& a, cudaStream_t s) {
   rollout_recompute_kernel<16><<<unsigned((a.n * a.s_cnt + 31) / 32), 32, 0, s>>>(dm, a);
   return cudaGetLastError();

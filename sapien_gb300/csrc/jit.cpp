@@ -138,14 +138,16 @@ std::string list(It b, It e) {
 // The rollout's backward kernels stay generic: specialised, they came out slower (the
 // fully unrolled reverse sweep spills heavily).
 enum JitKind {
-  JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_RNEA_VJP = 2, JIT_ABA_VJP = 3, JIT_ROLLOUT_FWD3 = 4, JIT_ROLLOUT_REV3 = 5
+  JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_RNEA_VJP = 2, JIT_ABA_VJP = 3, JIT_ROLLOUT_FWD3 = 4, JIT_ROLLOUT_REV3 = 5,
+  JIT_ABA3 = 6
 };
 const char* kernel_name(int kind) {
   static const char* const names[] = {"sgjit_step",    "sgjit_rollout_forward",  "sgjit_rnea_vjp",
-                                      "sgjit_aba_vjp", "sgjit_rollout_forward3", "sgjit_rollout_reverse3"};
+                                      "sgjit_aba_vjp", "sgjit_rollout_forward3", "sgjit_rollout_reverse3",
+                                      "sgjit_aba3"};
   return names[kind];
 }
-bool team3_kind(int kind) { return kind == JIT_ROLLOUT_FWD3 || kind == JIT_ROLLOUT_REV3; }
+bool team3_kind(int kind) { return kind == JIT_ROLLOUT_FWD3 || kind == JIT_ROLLOUT_REV3 || kind == JIT_ABA3; }
 // Environments per 32-thread block of each kernel kind.
 int envs_per_block(int kind) { return team3_kind(kind) ? 10 : 32; }
 
@@ -180,7 +182,7 @@ std::string generate_source(const Model& M, int kind, int ops) {
   o << "};\n}  // namespace sgjit\n";
   const std::string tab = "sgdyn::StaticTab<" + std::to_string(nj) + ", " + std::to_string(hdr->nv) + ", " +
                           std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM>()";
-  const char* args = kind == JIT_STEP                                      ? "sgdyn::StepArgs"
+  const char* args = (kind == JIT_STEP || kind == JIT_ABA3)                 ? "sgdyn::StepArgs"
                      : (kind == JIT_ROLLOUT_FWD || team3_kind(kind)) ? "sgdyn::RolloutArgs"
                                                                              : "sgdyn::VjpArgs";
   o << "extern \"C\" __global__ void __launch_bounds__(32) " << kernel_name(kind) << "(const " << args << " a) {\n";
@@ -188,7 +190,9 @@ std::string generate_source(const Model& M, int kind, int ops) {
     o << "  sgdyn::Team3 t = sgdyn::team3_of_lane(threadIdx.x);\n"
       << "  const long long e0 = (long long)blockIdx.x * 10 + t.base / 3;\n"
       << "  t.valid = t.valid && e0 < a.n;\n"
-      << "  sgdyn::" << (kind == JIT_ROLLOUT_FWD3 ? "rollout_forward3_env" : "rollout_reverse3_env") << "<" << nj
+      << "  sgdyn::"
+      << (kind == JIT_ROLLOUT_FWD3 ? "rollout_forward3_env" : kind == JIT_ABA3 ? "aba3_env" : "rollout_reverse3_env")
+      << "<" << nj
       << ">(" << tab << ", t, a, e0 < a.n ? e0 : a.n - 1);\n}\n";
     return o.str();
   }
@@ -416,6 +420,18 @@ bool launch_rollout3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::st
 
 bool launch_rollout_reverse3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why) {
   return launch_jit(M, JIT_ROLLOUT_REV3, 0, a, s, why);
+}
+
+bool launch_aba3_jit(Model& M, const StepArgs& a, cudaStream_t s, std::string* why) {
+  return launch_jit(M, JIT_ABA3, 0, a, s, why);
+}
+
+std::string aba3_jit_source(const Model& M) { return generate_source(M, JIT_ABA3, 0); }
+
+bool prepare_aba3_jit(Model& M, std::string* why) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  return get_function(M, JIT_ABA3, 0, why) != nullptr;
 }
 
 std::string rollout3_jit_source(const Model& M, bool reverse) {

@@ -29,6 +29,10 @@ bool launch_rollout3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::st
 bool launch_rollout_reverse3_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why);
 std::string rollout3_jit_source(const Model& M, bool reverse);
 bool prepare_rollout3_jit(Model& M, bool reverse, std::string* why);
+// Forward dynamics alone with three lanes per environment (team3.cuh).
+bool launch_aba3_jit(Model& M, const StepArgs& a, cudaStream_t s, std::string* why);
+std::string aba3_jit_source(const Model& M);
+bool prepare_aba3_jit(Model& M, std::string* why);
 // Compiles (or loads from the cache) now; false with the reason if not possible.
 bool prepare_step_jit(Model& M, int ops, std::string* why);
 void set_jit_config(int enable, int64_t min_n);

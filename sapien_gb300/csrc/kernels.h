@@ -104,6 +104,8 @@ int stash_bucket(int nj);
 
 // Fused world-frame sweep: any subset of {FK poses, full WORLD Jacobian, CRBA, RNEA, ABA}.
 cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cudaStream_t s);
+// Forward dynamics alone with three lanes per environment (team3.cuh; one-DoF joints only).
+cudaError_t launch_aba3(const DModel* dm, int nj, const StepArgs& a, cudaStream_t s);
 // The same sweep with `lanes` lanes per environment (team table `team` on the device).
 cudaError_t launch_step_team(const DModel* dm, int nj, const int* team, int lanes, int ops, const StepArgs& a,
                              cudaStream_t s);

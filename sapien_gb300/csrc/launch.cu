@@ -105,6 +105,7 @@ SG_DISPATCH(rollout_forward3, RolloutArgs)
 SG_DISPATCH(rollout_recompute, RolloutArgs)
 SG_DISPATCH(rollout_reverse, RolloutArgs)
 SG_DISPATCH(rollout_reverse3, RolloutArgs)
+SG_DISPATCH(aba3, StepArgs)
 #undef SG_DISPATCH
 
 int64_t rollout_scratch_doubles_per_env(int nj, int nq, int nv, int K) {

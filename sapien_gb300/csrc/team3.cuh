@@ -266,6 +266,31 @@ __device__ __forceinline__ void rollout_forward3_env(const Tab& T, const Team3& 
   }
 }
 
+// Batched forward dynamics (computeForwardDynamics, pinocchio_model.cpp:221-226) with a team
+// of three lanes per environment: q, qd, tau read through the call's layout, lane 0 writes
+// qdd.
+template <int MAXJ, class Tab>
+__device__ __forceinline__ void aba3_env(const Tab& T, const Team3& tm, const StepArgs& a, const int64_t e) {
+  constexpr int MAXV = MAXJ + 5, MAXQ = MAXJ + 6;
+  const int nv = T.nv(), nq = T.nq_ext();
+  double q[MAXQ], qd[MAXV], tau[MAXV], qdd[MAXV];
+  for (int c = 0; c < nq; c++) q[c] = ldv(a.q, e, c);
+  for (int c = 0; c < nv; c++) qd[c] = ldv(a.qd, e, c);
+  for (int c = 0; c < nv; c++) tau[c] = ldv(a.tau, e, c);
+  Aba3Work<MAXJ> W;
+  aba3<MAXJ>(T, tm, q, qd, tau, qdd, W);
+  if (tm.valid && tm.k == 0)
+    for (int c = 0; c < nv; c++) stv(a.qdd_out, e, c, qdd[c]);
+}
+
+template <int MAXJ>
+__global__ void __launch_bounds__(32) aba3_kernel(const DModel* __restrict__ model, const StepArgs a) {
+  Team3 tm = team3_of_lane(threadIdx.x);
+  const int64_t e0 = int64_t(blockIdx.x) * 10 + tm.base / 3;
+  tm.valid = tm.valid && e0 < a.n;
+  aba3_env<MAXJ>(RuntimeTab{model}, tm, a, e0 < a.n ? e0 : a.n - 1);
+}
+
 // ---- reverse rollout with three lanes per environment ----------------------------------
 // The same reverse step as rollout_reverse_env (M^-1 solve through ABA's factorisation, then
 // the world-frame RNEA adjoint of diff_core.cuh, then the semi-implicit Euler adjoint), each

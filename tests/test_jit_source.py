@@ -1,7 +1,8 @@
 """The run-time-specialised kernels' generated source compiles with NVRTC for sm_103a (CPU
 test: NVRTC needs no GPU). ``ops`` > 0 selects the fused sweep with that op set, -1 the forward
-rollout kernel, -2 / -3 the RNEA / ABA vector-Jacobian product kernels, -4 / -5 the forward rollout
-and the backward's reverse sweep with three lanes per environment. GPU parity of the specialised kernels is in
+rollout kernel, -2 / -3 the RNEA / ABA vector-Jacobian product kernels, -4 / -5 / -6 the forward
+rollout, the backward's reverse sweep and forward dynamics alone with three lanes per
+environment. GPU parity of the specialised kernels is in
 test_jit_gpu.py."""
 import ctypes
 import ctypes.util
@@ -31,7 +32,7 @@ def _headers():
 
 @pytest.mark.parametrize("name,ops", [("arm9", 31), ("arm9", 3), ("humanoid", 28), ("mixed", 8), ("arm9", -1),
                                       ("mixed", -1), ("quadruped", -1), ("arm9", -2), ("humanoid", -3),
-                                      ("arm9", -4), ("mixed", -4), ("arm9", -5), ("chain40", -5)])
+                                      ("arm9", -4), ("mixed", -4), ("arm9", -5), ("chain40", -5), ("arm9", -6)])
 def test_generated_source_compiles(name, ops):
     robot = {"arm9": syn.arm_with_fingers(), "humanoid": syn.humanoid(), "quadruped": syn.quadruped(),
              "chain40": syn.serial_chain(40, seed=23),

@@ -473,3 +473,39 @@ def test_step_as_two_kinds_of_warps_matches_single_kind(name):
             tol = 1e-8 if k == "qacc" else 1e-10
             assert rel_per_env(g[k], w) <= tol, (key, k)
             assert rel_per_env(g[k], outs[(0, 0)][k]) <= (1e-11 if k == "qacc" else 1e-13), (key, k)
+
+
+@pytest.mark.parametrize("name", ["arm9", "arm9_sapien", "mixed_chain", "chain40"])
+def test_three_lane_forward_dynamics_matches_oracle(name):
+    """compute_forward_dynamics_batched on a small batch runs one team of three lanes per
+    environment (sgdyn_rollout_lanes automatic); forced one lane and three lanes, generic and
+    run-time compiled, against the oracle, env-major and structure-of-arrays."""
+    import ctypes
+
+    T = torch()
+    robot = ROBOTS[name]()
+    pm, o = pair(robot)
+    n = 57
+    q, qd, _, tau = robot.sample(n, seed=19)
+    ref = o.batch_step(q, qd, None, tau, ops=16, nthreads=8)["qdd"]
+    L = N.load()
+    old_jit, old_min = ctypes.c_int(), ctypes.c_int64()
+    L.sgdyn_jit_config(-1, -1, ctypes.byref(old_jit), ctypes.byref(old_min))
+    try:
+        for jit in (0, 1):
+            L.sgdyn_jit_config(jit, 0, None, None)
+            for lanes in (0, 1, 3):
+                assert L.sgdyn_rollout_lanes(lanes, None) == N.OK
+                t = lambda a: T.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+                g = pm.compute_forward_dynamics_batched(t(q), t(qd), t(tau)).cpu().numpy()
+                assert rel_per_env(g, ref) <= 1e-8, (jit, lanes)
+                # structure of arrays through the C ABI
+                qs, qds, taus = (t(a.T) for a in (q, qd, tau))
+                out = T.empty(robot.nv, n, dtype=T.float64, device="cuda")
+                P = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+                assert L.sgdyn_compute_forward_dynamics(pm._h, n, P(qs), P(qds), P(taus), P(out), N.COL_MAJOR,
+                                                        ctypes.c_void_p(T.cuda.current_stream().cuda_stream)) == N.OK
+                assert rel_per_env(out.cpu().numpy().T, ref) <= 1e-8, (jit, lanes, "soa")
+    finally:
+        L.sgdyn_rollout_lanes(0, None)
+        L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
