@@ -269,3 +269,9 @@ def test_random_configuration_refuses_free_flyer():
     pm.set_joint_order(r.joint_names)
     with pytest.raises(RuntimeError, match="free-flyer"):
         pm.get_random_configuration()
+
+
+def test_reference_module_name_is_kept():
+    from sapien_gb300 import pysapien_pinocchio
+
+    assert pysapien_pinocchio.PinocchioModel is PinocchioModel
