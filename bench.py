@@ -47,7 +47,7 @@ KERNEL_COUNTERS = {
     # where most of the 29 MB of results is still held in L2 when the launches end
     "specialised": {"fp64_inst_per_env": 2810368 * 32 / 16384, "dram_bytes_per_env": 9.82e6 / 16384},
 }
-KERNEL_SOURCE_SHA256 = "23d543a002d619cb51743756bf20c6e1e4843e5d593834b0c7cc6d6b98737431"
+KERNEL_SOURCE_SHA256 = "3dcc8129322c7717668e30b220c80cf83db5c965648e77de1c90f4c609c8eff6"
 KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
 STEP_OPS = (3, 28)  # sgdyn_step at N = 16384: FK + Jacobian beside CRBA + RNEA + ABA, two launches
 

@@ -339,7 +339,7 @@ int sgdyn_rollout_forward(const sgdyn_model* m, int64_t n, int T, double dt, con
  * three lanes while one warp per ten environments leaves no FP64 scheduler with two warps),
  * 1, or 3 (one lane per Cartesian axis of every spatial quantity, warp shuffles between
  * them, so each lane issues about half the FP64 instructions of one lane per environment;
- * one-DoF joints only, a model with a free flyer keeps one lane); -1 only reads the
+ * one-DoF joints and a free-flyer root); -1 only reads the
  * setting. Results agree to rounding. */
 int sgdyn_rollout_lanes(int lanes, int* lanes_out);
 

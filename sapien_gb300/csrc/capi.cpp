@@ -133,15 +133,14 @@ int device_schedulers() {
 
 // Lanes per environment of the forward rollout, of the backward's reverse sweep (the
 // recompute keeps one lane: all its segments run at once and fill the GPU) and of forward
-// dynamics requested alone: 1, or 3
-// (team3.cuh: one lane per axis,
-// one-DoF joints only). The setting: 0 automatic (the default: three lanes while one warp
-// per ten environments leaves no FP64 scheduler with two warps), 1 or 3.
+// dynamics requested alone: 1, or 3 (team3.cuh: one lane per axis; one-DoF joints and a
+// free-flyer root). The setting: 0 automatic (the default: three lanes while one warp per ten
+// environments leaves no FP64 scheduler with two warps), 1 or 3.
 std::atomic<int> g_rollout_lanes{0};
 
 int rollout_lanes(const Model& M, int64_t n) {
   for (auto& J : M.joints)
-    if (J.kind == JK_FREEFLYER) return 1;
+    if (J.kind == JK_FREEFLYER && J.parent != 0) return 1;  // a free flyer only as the root
   const int mode = g_rollout_lanes.load();
   if (mode != 0) return mode;
   return (n + 9) / 10 <= int64_t(device_schedulers()) ? 3 : 1;

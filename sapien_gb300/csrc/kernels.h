@@ -104,7 +104,8 @@ int stash_bucket(int nj);
 
 // Fused world-frame sweep: any subset of {FK poses, full WORLD Jacobian, CRBA, RNEA, ABA}.
 cudaError_t launch_step(const DModel* dm, int nj, int ops, const StepArgs& a, cudaStream_t s);
-// Forward dynamics alone with three lanes per environment (team3.cuh; one-DoF joints only).
+// Forward dynamics alone with three lanes per environment (team3.cuh; one-DoF joints and a
+// free-flyer root).
 cudaError_t launch_aba3(const DModel* dm, int nj, const StepArgs& a, cudaStream_t s);
 // The same sweep with `lanes` lanes per environment (team table `team` on the device).
 cudaError_t launch_step_team(const DModel* dm, int nj, const int* team, int lanes, int ops, const StepArgs& a,
@@ -118,11 +119,13 @@ cudaError_t launch_fk_vjp(const DModel* dm, int nj, const FkVjpArgs& a, cudaStre
 cudaError_t launch_rnea_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
 cudaError_t launch_aba_derivatives(const DModel* dm, int nj, const DerivArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_forward(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
-// The forward rollout with three lanes per environment (team3.cuh; one-DoF joints only).
+// The forward rollout with three lanes per environment (team3.cuh; one-DoF joints and a
+// free-flyer root).
 cudaError_t launch_rollout_forward3(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_recompute(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 cudaError_t launch_rollout_reverse(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
-// The reverse rollout with three lanes per environment (team3.cuh; one-DoF joints only).
+// The reverse rollout with three lanes per environment (team3.cuh; one-DoF joints and a
+// free-flyer root).
 cudaError_t launch_rollout_reverse3(const DModel* dm, int nj, const RolloutArgs& a, cudaStream_t s);
 // Fields: S, P, Q: 6 per tree column; v, a, F, H: 6 per joint; Ib, Db: 10 per joint
 // (m, h, I xx xy xz yy yz zz); L: the packed factor (nv (nv + 1) / 2), Dinv: nv (ABA only).

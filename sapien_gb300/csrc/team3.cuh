@@ -16,8 +16,9 @@
 // The recursions are those of aba_forward (world-frame ABA): pass 1 poses, motion subspaces,
 // world inertias, velocities and bias forces; pass 2 articulated inertias
 // IA_p += IA - U D^-1 U^T, pA_p += pA + Ia c + U D^-1 u; pass 3 accelerations
-// (pinocchio_model.cpp:221-226). Joints with one degree of freedom only; a model with a
-// free flyer keeps the one-lane kernels.
+// (pinocchio_model.cpp:221-226). Joints with one degree of freedom, plus a free-flyer root:
+// its six motion-subspace columns are distributed like any motion, and its 6x6 D = S^T IA S
+// is factored (chol6) identically on the three lanes.
 #pragma once
 #include "kernels.h"
 #include "spatial.cuh"
@@ -75,6 +76,8 @@ struct Aba3Work {
   double vl[MAXJ], va[MAXJ], cl[MAXJ], ca[MAXJ], pl[MAXJ], pa[MAXJ], al[MAXJ], aa[MAXJ];
   V3 A[MAXJ], B[MAXJ], BT[MAXJ], C[MAXJ];  // articulated inertia [[A, B], [B^T, C]], row k
   double Ul[MAXJ], Ua[MAXJ], u[MAXJ], Dinv[MAXJ];
+  // free-flyer root: its six subspace columns, U = IA S, u, and the Cholesky factor of D
+  double Sl6[6], Sa6[6], Ul6[6], Ua6[6], u6[6], Lff[21];
 };
 
 // World-frame ABA of one environment on a team: qdd (external order) from q, qd, tau, all
@@ -96,7 +99,16 @@ __device__ __forceinline__ void aba3(const Tab& T, const Team3& tm, const double
     V3 Ro;      // row k of this joint's world rotation
     double po;  // component k of its world position
     double u;   // component k of its world axis
-    if (J.axis_kind == AX_Z) {
+    const bool ff = J.kind == JK_FREEFLYER;  // the root (p == 0), as the host checks
+    if (ff) {
+      const int c0 = J.qcol;
+      const M3 RJ = quat_to_R(q[c0 + 3], q[c0 + 4], q[c0 + 5], q[c0 + 6]);
+      const V3 t = mk(q[c0], q[c0 + 1], q[c0 + 2]);
+      const V3 rk = rot_id ? ek : row_of(J.R, k);  // row k of the placement rotation
+      Ro = row_mul(rk, row_of(RJ.a, 0), row_of(RJ.a, 1), row_of(RJ.a, 2));
+      po = fma(rk.z, t.z, fma(rk.y, t.y, fma(rk.x, t.x, tm.pick(ppl))));
+      u = 0.0;
+    } else if (J.axis_kind == AX_Z) {
       const V3 B = rot_id ? Rp : row_mul(Rp, row_of(J.R, 0), row_of(J.R, 1), row_of(J.R, 2));
       const double o = p == 0 ? tm.pick(ppl) : fma(Rp.z, ppl.z, fma(Rp.y, ppl.y, fma(Rp.x, ppl.x, W.op[p])));
       if (J.kind == JK_PRISMATIC) {
@@ -137,12 +149,33 @@ __device__ __forceinline__ void aba3(const Tab& T, const Team3& tm, const double
     W.oR[i] = Ro;
     W.op[i] = po;
     double Sl, Sa;
-    if (J.kind == JK_PRISMATIC) {
-      Sl = u;
-      Sa = 0.0;
+    double vJl, vJa;
+    if (ff) {  // columns (Ro e_c, 0) and (po x Ro e_c, Ro e_c); component k of Ro e_c is Ro[k][c]
+      const double r[3] = {Ro.x, Ro.y, Ro.z};
+      vJl = vJa = 0.0;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        W.Sl6[c] = r[c];
+        W.Sa6[c] = 0.0;
+        W.Sl6[3 + c] = tm.cross(po, r[c]);
+        W.Sa6[3 + c] = r[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 6; c++) {
+        vJl = fma(qd[J.vcol + c], W.Sl6[c], vJl);
+        vJa = fma(qd[J.vcol + c], W.Sa6[c], vJa);
+      }
+      Sl = Sa = 0.0;
     } else {
-      Sl = tm.cross(po, u);
-      Sa = u;
+      if (J.kind == JK_PRISMATIC) {
+        Sl = u;
+        Sa = 0.0;
+      } else {
+        Sl = tm.cross(po, u);
+        Sa = u;
+      }
+      vJl = qd[J.vcol] * Sl;
+      vJa = qd[J.vcol] * Sa;
     }
     W.Sl[i] = Sl;
     W.Sa[i] = Sa;
@@ -162,8 +195,6 @@ __device__ __forceinline__ void aba3(const Tab& T, const Team3& tm, const double
     Ik.y = fma(-hr, pv.y, fma(-po, sv.y, dot(Tk, R1) + (k == 1 ? d : 0.0)));
     Ik.z = fma(-hr, pv.z, fma(-po, sv.z, dot(Tk, R2) + (k == 2 ? d : 0.0)));
     // velocity, momentum (f, n) = Y v, bias force v x* Y v, velocity-product acceleration
-    const double qdi = qd[J.vcol];
-    const double vJl = qdi * Sl, vJa = qdi * Sa;
     const double vl = p == 0 ? vJl : W.vl[p] + vJl;
     const double va = p == 0 ? vJa : W.va[p] + vJa;
     W.vl[i] = vl;
@@ -186,8 +217,23 @@ __device__ __forceinline__ void aba3(const Tab& T, const Team3& tm, const double
   for (int i = nj - 1; i >= 1; i--) {
     const DJoint& J = T.joint(i);
     const int p = J.parent;
-    const V3 Slv = tm.all(W.Sl[i]), Sav = tm.all(W.Sa[i]);
     const V3 A = W.A[i], B = W.B[i], BT = W.BT[i], C = W.C[i];
+    if (J.kind == JK_FREEFLYER) {  // root: U = IA S per column, D = S^T U factored, u
+#pragma unroll
+      for (int c = 0; c < 6; c++) {
+        const V3 Slv = tm.all(W.Sl6[c]), Sav = tm.all(W.Sa6[c]);
+        W.Ul6[c] = dot(A, Slv) + dot(B, Sav);
+        W.Ua6[c] = dot(BT, Slv) + dot(C, Sav);
+        W.u6[c] = tau[J.vcol + c] - tm.sum(fma(W.Sl6[c], W.pl[i], W.Sa6[c] * W.pa[i]));
+      }
+#pragma unroll
+      for (int r = 0; r < 6; r++)
+#pragma unroll
+        for (int c = 0; c <= r; c++) W.Lff[r * (r + 1) / 2 + c] = tm.sum(fma(W.Sl6[r], W.Ul6[c], W.Sa6[r] * W.Ua6[c]));
+      chol6(W.Lff);
+      continue;
+    }
+    const V3 Slv = tm.all(W.Sl[i]), Sav = tm.all(W.Sa[i]);
     const double Ul = dot(A, Slv) + dot(B, Sav);
     const double Ua = dot(BT, Slv) + dot(C, Sav);
     const double D = tm.sum(fma(W.Sl[i], Ul, W.Sa[i] * Ua));
@@ -223,6 +269,21 @@ __device__ __forceinline__ void aba3(const Tab& T, const Team3& tm, const double
     const int p = J.parent;
     double al = (p == 0 ? gk : W.al[p]) + W.cl[i];
     double aa = (p == 0 ? 0.0 : W.aa[p]) + W.ca[i];
+    if (J.kind == JK_FREEFLYER) {
+      double b[6];
+#pragma unroll
+      for (int c = 0; c < 6; c++) b[c] = W.u6[c] - tm.sum(fma(W.Ul6[c], al, W.Ua6[c] * aa));
+      chol6_solve(W.Lff, b);
+#pragma unroll
+      for (int c = 0; c < 6; c++) {
+        al = fma(b[c], W.Sl6[c], al);
+        aa = fma(b[c], W.Sa6[c], aa);
+        qdd[J.vcol + c] = b[c];
+      }
+      W.al[i] = al;
+      W.aa[i] = aa;
+      continue;
+    }
     const double x = W.Dinv[i] * (W.u[i] - tm.sum(fma(W.Ul[i], al, W.Ua[i] * aa)));
     al = fma(x, W.Sl[i], al);
     aa = fma(x, W.Sa[i], aa);
@@ -254,11 +315,7 @@ __device__ __forceinline__ void rollout_forward3_env(const Tab& T, const Team3& 
     for (int c = 0; c < nv; c++) tau[c] = a.tau[(int64_t(t) * n + e) * nv + c];
     aba3<MAXJ>(T, tm, q, qd, tau, qdd, W);
     for (int c = 0; c < nv; c++) qd[c] = fma(a.dt, qdd[c], qd[c]);
-#pragma unroll
-    for (int i = 1; i < T.nj(); i++) {
-      const DJoint& J = T.joint(i);
-      q[J.qcol] = fma(a.dt, qd[J.vcol], q[J.qcol]);
-    }
+    euler_positions(T, q, qd, a.dt);  // a free flyer moves on SE(3), identically on the lanes
   }
   if (st) {
     for (int c = 0; c < nq; c++) a.qT[e * nq + c] = q[c];
@@ -306,6 +363,9 @@ struct Rev3Work {
   // scratch of the solve and of the adjoint sweep
   double us[MAXJ], xl[MAXJ], xa[MAXJ];
   double wl[MAXJ], wa[MAXJ], Pl[MAXJ], Pa[MAXJ], Ql[MAXJ], Qa[MAXJ], Rl[MAXJ], Ra[MAXJ], Tl[MAXJ], Ta[MAXJ];
+  // free-flyer root: its six subspace columns and U, the Cholesky factor of its D, the
+  // step's displacement dt qd' and the solve's u
+  double Sl6[6], Sa6[6], Ul6[6], Ua6[6], Lff[21], ffd[6], us6[6];
 };
 
 // Component k of x x* f = (x_ang x f_lin, x_ang x f_ang + x_lin x f_lin).
@@ -343,21 +403,31 @@ __device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& 
     for (int t = t1 - 1; t >= t0; t--) {
       const double* base = a.scratch + (int64_t(s - a.s_lo) * a.K + (t - t0)) * per_step * n;
       auto ld = [&](int64_t f) { return base[f * n + e]; };
-      // q' = q + dt qd' and qd' = qd + dt qdd, reversed: qdd_bar = dt qd'_bar
-#pragma unroll
-      for (int i = 1; i < nj; i++) {
-        const DJoint& J = T.joint(i);
-        qdb[J.vcol] = fma(a.dt, qb[J.qcol], qdb[J.vcol]);
-      }
       // this lane's components of the stored intermediates (stash_io's layout)
 #pragma unroll
       for (int i = 1; i < nj; i++) {
         const int iv = T.joint(i).ivx;
         const int64_t jb = 12 * int64_t(nv) + int64_t(i - 1) * 35;
-        W.Sl[i] = ld(6 * iv + k);
-        W.Sa[i] = ld(6 * iv + 3 + k);
-        W.Ul[i] = ld(6 * nv + 6 * iv + k);
-        W.Ua[i] = ld(6 * nv + 6 * iv + 3 + k);
+        if (T.joint(i).kind == JK_FREEFLYER) {
+#pragma unroll
+          for (int c = 0; c < 6; c++) {
+            W.Sl6[c] = ld(6 * (iv + c) + k);
+            W.Sa6[c] = ld(6 * (iv + c) + 3 + k);
+            W.Ul6[c] = ld(6 * nv + 6 * (iv + c) + k);
+            W.Ua6[c] = ld(6 * nv + 6 * (iv + c) + 3 + k);
+          }
+          const int64_t tb = 12 * int64_t(nv) + int64_t(nj - 1) * 35;
+#pragma unroll
+          for (int c = 0; c < 21; c++) W.Lff[c] = ld(tb + c);
+#pragma unroll
+          for (int c = 0; c < 6; c++) W.ffd[c] = ld(tb + 21 + c);
+          W.Sl[i] = W.Sa[i] = W.Ul[i] = W.Ua[i] = 0.0;
+        } else {
+          W.Sl[i] = ld(6 * iv + k);
+          W.Sa[i] = ld(6 * iv + 3 + k);
+          W.Ul[i] = ld(6 * nv + 6 * iv + k);
+          W.Ua[i] = ld(6 * nv + 6 * iv + 3 + k);
+        }
         W.Dinv[i] = ld(jb);
         W.vl[i] = ld(jb + 1 + k);
         W.va[i] = ld(jb + 4 + k);
@@ -373,6 +443,25 @@ __device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& 
         W.Fl[i] = ld(jb + 29 + k);
         W.Fa[i] = ld(jb + 32 + k);
       }
+      // q' = q (+) dt qd' and qd' = qd + dt qdd, reversed: qdd_bar = dt qd'_bar; a free
+      // flyer's block of qb holds its tangent adjoint (identically on the three lanes)
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+        if (J.kind != JK_FREEFLYER) {
+          qdb[J.vcol] = fma(a.dt, qb[J.qcol], qdb[J.vcol]);
+          continue;
+        }
+        const int qc = J.qcol, vc = J.vcol;
+        const Mot g{mk(qb[qc], qb[qc + 1], qb[qc + 2]), mk(qb[qc + 3], qb[qc + 4], qb[qc + 5])};
+        Mot vb{mk(qdb[vc], qdb[vc + 1], qdb[vc + 2]), mk(qdb[vc + 3], qdb[vc + 4], qdb[vc + 5])};
+        const Mot gq = free_flyer_integrate_adjoint(
+            Mot{mk(W.ffd[0], W.ffd[1], W.ffd[2]), mk(W.ffd[3], W.ffd[4], W.ffd[5])}, g, a.dt, vb);
+        qb[qc] = gq.v.x; qb[qc + 1] = gq.v.y; qb[qc + 2] = gq.v.z;
+        qb[qc + 3] = gq.w.x; qb[qc + 4] = gq.w.y; qb[qc + 5] = gq.w.z;
+        qdb[vc] = vb.v.x; qdb[vc + 1] = vb.v.y; qdb[vc + 2] = vb.v.z;
+        qdb[vc + 3] = vb.w.x; qdb[vc + 4] = vb.w.y; qdb[vc + 5] = vb.w.z;
+      }
       // lam = M^-1 (dt qd'_bar): the ABA recursion with zero velocity and gravity
 #pragma unroll
       for (int i = 1; i < nj; i++) W.xl[i] = W.xa[i] = 0.0;
@@ -380,6 +469,12 @@ __device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& 
       for (int i = nj - 1; i >= 1; i--) {
         const DJoint& J = T.joint(i);
         const int p = J.parent;
+        if (J.kind == JK_FREEFLYER) {  // the root: no parent to pass to
+#pragma unroll
+          for (int c = 0; c < 6; c++)
+            W.us6[c] = a.dt * qdb[J.vcol + c] - tm.sum(fma(W.Sl6[c], W.xl[i], W.Sa6[c] * W.xa[i]));
+          continue;
+        }
         const double u = a.dt * qdb[J.vcol] - tm.sum(fma(W.Sl[i], W.xl[i], W.Sa[i] * W.xa[i]));
         W.us[i] = u;
         if (p > 0) {
@@ -393,6 +488,22 @@ __device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& 
         const DJoint& J = T.joint(i);
         const int p = J.parent;
         const double pl = p == 0 ? 0.0 : W.xl[p], pa = p == 0 ? 0.0 : W.xa[p];
+        if (J.kind == JK_FREEFLYER) {  // the root: zero parent acceleration
+          double b[6];
+#pragma unroll
+          for (int c = 0; c < 6; c++) b[c] = W.us6[c];
+          chol6_solve(W.Lff, b);
+          double xl = 0.0, xa = 0.0;
+#pragma unroll
+          for (int c = 0; c < 6; c++) {
+            xl = fma(b[c], W.Sl6[c], xl);
+            xa = fma(b[c], W.Sa6[c], xa);
+            lam[J.vcol + c] = b[c];
+          }
+          W.xl[i] = xl;
+          W.xa[i] = xa;
+          continue;
+        }
         const double z = W.Dinv[i] * (W.us[i] - tm.sum(fma(W.Ul[i], pl, W.Ua[i] * pa)));
         W.xl[i] = fma(z, W.Sl[i], pl);  // accelerations of the solve (the bias forces are spent)
         W.xa[i] = fma(z, W.Sa[i], pa);
@@ -405,9 +516,19 @@ __device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& 
       for (int i = 1; i < nj; i++) {
         const DJoint& J = T.joint(i);
         const int p = J.parent;
-        const double x = lam[J.vcol];
-        const double wl = p == 0 ? x * W.Sl[i] : fma(x, W.Sl[i], W.wl[p]);
-        const double wa = p == 0 ? x * W.Sa[i] : fma(x, W.Sa[i], W.wa[p]);
+        double wl, wa;
+        if (J.kind == JK_FREEFLYER) {  // the root
+          wl = wa = 0.0;
+#pragma unroll
+          for (int c = 0; c < 6; c++) {
+            wl = fma(lam[J.vcol + c], W.Sl6[c], wl);
+            wa = fma(lam[J.vcol + c], W.Sa6[c], wa);
+          }
+        } else {
+          const double x = lam[J.vcol];
+          wl = p == 0 ? x * W.Sl[i] : fma(x, W.Sl[i], W.wl[p]);
+          wa = p == 0 ? x * W.Sa[i] : fma(x, W.Sa[i], W.wa[p]);
+        }
         W.wl[i] = wl;
         W.wa[i] = wa;
         double Pl, Pa, Ql, Qa, Rl, Ra, cl, ca, Tl, Ta;
@@ -440,13 +561,19 @@ __device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& 
         crossf3(tm, Wll, Wla, W.Fl[j], W.Fa[j], zl, za);
         Gl = Gl - yl - zl;
         Ga = Ga - ya - za;
-        const double o1 = -tm.sum(fma(W.Sl[j], Gl, W.Sa[j] * Ga));
         // Gd = Q - (v_parent + v) x* P - R - T
         crossf3(tm, vll + W.vl[j], vla + W.va[j], Pl, Pa, yl, ya);
         const double Gdl = Ql - yl - (Rl + Tl), Gda = Qa - ya - (Ra + Ta);
-        const double o2 = -tm.sum(fma(W.Sl[j], Gdl, W.Sa[j] * Gda));
-        qb[J.qcol] += o1;
-        qdb[J.vcol] += o2;
+        if (J.kind == JK_FREEFLYER) {
+#pragma unroll
+          for (int c = 0; c < 6; c++) {
+            qb[J.qcol + c] -= tm.sum(fma(W.Sl6[c], Gl, W.Sa6[c] * Ga));
+            qdb[J.vcol + c] -= tm.sum(fma(W.Sl6[c], Gdl, W.Sa6[c] * Gda));
+          }
+        } else {
+          qb[J.qcol] -= tm.sum(fma(W.Sl[j], Gl, W.Sa[j] * Ga));
+          qdb[J.vcol] -= tm.sum(fma(W.Sl[j], Gdl, W.Sa[j] * Gda));
+        }
         if (p > 0) {
           W.Pl[p] += Pl; W.Pa[p] += Pa; W.Ql[p] += Ql; W.Qa[p] += Qa;
           W.Rl[p] += Rl; W.Ra[p] += Ra; W.Tl[p] += Tl; W.Ta[p] += Ta;
@@ -454,6 +581,8 @@ __device__ __forceinline__ void rollout_reverse3_env(const Tab& T, const Team3& 
       }
     }
   }
+  for (int i = 1; i < nj; i++)
+    if (T.joint(i).kind == JK_FREEFLYER) qb[T.joint(i).qcol + 6] = 0.0;
   if (st) {
     for (int c = 0; c < nq; c++) a.q0_bar[e * nq + c] = qb[c];
     for (int c = 0; c < nv; c++) a.qd0_bar[e * nv + c] = qdb[c];

@@ -390,6 +390,8 @@ ROLLOUT3 = {
     "mixed_chain": lambda: syn.serial_chain(6, seed=11, kinds=["revolute", "continuous", "prismatic", "revolute",
                                                                 "continuous", "prismatic"]),
     "chain40": lambda: syn.serial_chain(40, seed=23),
+    "quadruped18": lambda: syn.quadruped(),
+    "humanoid": lambda: syn.humanoid(),
 }
 
 
@@ -427,10 +429,11 @@ def test_three_lane_rollout_forward_matches_one_lane_and_oracle(name):
         assert rel(qc, ref[2]) < 1e-11 and rel(qdc, ref[3]) < 1e-11, key  # checkpoints
 
 
-@pytest.mark.parametrize("name", ["arm9", "mixed_chain", "chain40"])
+@pytest.mark.parametrize("name", ["arm9", "mixed_chain", "chain40", "quadruped18", "humanoid"])
 def test_three_lane_rollout_backward_matches_one_lane(name):
     """The reverse sweep with one lane per Cartesian axis against one lane per environment,
-    on the allocating and the allocation-free entry points: same adjoints to rounding."""
+    on the allocating and the allocation-free entry points: same adjoints to rounding (for
+    a free-flyer root its tangent adjoint, the seventh slot zero)."""
     import ctypes
 
     import torch
@@ -473,3 +476,5 @@ def test_three_lane_rollout_backward_matches_one_lane(name):
     for key in (3, "jit", "noalloc"):
         for a, b in zip(outs[key], outs[1]):
             assert rel(a, b) < 1e-10, key
+    if robot.nq_ext > robot.nv:
+        assert all((outs[key][0][:, 6] == 0).all() for key in outs)

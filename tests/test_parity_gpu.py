@@ -475,7 +475,8 @@ def test_step_as_two_kinds_of_warps_matches_single_kind(name):
             assert rel_per_env(g[k], outs[(0, 0)][k]) <= (1e-11 if k == "qacc" else 1e-13), (key, k)
 
 
-@pytest.mark.parametrize("name", ["arm9", "arm9_sapien", "mixed_chain", "chain40"])
+@pytest.mark.parametrize("name", ["arm9", "arm9_sapien", "mixed_chain", "chain40", "quadruped18", "humanoid",
+                                  "humanoid_sapien"])
 def test_three_lane_forward_dynamics_matches_oracle(name):
     """compute_forward_dynamics_batched on a small batch runs one team of three lanes per
     environment (sgdyn_rollout_lanes automatic); forced one lane and three lanes, generic and
