@@ -42,12 +42,13 @@ WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs p
 # kernel source whose digest is KERNEL_SOURCE_SHA256 (kernel_source_digest()); a CPU test
 # fails when the source changes, so the figures are re-captured with every kernel change.
 KERNEL_COUNTERS = {
-    # two launches (FK + Jacobian: 507,392 FP64 warp instructions; CRBA + RNEA + ABA:
-    # 2,302,976) per 16384 environments; DRAM bytes as ncu counted them in a cold capture,
-    # where most of the 29 MB of results is still held in L2 when the launches end
-    "specialised": {"fp64_inst_per_env": 2810368 * 32 / 16384, "dram_bytes_per_env": 9.82e6 / 16384},
+    # two launches (FK + Jacobian: 507,392 FP64 warp instructions; CRBA + RNEA + ABA with
+    # forward dynamics from the mass matrix: 1,650,688) per 16384 environments; DRAM bytes as
+    # ncu counted them in a cold capture, where most of the 29 MB of results is still held in
+    # L2 when the launches end
+    "specialised": {"fp64_inst_per_env": 2158080 * 32 / 16384, "dram_bytes_per_env": 8.49e6 / 16384},
 }
-KERNEL_SOURCE_SHA256 = "3dcc8129322c7717668e30b220c80cf83db5c965648e77de1c90f4c609c8eff6"
+KERNEL_SOURCE_SHA256 = "5c2ee71c2497e87ecbe3aaad69449d53424a007e007222a35f21e480332d1888"
 KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
 STEP_OPS = (3, 28)  # sgdyn_step at N = 16384: FK + Jacobian beside CRBA + RNEA + ABA, two launches
 

@@ -203,6 +203,15 @@ int sgdyn_model_team_table(const sgdyn_model* m, int lanes, const int** data, in
 int sgdyn_jit_config(int enable, int64_t min_n, int* enabled, int64_t* min_n_out);
 /* Size limit of run-time specialisation (joints incl. the universe; < 0 leaves it). */
 int sgdyn_jit_max_joints(int max_joints, int* max_joints_out);
+/* How the run-time-specialised sweep computes forward dynamics (addition): 0 automatic (the
+ * default: the route with fewer FP64 operations for the model and op set), 1 the
+ * articulated-body passes (ABA), 2 from the mass matrix (CRBA, the bias forces by RNEA at
+ * zero acceleration, M = L^T D L with the tree's sparsity, qdd = M^-1 (tau - b); inverse
+ * dynamics in the same sweep then reads tau = b + M qdd); -1 only reads the setting.
+ * Results agree to rounding. The generic kernels always run the articulated-body passes. */
+int sgdyn_fd_method(int mode, int* mode_out);
+/* Whether the specialised sweep for (model, ops) takes the mass-matrix route (*yes = 1). */
+int sgdyn_fd_by_mass_matrix(const sgdyn_model* m, int ops, int* yes);
 int sgdyn_jit_prepare(const sgdyn_model* m, int ops);
 /* The generated translation unit for (model, ops); valid until the next call on this thread. */
 int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source);

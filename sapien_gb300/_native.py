@@ -73,6 +73,8 @@ EXPORTED = (
     "sgdyn_model_set_lanes",
     "sgdyn_model_team_table",
     "sgdyn_jit_max_joints",
+    "sgdyn_fd_method",
+    "sgdyn_fd_by_mass_matrix",
     "sgdyn_jit_config",
     "sgdyn_jit_prepare",
     "sgdyn_jit_source",
@@ -161,6 +163,8 @@ def load():
     L.sgdyn_model_set_lanes.argtypes = [vp, i32]
     L.sgdyn_model_team_table.argtypes = [vp, i32, P(P(i32)), P(i32)]
     L.sgdyn_jit_max_joints.argtypes = [i32, P(i32)]
+    L.sgdyn_fd_method.argtypes = [i32, P(i32)]
+    L.sgdyn_fd_by_mass_matrix.argtypes = [vp, i32, P(i32)]
     L.sgdyn_jit_prepare.argtypes = [vp, i32]
     L.sgdyn_jit_source.argtypes = [vp, i32, P(ctypes.c_char_p)]
     L.sgdyn_rollout_backward_noalloc.argtypes = [vp, i64, i32, dbl, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]

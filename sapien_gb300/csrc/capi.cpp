@@ -451,6 +451,19 @@ int sgdyn_jit_max_joints(int max_joints, int* max_joints_out) {
   return SGDYN_OK;
 }
 
+int sgdyn_fd_method(int mode, int* mode_out) {
+  if (mode != -1 && (mode < 0 || mode > 2)) return fail(SGDYN_ERR_RUNTIME, "forward-dynamics method must be -1, 0, 1 or 2");
+  fd_method(mode, mode_out);
+  return SGDYN_OK;
+}
+
+int sgdyn_fd_by_mass_matrix(const sgdyn_model* m, int ops, int* yes) {
+  if (int rc = check_model(m)) return rc;
+  if (!yes) return fail(SGDYN_ERR_NULL, "null argument");
+  *yes = fd_by_mass_matrix(*m->impl, ops) ? 1 : 0;
+  return SGDYN_OK;
+}
+
 int sgdyn_model_set_lanes(sgdyn_model* m, int lanes) {
   if (int rc = check_model(m)) return rc;
   if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)

@@ -19,6 +19,7 @@
 
 #include "../../include/sgdyn.h"
 #include "aux_kernels.cuh"
+#include "jit.h"
 #include "model.h"
 
 struct sgdyn_model {
@@ -93,6 +94,11 @@ bool step_bucket(int ops, const DModel* dm, const StepArgs& a, int64_t lo, int64
     SG_CASE(OP_RNEA | OP_ABA)
     SG_CASE(OP_CRBA | OP_RNEA | OP_ABA)
     SG_CASE(OP_ALL)
+    // forward dynamics from the mass matrix
+    SG_CASE(OP_ABA | OP_FD_CRBA)
+    SG_CASE(OP_RNEA | OP_ABA | OP_FD_CRBA)
+    SG_CASE(OP_CRBA | OP_RNEA | OP_ABA | OP_FD_CRBA)
+    SG_CASE(OP_ALL | OP_FD_CRBA)
 #undef SG_CASE
     default: return false;
   }
@@ -165,6 +171,8 @@ int sgdyn_host_step(const sgdyn_model* m, int64_t n, int ops, const double* q, c
       }
     for (int b = 1; b <= OP_ABA; b <<= 1)
       if (rest & b) parts.push_back(b);
+    for (int& o : parts)  // the forward-dynamics route with fewer operations (sgdyn_fd_method)
+      if (fd_by_mass_matrix(Mo, o)) o |= OP_FD_CRBA;
     const DModel* dm = table(m);
     const int bucket = stash_bucket(Mo.njoints());
     parallel_envs(n, nthreads, [&](int64_t lo, int64_t hi) {

@@ -18,6 +18,7 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -151,6 +152,94 @@ bool team3_kind(int kind) { return kind == JIT_ROLLOUT_FWD3 || kind == JIT_ROLLO
 // Environments per 32-thread block of each kernel kind.
 int envs_per_block(int kind) { return team3_kind(kind) ? 10 : 32; }
 
+// Tree columns of the joint table: ancestors of each column, nearest first (empty if the
+// numbering does not put parents first), and external column numbers.
+struct Columns {
+  std::vector<std::vector<int>> anc;
+  std::vector<int> ext;
+  bool ok = true;
+};
+Columns tree_columns(const DJoint* J, int nj, int nv) {
+  Columns C;
+  C.anc.resize(size_t(nv));
+  C.ext.assign(size_t(nv), 0);
+  std::vector<int> par(size_t(nv), -1);
+  for (int i = 1; i < nj; i++)
+    for (int k = 0; k < J[i].nv; k++) {
+      const int a = J[i].ivx + k;
+      C.ext[a] = J[i].vcol + k;
+      par[a] = k > 0 ? a - 1 : (J[i].parent > 0 ? J[J[i].parent].ivx + J[J[i].parent].nv - 1 : -1);
+      if (par[a] >= a) C.ok = false;
+    }
+  if (C.ok)
+    for (int a = 0; a < nv; a++)
+      for (int c = par[a]; c >= 0; c = par[c]) C.anc[a].push_back(c);
+  return C;
+}
+
+// The mass-matrix route of forward dynamics as straight-line code for one tree (the steps of
+// FdLoops in step_kernel.cuh with every index a constant, so that M lives in registers).
+void emit_fd(std::ostringstream& o, const Columns& C, int nv) {
+  auto at = [](int a, int b) { return a * (a + 1) / 2 + b; };
+  const char* head = "  template <class Tab";
+  o << "struct kFd {\n";
+  o << head << ">\n  static __device__ __forceinline__ void fill(const Tab&, double* H, const sgdyn::Mot* S, "
+       "const sgdyn::Mot* F) {\n";
+  for (int a = 0; a < nv; a++) {
+    o << "    H[" << at(a, a) << "] = sgdyn::dot6(S[" << a << "], F[" << a << "]);\n";
+    for (int c : C.anc[a]) o << "    H[" << at(a, c) << "] = sgdyn::dot6(S[" << c << "], F[" << a << "]);\n";
+  }
+  o << "  }\n";
+  o << head << ", class St>\n  static __device__ __forceinline__ void store_M(const Tab&, const double* H, const St& st) "
+       "{\n";
+  for (int a = 0; a < nv; a++)
+    for (int b = 0; b < nv; b++) {
+      int idx = -1;
+      if (a == b) idx = at(a, a);
+      for (int c : C.anc[a])
+        if (c == b) idx = at(a, b);
+      for (int c : C.anc[b])
+        if (c == a) idx = at(b, a);
+      o << "    st(" << C.ext[a] << ", " << C.ext[b] << ", " << (idx >= 0 ? "H[" + std::to_string(idx) + "]" : "0.0")
+        << ");\n";
+    }
+  o << "  }\n";
+  o << head << ">\n  static __device__ __forceinline__ void matvec_add(const Tab&, const double* H, const double* x, "
+       "double* y) {\n";
+  for (int a = 0; a < nv; a++) {
+    o << "    y[" << a << "] = fma(H[" << at(a, a) << "], x[" << a << "], y[" << a << "]);\n";
+    for (int c : C.anc[a]) {
+      o << "    y[" << a << "] = fma(H[" << at(a, c) << "], x[" << c << "], y[" << a << "]);\n";
+      o << "    y[" << c << "] = fma(H[" << at(a, c) << "], x[" << a << "], y[" << c << "]);\n";
+    }
+  }
+  o << "  }\n";
+  o << head << ">\n  static __device__ __forceinline__ void factor(const Tab&, double* H, double* D) {\n";
+  for (int a = nv - 1; a >= 0; a--) {
+    o << "    { const double r = 1.0 / H[" << at(a, a) << "]; D[" << a << "] = r;\n";
+    for (size_t t = 0; t < C.anc[a].size(); t++) {
+      const int c = C.anc[a][t];
+      o << "      { const double f = H[" << at(a, c) << "] * r;\n";
+      o << "        H[" << at(c, c) << "] = fma(-f, H[" << at(a, c) << "], H[" << at(c, c) << "]);\n";
+      for (int d : C.anc[c])
+        o << "        H[" << at(c, d) << "] = fma(-f, H[" << at(a, d) << "], H[" << at(c, d) << "]);\n";
+      o << "        H[" << at(a, c) << "] = f; }\n";
+    }
+    o << "    }\n";
+  }
+  o << "  }\n";
+  o << head << ">\n  static __device__ __forceinline__ void solve(const Tab&, const double* H, const double* D, "
+       "double* x) {\n";
+  for (int a = nv - 1; a >= 0; a--)
+    for (int c : C.anc[a])
+      o << "    x[" << c << "] = fma(-H[" << at(a, c) << "], x[" << a << "], x[" << c << "]);\n";
+  for (int a = 0; a < nv; a++) {
+    o << "    x[" << a << "] *= D[" << a << "];\n";
+    for (int c : C.anc[a]) o << "    x[" << a << "] = fma(-H[" << at(a, c) << "], x[" << c << "], x[" << a << "]);\n";
+  }
+  o << "  }\n};\n";
+}
+
 std::string generate_source(const Model& M, int kind, int ops) {
   const auto& t = M.host_table();
   const auto* hdr = reinterpret_cast<const DModel*>(t.data());
@@ -179,9 +268,13 @@ std::string generate_source(const Model& M, int kind, int ops) {
     o << " {{" << list(L[l].R, L[l].R + 9) << "}, {" << list(L[l].p, L[l].p + 3) << "}, " << L[l].joint << ", "
       << L[l].flags << ", {0, 0}},\n";
   if (nl == 0) o << " {{1,0,0,0,1,0,0,0,1}, {0,0,0}, 0, 1, {0, 0}},\n";
-  o << "};\n}  // namespace sgjit\n";
+  o << "};\n";
+  const bool fd = kind == JIT_STEP && (ops & OP_FD_CRBA);
+  if (fd) emit_fd(o, tree_columns(J, nj, hdr->nv), hdr->nv);
+  o << "}  // namespace sgjit\n";
   const std::string tab = "sgdyn::StaticTab<" + std::to_string(nj) + ", " + std::to_string(hdr->nv) + ", " +
-                          std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM>()";
+                          std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM" + (fd ? ", sgjit::kFd" : "") +
+                          ">()";
   const char* args = (kind == JIT_STEP || kind == JIT_ABA3)                 ? "sgdyn::StepArgs"
                      : (kind == JIT_ROLLOUT_FWD || team3_kind(kind)) ? "sgdyn::RolloutArgs"
                                                                              : "sgdyn::VjpArgs";
@@ -333,7 +426,61 @@ CUfunction get_function_slow(const Model& M, int kind, int ops, int dev, std::st
 
 }  // namespace
 
-std::string step_jit_source(const Model& M, int ops) { return generate_source(M, JIT_STEP, ops); }
+// How forward dynamics is computed in the specialised sweep: 0 automatic (the route with the
+// smaller FP64 operation count for this model and op set), 1 the articulated-body passes, 2
+// from the mass matrix (OP_FD_CRBA).
+std::atomic<int> g_fd_method{0};
+
+// Estimated FP64 operations of the two routes (counted from the sweep's source: per 1-DoF
+// joint the articulated-body passes take ~205, a root free flyer ~550 and another ~1400;
+// the mass-matrix route needs the composite inertias and the zero-acceleration forces when
+// the op set does not already compute them, the L^T D L factorisation (a reciprocal per
+// column and, per ancestor c of a column, depth(c) + 2), the solve (2 depth + 2 per column)
+// and, with inverse dynamics requested, M qdd (2 depth + 1 per column)).
+bool fd_by_mass_matrix(const Model& M, int ops) {
+  if (!(ops & OP_ABA)) return false;
+  const auto& t = M.host_table();
+  const auto* hdr = reinterpret_cast<const DModel*>(t.data());
+  const DJoint* J = model_joints(hdr);
+  const int nj = hdr->nj;
+  if (!tree_columns(J, nj, hdr->nv).ok) return false;
+  const int mode = g_fd_method.load();
+  if (mode != 0) return mode == 2;
+  std::vector<int> depth(size_t(hdr->nv > 0 ? hdr->nv : 1), 0);  // ancestor columns per column
+  double art = 0, mm = 0;
+  for (int i = 1; i < nj; i++) {
+    const int p = J[i].parent;
+    const int base = p > 0 ? depth[J[p].ivx + J[p].nv - 1] + 1 : 0;
+    for (int k = 0; k < J[i].nv; k++) depth[J[i].ivx + k] = base + k;
+    art += J[i].nv == 1 ? 205 : (p == 0 ? 550 : 1400);
+    if (!(ops & OP_CRBA)) mm += 10;
+    if (!(ops & OP_RNEA)) mm += 60;
+  }
+  for (int a = 0; a < hdr->nv; a++) {
+    const int d = depth[a];
+    if (!(ops & OP_CRBA)) mm += 24 + 6 * (d + 1);
+    mm += 5 + 2 * d + 2;                // reciprocal, solve
+    if (ops & OP_RNEA) mm += 2 * d + 1;  // M qdd
+  }
+  // factorisation: column a updates, for each ancestor c, c's row over c and its ancestors
+  for (int i = 1; i < nj; i++)
+    for (int k = 0; k < J[i].nv; k++) {
+      int d = depth[J[i].ivx + k];
+      for (int c = d - 1; c >= 0; c--) mm += c + 2;  // ancestors sit at depths d-1 .. 0
+    }
+  return mm < art;
+}
+
+int step_kernel_ops(const Model& M, int ops) { return fd_by_mass_matrix(M, ops) ? ops | OP_FD_CRBA : ops; }
+
+void fd_method(int mode, int* out) {
+  if (mode >= 0) g_fd_method.store(mode);
+  if (out) *out = g_fd_method.load();
+}
+
+std::string step_jit_source(const Model& M, int ops) {
+  return generate_source(M, JIT_STEP, step_kernel_ops(M, ops));
+}
 std::string rollout_jit_source(const Model& M) {
   return generate_source(M, JIT_ROLLOUT_FWD, 0);
 }
@@ -362,7 +509,7 @@ void jit_max_joints(int max_joints, int* out) {
 bool prepare_step_jit(Model& M, int ops, std::string* why) {
   std::lock_guard<std::mutex> lk(g_mu);
   read_env_config();
-  return get_function(M, JIT_STEP, ops, why) != nullptr;
+  return get_function(M, JIT_STEP, step_kernel_ops(M, ops), why) != nullptr;
 }
 
 bool prepare_rollout_jit(Model& M, std::string* why) {
@@ -407,7 +554,7 @@ bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std:
 }  // namespace
 
 bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why) {
-  return launch_jit(M, JIT_STEP, ops, a, s, why);
+  return launch_jit(M, JIT_STEP, step_kernel_ops(M, ops), a, s, why);
 }
 
 bool launch_rollout_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why) {

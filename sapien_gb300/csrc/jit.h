@@ -39,6 +39,11 @@ void set_jit_config(int enable, int64_t min_n);
 // The generated translation unit (for inspection and tests).
 std::string step_jit_source(const Model& M, int ops);
 void get_jit_config(int* enable, int64_t* min_n);
+// Forward dynamics in the specialised sweep: 0 automatic, 1 articulated-body passes, 2 from
+// the mass matrix (L^T D L); < 0 leaves the setting. out receives the setting.
+void fd_method(int mode, int* out);
+// Whether the specialised sweep for `ops` computes forward dynamics from the mass matrix.
+bool fd_by_mass_matrix(const Model& M, int ops);
 // Size limit (joints incl. the universe) for run-time specialisation; < 0 leaves it.
 void jit_max_joints(int max_joints, int* out);
 

@@ -18,6 +18,10 @@ struct Arr {
 };
 
 enum Ops : int { OP_FK = 1, OP_JAC = 2, OP_CRBA = 4, OP_RNEA = 8, OP_ABA = 16, OP_ALL = 31 };
+// Sweep variant bit (not an op): forward dynamics by the composite-rigid-body method, M from
+// CRBA factored as L^T D L with the tree's sparsity and qdd = M^-1 (tau - b), b the bias
+// forces (RNEA at zero acceleration); inverse dynamics then reads tau = b + M qdd.
+constexpr int OP_FD_CRBA = 32;
 // The five-op step split in two concurrent launches over the same environments: CRBA + RNEA +
 // ABA, and FK + Jacobian, whose short warps fill FP64 schedulers the long ones leave idle.
 enum SplitOps : int { OP_SPLIT_A = OP_FK | OP_JAC, OP_SPLIT_B = OP_CRBA | OP_RNEA | OP_ABA };

@@ -25,8 +25,10 @@ namespace sgdyn {
 // Table policies for the sweep: a table read through a device pointer at run time, or a
 // table whose contents are compile-time constants (run-time-compiled per model, so every
 // joint loop unrolls into straight-line code with constant parents, axes and inertias).
+struct FdLoops;
 struct RuntimeTab {
   static constexpr bool kStatic = false;
+  using Fd = FdLoops;
   const DModel* m;
   SG_HD int nj() const { return m->nj; }
   SG_HD int nv() const { return m->nv; }
@@ -36,9 +38,10 @@ struct RuntimeTab {
   SG_HD const DJoint& joint(int i) const { return model_joints(m)[i]; }
   SG_HD const DLink& link(int l) const { return model_links(m)[l]; }
 };
-template <int NJ, int NV, int NL, const DJoint* JT, const DLink* LT, const DModel* M>
+template <int NJ, int NV, int NL, const DJoint* JT, const DLink* LT, const DModel* M, class FD = FdLoops>
 struct StaticTab {
   static constexpr bool kStatic = true;
+  using Fd = FD;  // the mass-matrix route's steps (generated per model by the run-time compiler)
   SG_HD static constexpr int nj() { return NJ; }
   SG_HD static constexpr int nv() { return NV; }
   SG_HD int nq_ext() const { return M->nq_ext; }
@@ -218,15 +221,123 @@ SG_HD double team_sum(double v, int L) {
   return v;
 }
 
+// Entry (a, b <= a) of a symmetric matrix over tree columns, lower triangle packed by rows.
+SG_HD constexpr int ltdm_at(int a, int b) { return a * (a + 1) / 2 + b; }
+
+// f(column, joint, dof) for the ancestors of tree column (joint i, dof k), nearest first:
+// the joint's earlier degrees of freedom, then each ancestor joint's from its last.
+template <class Tab, class F>
+SG_HD void ancestor_columns(const Tab& T, int i, int k, const F& f) {
+  for (int j = i; j > 0; j = T.joint(j).parent) {
+    const DJoint& A = T.joint(j);
+    for (int l = (j == i ? k - 1 : A.nv - 1); l >= 0; l--) f(A.ivx + l, j, l);
+  }
+}
+
+// Forward dynamics from the mass matrix over tree columns (joint i, degree of freedom k,
+// numbered ivx + k in depth-first order), whose nonzeros pair a column with its ancestors:
+// fill M from the column forces F_a = Y_composite S_a (M_ac = S_c . F_a), store it, y += M x,
+// factor M = L^T D L with L unit lower triangular on the same pattern (Featherstone, "Rigid
+// Body Dynamics Algorithms", 2008, sec. 6.5: sum depth^2 operations) and solve (2 sum
+// depth). These are the loops over run-time tables; the run-time compiler emits the same
+// steps per model as straight-line code with constant indices (jit.cpp), so that M stays
+// in registers.
+struct FdLoops {
+  template <class Tab>
+  SG_HD static void fill(const Tab& T, double* H, const Mot* S, const Mot* F) {
+    for (int i = 1; i < T.nj(); i++)
+      for (int k = 0; k < T.joint(i).nv; k++) {
+        const int a = T.joint(i).ivx + k;
+        H[ltdm_at(a, a)] = dot6(S[a], F[a]);
+        ancestor_columns(T, i, k, [&](int c, int, int) { H[ltdm_at(a, c)] = dot6(S[c], F[a]); });
+      }
+  }
+  // st(row, column, value) for every entry of M in external column order
+  template <class Tab, class St>
+  SG_HD static void store_M(const Tab& T, const double* H, const St& st) {
+    for (int i = 1; i < T.nj(); i++) {
+      const DJoint& J = T.joint(i);
+      for (int k = 0; k < J.nv; k++) {
+        const int a = J.ivx + k, ra = J.vcol + k;
+        st(ra, ra, H[ltdm_at(a, a)]);
+        ancestor_columns(T, i, k, [&](int c, int j, int l) {
+          const int rc = T.joint(j).vcol + l;
+          st(ra, rc, H[ltdm_at(a, c)]);
+          st(rc, ra, H[ltdm_at(a, c)]);
+        });
+        // joints after this one's subtree are neither its ancestors nor its descendants
+        for (int j = J.subtree_end; j < T.nj(); j++)
+          for (int l = 0; l < T.joint(j).nv; l++) {
+            st(ra, T.joint(j).vcol + l, 0.0);
+            st(T.joint(j).vcol + l, ra, 0.0);
+          }
+      }
+    }
+  }
+  template <class Tab>
+  SG_HD static void matvec_add(const Tab& T, const double* H, const double* x, double* y) {
+    for (int i = 1; i < T.nj(); i++)
+      for (int k = 0; k < T.joint(i).nv; k++) {
+        const int a = T.joint(i).ivx + k;
+        y[a] = fma(H[ltdm_at(a, a)], x[a], y[a]);
+        ancestor_columns(T, i, k, [&](int c, int, int) {
+          y[a] = fma(H[ltdm_at(a, c)], x[c], y[a]);
+          y[c] = fma(H[ltdm_at(a, c)], x[a], y[c]);
+        });
+      }
+  }
+  template <class Tab>
+  SG_HD static void factor(const Tab& T, double* H, double* D) {
+    for (int i = T.nj() - 1; i >= 1; i--)
+      for (int k = T.joint(i).nv - 1; k >= 0; k--) {
+        const int a = T.joint(i).ivx + k;
+        const double r = 1.0 / H[ltdm_at(a, a)];
+        D[a] = r;
+        ancestor_columns(T, i, k, [&](int c, int j, int l) {
+          const double f = H[ltdm_at(a, c)] * r;
+          H[ltdm_at(c, c)] = fma(-f, H[ltdm_at(a, c)], H[ltdm_at(c, c)]);
+          ancestor_columns(T, j, l, [&](int d, int, int) { H[ltdm_at(c, d)] = fma(-f, H[ltdm_at(a, d)], H[ltdm_at(c, d)]); });
+          H[ltdm_at(a, c)] = f;
+        });
+      }
+  }
+  // x <- M^-1 x: L^T y = x (columns descending), then L x = D^-1 y (ascending)
+  template <class Tab>
+  SG_HD static void solve(const Tab& T, const double* H, const double* D, double* x) {
+    for (int i = T.nj() - 1; i >= 1; i--)
+      for (int k = T.joint(i).nv - 1; k >= 0; k--) {
+        const int a = T.joint(i).ivx + k;
+        const double xa = x[a];
+        ancestor_columns(T, i, k, [&](int c, int, int) { x[c] = fma(-H[ltdm_at(a, c)], xa, x[c]); });
+      }
+    for (int i = 1; i < T.nj(); i++)
+      for (int k = 0; k < T.joint(i).nv; k++) {
+        const int a = T.joint(i).ivx + k;
+        double xa = x[a] * D[a];
+        ancestor_columns(T, i, k, [&](int c, int, int) { xa = fma(-H[ltdm_at(a, c)], x[c], xa); });
+        x[a] = xa;
+      }
+  }
+};
+
 // The whole fused sweep for environment e (rows of the StepArgs arrays).
 template <int MAXJ, int OPS, class Tab, class Team = NoTeam>
 SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const Team& tm = Team{}) {
   constexpr int MAXV = MAXJ + 5;
   constexpr bool kFK = OPS & OP_FK, kJAC = OPS & OP_JAC, kCRBA = OPS & OP_CRBA, kRNEA = OPS & OP_RNEA,
                  kABA = OPS & OP_ABA;
+  // Forward dynamics either by the articulated-body passes (kArt) or from the mass matrix
+  // (kFdM: OP_FD_CRBA, chosen per model on the host when it costs fewer FP64 operations).
+  // With kFdM the acceleration pass runs at zero joint acceleration (bias forces b, bz) and
+  // inverse dynamics reads tau = b + M qdd.
+  constexpr bool kFdM = kABA && (OPS & OP_FD_CRBA);
+  constexpr bool kArt = kABA && !kFdM;
+  constexpr bool kForces = kRNEA || kFdM;  // accelerations and forces of the RNEA pass
+  constexpr bool kComposite = kCRBA || kFdM;
   constexpr bool kVel = kRNEA || kABA;
   constexpr bool kInertia = kCRBA || kRNEA || kABA;
   constexpr bool kTeam = Team::kOn;
+  static_assert(!(kFdM && kTeam), "teams run the articulated-body passes");
   const int nj = T.nj();
 
   M3 oR[MAXJ];
@@ -234,17 +345,20 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
   Mot Sw[MAXV];
   Mot vel[kVel ? MAXJ : 1];
   Mot acc[(kRNEA || kABA) ? MAXJ : 1];
-  Mot frc[kRNEA ? MAXJ : 1];
+  Mot frc[kForces ? MAXJ : 1];
   // Pass 2 rebuilds each joint's composite (CRBA) and articulated (ABA) inertia as its own
   // body inertia Yb plus what its children passed up (CC, AC). The last child in
   // depth-first order is processed first and initialises its parent's slot, so no slot is
   // zero-filled and only joints with children carry one (teams zero their trunk's slots).
   RBI Yb[(kCRBA || kABA) ? MAXJ : 1];
-  RBI CC[kCRBA ? MAXJ : 1];
-  Sym6 AC[kABA ? MAXJ : 1];
-  Mot pA[kABA ? MAXJ : 1], cb[kABA ? MAXJ : 1], Uv[kABA ? MAXV : 1];
-  double uv[kABA ? MAXV : 1], Dinv[kABA ? MAXJ : 1];
-  double Lff[kABA ? 21 : 1];  // Cholesky factor of D for the (single) free-flyer joint
+  RBI CC[kComposite ? MAXJ : 1];
+  Sym6 AC[kArt ? MAXJ : 1];
+  Mot pA[kArt ? MAXJ : 1], cb[kArt ? MAXJ : 1], Uv[kArt ? MAXV : 1];
+  double uv[kArt ? MAXV : 1], Dinv[kArt ? MAXJ : 1];
+  double Lff[kArt ? 21 : 1];  // Cholesky factor of D for the (single) free-flyer joint
+  // kFdM: the bias forces and the composite-inertia forces F = Y_c S per tree column
+  double bz[kFdM ? MAXV : 1];
+  Mot Fcol[kFdM ? MAXV : 1];
 
   const Mot a0{mk(-T.gravity(0), -T.gravity(1), -T.gravity(2)), mk(0, 0, 0)};
 
@@ -317,14 +431,15 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
         const Mot hY = rbi_mul(Y, v);  // momentum I v
         const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
         const Mot bias = add_crossf(zero, v, hY);  // v x* I v
-        if constexpr (kRNEA) {
+        if constexpr (kForces) {
           Mot a = (p == 0) ? a0 : acc[p];
-          for (int k = 0; k < nvi; k++) a = axpy6(qddin[vc + k], Sw[iv + k], a);
+          if constexpr (!kFdM)
+            for (int k = 0; k < nvi; k++) a = axpy6(qddin[vc + k], Sw[iv + k], a);
           a = add_crossm(a, v, vJ);
           acc[i] = a;
           frc[i] = rbi_mul_add(Y, a, bias);
         }
-        if constexpr (kABA) {
+        if constexpr (kArt) {
           cb[i] = add_crossm(zero, v, vJ);
           pA[i] = bias;
         }
@@ -341,16 +456,22 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
     // the last child of p in depth-first order ends where p's subtree ends
     const bool first_of_parent = p > 0 && !in_trunk(p) && J.subtree_end == T.joint(p).subtree_end;
     const bool out = writes(i);
-    if constexpr (kRNEA) {
+    if constexpr (kForces) {
       const Mot f = frc[i];
-      if (out)
-        for (int k = 0; k < nvi; k++) stv(args.tau_out, e, vc + k, dot6(Sw[iv + k], f));
+      if constexpr (kFdM) {
+        for (int k = 0; k < nvi; k++) bz[iv + k] = dot6(Sw[iv + k], f);
+      } else {
+        if (out)
+          for (int k = 0; k < nvi; k++) stv(args.tau_out, e, vc + k, dot6(Sw[iv + k], f));
+      }
       if (p > 0) frc[p] = add6(frc[p], f);
     }
-    if constexpr (kCRBA) {
+    if constexpr (kComposite) {
       const int nv = T.nv();
       const RBI Y = has_children ? rbi_add(Yb[i], CC[i]) : Yb[i];
-      if (out) {
+      if constexpr (kFdM) {  // M's entries are formed after the pass
+        for (int k = 0; k < nvi; k++) Fcol[iv + k] = rbi_mul(Y, Sw[iv + k]);
+      } else if (out) {
         for (int k = 0; k < nvi; k++) {
           const Mot F = rbi_mul(Y, Sw[iv + k]);
           for (int l = 0; l <= k; l++) {  // own block, upper triangle mirrored
@@ -382,7 +503,7 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
       }
       if (p > 0) CC[p] = first_of_parent ? Y : rbi_add(CC[p], Y);
     }
-    if constexpr (kABA) {
+    if constexpr (kArt) {
       const Sym6 IAi = has_children ? sym6_rbi_add(Yb[i], AC[i]) : sym6_from_rbi(Yb[i]);
       if (nvi == 1) {
         const Mot S = Sw[iv];
@@ -536,6 +657,58 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
       if (T.link(l).joint == i) link_pose(l);
   };
 
+  // ---------------- forward (and inverse) dynamics from the mass matrix ----------------
+  // M over tree columns from the column forces, then tau = b + M qdd and qdd = M^-1 (tau - b)
+  // (Tab::Fd: straight-line code per model with compile-time tables, loops otherwise).
+  auto mass_matrix_dynamics = [&]() {
+    if constexpr (kFdM) {
+      using Fd = typename Tab::Fd;
+      double Hm[MAXV * (MAXV + 1) / 2], Dm[MAXV], x[MAXV];
+      Fd::fill(T, Hm, Sw, Fcol);
+      if constexpr (kCRBA) {
+        const int nv = T.nv();
+        Fd::store_M(T, Hm, [&](int r, int c, double v) { stv(args.M, e, r * nv + c, v); });
+      }
+      if constexpr (kRNEA) {
+        double t[MAXV];
+#pragma unroll
+        for (int i = 1; i < nj; i++) {
+          const DJoint& J = T.joint(i);
+#pragma unroll
+          for (int k = 0; k < 6; k++)
+            if (k < J.nv) {
+              t[J.ivx + k] = bz[J.ivx + k];
+              x[J.ivx + k] = qddin[J.vcol + k];
+            }
+        }
+        Fd::matvec_add(T, Hm, x, t);
+#pragma unroll
+        for (int i = 1; i < nj; i++) {
+          const DJoint& J = T.joint(i);
+#pragma unroll
+          for (int k = 0; k < 6; k++)
+            if (k < J.nv && writes(i)) stv(args.tau_out, e, J.vcol + k, t[J.ivx + k]);
+        }
+      }
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+          if (k < J.nv) x[J.ivx + k] = tauin[J.vcol + k] - bz[J.ivx + k];
+      }
+      Fd::factor(T, Hm, Dm);
+      Fd::solve(T, Hm, Dm, x);
+#pragma unroll
+      for (int i = 1; i < nj; i++) {
+        const DJoint& J = T.joint(i);
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+          if (k < J.nv && writes(i)) stv(args.qdd_out, e, J.vcol + k, x[J.ivx + k]);
+      }
+    }
+  };
+
   auto load_tau = [&]() {
     if constexpr (kABA) {
       const int nv = T.nv();
@@ -558,7 +731,8 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
 #pragma unroll
       for (int i = nj - 1; i >= 1; i--) pass2(i);
     }
-    if constexpr (kABA) {
+    if constexpr (kFdM) mass_matrix_dynamics();
+    if constexpr (kArt) {
 #pragma unroll
       for (int i = 1; i < nj; i++) pass3(i);
     }
@@ -574,11 +748,11 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
     if constexpr (kCRBA || kRNEA || kABA) {
       // trunk slots start at zero; attach joints keep their own force / bias aside so that
       // the branch contributions alone are summed across the team
-      Mot fbase[kRNEA ? MAXJ : 1], pbase[kABA ? MAXJ : 1];
+      Mot fbase[kRNEA ? MAXJ : 1], pbase[kArt ? MAXJ : 1];
       for (int k = 0; k < nt; k++) {
         const int t = tm.trunk(k);
         if constexpr (kCRBA) CC[t] = RBI{0.0, mk(0, 0, 0), {0, 0, 0, 0, 0, 0}};
-        if constexpr (kABA) AC[t] = Sym6{{0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}};
+        if constexpr (kArt) AC[t] = Sym6{{0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}};
       }
       const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
       for (int k = 0; k < na; k++) {
@@ -587,7 +761,7 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
           fbase[t] = frc[t];
           frc[t] = zero;
         }
-        if constexpr (kABA) {
+        if constexpr (kArt) {
           pbase[t] = pA[t];
           pA[t] = zero;
         }
@@ -612,7 +786,7 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
           c.h.x = team_sum(c.h.x, L); c.h.y = team_sum(c.h.y, L); c.h.z = team_sum(c.h.z, L);
           for (int q = 0; q < 6; q++) c.I[q] = team_sum(c.I[q], L);
         }
-        if constexpr (kABA) {
+        if constexpr (kArt) {
           Sym6& s = AC[t];
           for (int q = 0; q < 6; q++) {
             s.A[q] = team_sum(s.A[q], L);
@@ -625,7 +799,7 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
       }
       for (int k = nt - 1; k >= 0; k--) pass2(tm.trunk(k));
     }
-    if constexpr (kABA) {
+    if constexpr (kArt) {
       for (int k = 0; k < nt; k++) pass3(tm.trunk(k));
       for (int k = 0; k < sm; k++) {
         const int j = tm.sched(k);

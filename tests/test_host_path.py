@@ -86,6 +86,44 @@ def test_host_batch_step_matches_oracle(name):
         assert rel(out["qdd"][e], r["qdd"][e]) <= 1e-8
 
 
+@pytest.mark.parametrize("name", ["arm9", "quadruped18", "humanoid", "chain40", "fetch"])
+def test_host_forward_dynamics_routes_match_oracle(name):
+    """Forward dynamics by the articulated-body passes (sgdyn_fd_method 1) and from the mass
+    matrix (method 2: L^T D L with the tree's sparsity, the loop form of the steps the
+    run-time compiler emits per model; inverse dynamics in the same sweep as b + M qdd), for
+    every op set holding ABA, against the oracle and each other."""
+    robot = ROBOTS[name]()
+    pm, o = pair(robot)
+    n, nv, nl = 24, robot.nv, len(robot.link_names)
+    q, qd, qdd, tau = robot.sample(n, seed=5)
+    r = o.batch_step(q, qd, qdd, tau, nthreads=4)
+    L = N.load()
+    a = lambda x: x.ctypes.data_as(ctypes.c_void_p) if x is not None else None  # noqa: E731
+    old = ctypes.c_int()
+    assert L.sgdyn_fd_method(-1, ctypes.byref(old)) == N.OK
+    outs = {}
+    try:
+        for mode in (1, 2):
+            assert L.sgdyn_fd_method(mode, None) == N.OK
+            for ops in (16, 24, 28, 31):
+                o_ = {"M": np.full((n, nv, nv), np.nan) if ops & 4 else None,
+                      "tau": np.full((n, nv), np.nan) if ops & 8 else None, "qdd": np.full((n, nv), np.nan)}
+                poses = np.empty((n, nl, 7)) if ops & 1 else None
+                J = np.empty((n, 6, nv)) if ops & 2 else None
+                N.check(L.sgdyn_host_step(pm._h, n, ops, a(q), a(qd), a(qdd), a(tau), a(poses), a(J), a(o_["M"]),
+                                          a(o_["tau"]), a(o_["qdd"]), N.ENV_MAJOR, 4))
+                outs[(mode, ops)] = {k: v for k, v in o_.items() if v is not None}
+    finally:
+        L.sgdyn_fd_method(old.value, None)
+    want = {"M": r["M"], "tau": r["tau"], "qdd": r["qdd"]}
+    for (mode, ops), g in outs.items():
+        for k, v in g.items():
+            tol = 1e-8 if k == "qdd" else 1e-10
+            for e in range(n):
+                assert rel(v[e], want[k][e]) <= tol, (mode, ops, k, e)
+                assert rel(v[e], outs[(3 - mode, ops)][k][e]) <= (1e-10 if k == "qdd" else 1e-12), (mode, ops, k)
+
+
 def test_chain7_single_instance_1000_samples_on_host():
     """The CPU-runnable reference configuration (seeded 7-DoF revolute chain, 1000 samples)
     through the single-instance drop-in methods, answered on the host."""

@@ -510,3 +510,69 @@ def test_three_lane_forward_dynamics_matches_oracle(name):
     finally:
         L.sgdyn_rollout_lanes(0, None)
         L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
+
+
+def step_ops(pm, ops, q, qd, qdd, tau):
+    """sgdyn_step with an op mask through the C ABI (env-major device buffers)."""
+    T = torch()
+    dev = T.device("cuda", 0)
+    t = lambda a: T.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    n, nv, nl = q.shape[0], pm.nv, pm.nlinks
+    outs = {"link_poses": (N.OP_FK, (n, nl, 7)), "jacobian": (N.OP_JACOBIAN, (n, 6, nv)),
+            "mass_matrix": (N.OP_MASS_MATRIX, (n, nv, nv)), "qf": (N.OP_INVERSE_DYNAMICS, (n, nv)),
+            "qacc": (N.OP_FORWARD_DYNAMICS, (n, nv))}
+    bufs = {k: T.full(shape, np.nan, dtype=T.float64, device=dev) if ops & bit else None
+            for k, (bit, shape) in outs.items()}
+    P = lambda x: ctypes.c_void_p(x.data_ptr() if x is not None else 0)  # noqa: E731
+    ins = [t(q), t(qd), t(qdd), t(tau)]
+    rc = N.load().sgdyn_step(pm._h, n, ops, *[P(x) for x in ins], *[P(bufs[k]) for k in outs], N.ENV_MAJOR,
+                             ctypes.c_void_p(T.cuda.current_stream().cuda_stream))
+    assert rc == N.OK, N.last_error()
+    T.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in bufs.items() if v is not None}
+
+
+@pytest.mark.parametrize("name", ["arm9", "arm9_sapien", "chain7", "mixed_chain", "quadruped18", "humanoid",
+                                  "humanoid_sapien", "chain40"])
+def test_forward_dynamics_routes_match_oracle(name):
+    """The run-time-specialised sweep computes forward dynamics by the articulated-body passes
+    (sgdyn_fd_method 1) or from the mass matrix (method 2: CRBA, bias forces at zero
+    acceleration, M = L^T D L with the tree's sparsity; inverse dynamics in the same sweep as
+    b + M qdd). The op sets holding ABA (two of them on the large trees, whose unrolled sweeps
+    take long to compile), both methods, against the oracle and each other."""
+    robot = ROBOTS[name]()
+    pm, o = pair(robot)
+    op_sets = (16, 24, 28, 31) if robot.nv <= 18 else (16, 28)
+    n = 96
+    q, qd, qdd, tau = robot.sample(n, seed=23)
+    r = o.batch_step(q, qd, qdd, tau, nthreads=8)
+    want = {"link_poses": oracle_pose7(r["poses"]), "jacobian": r["J"], "mass_matrix": r["M"], "qf": r["tau"],
+            "qacc": r["qdd"]}
+    tol = {"link_poses": TOL["poses"], "jacobian": TOL["J"], "mass_matrix": TOL["M"], "qf": TOL["tau"],
+           "qacc": TOL["qdd"]}
+    L = N.load()
+    old_jit, old_min, old_max, old_fd = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int()
+    L.sgdyn_jit_config(-1, -1, ctypes.byref(old_jit), ctypes.byref(old_min))
+    L.sgdyn_jit_max_joints(-1, ctypes.byref(old_max))
+    assert L.sgdyn_fd_method(-1, ctypes.byref(old_fd)) == N.OK and old_fd.value == 0
+    outs = {}
+    try:
+        L.sgdyn_jit_config(1, 0, None, None)
+        L.sgdyn_jit_max_joints(64, None)
+        for mode in (1, 2):
+            assert L.sgdyn_fd_method(mode, None) == N.OK
+            for ops in op_sets:
+                route = ctypes.c_int()
+                assert L.sgdyn_fd_by_mass_matrix(pm._h, ops, ctypes.byref(route)) == N.OK
+                assert route.value == (mode == 2)
+                outs[(mode, ops)] = step_ops(pm, ops, q, qd, qdd, tau)
+    finally:
+        L.sgdyn_fd_method(old_fd.value, None)
+        L.sgdyn_jit_max_joints(old_max.value, None)
+        L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
+    for key, g in outs.items():
+        for k, v in g.items():
+            assert not np.isnan(v).any(), (key, k)
+            assert rel_per_env(v, want[k]) <= tol[k], (key, k, rel_per_env(v, want[k]))
+            other = outs[(3 - key[0], key[1])][k]
+            assert rel_per_env(v, other) <= (1e-10 if k == "qacc" else 1e-12), (key, k)
