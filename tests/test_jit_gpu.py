@@ -58,7 +58,8 @@ def test_specialised_sweep_matches_generic_and_oracle(name):
         jit_config(*old)
     for k in gen:
         assert rel_per_env(spec[k], gen[k]) <= 1e-13, k
-    assert rel_per_env(single, gen["qacc"]) <= 1e-13
+    # forward dynamics alone may run on three lanes per environment (another summation order)
+    assert rel_per_env(single, gen["qacc"]) <= 1e-12
     o = Oracle(robot.urdf)
     o.set_joint_order(robot.joint_names)
     o.set_link_order(robot.link_names)
