@@ -684,6 +684,23 @@ def main():
     ms_e2e = time_e2e(e2e_mapped)
     e2e_value = aggregate_throughput(n, world, ms_e2e * 1e-3)
     ms_e2e_staged = time_e2e(e2e_staged)
+
+    # the host link's own bandwidth (copy-engine copies of the same buffers, each direction
+    # alone): the step cannot move its bytes faster than this
+    def link_ms(copies):
+        for _ in range(2):
+            copies()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(5):
+            copies()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 5
+
+    d2h_ms = link_ms(lambda: [h.copy_(d, non_blocking=True) for h, d in zip(outs_h, outs_d)])
+    h2d_ms = link_ms(lambda: [d.copy_(h, non_blocking=True) for d, h in zip(ins_d, ins_h)])
     # the mapped-host run must give the device run's results bit for bit
     step(q, qd, qdd, tau)
     e2e_mapped()
@@ -801,6 +818,12 @@ def main():
                 "transfer": "sgdyn_step on mapped pinned host buffers (SoA): the kernel reads inputs from and "
                             "writes results to host memory over the host link",
                 "results_identical_to_device_run": e2e_identical,
+                "link": {"d2h_gbs": d2h / (d2h_ms * 1e6), "h2d_gbs": h2d / (h2d_ms * 1e6),
+                         "floor_ms": max(d2h_ms, h2d_ms, ms),
+                         "frac": max(d2h_ms, h2d_ms, ms) / ms_e2e,
+                         "what": "copy-engine bandwidth of the host link for this step's outputs and inputs "
+                                 "(each direction alone); floor = the larger of the outputs' transfer time, the "
+                                 "inputs' and the device-resident step; frac = floor / e2e ms_per_step"},
                 "staged_copies": {"value": aggregate_throughput(n, world, ms_e2e_staged * 1e-3),
                                   "ms_per_step": ms_e2e_staged,
                                   "transfer": "cudaMemcpyAsync host->device, kernel, device->host on one stream"}},
