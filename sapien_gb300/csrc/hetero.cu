@@ -43,6 +43,12 @@ struct HeteroArgs {
   const int4* tiles;  // (model, start, count, lanes per environment)
   int ntiles;
   unsigned int* head;
+  // per-model byte sizes of the packed tables and int counts of the team tables; each warp
+  // stages its tile's tables in its slice of the dynamic shared memory (stage_bytes each:
+  // the largest model table, then the largest team table)
+  const int* table_bytes;
+  const int* team_ints;
+  int stage_bytes, stage_team_at;
   StepArgs io;
   // semi-implicit Euler after the sweep (integrate != 0): q / qd rows updated in place
   int integrate;
@@ -76,14 +82,34 @@ __device__ __forceinline__ void integrate_env(const DModel* m, double* q, double
 
 template <int MAXJ, int OPS>
 __global__ void hetero_kernel(const HeteroArgs a) {
+  extern __shared__ __align__(16) unsigned char stage[];
   const int lane = threadIdx.x & 31;
+  unsigned char* const mine = stage + int64_t(threadIdx.x >> 5) * a.stage_bytes;
+  const DModel* m = reinterpret_cast<const DModel*>(mine);
+  const int* team = reinterpret_cast<const int*>(mine + a.stage_team_at);
+  int staged = -1;  // model whose tables this warp holds
   for (;;) {
     unsigned t = 0;
     if (lane == 0) t = atomicAdd(a.head, 1u);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= unsigned(a.ntiles)) break;
     const int4 tile = a.tiles[t];
-    const DModel* m = reinterpret_cast<const DModel*>(a.tables + a.table_offset[tile.x]);
+    if (tile.x != staged) {
+      // the sweeps read the model's joint and link tables (and the team table) over and
+      // over; from shared memory those reads do not compete with the sweep's local-memory
+      // working set in L1
+      __syncwarp();
+      const int4* src = reinterpret_cast<const int4*>(a.tables + a.table_offset[tile.x]);
+      int4* dst = reinterpret_cast<int4*>(mine);
+      for (int k = lane; k < a.table_bytes[tile.x] / 16; k += 32) dst[k] = src[k];
+      if (a.team_offset[tile.x] >= 0) {
+        int* tdst = reinterpret_cast<int*>(mine + a.stage_team_at);
+        const int* tsrc = a.teams + a.team_offset[tile.x];
+        for (int k = lane; k < a.team_ints[tile.x]; k += 32) tdst[k] = tsrc[k];
+      }
+      __syncwarp();
+      staged = tile.x;
+    }
     if (tile.w <= 1) {
       if (lane < tile.z) step_env<MAXJ, OPS>(m, a.io, int64_t(a.perm[tile.y + lane]));
     } else {
@@ -91,7 +117,7 @@ __global__ void hetero_kernel(const HeteroArgs a) {
       // slot repeat the tile's first environment and store nothing
       const int slot = lane / tile.w;
       const bool valid = slot < tile.z;
-      const TeamLanes tm{a.teams + a.team_offset[tile.x], lane % tile.w, valid};
+      const TeamLanes tm{team, lane % tile.w, valid};
       step_env_t<MAXJ, OPS>(RuntimeTab{m}, a.io, int64_t(a.perm[tile.y + (valid ? slot : 0)]), tm);
     }
     if (a.integrate) {
@@ -173,9 +199,16 @@ __global__ void __launch_bounds__(kIntegrateThreads) hetero_integrate_kernel(con
 
 template <int MAXJ>
 cudaError_t launch_hetero_bucket(int ops, const HeteroArgs& a, dim3 grid, dim3 block, cudaStream_t s) {
+  const size_t smem = size_t(a.stage_bytes) * (block.x / 32);
   switch (ops) {
-#define SG_CASE(O) \
-  case O: hetero_kernel<MAXJ, O><<<grid, block, 0, s>>>(a); break;
+#define SG_CASE(O)                                                                                            \
+  case O:                                                                                                     \
+    if (smem > 48 * 1024 &&                                                                                   \
+        cudaFuncSetAttribute(hetero_kernel<MAXJ, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != \
+            cudaSuccess)                                                                                      \
+      return cudaErrorInvalidValue;                                                                           \
+    hetero_kernel<MAXJ, O><<<grid, block, smem, s>>>(a);                                                      \
+    break;
     SG_CASE(OP_CRBA | OP_RNEA | OP_ABA)
     SG_CASE(OP_RNEA | OP_ABA)
     SG_CASE(OP_ALL)
@@ -201,6 +234,9 @@ struct sgdyn_batch {
   // device
   unsigned char* tables = nullptr;
   int64_t* offsets = nullptr;
+  int* table_bytes = nullptr;  // per model, rounded up to 16
+  int* team_ints = nullptr;    // per model (0 with one lane per environment)
+  int max_table_bytes = 0, max_team_ints = 0;
   int* teams = nullptr;
   int64_t* team_offsets = nullptr;
   int* model_of_env_dev = nullptr;
@@ -219,6 +255,10 @@ namespace {
 void free_device(sgdyn_batch* b) {
   cudaFree(b->tables);
   cudaFree(b->offsets);
+  cudaFree(b->table_bytes);
+  cudaFree(b->team_ints);
+  b->table_bytes = nullptr;
+  b->team_ints = nullptr;
   cudaFree(b->teams);
   cudaFree(b->team_offsets);
   cudaFree(b->model_of_env_dev);
@@ -289,23 +329,30 @@ int upload_plan(sgdyn_batch* b) {
 }
 
 int upload_teams(sgdyn_batch* b) {
-  std::vector<int> all;
+  std::vector<int> all, counts;
   std::vector<int64_t> offs;
   for (size_t m = 0; m < b->models.size(); m++) {
     if (b->lanes[m] <= 1) {
       offs.push_back(-1);
+      counts.push_back(0);
       continue;
     }
     offs.push_back(int64_t(all.size()));
     const auto t = b->models[m]->impl->team_table(b->lanes[m]);
     all.insert(all.end(), t.begin(), t.end());
+    counts.push_back(int(t.size()));
   }
+  b->max_team_ints = counts.empty() ? 0 : *std::max_element(counts.begin(), counts.end());
   cudaFree(b->teams);
   cudaFree(b->team_offsets);
+  cudaFree(b->team_ints);
   b->teams = nullptr;
   b->team_offsets = nullptr;
+  b->team_ints = nullptr;
   if (cudaMalloc(&b->teams, sizeof(int) * std::max<size_t>(all.size(), 1)) != cudaSuccess ||
-      cudaMalloc(&b->team_offsets, sizeof(int64_t) * offs.size()) != cudaSuccess)
+      cudaMalloc(&b->team_offsets, sizeof(int64_t) * offs.size()) != cudaSuccess ||
+      cudaMalloc(&b->team_ints, sizeof(int) * counts.size()) != cudaSuccess ||
+      cudaMemcpy(b->team_ints, counts.data(), sizeof(int) * counts.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return SGDYN_ERR_CUDA;
   if (!all.empty() && cudaMemcpy(b->teams, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return SGDYN_ERR_CUDA;
@@ -359,14 +406,19 @@ int sgdyn_batch_create(const sgdyn_model* const* models, int nmodels, const int*
   // pack tables (16-byte aligned offsets)
   std::vector<unsigned char> packed;
   std::vector<int64_t> offs;
+  std::vector<int> sizes;
   for (auto* m : b->models) {
     const auto& t = m->impl->host_table();
     offs.push_back(int64_t(packed.size()));
+    sizes.push_back(int((t.size() + 15) / 16 * 16));
     packed.insert(packed.end(), t.begin(), t.end());
     while (packed.size() % 256) packed.push_back(0);
   }
+  b->max_table_bytes = *std::max_element(sizes.begin(), sizes.end());
   if (cudaMalloc(&b->tables, packed.size()) != cudaSuccess ||
       cudaMalloc(&b->offsets, sizeof(int64_t) * offs.size()) != cudaSuccess ||
+      cudaMalloc(&b->table_bytes, sizeof(int) * sizes.size()) != cudaSuccess ||
+      cudaMemcpy(b->table_bytes, sizes.data(), sizeof(int) * sizes.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMalloc(&b->head, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemcpy(b->tables, packed.data(), packed.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->offsets, offs.data(), sizeof(int64_t) * offs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -466,6 +518,10 @@ static int batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd
   a.table_offset = b->offsets;
   a.teams = b->teams;
   a.team_offset = b->team_offsets;
+  a.table_bytes = b->table_bytes;
+  a.team_ints = b->team_ints;
+  a.stage_team_at = b->max_table_bytes;
+  a.stage_bytes = (b->max_table_bytes + 4 * b->max_team_ints + 15) / 16 * 16;
   a.perm = b->perm;
   a.tiles = b->tiles;
   a.ntiles = b->ntiles;
