@@ -101,6 +101,10 @@ def parse_args():
     ap.add_argument("--n", type=int, default=N_ENVS)
     ap.add_argument("--only-rollout", action="store_true",
                     help="run only the differentiable-rollout workload (for profiling its kernels)")
+    ap.add_argument("--only-hetero", choices=["mix", "humanoid"],
+                    help="run only the heterogeneous RNEA + ABA + CRBA step, on the 8192-robot mix or on its 1638 "
+                         "humanoids alone, at a fixed launch shape (2 CTAs per SM, one warp each) and lanes (1, 1, 4), "
+                         "three steps (for profiling its kernel)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the secondary workloads (rollout, heterogeneous batch, IK, derivatives)")
     return ap.parse_args()
@@ -243,6 +247,40 @@ def _event_ms(torch, fn, reps=5, warm=2):
     b.record()
     torch.cuda.synchronize()
     return a.elapsed_time(b) / reps
+
+
+def hetero_only(dev, which):
+    """The heterogeneous step alone at a fixed launch shape: the 8192-robot mix, or its
+    humanoids alone; three steps after one warm-up, CUDA events."""
+    import torch
+
+    from sapien_gb300 import PinocchioModel, synthetic
+    from sapien_gb300.hetero import OPS_DYNAMICS, HeteroBatch
+
+    robots, moe = synthetic.hetero_mix(8192, seed=0)
+    if which == "humanoid":
+        moe = np.full(int((moe == 2).sum()), 2, dtype=np.int32)
+    models = []
+    for r in robots:
+        m = PinocchioModel(r.urdf, [0.0, 0.0, -9.81])
+        m.set_joint_order(r.joint_names)
+        m.set_link_order(r.link_names)
+        models.append(m)
+    ins = []
+    for k, r in enumerate(robots):
+        c = int((moe == k).sum())
+        ins.append([a[:c] for a in r.sample(max(c, 1), seed=k)])
+    hb = HeteroBatch(models, moe, device=dev)
+    args = (hb.pad_q([x[0] for x in ins]), hb.pad_v([x[1] for x in ins]), hb.pad_v([x[2] for x in ins]),
+            hb.pad_v([x[3] for x in ins]))
+    out = hb.alloc_outputs(OPS_DYNAMICS)
+    hb.set_launch(2, 1, 0)
+    hb.set_lanes([1, 1, 4])
+    hb.step(*args, OPS_DYNAMICS, out)
+    torch.cuda.synchronize()
+    ms = _event_ms(torch, lambda: hb.step(*args, OPS_DYNAMICS, out), reps=3, warm=0)
+    return {"workload": f"{len(moe)} envs ({which}), RNEA+ABA+CRBA", "ms_per_step": ms, "launch_shape": [2, 1, 0],
+            "lanes_per_env": [1, 1, 4]}
 
 
 def secondary_workloads(dev, only_rollout=False):
@@ -564,6 +602,11 @@ def main():
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
         torch.cuda.set_device(dev)
         print(json.dumps({"secondary": secondary_workloads(dev, only_rollout=True)}), flush=True)
+        return
+    if args.only_hetero:
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        torch.cuda.set_device(dev)
+        print(json.dumps({"hetero_only": hetero_only(dev, args.only_hetero)}), flush=True)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
