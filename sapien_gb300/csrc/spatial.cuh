@@ -122,9 +122,12 @@ SG_HD void R_to_quat(const M3& R, double* q) {
     if (a[8] > a[i * 4]) i = 2;
     c = 1 + i;
   }
-  // sqrt argument: t + 1, or R_ii - R_jj - R_kk + 1 with (i, j, k) cyclic
-  const int i = c > 0 ? c - 1 : 0, j = i == 2 ? 0 : i + 1, k = j == 2 ? 0 : j + 1;
-  const double diag = a[i * 4] - a[j * 4] - a[k * 4] + 1.0;
+  // sqrt argument: t + 1, or R_ii - R_jj - R_kk + 1 with (i, j, k) cyclic (the diagonal
+  // entries picked by selects, so that R stays in registers)
+  const double di = c <= 1 ? a[0] : (c == 2 ? a[4] : a[8]);
+  const double dj = c <= 1 ? a[4] : (c == 2 ? a[8] : a[0]);
+  const double dk = c <= 1 ? a[8] : (c == 2 ? a[0] : a[4]);
+  const double diag = di - dj - dk + 1.0;
   const double r = sqrt(c == 0 ? t + 1.0 : diag);
   const double kk = 0.5 / r;
   const double d1 = a[7] - a[5], d2 = a[2] - a[6], d3 = a[3] - a[1];
