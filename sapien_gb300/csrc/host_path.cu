@@ -43,7 +43,8 @@ Arr host_arr(const void* p, int64_t n, int64_t cols, int layout) {
 
 // Contiguous ranges of [0, n) over up to nthreads threads (the caller's thread takes the
 // first range).
-void parallel_envs(int64_t n, int nthreads, const std::function<void(int64_t, int64_t)>& body) {
+template <class Body>
+void parallel_envs(int64_t n, int nthreads, const Body& body) {
   const int64_t t = nthreads <= 1 ? 1 : std::min<int64_t>(nthreads, n);
   if (t <= 1) {
     body(0, n);
@@ -162,21 +163,21 @@ int sgdyn_host_step(const sgdyn_model* m, int64_t n, int ops, const double* q, c
     a.tau_out = host_arr(tau_out, n, nv, layout);
     a.qdd_out = host_arr(qdd_out, n, nv, layout);
     // the op set as the fused sweeps the device side also uses, then single ops
-    std::vector<int> parts;
+    int parts[8], np = 0;
     int rest = ops;
     for (int f : {int(OP_ALL), OP_CRBA | OP_RNEA | OP_ABA, OP_RNEA | OP_ABA, OP_FK | OP_JAC})
       if ((rest & f) == f) {
-        parts.push_back(f);
+        parts[np++] = f;
         rest &= ~f;
       }
     for (int b = 1; b <= OP_ABA; b <<= 1)
-      if (rest & b) parts.push_back(b);
-    for (int& o : parts)  // the forward-dynamics route with fewer operations (sgdyn_fd_method)
-      if (fd_by_mass_matrix(Mo, o)) o |= OP_FD_CRBA;
+      if (rest & b) parts[np++] = b;
+    for (int k = 0; k < np; k++)  // the forward-dynamics route with fewer operations (sgdyn_fd_method)
+      if (fd_by_mass_matrix(Mo, parts[k])) parts[k] |= OP_FD_CRBA;
     const DModel* dm = table(m);
     const int bucket = stash_bucket(Mo.njoints());
     parallel_envs(n, nthreads, [&](int64_t lo, int64_t hi) {
-      for (int o : parts) run_ops(bucket, o, dm, a, lo, hi);
+      for (int k = 0; k < np; k++) run_ops(bucket, parts[k], dm, a, lo, hi);
     });
     return SGDYN_OK;
   });

@@ -152,6 +152,9 @@ bool team3_kind(int kind) { return kind == JIT_ROLLOUT_FWD3 || kind == JIT_ROLLO
 // Environments per 32-thread block of each kernel kind.
 int envs_per_block(int kind) { return team3_kind(kind) ? 10 : 32; }
 
+// Columns of the largest tree a model may have (63 moving joints, one of them a free flyer).
+constexpr int kMaxTreeColumns = 63 + 5;
+
 // Tree columns of the joint table: ancestors of each column, nearest first (empty if the
 // numbering does not put parents first), and external column numbers.
 struct Columns {
@@ -442,32 +445,34 @@ bool fd_by_mass_matrix(const Model& M, int ops) {
   const auto& t = M.host_table();
   const auto* hdr = reinterpret_cast<const DModel*>(t.data());
   const DJoint* J = model_joints(hdr);
-  const int nj = hdr->nj;
-  if (!tree_columns(J, nj, hdr->nv).ok) return false;
-  const int mode = g_fd_method.load();
-  if (mode != 0) return mode == 2;
-  std::vector<int> depth(size_t(hdr->nv > 0 ? hdr->nv : 1), 0);  // ancestor columns per column
-  double art = 0, mm = 0;
+  const int nj = hdr->nj, nv = hdr->nv;
+  // ancestor columns per column (no allocation: this runs on every host-path call); the
+  // route needs parents numbered before children
+  int depth[kMaxTreeColumns];
+  if (nv > kMaxTreeColumns) return false;
   for (int i = 1; i < nj; i++) {
     const int p = J[i].parent;
+    if (p > 0 && J[p].ivx + J[p].nv > J[i].ivx) return false;
     const int base = p > 0 ? depth[J[p].ivx + J[p].nv - 1] + 1 : 0;
     for (int k = 0; k < J[i].nv; k++) depth[J[i].ivx + k] = base + k;
-    art += J[i].nv == 1 ? 205 : (p == 0 ? 550 : 1400);
+  }
+  const int mode = g_fd_method.load();
+  if (mode != 0) return mode == 2;
+  double art = 0, mm = 0;
+  for (int i = 1; i < nj; i++) {
+    art += J[i].nv == 1 ? 205 : (J[i].parent == 0 ? 550 : 1400);
     if (!(ops & OP_CRBA)) mm += 10;
     if (!(ops & OP_RNEA)) mm += 60;
   }
-  for (int a = 0; a < hdr->nv; a++) {
+  for (int a = 0; a < nv; a++) {
     const int d = depth[a];
     if (!(ops & OP_CRBA)) mm += 24 + 6 * (d + 1);
     mm += 5 + 2 * d + 2;                // reciprocal, solve
     if (ops & OP_RNEA) mm += 2 * d + 1;  // M qdd
+    // factorisation: column a updates, for each ancestor c (depths d-1 .. 0), c's row over
+    // c and its ancestors
+    mm += double(d) * (d - 1) / 2 + 2.0 * d;
   }
-  // factorisation: column a updates, for each ancestor c, c's row over c and its ancestors
-  for (int i = 1; i < nj; i++)
-    for (int k = 0; k < J[i].nv; k++) {
-      int d = depth[J[i].ivx + k];
-      for (int c = d - 1; c >= 0; c--) mm += c + 2;  // ancestors sit at depths d-1 .. 0
-    }
   return mm < art;
 }
 
