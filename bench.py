@@ -388,7 +388,42 @@ def secondary_workloads(dev, only_rollout=False):
                           "aba_derivatives_evals_per_s": 8192 / (adr * 1e-3)}
     out["derivatives"].update(_derivative_parity(ad, hum, hm, hq2, hqd2, hqdd2, htau2))
     out["reference_robots"] = _reference_robot_parity(torch, dev)
+    out["single_instance"] = _single_instance_latency(arm)
     return out
+
+
+def _single_instance_latency(arm, calls=2000):
+    """The drop-in's one-configuration calls (`PinocchioModel` methods with numpy vectors, as
+    the reference's callers make them), answered on the host by the library's sweeps: mean
+    wall-clock microseconds per call on this machine's CPU, Python and ctypes included."""
+    import time
+
+    from sapien_gb300 import PinocchioModel
+
+    pm = PinocchioModel(arm.urdf, [0.0, 0.0, -9.81])
+    pm.set_joint_order(arm.joint_names)
+    pm.set_link_order(arm.link_names)
+    q, qd, qdd, tau = (a[0].copy() for a in arm.sample(1, seed=5))
+
+    def per_call(fn, n=calls):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            fn()
+        return (time.perf_counter() - t0) / n * 1e6
+
+    pm.compute_forward_kinematics(q)
+    target = pm.get_link_pose(arm.ee_link)
+    return {"workload": "arm9, one configuration per call through PinocchioModel (host path)",
+            "unit": "us per call",
+            "forward_dynamics": per_call(lambda: pm.compute_forward_dynamics(q, qd, tau)),
+            "inverse_dynamics": per_call(lambda: pm.compute_inverse_dynamics(q, qd, qdd)),
+            "mass_matrix": per_call(lambda: pm.compute_generalized_mass_matrix(q)),
+            "forward_kinematics_and_link_pose": per_call(lambda: (pm.compute_forward_kinematics(q),
+                                                                  pm.get_link_pose(arm.ee_link))),
+            "inverse_kinematics_100_iterations": per_call(
+                lambda: pm.compute_inverse_kinematics(arm.ee_link, target, initial_qpos=q * 0.9, eps=0.0,
+                                                      max_iterations=100), n=100)}
 
 
 def _oracle_of(robot):
