@@ -199,7 +199,11 @@ int sgdyn_model_team_table(const sgdyn_model* m, int lanes, const int** data, in
  * slower). Compile
  * ahead with sgdyn_jit_prepare (needed before capturing launches into a CUDA graph).
  * `ops`: an SGDYN_OP_* mask for the fused sweep, -1 for the forward rollout kernel, -2 / -3
- * for the RNEA / ABA vector-Jacobian product kernels. */
+ * for the RNEA / ABA vector-Jacobian product kernels, -4 / -5 for the forward rollout and the
+ * reverse sweep with three lanes per environment, -6 for forward dynamics on three lanes, -7
+ * for the CRBA + RNEA + ABA sweep of a model run with teams (sgdyn_model_set_lanes 2, 4 or 8)
+ * as one warp per role of the team (the size limit then counts the trunk and the longest
+ * role). */
 int sgdyn_jit_config(int enable, int64_t min_n, int* enabled, int64_t* min_n_out);
 /* Size limit of run-time specialisation (joints incl. the universe; < 0 leaves it). */
 int sgdyn_jit_max_joints(int max_joints, int* max_joints_out);

@@ -268,6 +268,8 @@ int run_step(const sgdyn_model* m, int64_t n, int ops, const double* q, const do
   }
   for (int o : launches) {
     if (team) {  // several lanes per environment
+      std::string why;
+      if (launch_step_roles_jit(Mo, lanes, o, a, s, &why)) continue;  // one warp per role, specialised
       cudaError_t e = launch_step_team(dm, Mo.njoints(), team, lanes, o, a, s);
       if (e != cudaSuccess) return fail(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
       continue;
@@ -482,7 +484,7 @@ int sgdyn_jit_config(int enable, int64_t min_n, int* enabled_out, int64_t* min_n
 // RNEA / ABA vector-Jacobian product kernels; -4: the forward rollout with three lanes per
 // environment; -5: the backward's reverse sweep with three lanes per environment; -6:
 // forward dynamics alone with three lanes per environment
-static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -6 && ops <= -1); }
+static bool jit_kind_ok(int ops) { return (ops > 0 && ops <= OP_ALL) || (ops >= -7 && ops <= -1); }
 
 int sgdyn_rollout_lanes(int lanes, int* lanes_out) {
   if (lanes != -1 && lanes != 0 && lanes != 1 && lanes != 3)
@@ -502,8 +504,10 @@ int sgdyn_step_split(int mode, int* mode_out) {
 int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
   if (!m) return fail(SGDYN_ERR_NULL, "null model");
   if (!jit_kind_ok(ops)) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
+  if (ops == -7 && m->impl->lanes <= 1) return fail(SGDYN_ERR_RUNTIME, "the model runs with one lane per environment");
   std::string why;
   const bool ok = ops > 0     ? prepare_step_jit(*m->impl, ops, &why)
+                  : ops == -7 ? prepare_step_roles_jit(*m->impl, m->impl->lanes, OP_CRBA | OP_RNEA | OP_ABA, &why)
                   : ops == -1 ? prepare_rollout_jit(*m->impl, &why)
                   : ops == -6 ? prepare_aba3_jit(*m->impl, &why)
                   : ops <= -4 ? prepare_rollout3_jit(*m->impl, ops == -5, &why)
@@ -515,8 +519,10 @@ int sgdyn_jit_prepare(const sgdyn_model* m, int ops) {
 int sgdyn_jit_source(const sgdyn_model* m, int ops, const char** source) {
   if (!m || !source) return fail(SGDYN_ERR_NULL, "null argument");
   if (!jit_kind_ok(ops)) return fail(SGDYN_ERR_RUNTIME, "bad op mask");
+  if (ops == -7 && m->impl->lanes <= 1) return fail(SGDYN_ERR_RUNTIME, "the model runs with one lane per environment");
   thread_local std::string buf;
   buf = ops > 0     ? step_jit_source(*m->impl, ops)
+        : ops == -7 ? step_roles_jit_source(*m->impl, m->impl->lanes, OP_CRBA | OP_RNEA | OP_ABA)
         : ops == -1 ? rollout_jit_source(*m->impl)
         : ops == -6 ? aba3_jit_source(*m->impl)
         : ops <= -4 ? rollout3_jit_source(*m->impl, ops == -5)

@@ -22,6 +22,7 @@
 
 #include "../../include/sgdyn.h"
 #include "trace.h"
+#include "jit.h"
 #include "model.h"
 #include "se3.cuh"
 #include "step_kernel.cuh"
@@ -243,6 +244,13 @@ struct sgdyn_batch {
   int* perm = nullptr;
   int4* tiles = nullptr;
   int ntiles = 0;
+  // the models run with teams can take the specialised one-warp-per-role sweep (a launch
+  // each, beside the persistent kernel, which then takes the other models' tiles only)
+  int* model_rows = nullptr;  // environments of each model, model after model
+  std::vector<int64_t> model_row_start, model_row_count;
+  int4* rest_tiles = nullptr;  // the tiles of the models with one lane per environment
+  int nrest = 0;
+  std::vector<cudaStream_t> side;
   unsigned int* head = nullptr;
   int device = -1;
   // launch shape (autotuned)
@@ -268,6 +276,10 @@ void free_device(sgdyn_batch* b) {
   cudaFree(b->perm);
   cudaFree(b->tiles);
   cudaFree(b->head);
+  cudaFree(b->model_rows);
+  cudaFree(b->rest_tiles);
+  b->model_rows = nullptr;
+  b->rest_tiles = nullptr;
   b->tables = nullptr;
   b->offsets = nullptr;
   b->perm = nullptr;
@@ -312,13 +324,37 @@ int upload_plan(sgdyn_batch* b) {
       tiles.push_back(make_int4(m, start, cnt, b->lanes[m]));
     }
   }
+  std::vector<int> rows;
+  b->model_row_start.assign(nm, 0);
+  b->model_row_count.assign(nm, 0);
+  for (int m = 0; m < nm; m++) {
+    b->model_row_start[m] = int64_t(rows.size());
+    b->model_row_count[m] = int64_t(envs[m].size());
+    rows.insert(rows.end(), envs[m].begin(), envs[m].end());
+  }
+  std::vector<int4> rest;
+  for (const int4& t : tiles)
+    if (t.w <= 1) rest.push_back(t);
   cudaFree(b->perm);
   cudaFree(b->tiles);
+  cudaFree(b->model_rows);
+  cudaFree(b->rest_tiles);
   b->perm = nullptr;
   b->tiles = nullptr;
+  b->model_rows = nullptr;
+  b->rest_tiles = nullptr;
   if (cudaMalloc(&b->perm, sizeof(int) * std::max<size_t>(perm.size(), 1)) != cudaSuccess ||
-      cudaMalloc(&b->tiles, sizeof(int4) * std::max<size_t>(tiles.size(), 1)) != cudaSuccess)
+      cudaMalloc(&b->tiles, sizeof(int4) * std::max<size_t>(tiles.size(), 1)) != cudaSuccess ||
+      cudaMalloc(&b->model_rows, sizeof(int) * std::max<size_t>(rows.size(), 1)) != cudaSuccess ||
+      cudaMalloc(&b->rest_tiles, sizeof(int4) * std::max<size_t>(rest.size(), 1)) != cudaSuccess)
     return SGDYN_ERR_CUDA;
+  if (!rows.empty() && cudaMemcpy(b->model_rows, rows.data(), sizeof(int) * rows.size(), cudaMemcpyHostToDevice) !=
+                           cudaSuccess)
+    return SGDYN_ERR_CUDA;
+  if (!rest.empty() &&
+      cudaMemcpy(b->rest_tiles, rest.data(), sizeof(int4) * rest.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return SGDYN_ERR_CUDA;
+  b->nrest = int(rest.size());
   if (!perm.empty() && cudaMemcpy(b->perm, perm.data(), sizeof(int) * perm.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return SGDYN_ERR_CUDA;
   if (!tiles.empty() &&
@@ -437,6 +473,8 @@ int sgdyn_batch_create(const sgdyn_model* const* models, int nmodels, const int*
 void sgdyn_batch_free(sgdyn_batch* b) {
   if (!b) return;
   free_device(b);
+  for (cudaStream_t st : b->side)
+    if (st) cudaStreamDestroy(st);
   delete b;
 }
 
@@ -541,11 +579,60 @@ static int batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd
   a.q_state = const_cast<double*>(q);
   a.qd_state = const_cast<double*>(qd);
   auto s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(b->head, 0, sizeof(unsigned int), s);
-  if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("memset failed: ") + cudaGetErrorString(e));
-  dim3 grid(unsigned(b->sms * b->ctas_per_sm)), block(unsigned(32 * b->warps_per_cta));
-  e = (b->max_nj <= 16) ? launch_hetero_bucket<16>(ops, a, grid, block, s)
-                        : launch_hetero_bucket<32>(ops, a, grid, block, s);
+  // models run with teams: the specialised one-warp-per-role sweep when it is available for
+  // every one of them (run-time compilation on, sizes within its limits), each on a side
+  // stream of the batch beside the persistent kernel, which takes the remaining tiles
+  std::vector<int> roles;
+  if (!integrate) {
+    bool ok = true;
+    for (size_t m = 0; m < b->models.size() && ok; m++)
+      if (b->lanes[m] > 1 && b->model_row_count[m] > 0) {
+        std::string why;
+        ok = step_roles_jit_ready(*b->models[m]->impl, b->lanes[m], ops, b->n, &why);
+        roles.push_back(int(m));
+      }
+    if (!ok) roles.clear();
+  }
+  while (b->side.size() < roles.size()) {
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+      return set_last_error(SGDYN_ERR_CUDA, "stream creation failed");
+    b->side.push_back(st);
+  }
+  cudaError_t e = cudaSuccess;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  if (!roles.empty()) {
+    e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(fork, s);
+    for (size_t r = 0; r < roles.size() && e == cudaSuccess; r++) {
+      const int m = roles[r];
+      e = cudaStreamWaitEvent(b->side[r], fork, 0);
+      std::string why;
+      if (e == cudaSuccess &&
+          !launch_step_roles_rows_jit(*b->models[m]->impl, b->lanes[m], ops, a.io, b->model_rows + b->model_row_start[m],
+                                      b->model_row_count[m], b->side[r], &why))
+        e = cudaErrorLaunchFailure;
+      cudaEvent_t j = nullptr;
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(j, b->side[r]);
+      if (j) joins.push_back(j);
+    }
+    a.tiles = b->rest_tiles;
+    a.ntiles = b->nrest;
+  }
+  if (e == cudaSuccess && a.ntiles > 0) {
+    e = cudaMemsetAsync(b->head, 0, sizeof(unsigned int), s);
+    dim3 grid(unsigned(b->sms * b->ctas_per_sm)), block(unsigned(32 * b->warps_per_cta));
+    if (e == cudaSuccess)
+      e = (b->max_nj <= 16) ? launch_hetero_bucket<16>(ops, a, grid, block, s)
+                            : launch_hetero_bucket<32>(ops, a, grid, block, s);
+  }
+  for (cudaEvent_t j : joins) {
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, j, 0);
+    cudaEventDestroy(j);  // released once the recorded work completes
+  }
+  if (fork) cudaEventDestroy(fork);
   if (e != cudaSuccess) return set_last_error(SGDYN_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   return SGDYN_OK;
 }

@@ -19,6 +19,7 @@
 #include <unistd.h>
 
 #include <atomic>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -140,17 +141,20 @@ std::string list(It b, It e) {
 // fully unrolled reverse sweep spills heavily).
 enum JitKind {
   JIT_STEP = 0, JIT_ROLLOUT_FWD = 1, JIT_RNEA_VJP = 2, JIT_ABA_VJP = 3, JIT_ROLLOUT_FWD3 = 4, JIT_ROLLOUT_REV3 = 5,
-  JIT_ABA3 = 6
+  JIT_ABA3 = 6, JIT_STEP_ROLES = 7
 };
 const char* kernel_name(int kind) {
   static const char* const names[] = {"sgjit_step",    "sgjit_rollout_forward",  "sgjit_rnea_vjp",
                                       "sgjit_aba_vjp", "sgjit_rollout_forward3", "sgjit_rollout_reverse3",
-                                      "sgjit_aba3"};
+                                      "sgjit_aba3",    "sgjit_step_roles"};
   return names[kind];
 }
 bool team3_kind(int kind) { return kind == JIT_ROLLOUT_FWD3 || kind == JIT_ROLLOUT_REV3 || kind == JIT_ABA3; }
-// Environments per 32-thread block of each kernel kind.
+// Environments per block of each kernel kind (blocks of 32 threads, but JIT_STEP_ROLES: one
+// warp per role of the team, 32 environments).
 int envs_per_block(int kind) { return team3_kind(kind) ? 10 : 32; }
+// The role-warp sweep's key packs the lanes per environment above the op bits.
+constexpr int kRoleLanesShift = 8;
 
 // Columns of the largest tree a model may have (63 moving joints, one of them a free flyer).
 constexpr int kMaxTreeColumns = 63 + 5;
@@ -250,7 +254,7 @@ std::string generate_source(const Model& M, int kind, int ops) {
   const DLink* L = model_links(hdr);
   const int nj = hdr->nj, nl = hdr->nlinks;
   std::ostringstream o;
-  o << (kind == JIT_STEP        ? "#include \"step_kernel.cuh\"\n"
+  o << (kind == JIT_STEP || kind == JIT_STEP_ROLES ? "#include \"step_kernel.cuh\"\n"
         : team3_kind(kind) ? "#include \"team3.cuh\"\n"
                            : "#include \"diff_kernels.cuh\"\n");
   o << "namespace sgjit {\n";
@@ -275,9 +279,35 @@ std::string generate_source(const Model& M, int kind, int ops) {
   const bool fd = kind == JIT_STEP && (ops & OP_FD_CRBA);
   if (fd) emit_fd(o, tree_columns(J, nj, hdr->nv), hdr->nv);
   o << "}  // namespace sgjit\n";
+  int lanes = 0;
+  if (kind == JIT_STEP_ROLES) {  // the team table as constants (roles are the block's warps)
+    lanes = ops >> kRoleLanesShift;
+    ops &= (1 << kRoleLanesShift) - 1;
+    const std::vector<int> tt = M.team_table(lanes);
+    o << "namespace sgjit {\n__device__ constexpr int kTT[" << tt.size() << "] = {";
+    for (size_t k = 0; k < tt.size(); k++) o << (k ? ", " : "") << tt[k];
+    o << "};\n}  // namespace sgjit\n";
+  }
   const std::string tab = "sgdyn::StaticTab<" + std::to_string(nj) + ", " + std::to_string(hdr->nv) + ", " +
                           std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM" + (fd ? ", sgjit::kFd" : "") +
                           ">()";
+  if (kind == JIT_STEP_ROLES) {
+    // rows: the environments' row indices (null: 0 .. count - 1)
+    o << "extern \"C\" __global__ void __launch_bounds__(" << 32 * lanes
+      << ") sgjit_step_roles(const sgdyn::StepArgs a, const int* rows, long long count) {\n"
+      << "  __shared__ double xch[" << 32 * lanes << "];\n"
+      << "  const int role = threadIdx.x >> 5, lane = threadIdx.x & 31;\n"
+      << "  const long long i0 = (long long)blockIdx.x * 32 + lane;\n"
+      << "  const bool valid = i0 < count;\n"
+      << "  const long long i = valid ? i0 : count - 1;\n"
+      << "  const long long e = rows ? (long long)rows[i] : i;\n"
+      << "  switch (role) {\n";
+    for (int r = 0; r < lanes; r++)
+      o << "    case " << r << ": sgdyn::step_env_t<" << nj << ", " << ops << ">(" << tab << ", a, e, sgdyn::RoleTeam<" << r
+        << ", sgjit::kTT>{xch, lane, valid}); break;\n";
+    o << "  }\n}\n";
+    return o.str();
+  }
   const char* args = (kind == JIT_STEP || kind == JIT_ABA3)                 ? "sgdyn::StepArgs"
                      : (kind == JIT_ROLLOUT_FWD || team3_kind(kind)) ? "sgdyn::RolloutArgs"
                                                                              : "sgdyn::VjpArgs";
@@ -525,7 +555,8 @@ bool prepare_rollout_jit(Model& M, std::string* why) {
 
 namespace {
 template <class Args>
-bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std::string* why) {
+bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std::string* why, int joints = -1,
+                int threads = 32) {
   CUfunction fn;
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -538,7 +569,7 @@ bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std:
       *why = "batch below the run-time compilation threshold";
       return false;
     }
-    if (M.njoints() > g_max_joints) {
+    if ((joints >= 0 ? joints : M.njoints()) > g_max_joints) {
       *why = "tree above the run-time compilation size limit";
       return false;
     }
@@ -549,8 +580,8 @@ bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std:
   void* params[] = {&args};
   const int per = envs_per_block(kind);
   const unsigned blocks = unsigned((a.n + per - 1) / per);
-  if (api().launchKernel(fn, blocks, 1, 1, 32, 1, 1, 0, reinterpret_cast<CUstream>(s), params, nullptr) !=
-      CUDA_SUCCESS) {
+  if (api().launchKernel(fn, blocks, 1, 1, unsigned(threads), 1, 1, 0, reinterpret_cast<CUstream>(s), params,
+                         nullptr) != CUDA_SUCCESS) {
     *why = "cuLaunchKernel failed";
     return false;
   }
@@ -560,6 +591,72 @@ bool launch_jit(Model& M, int kind, int ops, const Args& a, cudaStream_t s, std:
 
 bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why) {
   return launch_jit(M, JIT_STEP, step_kernel_ops(M, ops), a, s, why);
+}
+
+namespace {
+// The size limit applies to what one warp sweeps: the trunk and the longest role.
+int role_joints(const Model& M, int lanes) {
+  const std::vector<int> tt = M.team_table(lanes);
+  return 1 + tt[1] + tt[2];
+}
+
+CUfunction roles_function(Model& M, int lanes, int ops, int64_t n, std::string* why) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  if (!g_enable) {
+    *why = "disabled";
+    return nullptr;
+  }
+  if (n < g_min_n) {
+    *why = "batch below the run-time compilation threshold";
+    return nullptr;
+  }
+  if (role_joints(M, lanes) > g_max_joints) {
+    *why = "tree above the run-time compilation size limit";
+    return nullptr;
+  }
+  return get_function(M, JIT_STEP_ROLES, ops | (lanes << kRoleLanesShift), why);
+}
+
+bool launch_roles(CUfunction fn, int lanes, const StepArgs& a, const int* rows, int64_t count, cudaStream_t s,
+                  std::string* why) {
+  StepArgs args = a;
+  long long cnt = count;
+  void* params[] = {&args, &rows, &cnt};
+  if (api().launchKernel(fn, unsigned((count + 31) / 32), 1, 1, unsigned(32 * lanes), 1, 1, 0,
+                         reinterpret_cast<CUstream>(s), params, nullptr) != CUDA_SUCCESS) {
+    *why = "cuLaunchKernel failed";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+bool launch_step_roles_jit(Model& M, int lanes, int ops, const StepArgs& a, cudaStream_t s, std::string* why) {
+  CUfunction fn = roles_function(M, lanes, ops, a.n, why);
+  return fn && launch_roles(fn, lanes, a, nullptr, a.n, s, why);
+}
+
+bool step_roles_jit_ready(Model& M, int lanes, int ops, int64_t n, std::string* why) {
+  return roles_function(M, lanes, ops, n, why) != nullptr;
+}
+
+bool launch_step_roles_rows_jit(Model& M, int lanes, int ops, const StepArgs& a, const int* rows, int64_t count,
+                                cudaStream_t s, std::string* why) {
+  // (the batch-size threshold was applied to the whole batch by step_roles_jit_ready)
+  CUfunction fn = roles_function(M, lanes, ops, INT64_MAX, why);
+  return fn && launch_roles(fn, lanes, a, rows, count, s, why);
+}
+
+bool prepare_step_roles_jit(Model& M, int lanes, int ops, std::string* why) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  read_env_config();
+  return get_function(M, JIT_STEP_ROLES, ops | (lanes << kRoleLanesShift), why) != nullptr;
+}
+
+std::string step_roles_jit_source(const Model& M, int lanes, int ops) {
+  return generate_source(M, JIT_STEP_ROLES, ops | (lanes << kRoleLanesShift));
 }
 
 bool launch_rollout_jit(Model& M, const RolloutArgs& a, cudaStream_t s, std::string* why) {

@@ -15,6 +15,18 @@ class Model;
 // the batch is large enough; returns false (with the reason) when the caller should use the
 // generic kernel. Compiles and caches on first use of (model tables, ops, device).
 bool launch_step_jit(Model& M, int ops, const StepArgs& a, cudaStream_t s, std::string* why);
+// The fused sweep with L lanes per environment as one warp per role of the team (a block of
+// L warps holds 32 environments; team table and roles compiled in), for models run with
+// teams; false (with the reason) when the caller should use the generic team kernel.
+bool launch_step_roles_jit(Model& M, int lanes, int ops, const StepArgs& a, cudaStream_t s, std::string* why);
+std::string step_roles_jit_source(const Model& M, int lanes, int ops);
+// For a heterogeneous batch of n environments: whether the role-warp sweep of (M, lanes, ops)
+// is available (compiling it if needed), and its launch over `count` environments whose
+// rows of the call's arrays are rows[0 .. count - 1] (device memory).
+bool step_roles_jit_ready(Model& M, int lanes, int ops, int64_t n, std::string* why);
+bool launch_step_roles_rows_jit(Model& M, int lanes, int ops, const StepArgs& a, const int* rows, int64_t count,
+                                cudaStream_t s, std::string* why);
+bool prepare_step_roles_jit(Model& M, int lanes, int ops, std::string* why);
 // Same for the RNEA / ABA vector-Jacobian product kernels.
 bool launch_vjp_jit(Model& M, bool aba, const VjpArgs& a, cudaStream_t s, std::string* why);
 std::string vjp_jit_source(const Model& M, bool aba);

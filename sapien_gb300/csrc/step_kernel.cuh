@@ -210,6 +210,7 @@ struct TeamLanes {
   SG_HD int sched(int k) const { return t[4 + ntrunk() + role * smax() + k]; }
   SG_HD int attach(int k) const { return t[4 + ntrunk() + L() * smax() + k]; }
   SG_HD int owner(int j) const { return t[4 + ntrunk() + L() * smax() + nattach() + j]; }
+  SG_HD double sum(double v) const;
 };
 
 // Sum over the L lanes of a team (L a power of two, teams aligned in the warp).
@@ -220,6 +221,43 @@ SG_HD double team_sum(double v, int L) {
 #endif
   return v;
 }
+SG_HD double TeamLanes::sum(double v) const { return team_sum(v, L()); }
+
+// A team whose roles are the warps of a block (L warps, 32 environments; warp r takes role
+// r for every lane) with the team table and the role known at compile time (run-time
+// compiled per model): each warp's sweep covers the trunk and its own branches with
+// constant indices, so its state stays in registers like a one-lane specialised sweep, and
+// the warps run different code without diverging. Sums over the team go through shared
+// memory (xch: L x 32 doubles), in a fixed order, so every warp holds the same bits.
+template <int ROLE, const int* TT>
+struct RoleTeam {
+  static constexpr bool kOn = true;
+  static constexpr int role = ROLE;
+  double* xch;
+  int lane;
+  bool valid;
+  SG_HD static constexpr int L() { return TT[0]; }
+  SG_HD static constexpr int ntrunk() { return TT[1]; }
+  SG_HD static constexpr int smax() { return TT[2]; }
+  SG_HD static constexpr int nattach() { return TT[3]; }
+  SG_HD static constexpr int trunk(int k) { return TT[4 + k]; }
+  SG_HD static constexpr int sched(int k) { return TT[4 + ntrunk() + ROLE * smax() + k]; }
+  SG_HD static constexpr int attach(int k) { return TT[4 + ntrunk() + L() * smax() + k]; }
+  SG_HD static constexpr int owner(int j) { return TT[4 + ntrunk() + L() * smax() + nattach() + j]; }
+  SG_HD double sum(double v) const {
+#ifdef __CUDA_ARCH__
+    xch[ROLE * 32 + lane] = v;
+    __syncthreads();
+    double s = xch[lane];
+#pragma unroll
+    for (int r = 1; r < L(); r++) s += xch[r * 32 + lane];
+    __syncthreads();
+    return s;
+#else
+    return v;
+#endif
+  }
+};
 
 // Entry (a, b <= a) of a symmetric matrix over tree columns, lower triangle packed by rows.
 SG_HD constexpr int ltdm_at(int a, int b) { return a * (a + 1) / 2 + b; }
@@ -737,8 +775,11 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
       for (int i = 1; i < nj; i++) pass3(i);
     }
   } else {
-    const int nt = tm.ntrunk(), sm = tm.smax(), na = tm.nattach(), L = tm.L();
+    // (loops unrolled: with compile-time team tables every joint index is a constant)
+    const int nt = tm.ntrunk(), sm = tm.smax(), na = tm.nattach();
+#pragma unroll
     for (int k = 0; k < nt; k++) pass1(tm.trunk(k));
+#pragma unroll
     for (int k = 0; k < sm; k++) {
       const int j = tm.sched(k);
       if (j > 0) pass1(j);
@@ -749,12 +790,14 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
       // trunk slots start at zero; attach joints keep their own force / bias aside so that
       // the branch contributions alone are summed across the team
       Mot fbase[kRNEA ? MAXJ : 1], pbase[kArt ? MAXJ : 1];
+#pragma unroll
       for (int k = 0; k < nt; k++) {
         const int t = tm.trunk(k);
         if constexpr (kCRBA) CC[t] = RBI{0.0, mk(0, 0, 0), {0, 0, 0, 0, 0, 0}};
         if constexpr (kArt) AC[t] = Sym6{{0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}};
       }
       const Mot zero{mk(0, 0, 0), mk(0, 0, 0)};
+#pragma unroll
       for (int k = 0; k < na; k++) {
         const int t = tm.attach(k);
         if constexpr (kRNEA) {
@@ -766,14 +809,16 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
           pA[t] = zero;
         }
       }
+#pragma unroll
       for (int k = sm - 1; k >= 0; k--) {
         const int j = tm.sched(k);
         if (j > 0) pass2(j);
       }
       auto sum6 = [&](Mot& m) {
-        m.v.x = team_sum(m.v.x, L); m.v.y = team_sum(m.v.y, L); m.v.z = team_sum(m.v.z, L);
-        m.w.x = team_sum(m.w.x, L); m.w.y = team_sum(m.w.y, L); m.w.z = team_sum(m.w.z, L);
+        m.v.x = tm.sum(m.v.x); m.v.y = tm.sum(m.v.y); m.v.z = tm.sum(m.v.z);
+        m.w.x = tm.sum(m.w.x); m.w.y = tm.sum(m.w.y); m.w.z = tm.sum(m.w.z);
       };
+#pragma unroll
       for (int k = 0; k < na; k++) {
         const int t = tm.attach(k);
         if constexpr (kRNEA) {
@@ -782,25 +827,31 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
         }
         if constexpr (kCRBA) {
           RBI& c = CC[t];
-          c.m = team_sum(c.m, L);
-          c.h.x = team_sum(c.h.x, L); c.h.y = team_sum(c.h.y, L); c.h.z = team_sum(c.h.z, L);
-          for (int q = 0; q < 6; q++) c.I[q] = team_sum(c.I[q], L);
+          c.m = tm.sum(c.m);
+          c.h.x = tm.sum(c.h.x); c.h.y = tm.sum(c.h.y); c.h.z = tm.sum(c.h.z);
+#pragma unroll
+          for (int q = 0; q < 6; q++) c.I[q] = tm.sum(c.I[q]);
         }
         if constexpr (kArt) {
           Sym6& s = AC[t];
+#pragma unroll
           for (int q = 0; q < 6; q++) {
-            s.A[q] = team_sum(s.A[q], L);
-            s.C[q] = team_sum(s.C[q], L);
+            s.A[q] = tm.sum(s.A[q]);
+            s.C[q] = tm.sum(s.C[q]);
           }
-          for (int q = 0; q < 9; q++) s.B[q] = team_sum(s.B[q], L);
+#pragma unroll
+          for (int q = 0; q < 9; q++) s.B[q] = tm.sum(s.B[q]);
           sum6(pA[t]);
           pA[t] = add6(pbase[t], pA[t]);
         }
       }
+#pragma unroll
       for (int k = nt - 1; k >= 0; k--) pass2(tm.trunk(k));
     }
     if constexpr (kArt) {
+#pragma unroll
       for (int k = 0; k < nt; k++) pass3(tm.trunk(k));
+#pragma unroll
       for (int k = 0; k < sm; k++) {
         const int j = tm.sched(k);
         if (j > 0) pass3(j);

@@ -206,3 +206,37 @@ def test_hetero_full_size_mix_matches_oracle(lanes):
     g.replay()
     torch.cuda.synchronize()
     check_against_oracle(batch, oracles, inputs, g.outputs)
+
+
+def test_hetero_role_warp_sweeps_match_generic_and_graph():
+    """With run-time compilation on, the models run with teams take the specialised
+    one-warp-per-role sweep (a launch each, on side streams beside the persistent kernel,
+    which keeps the one-lane models' tiles): results equal the generic team path to rounding
+    and the oracle within tolerance, and a CUDA-graph replay equals the direct step bit for
+    bit."""
+    import ctypes
+
+    import torch
+
+    from sapien_gb300 import _native as N
+
+    batch, oracles, inputs, (q, qd, qdd, tau) = setup(n=600, seed=5)
+    batch.set_lanes([1, 2, 4])
+    L = N.load()
+    old_jit, old_min = ctypes.c_int(), ctypes.c_int64()
+    L.sgdyn_jit_config(-1, -1, ctypes.byref(old_jit), ctypes.byref(old_min))
+    try:
+        L.sgdyn_jit_config(0, 0, None, None)
+        generic = batch.step(q, qd, qdd, tau, OPS_DYNAMICS)
+        L.sgdyn_jit_config(1, 0, None, None)
+        roles = batch.step(q, qd, qdd, tau, OPS_DYNAMICS)
+        check_against_oracle(batch, oracles, inputs, roles)
+        g = batch.capture(q, qd, qdd, tau, steps=2)
+        g.replay()
+        torch.cuda.synchronize()
+    finally:
+        L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
+    for a, b in zip(valid_blocks(batch, roles), valid_blocks(batch, generic)):
+        assert rel_per_env(a.cpu().numpy(), b.cpu().numpy()) <= 1e-11
+    for a, b in zip(valid_blocks(batch, g.outputs), valid_blocks(batch, roles)):
+        assert torch.equal(a, b)

@@ -139,3 +139,37 @@ def test_specialised_vjp_matches_generic(name):
         jit_config(*old)
     for a, b in zip(spec, gen):
         assert rel_per_env(a, b) <= 1e-13
+
+
+@pytest.mark.parametrize("name,lanes", [("humanoid", 4), ("humanoid", 2), ("quadruped", 2), ("quadruped", 4)])
+def test_role_warp_team_sweep_matches_generic_team_and_oracle(name, lanes):
+    """A model run with teams of L lanes: the specialised sweep with one warp per role of the
+    team (block of L warps, team sums through shared memory) against the generic team kernel
+    (sums by warp shuffles) and the oracle, for the five ops and for CRBA + RNEA + ABA; 77
+    environments, so the last block is partly empty."""
+    import torch
+
+    robot = {"humanoid": syn.humanoid(), "quadruped": syn.quadruped()}[name]
+    pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
+    pm.set_joint_order(robot.joint_names)
+    pm.set_link_order(robot.link_names)
+    pm.set_lanes(lanes)
+    q, qd, qdd, tau = (torch.from_numpy(a).cuda() for a in robot.sample(77, seed=29))
+    o = Oracle(robot.urdf)
+    o.set_joint_order(robot.joint_names)
+    o.set_link_order(robot.link_names)
+    r = o.batch_step(*(x.cpu().numpy() for x in (q, qd, qdd, tau)), ops=4 | 8 | 16)
+    for ops in (N.OP_ALL, N.OP_MASS_MATRIX | N.OP_INVERSE_DYNAMICS | N.OP_FORWARD_DYNAMICS):
+        outs = {}
+        old = jit_config(-1, -1)
+        try:
+            for jit in (0, 1):
+                jit_config(jit, 0)
+                outs[jit] = {k: v.cpu().numpy() for k, v in pm.step_batched(q, qd, qdd, tau, ops=ops).items()}
+        finally:
+            jit_config(*old)
+        for k in outs[0]:
+            assert rel_per_env(outs[1][k], outs[0][k]) <= (1e-11 if k == "qacc" else 1e-13), (ops, k)
+        assert rel_per_env(outs[1]["mass_matrix"], r["M"]) <= 1e-10
+        assert rel_per_env(outs[1]["qf"], r["tau"]) <= 1e-10
+        assert rel_per_env(outs[1]["qacc"], r["qdd"]) <= 1e-8

@@ -2,7 +2,7 @@
 test: NVRTC needs no GPU). ``ops`` > 0 selects the fused sweep with that op set, -1 the forward
 rollout kernel, -2 / -3 the RNEA / ABA vector-Jacobian product kernels, -4 / -5 / -6 the forward
 rollout, the backward's reverse sweep and forward dynamics alone with three lanes per
-environment. GPU parity of the specialised kernels is in
+environment, -7 the CRBA + RNEA + ABA sweep as one warp per role of a team. GPU parity of the specialised kernels is in
 test_jit_gpu.py."""
 import ctypes
 import ctypes.util
@@ -32,7 +32,8 @@ def _headers():
 
 @pytest.mark.parametrize("name,ops", [("arm9", 31), ("arm9", 3), ("humanoid", 28), ("mixed", 8), ("arm9", -1),
                                       ("mixed", -1), ("quadruped", -1), ("arm9", -2), ("humanoid", -3),
-                                      ("arm9", -4), ("mixed", -4), ("arm9", -5), ("chain40", -5), ("arm9", -6)])
+                                      ("arm9", -4), ("mixed", -4), ("arm9", -5), ("chain40", -5), ("arm9", -6),
+                                      ("humanoid", -7)])
 def test_generated_source_compiles(name, ops):
     robot = {"arm9": syn.arm_with_fingers(), "humanoid": syn.humanoid(), "quadruped": syn.quadruped(),
              "chain40": syn.serial_chain(40, seed=23),
@@ -41,6 +42,8 @@ def test_generated_source_compiles(name, ops):
     pm = PinocchioModel(robot.urdf, [0, 0, -9.81])
     pm.set_joint_order(robot.joint_names)
     pm.set_link_order(robot.link_names)
+    if ops == -7:  # one warp per role of a 4-lane team
+        pm.set_lanes(4)
     src = ctypes.c_char_p()
     assert N.load().sgdyn_jit_source(pm._h, ops, ctypes.byref(src)) == 0
     nv = _nvrtc()

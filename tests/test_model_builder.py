@@ -237,7 +237,9 @@ def test_lanes_and_run_time_compilation_settings_are_validated():
     assert L.sgdyn_jit_max_joints(-1, ctypes.byref(cur)) == N.OK and cur.value == 32
     assert L.sgdyn_jit_max_joints(old.value, None) == N.OK
     src = ctypes.c_char_p()
-    assert L.sgdyn_jit_source(pm._h, -7, ctypes.byref(src)) != N.OK  # no such kernel kind
+    pm.set_lanes(1)
+    assert L.sgdyn_jit_source(pm._h, -7, ctypes.byref(src)) != N.OK  # the model runs with one lane
+    assert L.sgdyn_jit_source(pm._h, -8, ctypes.byref(src)) != N.OK  # no such kernel kind
     assert L.sgdyn_rollout_lanes(2, None) != N.OK and "rollout lanes" in N.last_error()
 
 
