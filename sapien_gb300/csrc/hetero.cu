@@ -61,24 +61,7 @@ struct HeteroArgs {
 // qd += dt qdd, then q advanced by dt qd on one environment's padded rows (angles and
 // slides add; a free flyer moves on SE(3) by its body twist).
 __device__ __forceinline__ void integrate_env(const DModel* m, double* q, double* qd, const double* qdd, double dt) {
-  const DJoint* JT = model_joints(m);
-  for (int i = 1; i < m->nj; i++) {
-    const DJoint& J = JT[i];
-    if (J.kind == JK_FREEFLYER) {
-      double v[6];
-#pragma unroll
-      for (int k = 0; k < 6; k++) {
-        const double w = fma(dt, qdd[J.vcol + k], qd[J.vcol + k]);
-        qd[J.vcol + k] = w;
-        v[k] = dt * w;
-      }
-      free_flyer_integrate(q + J.qcol, v);
-    } else {
-      const double w = fma(dt, qdd[J.vcol], qd[J.vcol]);
-      qd[J.vcol] = w;
-      q[J.qcol] = fma(dt, w, q[J.qcol]);
-    }
-  }
+  integrate_env_t(RuntimeTab{m}, q, qd, qdd, dt);
 }
 
 template <int MAXJ, int OPS>
@@ -583,7 +566,7 @@ static int batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd
   // every one of them (run-time compilation on, sizes within its limits), each on a side
   // stream of the batch beside the persistent kernel, which takes the remaining tiles
   std::vector<int> roles;
-  if (!integrate) {
+  {
     bool ok = true;
     for (size_t m = 0; m < b->models.size() && ok; m++)
       if (b->lanes[m] > 1 && b->model_row_count[m] > 0) {
@@ -611,7 +594,7 @@ static int batch_step(sgdyn_batch* b, int ops, const double* q, const double* qd
       std::string why;
       if (e == cudaSuccess &&
           !launch_step_roles_rows_jit(*b->models[m]->impl, b->lanes[m], ops, a.io, b->model_rows + b->model_row_start[m],
-                                      b->model_row_count[m], b->side[r], &why))
+                                      b->model_row_count[m], integrate ? dt : 0.0, integrate, b->side[r], &why))
         e = cudaErrorLaunchFailure;
       cudaEvent_t j = nullptr;
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j, cudaEventDisableTiming);

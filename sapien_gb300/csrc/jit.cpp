@@ -254,6 +254,7 @@ std::string generate_source(const Model& M, int kind, int ops) {
   const DLink* L = model_links(hdr);
   const int nj = hdr->nj, nl = hdr->nlinks;
   std::ostringstream o;
+  if (kind == JIT_STEP_ROLES) o << "#include \"se3.cuh\"\n";
   o << (kind == JIT_STEP || kind == JIT_STEP_ROLES ? "#include \"step_kernel.cuh\"\n"
         : team3_kind(kind) ? "#include \"team3.cuh\"\n"
                            : "#include \"diff_kernels.cuh\"\n");
@@ -292,9 +293,10 @@ std::string generate_source(const Model& M, int kind, int ops) {
                           std::to_string(nl) + ", sgjit::kJT, sgjit::kLT, &sgjit::kM" + (fd ? ", sgjit::kFd" : "") +
                           ">()";
   if (kind == JIT_STEP_ROLES) {
-    // rows: the environments' row indices (null: 0 .. count - 1)
+    // rows: the environments' row indices (null: 0 .. count - 1); integrate != 0: then a
+    // semi-implicit Euler step of q, qd (rows of a.q, a.qd, in place) from a.qdd_out
     o << "extern \"C\" __global__ void __launch_bounds__(" << 32 * lanes
-      << ") sgjit_step_roles(const sgdyn::StepArgs a, const int* rows, long long count) {\n"
+      << ") sgjit_step_roles(const sgdyn::StepArgs a, const int* rows, long long count, double dt, int integrate) {\n"
       << "  __shared__ double xch[" << 32 * lanes << "];\n"
       << "  const int role = threadIdx.x >> 5, lane = threadIdx.x & 31;\n"
       << "  const long long i0 = (long long)blockIdx.x * 32 + lane;\n"
@@ -305,7 +307,12 @@ std::string generate_source(const Model& M, int kind, int ops) {
     for (int r = 0; r < lanes; r++)
       o << "    case " << r << ": sgdyn::step_env_t<" << nj << ", " << ops << ">(" << tab << ", a, e, sgdyn::RoleTeam<" << r
         << ", sgjit::kTT>{xch, lane, valid}); break;\n";
-    o << "  }\n}\n";
+    o << "  }\n"
+      << "  if (integrate) {  // after every role has written its part of qdd\n"
+      << "    __syncthreads();\n"
+      << "    if (role == 0 && valid)\n"
+      << "      sgdyn::integrate_env_t(" << tab << ", a.q.p + e * a.q.es, a.qd.p + e * a.qd.es, a.qdd_out.p + e * a.qdd_out.es, dt);\n"
+      << "  }\n}\n";
     return o.str();
   }
   const char* args = (kind == JIT_STEP || kind == JIT_ABA3)                 ? "sgdyn::StepArgs"
@@ -618,11 +625,11 @@ CUfunction roles_function(Model& M, int lanes, int ops, int64_t n, std::string* 
   return get_function(M, JIT_STEP_ROLES, ops | (lanes << kRoleLanesShift), why);
 }
 
-bool launch_roles(CUfunction fn, int lanes, const StepArgs& a, const int* rows, int64_t count, cudaStream_t s,
-                  std::string* why) {
+bool launch_roles(CUfunction fn, int lanes, const StepArgs& a, const int* rows, int64_t count, double dt,
+                  int integrate, cudaStream_t s, std::string* why) {
   StepArgs args = a;
   long long cnt = count;
-  void* params[] = {&args, &rows, &cnt};
+  void* params[] = {&args, &rows, &cnt, &dt, &integrate};
   if (api().launchKernel(fn, unsigned((count + 31) / 32), 1, 1, unsigned(32 * lanes), 1, 1, 0,
                          reinterpret_cast<CUstream>(s), params, nullptr) != CUDA_SUCCESS) {
     *why = "cuLaunchKernel failed";
@@ -635,7 +642,7 @@ bool launch_roles(CUfunction fn, int lanes, const StepArgs& a, const int* rows, 
 
 bool launch_step_roles_jit(Model& M, int lanes, int ops, const StepArgs& a, cudaStream_t s, std::string* why) {
   CUfunction fn = roles_function(M, lanes, ops, a.n, why);
-  return fn && launch_roles(fn, lanes, a, nullptr, a.n, s, why);
+  return fn && launch_roles(fn, lanes, a, nullptr, a.n, 0.0, 0, s, why);
 }
 
 bool step_roles_jit_ready(Model& M, int lanes, int ops, int64_t n, std::string* why) {
@@ -643,10 +650,10 @@ bool step_roles_jit_ready(Model& M, int lanes, int ops, int64_t n, std::string* 
 }
 
 bool launch_step_roles_rows_jit(Model& M, int lanes, int ops, const StepArgs& a, const int* rows, int64_t count,
-                                cudaStream_t s, std::string* why) {
+                                double dt, bool integrate, cudaStream_t s, std::string* why) {
   // (the batch-size threshold was applied to the whole batch by step_roles_jit_ready)
   CUfunction fn = roles_function(M, lanes, ops, INT64_MAX, why);
-  return fn && launch_roles(fn, lanes, a, rows, count, s, why);
+  return fn && launch_roles(fn, lanes, a, rows, count, dt, integrate ? 1 : 0, s, why);
 }
 
 bool prepare_step_roles_jit(Model& M, int lanes, int ops, std::string* why) {

@@ -22,10 +22,11 @@ bool launch_step_roles_jit(Model& M, int lanes, int ops, const StepArgs& a, cuda
 std::string step_roles_jit_source(const Model& M, int lanes, int ops);
 // For a heterogeneous batch of n environments: whether the role-warp sweep of (M, lanes, ops)
 // is available (compiling it if needed), and its launch over `count` environments whose
-// rows of the call's arrays are rows[0 .. count - 1] (device memory).
+// rows of the call's arrays are rows[0 .. count - 1] (device memory), with integrate: then
+// a semi-implicit Euler step of those rows of a.q, a.qd (in place) by dt from a.qdd_out.
 bool step_roles_jit_ready(Model& M, int lanes, int ops, int64_t n, std::string* why);
 bool launch_step_roles_rows_jit(Model& M, int lanes, int ops, const StepArgs& a, const int* rows, int64_t count,
-                                cudaStream_t s, std::string* why);
+                                double dt, bool integrate, cudaStream_t s, std::string* why);
 bool prepare_step_roles_jit(Model& M, int lanes, int ops, std::string* why);
 // Same for the RNEA / ABA vector-Jacobian product kernels.
 bool launch_vjp_jit(Model& M, bool aba, const VjpArgs& a, cudaStream_t s, std::string* why);

@@ -170,6 +170,30 @@ SG_HD void free_flyer_integrate(double* q, const double* v) {
   q[6] = s * qw[0];
 }
 
+// Semi-implicit Euler on one environment's rows: qd += dt qdd, then q advanced by dt qd
+// (angles and slides add; a free flyer moves on SE(3) by its body twist dt qd).
+template <class Tab>
+SG_HD void integrate_env_t(const Tab& T, double* q, double* qd, const double* qdd, double dt) {
+#pragma unroll
+  for (int i = 1; i < T.nj(); i++) {
+    const DJoint& J = T.joint(i);
+    if (J.kind == JK_FREEFLYER) {
+      double v[6];
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const double w = fma(dt, qdd[J.vcol + k], qd[J.vcol + k]);
+        qd[J.vcol + k] = w;
+        v[k] = dt * w;
+      }
+      free_flyer_integrate(q + J.qcol, v);
+    } else {
+      const double w = fma(dt, qdd[J.vcol], qd[J.vcol]);
+      qd[J.vcol] = w;
+      q[J.qcol] = fma(dt, w, q[J.qcol]);
+    }
+  }
+}
+
 // Jlog6 of the transform whose log6 is xi = (rho, phi), as its blocks: Jlog6 =
 // [[Jinv, -TR], [0, Jinv]] in (linear, angular) ordering, with Jinv = 1 + 1/2 [phi]x +
 // g(t) [phi]x^2 and TR = Jinv Q Jinv, Q = Q_l(-rho, -phi). The skew products in Barfoot's

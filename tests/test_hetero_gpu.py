@@ -212,8 +212,9 @@ def test_hetero_role_warp_sweeps_match_generic_and_graph():
     """With run-time compilation on, the models run with teams take the specialised
     one-warp-per-role sweep (a launch each, on side streams beside the persistent kernel,
     which keeps the one-lane models' tiles): results equal the generic team path to rounding
-    and the oracle within tolerance, and a CUDA-graph replay equals the direct step bit for
-    bit."""
+    and the oracle within tolerance, a CUDA-graph replay equals the direct step bit for bit,
+    and three rollout steps (ABA with the Euler update fused into each launch) equal the
+    generic path's to rounding."""
     import ctypes
 
     import torch
@@ -240,3 +241,19 @@ def test_hetero_role_warp_sweeps_match_generic_and_graph():
         assert rel_per_env(a.cpu().numpy(), b.cpu().numpy()) <= 1e-11
     for a, b in zip(valid_blocks(batch, g.outputs), valid_blocks(batch, roles)):
         assert torch.equal(a, b)
+    # the rollout step (ABA, then the semi-implicit Euler update fused into each launch)
+    states = {}
+    try:
+        for jit in (0, 1):
+            L.sgdyn_jit_config(jit, 0, None, None)
+            qs, qds = q.clone(), qd.clone()
+            out = batch.alloc_outputs(N.OP_FORWARD_DYNAMICS)
+            for _ in range(3):
+                batch.rollout_step(qs, qds, tau, 1.0 / 500, out)
+            torch.cuda.synchronize()
+            states[jit] = (qs, qds)
+    finally:
+        L.sgdyn_jit_config(old_jit.value, old_min.value, None, None)
+    for a, b in zip(states[1], states[0]):  # q, qd (padding untouched by both)
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        assert np.abs(a - b).max() <= 1e-11 * max(np.abs(b).max(), 1.0)
