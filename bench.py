@@ -43,12 +43,13 @@ WORKLOAD = ("arm9: 9-DoF tree (7 revolute + 2 prismatic fingers), N=16384 envs p
 # fails when the source changes, so the figures are re-captured with every kernel change.
 KERNEL_COUNTERS = {
     # two launches (FK + Jacobian: 507,392 FP64 warp instructions; CRBA + RNEA + ABA with
-    # forward dynamics from the mass matrix: 1,650,688) per 16384 environments; DRAM bytes as
+    # forward dynamics from the mass matrix: 1,650,688) per 16384 environments (the thread
+    # counts with all predicates on, 987.6 + 3223.0 per environment, agree); DRAM bytes as
     # ncu counted them in a cold capture, where most of the 29 MB of results is still held in
     # L2 when the launches end
-    "specialised": {"fp64_inst_per_env": 2158080 * 32 / 16384, "dram_bytes_per_env": 8.18e6 / 16384},
+    "specialised": {"fp64_inst_per_env": 2158080 * 32 / 16384, "dram_bytes_per_env": 8.20e6 / 16384},
 }
-KERNEL_SOURCE_SHA256 = "d94bc30e7dc497ce74f00425b535e8f09ea0ed43949305ba184be88a359125cb"
+KERNEL_SOURCE_SHA256 = "f60ef985dcdd53444d4239ecc74bca60d76d3fe5b53b91b3eba7282283c27e5e"
 KERNEL_HEADERS = ("device_model.h", "kernels.h", "spatial.cuh", "step_kernel.cuh")
 STEP_OPS = (3, 28)  # sgdyn_step at N = 16384: FK + Jacobian beside CRBA + RNEA + ABA, two launches
 
