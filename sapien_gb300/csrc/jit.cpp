@@ -297,7 +297,7 @@ std::string generate_source(const Model& M, int kind, int ops) {
     // semi-implicit Euler step of q, qd (rows of a.q, a.qd, in place) from a.qdd_out
     o << "extern \"C\" __global__ void __launch_bounds__(" << 32 * lanes
       << ") sgjit_step_roles(const sgdyn::StepArgs a, const int* rows, long long count, double dt, int integrate) {\n"
-      << "  __shared__ double xch[" << 32 * lanes << "];\n"
+      << "  __shared__ double xch[" << 32 * lanes << " * sgdyn::RoleTeam<0, sgjit::kTT>::kChunk];\n"
       << "  const int role = threadIdx.x >> 5, lane = threadIdx.x & 31;\n"
       << "  const long long i0 = (long long)blockIdx.x * 32 + lane;\n"
       << "  const bool valid = i0 < count;\n"

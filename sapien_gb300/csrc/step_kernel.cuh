@@ -211,6 +211,7 @@ struct TeamLanes {
   SG_HD int attach(int k) const { return t[4 + ntrunk() + L() * smax() + k]; }
   SG_HD int owner(int j) const { return t[4 + ntrunk() + L() * smax() + nattach() + j]; }
   SG_HD double sum(double v) const;
+  SG_HD void sum_many(double* v, int n) const;
 };
 
 // Sum over the L lanes of a team (L a power of two, teams aligned in the warp).
@@ -222,17 +223,22 @@ SG_HD double team_sum(double v, int L) {
   return v;
 }
 SG_HD double TeamLanes::sum(double v) const { return team_sum(v, L()); }
+SG_HD void TeamLanes::sum_many(double* v, int n) const {
+  for (int i = 0; i < n; i++) v[i] = team_sum(v[i], L());
+}
 
 // A team whose roles are the warps of a block (L warps, 32 environments; warp r takes role
 // r for every lane) with the team table and the role known at compile time (run-time
 // compiled per model): each warp's sweep covers the trunk and its own branches with
 // constant indices, so its state stays in registers like a one-lane specialised sweep, and
 // the warps run different code without diverging. Sums over the team go through shared
-// memory (xch: L x 32 doubles), in a fixed order, so every warp holds the same bits.
+// memory (xch: L x kChunk x 32 doubles; sum_many exchanges kChunk values per pair of block
+// barriers), in a fixed order, so every warp holds the same bits.
 template <int ROLE, const int* TT>
 struct RoleTeam {
   static constexpr bool kOn = true;
   static constexpr int role = ROLE;
+  static constexpr int kChunk = 8;
   double* xch;
   int lane;
   bool valid;
@@ -245,16 +251,29 @@ struct RoleTeam {
   SG_HD static constexpr int attach(int k) { return TT[4 + ntrunk() + L() * smax() + k]; }
   SG_HD static constexpr int owner(int j) { return TT[4 + ntrunk() + L() * smax() + nattach() + j]; }
   SG_HD double sum(double v) const {
-#ifdef __CUDA_ARCH__
-    xch[ROLE * 32 + lane] = v;
-    __syncthreads();
-    double s = xch[lane];
-#pragma unroll
-    for (int r = 1; r < L(); r++) s += xch[r * 32 + lane];
-    __syncthreads();
-    return s;
-#else
+    sum_many(&v, 1);
     return v;
+  }
+  SG_HD void sum_many(double* v, int n) const {
+#ifdef __CUDA_ARCH__
+#pragma unroll
+    for (int b = 0; b < n; b += kChunk) {
+      const int m = n - b < kChunk ? n - b : kChunk;
+#pragma unroll
+      for (int j = 0; j < m; j++) xch[(ROLE * kChunk + j) * 32 + lane] = v[b + j];
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < m; j++) {
+        double s = xch[j * 32 + lane];
+#pragma unroll
+        for (int r = 1; r < L(); r++) s += xch[(r * kChunk + j) * 32 + lane];
+        v[b + j] = s;
+      }
+      __syncthreads();
+    }
+#else
+    (void)v;
+    (void)n;
 #endif
   }
 };
@@ -814,34 +833,58 @@ SG_HD void step_env_t(const Tab& T, const StepArgs& args, const int64_t e, const
         const int j = tm.sched(k);
         if (j > 0) pass2(j);
       }
-      auto sum6 = [&](Mot& m) {
-        m.v.x = tm.sum(m.v.x); m.v.y = tm.sum(m.v.y); m.v.z = tm.sum(m.v.z);
-        m.w.x = tm.sum(m.w.x); m.w.y = tm.sum(m.w.y); m.w.z = tm.sum(m.w.z);
-      };
+      // each attach joint's branch contributions (forces, composite and articulated
+      // inertias, bias forces), summed over the team in one exchange
+      constexpr int kSums = (kRNEA ? 6 : 0) + (kCRBA ? 10 : 0) + (kArt ? 27 : 0);
 #pragma unroll
       for (int k = 0; k < na; k++) {
         const int t = tm.attach(k);
+        double v[kSums];
+        int c = 0;
+        auto put6 = [&](const Mot& m) {
+          v[c++] = m.v.x; v[c++] = m.v.y; v[c++] = m.v.z; v[c++] = m.w.x; v[c++] = m.w.y; v[c++] = m.w.z;
+        };
+        auto get6 = [&](Mot& m) {
+          m.v.x = v[c++]; m.v.y = v[c++]; m.v.z = v[c++]; m.w.x = v[c++]; m.w.y = v[c++]; m.w.z = v[c++];
+        };
+        if constexpr (kRNEA) put6(frc[t]);
+        if constexpr (kCRBA) {
+          const RBI& r = CC[t];
+          v[c++] = r.m; v[c++] = r.h.x; v[c++] = r.h.y; v[c++] = r.h.z;
+#pragma unroll
+          for (int q = 0; q < 6; q++) v[c++] = r.I[q];
+        }
+        if constexpr (kArt) {
+          const Sym6& a6 = AC[t];
+#pragma unroll
+          for (int q = 0; q < 6; q++) v[c++] = a6.A[q];
+#pragma unroll
+          for (int q = 0; q < 6; q++) v[c++] = a6.C[q];
+#pragma unroll
+          for (int q = 0; q < 9; q++) v[c++] = a6.B[q];
+          put6(pA[t]);
+        }
+        tm.sum_many(v, kSums);
+        c = 0;
         if constexpr (kRNEA) {
-          sum6(frc[t]);
+          get6(frc[t]);
           frc[t] = add6(fbase[t], frc[t]);
         }
         if constexpr (kCRBA) {
-          RBI& c = CC[t];
-          c.m = tm.sum(c.m);
-          c.h.x = tm.sum(c.h.x); c.h.y = tm.sum(c.h.y); c.h.z = tm.sum(c.h.z);
+          RBI& r = CC[t];
+          r.m = v[c++]; r.h.x = v[c++]; r.h.y = v[c++]; r.h.z = v[c++];
 #pragma unroll
-          for (int q = 0; q < 6; q++) c.I[q] = tm.sum(c.I[q]);
+          for (int q = 0; q < 6; q++) r.I[q] = v[c++];
         }
         if constexpr (kArt) {
-          Sym6& s = AC[t];
+          Sym6& a6 = AC[t];
 #pragma unroll
-          for (int q = 0; q < 6; q++) {
-            s.A[q] = tm.sum(s.A[q]);
-            s.C[q] = tm.sum(s.C[q]);
-          }
+          for (int q = 0; q < 6; q++) a6.A[q] = v[c++];
 #pragma unroll
-          for (int q = 0; q < 9; q++) s.B[q] = tm.sum(s.B[q]);
-          sum6(pA[t]);
+          for (int q = 0; q < 6; q++) a6.C[q] = v[c++];
+#pragma unroll
+          for (int q = 0; q < 9; q++) a6.B[q] = v[c++];
+          get6(pA[t]);
           pA[t] = add6(pbase[t], pA[t]);
         }
       }
