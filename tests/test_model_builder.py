@@ -277,3 +277,36 @@ def test_reference_module_name_is_kept():
     from sapien_gb300 import pysapien_pinocchio
 
     assert pysapien_pinocchio.PinocchioModel is PinocchioModel
+
+
+def test_forward_dynamics_route_choice():
+    """sgdyn_fd_by_mass_matrix reports the route the specialised sweep (and the host path)
+    takes: from the mass matrix where it costs fewer FP64 operations than the
+    articulated-body passes. Small trees take it for every op set holding ABA, the 35-DoF
+    humanoid only when CRBA is computed anyway, the 40-joint chain (sum of depth^2 ~ nv^3 / 6)
+    never; op sets without ABA never; sgdyn_fd_method forces either route."""
+    robots = {"arm9": syn.arm_with_fingers(), "quadruped": syn.quadruped(), "humanoid": syn.humanoid(),
+              "chain40": syn.serial_chain(40, seed=23)}
+    L = N.load()
+    old = ctypes.c_int()
+    assert L.sgdyn_fd_method(-1, ctypes.byref(old)) == N.OK and old.value == 0
+    for bad in (3, -2):
+        assert L.sgdyn_fd_method(bad, None) != N.OK
+    want = {"arm9": (1, 1, 1, 1), "quadruped": (1, 1, 1, 1), "humanoid": (0, 0, 1, 1), "chain40": (0, 0, 0, 0)}
+    for name, r in robots.items():
+        pm = PinocchioModel(r.urdf, [0, 0, -9.81])
+        pm.set_joint_order(r.joint_names)
+        got = []
+        for ops in (16, 24, 28, 31):
+            y = ctypes.c_int()
+            assert L.sgdyn_fd_by_mass_matrix(pm._h, ops, ctypes.byref(y)) == N.OK
+            got.append(y.value)
+        assert tuple(got) == want[name], name
+        y = ctypes.c_int()
+        assert L.sgdyn_fd_by_mass_matrix(pm._h, 8 | 4 | 1 | 2, ctypes.byref(y)) == N.OK and y.value == 0
+        try:
+            for mode, forced in ((1, 0), (2, 1)):
+                assert L.sgdyn_fd_method(mode, None) == N.OK
+                assert L.sgdyn_fd_by_mass_matrix(pm._h, 16, ctypes.byref(y)) == N.OK and y.value == forced
+        finally:
+            L.sgdyn_fd_method(old.value, None)
