@@ -212,7 +212,8 @@ int sgdyn_jit_max_joints(int max_joints, int* max_joints_out);
  * articulated-body passes (ABA), 2 from the mass matrix (CRBA, the bias forces by RNEA at
  * zero acceleration, M = L^T D L with the tree's sparsity, qdd = M^-1 (tau - b); inverse
  * dynamics in the same sweep then reads tau = b + M qdd); -1 only reads the setting.
- * Results agree to rounding. The generic kernels always run the articulated-body passes. */
+ * Results agree to rounding. The generic kernels always run the articulated-body passes, and
+ * the host path (sgdyn_host_*) unless the mode is 2. */
 int sgdyn_fd_method(int mode, int* mode_out);
 /* Whether the specialised sweep for (model, ops) takes the mass-matrix route (*yes = 1). */
 int sgdyn_fd_by_mass_matrix(const sgdyn_model* m, int ops, int* yes);

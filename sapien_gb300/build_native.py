@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import glob
 import os
+import platform
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
@@ -20,8 +21,14 @@ LIB = os.path.join(LIBDIR, "libsgdyn.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# The host instantiation of the sweeps (single-configuration calls) calls fma() throughout:
+# on x86-64 it needs the FMA instructions (every x86-64 CPU since 2013 has them) or each
+# call goes to the C library; aarch64 always has them. fma rounds once either way, and the
+# compiler is kept from fusing other products and sums, so host results stay what they were.
+HOST_FLAGS = (["-Xcompiler", "-mfma", "-Xcompiler", "-ffp-contract=off"]
+              if platform.machine() in ("x86_64", "AMD64") else [])
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-                     "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
+                     "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC] + HOST_FLAGS
 
 
 def _nvcc():

@@ -172,8 +172,12 @@ int sgdyn_host_step(const sgdyn_model* m, int64_t n, int ops, const double* q, c
       }
     for (int b = 1; b <= OP_ABA; b <<= 1)
       if (rest & b) parts[np++] = b;
-    for (int k = 0; k < np; k++)  // the forward-dynamics route with fewer operations (sgdyn_fd_method)
-      if (fd_by_mass_matrix(Mo, parts[k])) parts[k] |= OP_FD_CRBA;
+    // forward dynamics from the mass matrix only when sgdyn_fd_method forces it: on the host
+    // its loops over run-time tables measured no faster than the articulated-body passes
+    int fd_mode = 0;
+    fd_method(-1, &fd_mode);
+    for (int k = 0; k < np; k++)
+      if (fd_mode == 2 && fd_by_mass_matrix(Mo, parts[k])) parts[k] |= OP_FD_CRBA;
     const DModel* dm = table(m);
     const int bucket = stash_bucket(Mo.njoints());
     parallel_envs(n, nthreads, [&](int64_t lo, int64_t hi) {
